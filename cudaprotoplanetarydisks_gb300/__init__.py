@@ -1,0 +1,129 @@
+"""GB300-native FARGO-ADSG 2D polar-grid hydro step (host-side Python API).
+
+The compute path is libfargo_gb300.so (CUDA kernels for sm_103a behind the C-ABI
+of include/fargo_gb300.h).  This module mirrors the reference's per-step entry
+points (AlgoGas, Substep1/2/3, Transport, ConditionCFL, ...) on a Disk object;
+it never computes anything itself and raises when the library is missing.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _capi
+from ._capi import (FARGO_FP32_BULK, FARGO_FP64, FIELDS, SUB_BOUNDARY, SUB_ENERGY,  # noqa: F401
+                    SUB_POTENTIAL, SUB_SOUNDSPEED, SUB_SOURCE, SUB_TEMPERATURE, SUB_TRANSPORT,
+                    FargoParams, FargoPlanet, FargoScalars)
+from .config import default_params, load_config, read_par, read_planets  # noqa: F401
+
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+class FargoError(RuntimeError):
+    pass
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_DP)
+
+
+class Disk:
+    """One disk on one GPU.  precision: FARGO_FP64 (parity mode) or FARGO_FP32_BULK."""
+
+    def __init__(self, params, planets, precision=FARGO_FP64, stream=None):
+        self.lib = _capi.load()
+        self.params = params
+        self.nrad, self.nsec = params.nrad, params.nsec
+        self.precision = precision
+        arr = (FargoPlanet * max(1, len(planets)))(*planets)
+        h = ctypes.c_void_p()
+        rc = self.lib.fargo_ctx_create(ctypes.byref(params), arr, len(planets), precision,
+                                       ctypes.c_void_p(stream) if stream else None, ctypes.byref(h))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_ctx_create failed with status {rc}")
+        self.h = h
+
+    def _check(self, rc, what):
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"{what}: status {rc}: {self.lib.fargo_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fargo_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state -------------------------------------------------------------
+    def field(self, name):
+        out = np.empty((self.nrad + 1, self.nsec), dtype=np.float64)
+        self._check(self.lib.fargo_get_field(self.h, FIELDS[name], _ptr(out)), f"get_field({name})")
+        return out
+
+    def fields(self):
+        return {k: self.field(k) for k in ("dens", "vrad", "vtheta", "energy", "temperature")}
+
+    def set_fields(self, dens=None, vrad=None, vtheta=None, energy=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (dens, vrad, vtheta, energy)]
+        self._check(self.lib.fargo_set_fields(self.h, *[_ptr(a) for a in arrs]), "set_fields")
+
+    def planets(self):
+        arr = (FargoPlanet * 64)()
+        nb = ctypes.c_int(0)
+        self._check(self.lib.fargo_get_planets(self.h, arr, 64, ctypes.byref(nb)), "get_planets")
+        return [arr[k] for k in range(nb.value)]
+
+    def scalars(self):
+        s = FargoScalars()
+        self._check(self.lib.fargo_get_scalars(self.h, ctypes.byref(s)), "get_scalars")
+        return s
+
+    def mesh(self):
+        n = self.nrad + 1
+        rinf, rmed, rsup, surf = (np.empty(n) for _ in range(4))
+        self._check(self.lib.fargo_get_mesh(self.h, _ptr(rinf), _ptr(rmed), _ptr(rsup), _ptr(surf)), "get_mesh")
+        return rinf, rmed, rsup, surf
+
+    # -- stepping (reference entry points) ----------------------------------
+    def step_DT(self):
+        """AlgoGas: one DT; returns the number of hydro substeps."""
+        n = ctypes.c_int(0)
+        self._check(self.lib.fargo_step_DT(self.h, ctypes.byref(n)), "step_DT")
+        return n.value
+
+    def run(self, ndt):
+        n = ctypes.c_longlong(0)
+        self._check(self.lib.fargo_run(self.h, int(ndt), ctypes.byref(n)), "run")
+        return n.value
+
+    def run_async(self, ndt):
+        self._check(self.lib.fargo_run_async(self.h, int(ndt)), "run_async")
+
+    def sync(self):
+        self._check(self.lib.fargo_sync(self.h), "sync")
+
+    def substep_full(self, dt):
+        self._check(self.lib.fargo_substep_full(self.h, float(dt)), "substep_full")
+
+    def substep(self, which, dt):
+        self._check(self.lib.fargo_substep(self.h, int(which), float(dt)), f"substep({which})")
+
+    def condition_cfl(self, deltaT):
+        c = ctypes.c_int(0)
+        self._check(self.lib.fargo_condition_cfl(self.h, float(deltaT), ctypes.byref(c)), "condition_cfl")
+        return c.value
+
+    def write_outputs(self, index):
+        self._check(self.lib.fargo_write_outputs(self.h, int(index)), "write_outputs")
+
+    def write_dims(self):
+        self._check(self.lib.fargo_write_dims(self.h), "write_dims")

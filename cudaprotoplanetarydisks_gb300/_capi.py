@@ -1,0 +1,134 @@
+"""ctypes view of include/fargo_gb300.h (the C-ABI of libfargo_gb300.so)."""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfargo_gb300.so")
+
+FARGO_OK = 0
+FARGO_ERR_INVALID = 1
+FARGO_ERR_CUDA = 2
+FARGO_ERR_IO = 3
+FARGO_ERR_NUMERIC = 4
+FARGO_ERR_STATE = 5
+
+FARGO_FP64 = 0
+FARGO_FP32_BULK = 1
+
+SUB_BOUNDARY = 1
+SUB_SOURCE = 2
+SUB_ENERGY = 3
+SUB_TRANSPORT = 4
+SUB_TEMPERATURE = 5
+SUB_SOUNDSPEED = 6
+SUB_POTENTIAL = 7
+
+FIELDS = {
+    "dens": 0, "vrad": 1, "vtheta": 2, "energy": 3, "temperature": 4,
+    "pressure": 5, "soundspeed": 6, "potential": 7, "qplus": 8,
+    "divergence": 9, "sg_accr": 10, "sg_acct": 11,
+}
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+
+
+class FargoParams(ctypes.Structure):
+    _fields_ = [
+        ("nrad", _I), ("nsec", _I), ("rmin", _D), ("rmax", _D), ("log_grid", _I),
+        ("dt", _D), ("ntot", _I), ("ninterm", _I),
+        ("sigma0", _D), ("sigmaslope", _D), ("aspectratio", _D), ("flaringindex", _D),
+        ("viscosity", _D), ("alphaviscosity", _D), ("imposeddiskdrift", _D), ("eccentricity", _D),
+        ("cavityradius", _D), ("cavityratio", _D), ("cavitywidth", _D),
+        ("transitionradius", _D), ("transitionratio", _D), ("transitionwidth", _D),
+        ("lambdadoubling", _D), ("adiabaticindex", _D), ("coolingtime0", _D),
+        ("thicknesssmoothing", _D), ("rochesmoothing", _D), ("masstaper", _D),
+        ("releaseradius", _D), ("releasedate", _D), ("omegaframe", _D),
+        ("fast_transport", _I), ("open_inner", _I), ("non_reflecting", _I), ("evanescent", _I),
+        ("is_disk", _I), ("corotating", _I), ("guiding_center", _I), ("indirect_term", _I),
+        ("exclude_hill", _I), ("self_gravity", _I), ("sg_zero_mode", _I),
+        ("adiabatic", _I), ("cooling", _I), ("cic_planet", _I), ("forced_circular", _I),
+        ("viscosity_alpha", _I), ("roche_smoothing", _I), ("advect_label", _I),
+        ("outer_source_mass", _I),
+        ("write_density", _I), ("write_velocity", _I), ("write_energy", _I),
+        ("write_temperature", _I), ("write_divv", _I), ("write_qplus", _I),
+        ("sloppy_cfl", _I), ("centrifugal_balance", _I), ("scaling_factor", _D),
+        ("outputdir", ctypes.c_char * 512), ("planetconfig", ctypes.c_char * 512),
+        ("sigma_noise", _D), ("energy_noise", _D), ("noise_seed", ctypes.c_ulonglong),
+    ]
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = v.decode() if isinstance(v, bytes) else v
+        return out
+
+
+class FargoPlanet(ctypes.Structure):
+    _fields_ = [("x", _D), ("y", _D), ("vx", _D), ("vy", _D), ("mass", _D), ("acc", _D),
+                ("feel_disk", _I), ("feel_others", _I)]
+
+
+class FargoScalars(ctypes.Structure):
+    _fields_ = [("physical_time", _D), ("omega_frame", _D), ("lost_mass", _D),
+                ("last_dt", _D), ("substeps", ctypes.c_longlong), ("last_cfl", _I), ("nb", _I)]
+
+
+_DP = ctypes.POINTER(_D)
+_P = ctypes.c_void_p
+
+# (name, restype, argtypes) for every entry point declared in include/fargo_gb300.h
+SIGNATURES = [
+    ("fargo_params_default", None, [ctypes.POINTER(FargoParams)]),
+    ("fargo_params_read", _I, [ctypes.c_char_p, ctypes.POINTER(FargoParams)]),
+    ("fargo_params_apply_switches", _I, [ctypes.c_char_p, ctypes.POINTER(FargoParams)]),
+    ("fargo_planets_read", _I, [ctypes.c_char_p, ctypes.POINTER(FargoParams),
+                                ctypes.POINTER(FargoPlanet), _I, ctypes.POINTER(_I)]),
+    ("fargo_ctx_create", _I, [ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), _I, _I,
+                              _P, ctypes.POINTER(_P)]),
+    ("fargo_ctx_destroy", None, [_P]),
+    ("fargo_last_error", ctypes.c_char_p, [_P]),
+    ("fargo_get_fields", _I, [_P, _DP, _DP, _DP, _DP, _DP]),
+    ("fargo_set_fields", _I, [_P, _DP, _DP, _DP, _DP]),
+    ("fargo_get_field", _I, [_P, _I, _DP]),
+    ("fargo_get_planets", _I, [_P, ctypes.POINTER(FargoPlanet), _I, ctypes.POINTER(_I)]),
+    ("fargo_get_scalars", _I, [_P, ctypes.POINTER(FargoScalars)]),
+    ("fargo_get_mesh", _I, [_P, _DP, _DP, _DP, _DP]),
+    ("fargo_step_DT", _I, [_P, ctypes.POINTER(_I)]),
+    ("fargo_run", _I, [_P, _I, ctypes.POINTER(ctypes.c_longlong)]),
+    ("fargo_run_async", _I, [_P, _I]),
+    ("fargo_sync", _I, [_P]),
+    ("fargo_substep_full", _I, [_P, _D]),
+    ("fargo_substep", _I, [_P, _I, _D]),
+    ("fargo_condition_cfl", _I, [_P, _D, ctypes.POINTER(_I)]),
+    ("fargo_write_outputs", _I, [_P, _I]),
+    ("fargo_write_dims", _I, [_P]),
+]
+
+_lib = None
+
+
+def load(path=None):
+    """Load libfargo_gb300.so; raise (never fall back) when it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"{p} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(p)
+    lib.missing_symbols = []
+    for name, res, args in SIGNATURES:
+        try:
+            fn = getattr(lib, name)
+        except AttributeError:
+            lib.missing_symbols.append(name)
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib

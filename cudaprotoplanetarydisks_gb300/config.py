@@ -1,0 +1,79 @@
+"""The reference's .par / .cfg parameter interface, through the C-ABI parser.
+
+read_par mirrors ReadVariables (src/Interpret.cu:100-212); read_planets mirrors
+InitPlanetarySystem (src/Psys.cu:168-217).  The workloads of the benchmark and
+of the parity tests are shipped as .par/.cfg files in configs/.
+"""
+import ctypes
+import os
+
+from . import _capi
+
+CONFIG_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "configs")
+
+NAMED = {
+    "c1": "c1_isothermal.par",
+    "c2": "c2_selfgravity.par",
+    "c3": "c3_adiabatic.par",
+}
+
+
+def default_params():
+    p = _capi.FargoParams()
+    _capi.load().fargo_params_default(ctypes.byref(p))
+    return p
+
+
+def read_par(path, switches=None):
+    """Parse a .par file; switches is an optional CLI switch string such as "-c"."""
+    lib = _capi.load()
+    p = default_params()
+    rc = lib.fargo_params_read(os.fsencode(path), ctypes.byref(p))
+    if rc == _capi.FARGO_ERR_IO:
+        raise FileNotFoundError(path)
+    if rc != _capi.FARGO_OK:
+        raise ValueError(f"{path}: conflicting parameters (status {rc})")
+    if switches:
+        rc = lib.fargo_params_apply_switches(switches.encode(), ctypes.byref(p))
+        if rc != _capi.FARGO_OK:
+            raise ValueError(f"bad switches {switches!r}")
+    return p
+
+
+def resolve_planet_config(params, par_path=None):
+    """PlanetConfig is relative to the working directory in the reference; fall back
+    to the directory of the .par file."""
+    name = params.planetconfig.decode()
+    if os.path.exists(name):
+        return name
+    if par_path is not None:
+        cand = os.path.join(os.path.dirname(os.path.abspath(par_path)), name)
+        if os.path.exists(cand):
+            return cand
+    raise FileNotFoundError(name)
+
+
+def read_planets(params, par_path=None, cap=64):
+    lib = _capi.load()
+    path = resolve_planet_config(params, par_path)
+    arr = (_capi.FargoPlanet * cap)()
+    nb = ctypes.c_int(0)
+    rc = lib.fargo_planets_read(os.fsencode(path), ctypes.byref(params), arr, cap, ctypes.byref(nb))
+    if rc != _capi.FARGO_OK:
+        raise ValueError(f"{path}: cannot read planets (status {rc})")
+    return [arr[k] for k in range(nb.value)]
+
+
+def load_config(name_or_path, **overrides):
+    """(params, planets) of a named workload (c1, c2, c3) or of a .par path.
+    Keyword overrides set FargoParams members (e.g. nrad=64, nsec=192)."""
+    path = name_or_path
+    if name_or_path in NAMED:
+        path = os.path.join(CONFIG_DIR, NAMED[name_or_path])
+    params = read_par(path)
+    planets = read_planets(params, path)
+    for k, v in overrides.items():
+        if isinstance(v, str):
+            v = v.encode()
+        setattr(params, k, v)
+    return params, planets

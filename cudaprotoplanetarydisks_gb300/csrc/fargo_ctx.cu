@@ -1,0 +1,726 @@
+// fargo_ctx.cu -- disk context, device memory, graph of one DT, and the C-ABI.
+//
+// A context owns every device buffer of one disk (the reference keeps them in
+// file-scope globals allocated by Cudamalloc, src/Main.cu:660-827, and friends).
+// One DT (AlgoGas, src/SourceEuler.cu:199-307) is one CUDA graph: a prefix
+// (DT start, sound speed of the energy equation) followed by a conditional WHILE
+// node whose body is one hydro substep; the substep's last kernel sets the loop
+// condition from the device-side dtemp, so a DT runs without any host sync.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fargo_device.cuh"
+#include "fargo_internal.h"
+#include "fargo_kernels.cuh"
+
+struct fargo_ctx {
+  fargo_params P;
+  DevParams dp;
+  int precision = FARGO_FP64;
+  int nb = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  HostState h;
+  std::string err = "no error";
+  Ctl *d_ctl = nullptr;
+  Ctl *pin_ctl = nullptr;
+  std::vector<void *> allocs;
+  size_t esize = 8;
+  // fields (element type T = double or float)
+  void *dens = nullptr, *vrad = nullptr, *vtheta = nullptr, *energy = nullptr, *cs = nullptr;
+  void *pressure = nullptr, *temperature = nullptr, *potential = nullptr;
+  void *vradint = nullptr, *vthetaint = nullptr, *energyint = nullptr;
+  void *qplus = nullptr, *divv = nullptr, *taurr = nullptr, *taurp = nullptr, *taupp = nullptr;
+  void *densr = nullptr, *energyr = nullptr, *radmomp = nullptr, *radmomm = nullptr;
+  void *thetamomp = nullptr, *thetamomm = nullptr, *sg_accr = nullptr, *sg_acct = nullptr;
+  void *az_scratch = nullptr, *rt = nullptr, *nu = nullptr, *cosP = nullptr, *sinP = nullptr;
+  double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
+  double *ring_vmoy = nullptr, *ring_newdt = nullptr, *ring_force = nullptr, *lostbydisk = nullptr;
+  // self-gravity
+  double2 *spec_r = nullptr, *spec_t = nullptr, *khat_r = nullptr, *khat_t = nullptr, *tw1 = nullptr, *tw0 = nullptr;
+  double *kr = nullptr, *kt = nullptr;
+  int rad1[16], nst1 = 0, rad0[16], nst0 = 0;
+  size_t az_smem = 0;
+  // graph of one DT
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long cond_handle = 0;
+  bool use_graph = true;
+};
+
+namespace {
+
+int set_err(fargo_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                      \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess)                                                                            \
+      return set_err(c, FARGO_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+template <class T>
+KArgs<T> make_args(const fargo_ctx *c) {
+  KArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.P = c->dp;
+  DiskPtrs<T> &d = a.d;
+  d.dens = (T *)c->dens;
+  d.vrad = (T *)c->vrad;
+  d.vtheta = (T *)c->vtheta;
+  d.energy = (T *)c->energy;
+  d.cs = (T *)c->cs;
+  d.pressure = (T *)c->pressure;
+  d.temperature = (T *)c->temperature;
+  d.potential = (T *)c->potential;
+  d.vradint = (T *)c->vradint;
+  d.vthetaint = (T *)c->vthetaint;
+  d.energyint = (T *)c->energyint;
+  d.qplus = (T *)c->qplus;
+  d.divv = (T *)c->divv;
+  d.taurr = (T *)c->taurr;
+  d.taurp = (T *)c->taurp;
+  d.taupp = (T *)c->taupp;
+  d.densr = (T *)c->densr;
+  d.energyr = (T *)c->energyr;
+  d.radmomp = (T *)c->radmomp;
+  d.radmomm = (T *)c->radmomm;
+  d.thetamomp = (T *)c->thetamomp;
+  d.thetamomm = (T *)c->thetamomm;
+  d.sg_accr = (T *)c->sg_accr;
+  d.sg_acct = (T *)c->sg_acct;
+  d.az_scratch = (T *)c->az_scratch;
+  d.rt = (const T *)c->rt;
+  d.rt64 = c->rt64;
+  d.nu = (T *)c->nu;
+  d.csmean = c->csmean;
+  d.cosF = c->cosF;
+  d.sinF = c->sinF;
+  d.cosP = (const T *)c->cosP;
+  d.sinP = (const T *)c->sinP;
+  d.ring_vmoy = c->ring_vmoy;
+  d.ring_newdt = c->ring_newdt;
+  d.ring_force = c->ring_force;
+  d.lostbydisk = c->lostbydisk;
+  d.ctl = c->d_ctl;
+  a.invdphi = 1.0 / (2.0 * M_PI / (double)c->P.nsec);
+  if (c->P.nrad >= 3) {
+    a.lr01 = log(c->h.Rmed[0] / c->h.Rmed[1]);
+    a.lr12 = log(c->h.Rmed[1] / c->h.Rmed[2]);
+  }
+  a.mode = c->P.sloppy_cfl ? 2 : 0;
+  a.az_smem = 0;
+  a.cond_handle = 0;
+  a.use_cond = 0;
+  a.sg.spec_r = c->spec_r;
+  a.sg.spec_t = c->spec_t;
+  a.sg.khat_r = c->khat_r;
+  a.sg.khat_t = c->khat_t;
+  a.sg.tw1 = c->tw1;
+  a.sg.tw0 = c->tw0;
+  a.sg.kr = c->kr;
+  a.sg.kt = c->kt;
+  for (int k = 0; k < 16; k++) {
+    a.sg.rad1[k] = c->rad1[k];
+    a.sg.rad0[k] = c->rad0[k];
+  }
+  a.sg.nst1 = c->nst1;
+  a.sg.nst0 = c->nst0;
+  a.sg.M = c->P.nsec / 2 + 1;
+  return a;
+}
+
+int dev_alloc(fargo_ctx *c, void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return set_err(c, FARGO_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back(*p);
+  e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return set_err(c, FARGO_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+  return FARGO_OK;
+}
+
+// host double -> device T
+int upload(fargo_ctx *c, void *dst, const double *src, size_t n) {
+  if (c->esize == 8) {
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  } else {
+    std::vector<float> tmp(n);
+    for (size_t k = 0; k < n; k++) tmp[k] = (float)src[k];
+    CK(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return FARGO_OK;
+}
+
+int download(fargo_ctx *c, double *dst, const void *src, size_t n) {
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->esize == 8) {
+    CK(cudaMemcpy(dst, src, n * 8, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(n);
+    CK(cudaMemcpy(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < n; k++) dst[k] = (double)tmp[k];
+  }
+  return FARGO_OK;
+}
+
+int read_ctl(fargo_ctx *c) {
+  CK(cudaMemcpyAsync(c->pin_ctl, c->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return FARGO_OK;
+}
+
+int write_ctl(fargo_ctx *c) {
+  CK(cudaMemcpyAsync(c->d_ctl, c->pin_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return FARGO_OK;
+}
+
+int check_launch(fargo_ctx *c, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(c, FARGO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return FARGO_OK;
+}
+
+int device_error(fargo_ctx *c) {
+  int e = c->pin_ctl->err;
+  if (!e) return FARGO_OK;
+  std::string m = "device error:";
+  if (e & FARGO_DEVERR_CFL) m += " non-finite or non-positive CFL time step;";
+  if (e & FARGO_DEVERR_CAP) m += " substep cap per DT exceeded;";
+  if (e & FARGO_DEVERR_NAN) m += " non-finite density;";
+  return set_err(c, FARGO_ERR_NUMERIC, m);
+}
+
+template <class T>
+int build_graph(fargo_ctx *c) {
+  KArgs<T> a = make_args<T>(c);
+  cudaGraph_t g = nullptr, gp = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  launch_dt_prefix<T>(a, c->stream);
+  CK(cudaStreamEndCapture(c->stream, &gp));
+  cudaGraphNode_t np, nc;
+  CK(cudaGraphAddChildGraphNode(&np, g, nullptr, 0, gp));
+  CK(cudaGraphDestroy(gp));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  CK(cudaGraphAddNode(&nc, g, &np, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  a.cond_handle = (unsigned long long)h;
+  a.use_cond = 1;
+  CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+  CK(cudaStreamEndCapture(c->stream, &body));
+  CK(cudaGraphInstantiate(&c->exec, g, 0));
+  c->graph = g;
+  c->cond_handle = a.cond_handle;
+  return FARGO_OK;
+}
+
+// one DT with a host loop (fallback when conditional graph nodes are unavailable)
+template <class T>
+int run_dt_hostloop(fargo_ctx *c) {
+  KArgs<T> a = make_args<T>(c);
+  launch_dt_prefix<T>(a, c->stream);
+  for (int n = 0; n < FARGO_MAX_SUBSTEPS_PER_DT + 1; n++) {
+    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+    int rc = check_launch(c, "substep");
+    if (rc) return rc;
+    if ((rc = read_ctl(c))) return rc;
+    if (c->pin_ctl->done) break;
+  }
+  return FARGO_OK;
+}
+
+template <class T>
+int enqueue_dt(fargo_ctx *c) {
+  if (c->use_graph) {
+    cudaError_t e = cudaGraphLaunch(c->exec, c->stream);
+    if (e != cudaSuccess) return set_err(c, FARGO_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+    return FARGO_OK;
+  }
+  return run_dt_hostloop<T>(c);
+}
+
+template <class T>
+int init_typed(fargo_ctx *c, const fargo_planet *planets) {
+  const fargo_params &p = c->P;
+  HostState &h = c->h;
+  const size_t sg = h.size_grid, n1 = (size_t)p.nrad + 1;
+  const size_t E = sizeof(T);
+  Ctl &ctl = *c->pin_ctl;
+  std::memset(&ctl, 0, sizeof(Ctl));
+  host_init_planets(p, h, planets, c->nb, ctl);
+  ctl.DT = p.dt;
+  // device arrays
+  void **fields[] = {&c->dens, &c->vrad, &c->vtheta, &c->energy, &c->pressure, &c->temperature, &c->potential,
+                     &c->vradint, &c->vthetaint, &c->energyint, &c->qplus, &c->divv, &c->taurr, &c->taurp,
+                     &c->taupp, &c->densr, &c->energyr, &c->radmomp, &c->radmomm, &c->thetamomp, &c->thetamomm};
+  int rc;
+  for (void **f : fields)
+    if ((rc = dev_alloc(c, f, sg * E))) return rc;
+  if (p.adiabatic && (rc = dev_alloc(c, &c->cs, sg * E))) return rc;
+  if ((rc = dev_alloc(c, &c->rt, (size_t)RT_COUNT * n1 * E))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->rt64, (size_t)RT_COUNT * n1 * 8))) return rc;
+  if ((rc = dev_alloc(c, &c->nu, n1 * E))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->csmean, n1 * 8))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->cosF, (size_t)p.nsec * 8))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->sinF, (size_t)p.nsec * 8))) return rc;
+  if ((rc = dev_alloc(c, &c->cosP, (size_t)p.nsec * E))) return rc;
+  if ((rc = dev_alloc(c, &c->sinP, (size_t)p.nsec * E))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->ring_vmoy, n1 * 8))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->ring_newdt, n1 * 8))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->ring_force, n1 * (FARGO_MAXPL + 1) * 2 * 8))) return rc;
+  if ((rc = dev_alloc(c, (void **)&c->lostbydisk, (size_t)p.nsec * 8))) return rc;
+  // azimuthal transport ring buffers: shared memory when they fit
+  {
+    int dev = 0, maxsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    size_t need = (size_t)11 * p.nsec * E;
+    if (need + 1024 <= (size_t)maxsm) {
+      c->az_smem = need;
+      CK(prepare_kernels<T>(need));
+    } else {
+      c->az_smem = 0;
+      if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * 11 * p.nsec * E))) return rc;
+    }
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  // density first: self-gravity set-up needs it
+  if ((rc = upload(c, c->dens, h.Dens.data(), sg))) return rc;
+  std::vector<double> tmpd;
+  if (p.self_gravity) {
+    const int n0 = 2 * p.nrad, M = p.nsec / 2 + 1;
+    c->nst1 = sg_radices(p.nsec, c->rad1);
+    c->nst0 = sg_radices(n0, c->rad0);
+    if (c->nst1 < 0 || c->nst0 < 0)
+      return set_err(c, FARGO_ERR_INVALID, "self-gravity needs NSEC and 2*NRAD of the form 2^a 3^b");
+    host_sg_kernel(p, h, c->dp);
+    if ((rc = dev_alloc(c, (void **)&c->spec_r, (size_t)M * p.nrad * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->spec_t, (size_t)M * p.nrad * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->khat_r, (size_t)M * n0 * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->khat_t, (size_t)M * n0 * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->tw1, (size_t)p.nsec * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->tw0, (size_t)n0 * 16))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->kr, (size_t)n0 * p.nsec * 8))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->kt, (size_t)n0 * p.nsec * 8))) return rc;
+    if ((rc = dev_alloc(c, &c->sg_accr, sg * E))) return rc;
+    if ((rc = dev_alloc(c, &c->sg_acct, sg * E))) return rc;
+    auto twiddles = [](int n) {
+      std::vector<double> t(2 * (size_t)n);
+      for (int k = 0; k < n; k++) {
+        long double ang = 2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)n;
+        t[2 * k] = (double)cosl(ang);
+        t[2 * k + 1] = (double)(-sinl(ang));
+      }
+      return t;
+    };
+    std::vector<double> t1 = twiddles(p.nsec), t0 = twiddles(n0);
+    CK(cudaMemcpy(c->tw1, t1.data(), t1.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->tw0, t0.data(), t0.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->kr, h.Kr.data(), h.Kr.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->kt, h.Kt.data(), h.Kt.size() * 8, cudaMemcpyHostToDevice));
+    CK(prepare_sg_kernels<T>(p.nsec, n0));
+    // ring table rows the SG kernels read
+    std::vector<double> tab;
+    host_ring_table(p, h, c->dp, tab);  // uses only mesh rows at this point
+    CK(cudaMemcpy(c->rt64, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
+    KArgs<T> a = make_args<T>(c);
+    a.P = c->dp;
+    launch_sg_kernel_spectra<T>(a, c->stream);
+    if ((rc = check_launch(c, "sg kernel spectra"))) return rc;
+    launch_selfgravity<T>(a, c->stream);
+    if ((rc = check_launch(c, "sg set-up"))) return rc;
+    std::vector<double> accr(sg);
+    if ((rc = download(c, accr.data(), c->sg_accr, sg))) return rc;
+    std::vector<double> axi(p.nrad + 1, 0.0);
+    for (int i = 0; i < p.nrad; i++) {
+      double s = 0.0;
+      for (int j = 0; j < p.nsec; j++) s += accr[(size_t)i * p.nsec + j];
+      axi[i] = s / (double)p.nsec;
+    }
+    host_init_planets_sg(p, h, axi, ctl);
+  }
+  host_init_euler(p, h, c->dp, ctl);
+  std::vector<double> tab;
+  host_ring_table(p, h, c->dp, tab);
+  CK(cudaMemcpy(c->rt64, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
+  if ((rc = upload(c, c->rt, tab.data(), tab.size()))) return rc;
+  if ((rc = upload(c, c->nu, h.nu.data(), n1))) return rc;
+  CK(cudaMemcpy(c->csmean, h.cs_mean.data(), n1 * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->cosF, h.cosF.data(), (size_t)p.nsec * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->sinF, h.sinF.data(), (size_t)p.nsec * 8, cudaMemcpyHostToDevice));
+  if ((rc = upload(c, c->cosP, h.cosP.data(), p.nsec))) return rc;
+  if ((rc = upload(c, c->sinP, h.sinP.data(), p.nsec))) return rc;
+  if ((rc = upload(c, c->vrad, h.Vrad.data(), sg))) return rc;
+  if ((rc = upload(c, c->vtheta, h.Vtheta.data(), sg))) return rc;
+  if ((rc = upload(c, c->energy, h.Energy.data(), sg))) return rc;
+  if ((rc = upload(c, c->pressure, h.Pressure.data(), sg))) return rc;
+  if ((rc = upload(c, c->temperature, h.Temperature.data(), sg))) return rc;
+  if (p.adiabatic && (rc = upload(c, c->cs, h.SoundSpeed.data(), sg))) return rc;
+  ctl.PhysicalTime = 0.0;
+  ctl.PhysicalTimeInitial = 0.0;
+  ctl.OmegaFrame = h.OmegaFrame;
+  if ((rc = write_ctl(c))) return rc;
+  // the SG spectra are no longer needed on the host
+  h.Kr.clear();
+  h.Kt.clear();
+  if (c->use_graph) {
+    rc = build_graph<T>(c);
+    if (rc != FARGO_OK) {
+      // conditional graph nodes unavailable: fall back to the host loop
+      cudaGetLastError();
+      c->use_graph = false;
+      c->err = "graph fallback: " + c->err;
+    }
+  }
+  return FARGO_OK;
+}
+
+template <class T>
+int substep_typed(fargo_ctx *c, int which, double dt) {
+  KArgs<T> a = make_args<T>(c);
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  c->pin_ctl->dt = dt;
+  c->pin_ctl->sloppy_dt = dt;
+  if ((rc = write_ctl(c))) return rc;
+  unsigned mask = 0;
+  switch (which) {
+    case FARGO_SUB_BOUNDARY: launch_boundaries<T>(a, c->stream); break;
+    case FARGO_SUB_SOURCE: mask = SUBK_SG | SUBK_SOURCE; break;
+    case FARGO_SUB_ENERGY:
+      if (!c->P.adiabatic) return set_err(c, FARGO_ERR_INVALID, "no energy equation");
+      mask = SUBK_ENERGY;
+      break;
+    case FARGO_SUB_TRANSPORT: mask = SUBK_TRANSPORT; break;
+    case FARGO_SUB_TEMPERATURE: mask = SUBK_TEMPERATURE; break;
+    case FARGO_SUB_SOUNDSPEED:
+      if (c->P.adiabatic) {
+        KArgs<T> b = a;
+        launch_dt_prefix<T>(b, c->stream);  // resets the DT counters and computes cs
+      }
+      break;
+    case FARGO_SUB_POTENTIAL:
+      a.mode = 3;
+      mask = SUBK_CFL_FORCES;
+      break;
+    default: return set_err(c, FARGO_ERR_INVALID, "unknown substep");
+  }
+  if (!c->P.self_gravity) mask &= ~SUBK_SG;
+  if (mask) launch_substep_kernels<T>(a, c->stream, mask, c->az_smem);
+  if ((rc = check_launch(c, "substep"))) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return FARGO_OK;
+}
+
+template <class T>
+int substep_full_typed(fargo_ctx *c, double dt) {
+  KArgs<T> a = make_args<T>(c);
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  Ctl &k = *c->pin_ctl;
+  k.sloppy_dt = dt;
+  k.DT = dt;
+  k.dtemp = 0.0;
+  k.nsub_dt = 0;
+  k.done = 0;
+  if ((rc = write_ctl(c))) return rc;
+  a.mode = 2;
+  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+  if ((rc = check_launch(c, "substep_full"))) return rc;
+  if ((rc = read_ctl(c))) return rc;
+  c->pin_ctl->DT = c->P.dt;
+  if ((rc = write_ctl(c))) return rc;
+  return device_error(c);
+}
+
+template <class T>
+int cfl_typed(fargo_ctx *c, double deltaT, int *cfl) {
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  const double saved = c->pin_ctl->DT;
+  c->pin_ctl->DT = deltaT;
+  if ((rc = write_ctl(c))) return rc;
+  launch_cfl_only<T>(make_args<T>(c), c->stream);
+  if ((rc = check_launch(c, "cfl"))) return rc;
+  if ((rc = read_ctl(c))) return rc;
+  *cfl = c->pin_ctl->cfl;
+  c->pin_ctl->DT = saved;
+  c->pin_ctl->err = 0;
+  c->pin_ctl->done = 0;
+  return write_ctl(c);
+}
+
+void *field_ptr(fargo_ctx *c, int which) {
+  switch (which) {
+    case FARGO_FIELD_DENS: return c->dens;
+    case FARGO_FIELD_VRAD: return c->vrad;
+    case FARGO_FIELD_VTHETA: return c->vtheta;
+    case FARGO_FIELD_ENERGY: return c->energy;
+    case FARGO_FIELD_TEMPERATURE: return c->temperature;
+    case FARGO_FIELD_PRESSURE: return c->pressure;
+    case FARGO_FIELD_SOUNDSPEED: return c->cs;
+    case FARGO_FIELD_POTENTIAL: return c->potential;
+    case FARGO_FIELD_QPLUS: return c->qplus;
+    case FARGO_FIELD_DIVERGENCE: return c->divv;
+    case FARGO_FIELD_SG_ACCR: return c->sg_accr;
+    case FARGO_FIELD_SG_ACCT: return c->sg_acct;
+  }
+  return nullptr;
+}
+
+}  // namespace
+
+#define DISPATCH(c, fn, ...) ((c)->precision == FARGO_FP64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+extern "C" {
+
+int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb, int precision, void *stream,
+                     fargo_ctx **out) {
+  if (!p || !out || nb < 0 || nb > FARGO_MAXPL || (nb > 0 && !planets)) return FARGO_ERR_INVALID;
+  if (precision != FARGO_FP64 && precision != FARGO_FP32_BULK) return FARGO_ERR_INVALID;
+  if (p->nrad < 8 || p->nsec < 8 || !p->is_disk || !(p->dt > 0.0)) return FARGO_ERR_INVALID;
+  fargo_ctx *c = new fargo_ctx();
+  c->P = *p;
+  c->nb = nb;
+  c->precision = precision;
+  c->esize = precision == FARGO_FP64 ? 8 : 4;
+  c->dp = host_dev_params(*p, nb);
+  const char *ng = std::getenv("FARGO_NO_GRAPH");
+  if (ng && ng[0] == '1') c->use_graph = false;
+  int rc = FARGO_OK;
+  cudaError_t e;
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete c;
+      return FARGO_ERR_CUDA;
+    }
+    c->own_stream = true;
+  }
+  e = cudaMallocHost((void **)&c->pin_ctl, sizeof(Ctl));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_ctl, sizeof(Ctl));
+  if (e != cudaSuccess) {
+    fargo_ctx_destroy(c);
+    return FARGO_ERR_CUDA;
+  }
+  host_fill_mesh(*p, c->h);
+  host_init_density_energy(*p, c->h);
+  rc = DISPATCH(c, init_typed, c, planets);
+  if (rc != FARGO_OK) {
+    std::fprintf(stderr, "fargo_ctx_create: %s\n", c->err.c_str());
+    fargo_ctx_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return FARGO_OK;
+}
+
+void fargo_ctx_destroy(fargo_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->d_ctl) cudaFree(c->d_ctl);
+  if (c->pin_ctl) cudaFreeHost(c->pin_ctl);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *fargo_last_error(const fargo_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+int fargo_get_fields(fargo_ctx *c, double *dens, double *vrad, double *vtheta, double *energy, double *temperature) {
+  if (!c) return FARGO_ERR_STATE;
+  const size_t n = c->h.size_grid;
+  int rc;
+  if (dens && (rc = download(c, dens, c->dens, n))) return rc;
+  if (vrad && (rc = download(c, vrad, c->vrad, n))) return rc;
+  if (vtheta && (rc = download(c, vtheta, c->vtheta, n))) return rc;
+  if (energy && (rc = download(c, energy, c->energy, n))) return rc;
+  if (temperature && (rc = download(c, temperature, c->temperature, n))) return rc;
+  return FARGO_OK;
+}
+
+int fargo_set_fields(fargo_ctx *c, const double *dens, const double *vrad, const double *vtheta, const double *energy) {
+  if (!c) return FARGO_ERR_STATE;
+  const size_t n = c->h.size_grid;
+  int rc;
+  if (dens && (rc = upload(c, c->dens, dens, n))) return rc;
+  if (vrad && (rc = upload(c, c->vrad, vrad, n))) return rc;
+  if (vtheta && (rc = upload(c, c->vtheta, vtheta, n))) return rc;
+  if (energy && (rc = upload(c, c->energy, energy, n))) return rc;
+  return FARGO_OK;
+}
+
+int fargo_get_field(fargo_ctx *c, int which, double *host) {
+  if (!c || !host) return FARGO_ERR_STATE;
+  void *p = field_ptr(c, which);
+  if (which == FARGO_FIELD_SOUNDSPEED && !p) {
+    // isothermal: the ring sound speed broadcast over the sectors
+    const HostState &h = c->h;
+    for (size_t q = 0; q < h.size_grid; q++) host[q] = q < h.SoundSpeed.size() ? h.SoundSpeed[q] : 0.0;
+    return FARGO_OK;
+  }
+  if (!p) return set_err(c, FARGO_ERR_INVALID, "field not available in this configuration");
+  return download(c, host, p, c->h.size_grid);
+}
+
+int fargo_get_planets(fargo_ctx *c, fargo_planet *out, int cap, int *nb) {
+  if (!c || !nb) return FARGO_ERR_STATE;
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  const Ctl &k = *c->pin_ctl;
+  *nb = k.nb;
+  for (int i = 0; i < k.nb && i < cap; i++) {
+    out[i].x = k.x[i];
+    out[i].y = k.y[i];
+    out[i].vx = k.vx[i];
+    out[i].vy = k.vy[i];
+    out[i].mass = k.mass[i];
+    out[i].acc = k.acc[i];
+    out[i].feel_disk = k.feeldisk[i];
+    out[i].feel_others = k.feelothers[i];
+  }
+  return FARGO_OK;
+}
+
+int fargo_get_scalars(fargo_ctx *c, fargo_scalars *s) {
+  if (!c || !s) return FARGO_ERR_STATE;
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  const Ctl &k = *c->pin_ctl;
+  s->physical_time = k.PhysicalTime;
+  s->omega_frame = k.OmegaFrame;
+  s->lost_mass = k.LostMass;
+  s->last_dt = k.dt;
+  s->substeps = k.substeps;
+  s->last_cfl = k.cfl;
+  s->nb = k.nb;
+  return FARGO_OK;
+}
+
+int fargo_get_mesh(fargo_ctx *c, double *rinf, double *rmed, double *rsup, double *surf) {
+  if (!c) return FARGO_ERR_STATE;
+  const size_t n = (size_t)c->P.nrad + 1;
+  if (rinf) std::memcpy(rinf, c->h.Rinf.data(), n * 8);
+  if (rmed) std::memcpy(rmed, c->h.Rmed.data(), n * 8);
+  if (rsup) std::memcpy(rsup, c->h.Rsup.data(), n * 8);
+  if (surf) std::memcpy(surf, c->h.Surf.data(), n * 8);
+  return FARGO_OK;
+}
+
+int fargo_step_DT(fargo_ctx *c, int *nsub) {
+  if (!c) return FARGO_ERR_STATE;
+  int rc = DISPATCH(c, enqueue_dt, c);
+  if (rc) return rc;
+  if ((rc = read_ctl(c))) return rc;
+  if (nsub) *nsub = c->pin_ctl->nsub_dt;
+  return device_error(c);
+}
+
+int fargo_run_async(fargo_ctx *c, int ndt) {
+  if (!c || ndt < 0) return FARGO_ERR_STATE;
+  for (int k = 0; k < ndt; k++) {
+    int rc = DISPATCH(c, enqueue_dt, c);
+    if (rc) return rc;
+  }
+  return FARGO_OK;
+}
+
+int fargo_sync(fargo_ctx *c) {
+  if (!c) return FARGO_ERR_STATE;
+  CK(cudaStreamSynchronize(c->stream));
+  return FARGO_OK;
+}
+
+int fargo_run(fargo_ctx *c, int ndt, long long *nsub) {
+  if (!c) return FARGO_ERR_STATE;
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  const long long s0 = c->pin_ctl->substeps;
+  if ((rc = fargo_run_async(c, ndt))) return rc;
+  if ((rc = read_ctl(c))) return rc;
+  if (nsub) *nsub = c->pin_ctl->substeps - s0;
+  return device_error(c);
+}
+
+int fargo_substep_full(fargo_ctx *c, double dt) {
+  if (!c || !(dt > 0.0)) return FARGO_ERR_INVALID;
+  return DISPATCH(c, substep_full_typed, c, dt);
+}
+
+int fargo_substep(fargo_ctx *c, int which, double dt) {
+  if (!c) return FARGO_ERR_STATE;
+  return DISPATCH(c, substep_typed, c, which, dt);
+}
+
+int fargo_condition_cfl(fargo_ctx *c, double deltaT, int *cfl) {
+  if (!c || !cfl) return FARGO_ERR_STATE;
+  return DISPATCH(c, cfl_typed, c, deltaT, cfl);
+}
+
+int fargo_write_outputs(fargo_ctx *c, int index) {
+  if (!c) return FARGO_ERR_STATE;
+  const fargo_params &p = c->P;
+  const size_t n = c->h.size_grid, nout = (size_t)p.nrad * p.nsec;
+  std::vector<double> buf(n);
+  std::string dir = p.outputdir;
+  struct Item {
+    int on;
+    int field;
+    const char *name;
+  } items[] = {{p.write_density, FARGO_FIELD_DENS, "dens"},
+               {p.write_velocity, FARGO_FIELD_VRAD, "vrad"},
+               {p.write_velocity, FARGO_FIELD_VTHETA, "vtheta"},
+               {p.write_energy, FARGO_FIELD_ENERGY, "energy"},
+               {p.write_temperature, FARGO_FIELD_TEMPERATURE, "temperature"},
+               {p.write_divv, FARGO_FIELD_DIVERGENCE, "divergence"},
+               {p.write_qplus, FARGO_FIELD_QPLUS, "qplus"}};
+  int rc;
+  for (const Item &it : items) {
+    if (!it.on) continue;
+    if ((rc = fargo_get_field(c, it.field, buf.data()))) return rc;
+    if ((rc = host_write_field(dir, it.name, index, buf.data(), nout)))
+      return set_err(c, rc, std::string("cannot write ") + it.name);
+  }
+  fargo_planet pl[FARGO_MAXPL];
+  int nb = 0;
+  if ((rc = fargo_get_planets(c, pl, FARGO_MAXPL, &nb))) return rc;
+  fargo_scalars s;
+  if ((rc = fargo_get_scalars(c, &s))) return rc;
+  for (int k = 0; k < nb; k++)
+    if ((rc = host_write_planet_row(dir, k, index, pl[k], s.lost_mass, s.physical_time, s.omega_frame)))
+      return set_err(c, rc, "cannot write planet file");
+  return FARGO_OK;
+}
+
+int fargo_write_dims(fargo_ctx *c) {
+  if (!c) return FARGO_ERR_STATE;
+  int rc;
+  if ((rc = host_write_used_rad(c->P, c->h))) return set_err(c, rc, "cannot write used_rad.dat");
+  if ((rc = host_write_dims(c->P, c->nb))) return set_err(c, rc, "cannot write dims.dat");
+  return FARGO_OK;
+}
+
+}  // extern "C"

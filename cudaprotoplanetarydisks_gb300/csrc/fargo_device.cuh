@@ -1,0 +1,94 @@
+// fargo_device.cuh -- device-side argument block and helpers for the step kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fargo_internal.h"
+
+// Pointers of one disk as the kernels see them (passed by value).
+template <class T>
+struct DiskPtrs {
+  // state
+  T *dens, *vrad, *vtheta, *energy;
+  // derived / scratch fields, (nrad+1)*nsec each unless noted
+  T *cs;            // per-cell sound speed (energy equation) or nullptr
+  T *pressure, *temperature, *potential;
+  T *vradint, *vthetaint, *energyint;
+  T *qplus, *divv, *taurr, *taurp, *taupp;
+  T *densr, *energyr, *radmomp, *radmomm, *thetamomp, *thetamomm;
+  T *sg_accr, *sg_acct;
+  T *az_scratch;    // global fallback of the azimuthal kernel's ring buffers
+  // 1D tables
+  const T *rt;      // RingTab rows in T
+  const double *rt64;  // RingTab rows in FP64
+  T *nu;            // viscosity profile (may be refreshed on the device)
+  double *csmean;   // ring means of the sound speed (energy equation)
+  const double *cosF, *sinF;  // force angle table (FP64)
+  const T *cosP, *sinP;       // potential angle table
+  // per-ring partial results of the CFL/force kernel
+  double *ring_vmoy, *ring_newdt, *ring_force;
+  double *lostbydisk;
+  Ctl *ctl;
+};
+
+// Self-gravity FFT plan and buffers (fargo_sg.cu)
+struct SgDev {
+  double2 *spec_r, *spec_t;   // work spectra, [m][i], M x nrad
+  double2 *khat_r, *khat_t;   // kernel spectra, [m][k], M x 2 nrad
+  const double2 *tw1, *tw0;   // exp(-2 pi i t / N) for N = nsec and N = 2 nrad
+  const double *kr, *kt;      // real kernel tables, 2 nrad x nsec (set-up only)
+  int rad1[16], nst1, rad0[16], nst0;
+  int M;                      // nsec / 2 + 1
+};
+
+template <class T>
+struct KArgs {
+  DevParams P;
+  DiskPtrs<T> d;
+  double invdphi;      // 1.0/(2.0*M_PI/(double)nsec)
+  double lr01, lr12;   // log(Rmed[0]/Rmed[1]), log(Rmed[1]/Rmed[2]) for the Qplus extrapolation
+  int mode;            // CFL/force kernel mode
+  int az_smem;         // azimuthal kernel keeps its ring in shared memory
+  unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
+  int use_cond;                    // 1: k_end sets the while-loop condition
+  SgDev sg;
+};
+
+#define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
+#define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])
+
+__device__ __forceinline__ double block_sum_d(double v, double *sh) {
+  // sh: >= 32 doubles of shared memory; every thread gets the block sum
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (lane < nw) ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[0] = v;
+  }
+  __syncthreads();
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_min_d(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (lane < nw) ? sh[lane] : 1e300;
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[0] = v;
+  }
+  __syncthreads();
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}

@@ -1,0 +1,58 @@
+// fargo_internal.h -- host-side definitions shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fargo_gb300.h"
+#include "fargo_physics.h"
+
+// Per-ring table rows (device arrays of (nrad+1) values each, stored row after row).
+enum RingTab {
+  RT_RINF = 0, RT_RMED, RT_RSUP, RT_SURF, RT_INVRINF, RT_INVSURF, RT_INVRMED,
+  RT_INVDIFFRSUP, RT_INVDIFFRMED,
+  RT_DXTHETA,      // 2.0*PI/(double)nsec*Rmed[i]       (Substep1Kernel, kernel, StarTheta)
+  RT_INVDXTHETA,   // 1.0/RT_DXTHETA
+  RT_DXTHETA_CFL,  // Rmed[i]*2.0*PI/(double)nsec       (ConditionCFLKernel2D1)
+  RT_SUPPTORQUE,   // IMPOSEDDISKDRIFT*0.5*pow(Rmed,-2.5+SIGMASLOPE)
+  RT_CS,           // isothermal sound speed of the ring
+  RT_NU,           // viscosity_array
+  RT_DRAD,         // Rsup - Rinf
+  RT_SIGMAMED, RT_ENERGYMED, RT_COOLTIME, RT_QPLUSMED,
+  RT_SGSQRT,       // sqrt(Rmed/Rmed0)
+  RT_SGRATIO,      // Rmed/Rmed0
+  RT_CSMEAN,       // ring mean of SoundSpeed (GLOBAL_bufarray)
+  RT_SGNORMR,      // normaccr of ComputeSgAccKernel (src/Kernels.cu:902-905)
+  RT_SGNORMT,      // normacct
+  RT_COUNT
+};
+
+struct HostState {
+  int nrad = 0, nsec = 0;
+  size_t size_grid = 0;
+  std::vector<double> Radii, Rinf, Rmed, Rsup, Surf, invRinf, invSurf, invRmed, invdiffRsup, invdiffRmed;
+  std::vector<double> SigmaMed, SigmaInf, EnergyMed, CoolingTimeMed, QplusMed, nu, cs_mean;
+  std::vector<double> Dens, Vrad, Vtheta, Energy, SoundSpeed, Pressure, Temperature;
+  std::vector<double> cosF, sinF, cosP, sinP;   // force and potential angle tables
+  std::vector<double> Kr, Kt;                   // self-gravity kernels, 2*nrad x nsec
+  double OmegaFrame = 0.0;
+};
+
+// setup.cpp
+void host_fill_mesh(const fargo_params &p, HostState &h);
+void host_init_density_energy(const fargo_params &p, HostState &h);
+void host_init_planets(const fargo_params &p, const HostState &h, const fargo_planet *pl, int nb, Ctl &c);
+void host_sg_kernel(const fargo_params &p, HostState &h, DevParams &dp);
+void host_init_planets_sg(const fargo_params &p, const HostState &h, const std::vector<double> &axi_accr, Ctl &c);
+void host_init_euler(const fargo_params &p, HostState &h, const DevParams &dp, Ctl &c);
+void host_ring_table(const fargo_params &p, const HostState &h, const DevParams &dp, std::vector<double> &tab);
+DevParams host_dev_params(const fargo_params &p, int nb);
+long fargo_nearest_pow2(long n);
+
+// output.cpp
+int host_write_field(const std::string &outdir, const char *name, int index, const double *data, size_t n);
+int host_write_planet_row(const std::string &outdir, int k, int index, const fargo_planet &b, double lost_mass,
+                          double physical_time, double omega_frame);
+int host_write_dims(const fargo_params &p, int nb);
+int host_write_used_rad(const fargo_params &p, const HostState &h);

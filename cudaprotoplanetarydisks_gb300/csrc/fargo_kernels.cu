@@ -1,0 +1,1007 @@
+// fargo_kernels.cu -- the hydro substep of FARGO-ADSG as sm_103a kernels.
+//
+// One substep (the body of the AlgoGas while loop, src/SourceEuler.cu:223-302)
+// is this launch sequence on one stream, captured once in a CUDA graph:
+//   k_cfl_forces        ConditionCFL + ComputeAccel(star, FeelDisk planets) + the
+//                       planet part of FillForcesArrays; its last block decides
+//                       dt and advances the planetary system (RK5, rotation)
+//   [boundary kernels]  ApplyBoundaryCondition, when a boundary is open
+//   [self-gravity]      fargo_sg.cu (azimuthal FFT, radial convolution, inverse)
+//   k_source            ComputePressureField + Substep1Kernel + Update_sgvelocity
+//   k_visc_tau          ViscousTermsKernel
+//   k_visc_update       UpdateVelocitiesKernel + ApplySubKeplerianBoundaryKernel
+//   k_artvisc           Substep2Kernel + kernel + ActualiseGasVrad/Vtheta
+//   [k_visc_tau, k_energy]  Substep3 (energy equation)
+//   k_transport_radial  LRMomenta + OneWindRad (all conserved quantities at once)
+//   k_transport_azimuthal  OneWindTheta: ring mean, FARGO split, two van Leer
+//                       sweeps and the integer shift, one CTA per ring
+//   k_velocities        ComputeVelocities (+ ComputeTemperatureField)
+//   k_end               PhysicalTime, LostMass, while-loop condition
+// Every kernel is templated on the field type T: double (FARGO_FP64, parity
+// mode) or float (FARGO_FP32_BULK: FP64 kept for the CFL decision, the force
+// sums, the planets, the ring means and the FARGO split).
+#include <cuda_runtime.h>
+
+#include "fargo_device.cuh"
+#include "fargo_kernels.cuh"
+
+#define PI FARGO_PI
+#define CVNR FARGO_CVNR
+#define CFLSECURITY FARGO_CFLSECURITY
+
+namespace {
+
+__device__ __forceinline__ int jm1(int j, int n) { return j == 0 ? n - 1 : j - 1; }
+__device__ __forceinline__ int jp1(int j, int n) { return j == n - 1 ? 0 : j + 1; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// ConditionCFL (src/SourceEuler.cu:520-546, kernels src/Kernels.cu:1267-1359),
+// ComputeAccel / ComputeForce (src/SideEuler.cu:242-255, src/Force.cu:372-405,
+// ComputeForceKernel src/Kernels.cu:693-729) and the planet part of
+// FillForcesArraysKernel (src/Kernels.cu:1226-1253).  One CTA per ring.
+// mode 0: full substep start.  mode 1: CFL only (sloppy CFL at the DT start, or
+// the ConditionCFL entry point).  mode 2: forces only, dt = sloppy_dt.
+template <class T>
+__global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
+  const DevParams &P = a.P;
+  const int i = blockIdx.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
+  Ctl *c = a.d.ctl;
+  __shared__ double s_red[32];
+  __shared__ double s_body[FARGO_MAXPL + 1][3];
+  __shared__ double s_pot[FARGO_MAXPL][5];
+  __shared__ int s_nbody, s_last;
+  const bool do_cfl = (a.mode == 0 || a.mode == 1);
+  const bool do_forces = (a.mode != 1);
+  const bool do_planets = (a.mode == 0 || a.mode == 2);
+  if (tid == 0) {
+    const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
+    const double taper = fargo_mass_taper(P, t);
+    int nbody = 1;
+    s_body[0][0] = 0.0;
+    s_body[0][1] = 0.0;
+    s_body[0][2] = 0.0;
+    for (int k = 0; k < P.nb; k++) {
+      double x = c->x[k], y = c->y[k], m = c->mass[k];
+      if (c->feeldisk[k]) {  // AdvanceSystemFromDisk src/Pframeforce.cu:105-111
+        double r = sqrt(x * x + y * y);
+        double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing : fargo_smoothing(P, r, t, t0);
+        s_body[nbody][0] = x;
+        s_body[nbody][1] = y;
+        s_body[nbody][2] = sm * sm;
+        nbody++;
+      }
+      // FillForcesArrays src/Pframeforce.cu:68-77
+      double mp = m * taper;
+      double PD = sqrt(x * x + y * y);
+      double invd3 = 1.0 / PD / PD / PD;
+      double RRoche = PD * pow((1.0 / 3.0 * mp), 1.0 / 3.0);
+      double sm = P.roche_smoothing ? RRoche * P.rochesmoothing : fargo_smoothing(P, PD, t, t0);
+      s_pot[k][0] = x;
+      s_pot[k][1] = y;
+      s_pot[k][2] = mp;
+      s_pot[k][3] = sm * sm;
+      s_pot[k][4] = invd3;
+    }
+    s_nbody = nbody;
+  }
+  __syncthreads();
+  const T *dens = a.d.dens + (size_t)i * nsec;
+  const T *vth = a.d.vtheta + (size_t)i * nsec;
+  if (do_cfl) {
+    // ConditionCFLKernel1D: ring mean of Vtheta
+    double s = 0.0;
+    for (int j = tid; j < nsec; j += blockDim.x) s += (double)vth[j];
+    const double vmoy = block_sum_d(s, s_red) / (double)nsec;
+    if (tid == 0) a.d.ring_vmoy[i] = vmoy;
+    // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum (i >= 1)
+    double mn = 1e30;
+    if (i > 0) {
+      const T dxrad = RT(a, RT_DRAD, i);
+      const T dxtheta = RT(a, RT_DXTHETA_CFL, i);
+      const T mind = (dxtheta < dxrad) ? dxtheta : dxrad;
+      const T *vr = a.d.vrad + (size_t)i * nsec;
+      for (int j = tid; j < nsec; j += blockDim.x) {
+        T vres = P.fast_transport ? (T)((double)vth[j] - vmoy) : vth[j];
+        T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
+        T invdt1 = cs / mind;
+        T invdt2 = fabs(vr[j]) / dxrad;
+        T invdt3 = fabs(vres) / dxtheta;
+        T dvr = vr[j + nsec] - vr[j];
+        T dvt = vth[jp1(j, nsec)] - vth[j];
+        if (dvr >= (T)0.0) dvr = (T)1e-10;
+        else dvr = -dvr;
+        if (dvt >= (T)0.0) dvt = (T)1e-10;
+        else dvt = -dvt;
+        T a4 = dvr / dxrad, b4 = dvt / dxtheta;
+        T invdt4 = (b4 > a4) ? b4 : a4;
+        invdt4 *= (T)(4.0 * CVNR * CVNR);
+        T dt = (T)CFLSECURITY / sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4);
+        mn = fmin(mn, (double)dt);
+      }
+    }
+    mn = block_min_d(mn, s_red);
+    if (tid == 0) a.d.ring_newdt[i] = mn;
+  }
+  const int nbody = s_nbody;
+  if (do_forces) {
+    // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0)
+    const double surf = RT64(a, RT_SURF, i), rmed = RT64(a, RT_RMED, i);
+    for (int b = 0; b < nbody; b++) {
+      const double x = s_body[b][0], y = s_body[b][1], rs2 = s_body[b][2];
+      double fx = 0.0, fy = 0.0;
+      for (int j = tid; j < nsec; j += blockDim.x) {
+        double cellmass = surf * (double)dens[j];
+        double dx = __dmul_rn(rmed, a.d.cosF[j]) - x;
+        double dy = __dmul_rn(rmed, a.d.sinF[j]) - y;
+        double d2 = dx * dx + dy * dy;
+        double dist2 = d2 + rs2;
+        double distance = sqrt(dist2);
+        double InvDist3 = 1.0 / dist2 / distance;
+        fx += cellmass * dx * InvDist3;
+        fy += cellmass * dy * InvDist3;
+      }
+      fx = block_sum_d(fx, s_red);
+      fy = block_sum_d(fy, s_red);
+      if (tid == 0) {
+        a.d.ring_force[((size_t)i * (FARGO_MAXPL + 1) + b) * 2 + 0] = fx;
+        a.d.ring_force[((size_t)i * (FARGO_MAXPL + 1) + b) * 2 + 1] = fy;
+      }
+    }
+    // planet part of the potential (positions at the start of the substep)
+    if (P.nb > 0) {
+      const T rm = RT(a, RT_RMED, i);
+      T *pot = a.d.potential + (size_t)i * nsec;
+      for (int j = tid; j < nsec; j += blockDim.x) {
+        const T x = rm * a.d.cosP[j], y = rm * a.d.sinP[j];
+        T phi = (T)0.0;
+        for (int k = 0; k < P.nb; k++) {
+          const T xp = (T)s_pot[k][0], yp = (T)s_pot[k][1], mp = (T)s_pot[k][2];
+          T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
+          T distancesmooth = sqrt(distance + (T)s_pot[k][3]);
+          T pt = -mp / distancesmooth;
+          if (P.indirect_term) pt += mp * (T)s_pot[k][4] * (x * xp + y * yp);
+          phi += pt;
+        }
+        pot[j] = phi;
+      }
+    }
+  }
+  // last block: CFL decision, force totals, planets
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  __shared__ double s_acc[FARGO_MAXPL + 1][2];
+  __shared__ double s_newdt;
+  if (do_cfl) {
+    double mn = 1e30;
+    for (int k = 1 + tid; k < nrad; k += blockDim.x) mn = fmin(mn, __ldcg(a.d.ring_newdt + k));
+    for (int k = tid; k < nrad - 1; k += blockDim.x) {
+      double v0 = __ldcg(a.d.ring_vmoy + k), v1 = __ldcg(a.d.ring_vmoy + k + 1);
+      double d1 = 2.0 * PI * CFLSECURITY / (double)nsec /
+                  fabs(v0 * RT64(a, RT_INVRMED, k) - v1 * RT64(a, RT_INVRMED, k + 1));
+      mn = fmin(mn, d1);
+    }
+    mn = block_min_d(mn, s_red);
+    if (tid == 0) s_newdt = mn;
+  }
+  if (do_forces) {
+    if (tid < 2 * nbody) {
+      const int b = tid >> 1, comp = tid & 1;
+      double s = 0.0;
+      for (int k = 0; k < nrad; k++) s += __ldcg(a.d.ring_force + ((size_t)k * (FARGO_MAXPL + 1) + b) * 2 + comp);
+      s_acc[b][comp] = s;
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    c->ticket = 0u;
+    double dt;
+    if (do_cfl) {
+      const double DeltaT = (a.mode == 1) ? c->DT : c->DT - c->dtemp;
+      double newdt = s_newdt;
+      if (DeltaT < newdt) newdt = DeltaT;
+      double q = DeltaT / newdt;
+      int cfl;
+      if (!(q > 0.0) || !(q < 1.0e8)) {
+        c->err |= FARGO_DEVERR_CFL;
+        cfl = 1;
+        c->done = 1;
+      } else {
+        cfl = (int)ceil(q);
+      }
+      c->cfl = cfl;
+      dt = DeltaT / (double)cfl;
+      if (a.mode == 1) c->sloppy_dt = dt;
+    } else {
+      dt = c->sloppy_dt;
+    }
+    if (do_forces) {
+      // DiskOnPrimaryAcceleration, ComputeIndirectTerm (src/Pframeforce.cu:86-94)
+      c->ind_x = P.indirect_term ? -s_acc[0][0] : 0.0;
+      c->ind_y = P.indirect_term ? -s_acc[0][1] : 0.0;
+    }
+    if (do_planets) {
+      if (c->err) dt = 0.0;
+      c->dt = dt;
+      c->dtemp += dt;
+      c->nsub_dt += 1;
+      if (P.corotating) fargo_psys_info(*c, P, 1);
+      // AdvanceSystemFromDisk src/Pframeforce.cu:97-121
+      int b = 1;
+      for (int k = 0; k < P.nb; k++) {
+        if (c->feeldisk[k]) {
+          c->vx[k] += dt * s_acc[b][0];
+          c->vy[k] += dt * s_acc[b][1];
+          c->vx[k] += dt * c->ind_x;
+          c->vy[k] += dt * c->ind_y;
+          b++;
+        }
+      }
+      fargo_advance_rk5(*c, P, dt);
+      c->domega = 0.0;
+      if (P.corotating && dt > 0.0) {
+        double OmegaNew = fargo_psys_info(*c, P, 0) / dt;
+        c->domega = OmegaNew - c->OmegaFrame;
+        c->OmegaFrame = OmegaNew;
+      }
+      fargo_rotate_psys(*c, c->OmegaFrame * dt);
+    }
+    if (do_forces) {
+      // ApplySubKeplerianBoundary values (src/SideEuler.cu:296-320)
+      const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
+      const double r0 = RT64(a, RT_RMED, 0), r1 = RT64(a, RT_RMED, nrad - 1);
+      const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
+      double in = 1.0 * 1.0 / r0 * (1.0 - f * pow(fargo_aspect_ratio(P, r0, t, t0), 2.0) * pow(r0, 2.0 * P.flaringindex));
+      double out = 1.0 * 1.0 / r1 * (1.0 - f * pow(fargo_aspect_ratio(P, r1, t, t0), 2.0) * pow(r1, 2.0 * P.flaringindex));
+      if (P.self_gravity) {
+        in -= r0 * a.d.csmean[0];
+        out -= r1 * a.d.csmean[nrad - 1];
+      }
+      c->vkep_in = sqrt(in);
+      c->vkep_out = sqrt(out);
+    }
+  }
+  // FViscosity profile when it changes in time (alpha viscosity with an energy
+  // equation, or a moving cavity)
+  if (do_forces && P.nu_dynamic) {
+    __syncthreads();
+    const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
+    for (int k = tid; k < nrad; k += blockDim.x)
+      a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ComputeSoundSpeed (energy equation) + Make1Dprofile(1) ring means; one CTA per ring.
+template <class T>
+__global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
+  __shared__ double s_red[32];
+  const int i = blockIdx.x, nsec = a.P.nsec;
+  const double g = a.P.adiabaticindex;
+  double s = 0.0;
+  for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
+    size_t q = (size_t)i * nsec + j;
+    T cs = sqrt((T)(g * (g - 1.0)) * a.d.energy[q] / a.d.dens[q]);
+    a.d.cs[q] = cs;
+    s += (double)cs;
+  }
+  s = block_sum_d(s, s_red);
+  if (threadIdx.x == 0) a.d.csmean[i] = s / (double)nsec;
+}
+
+// CorrectVthetaKernel src/Kernels.cu:1256-1263 (corotating frame)
+template <class T>
+__global__ void k_correct_vtheta(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.P.nrad || j >= a.P.nsec) return;
+  const size_t q = (size_t)i * a.P.nsec + j;
+  a.d.vtheta[q] = a.d.vtheta[q] - (T)a.d.ctl->domega * RT(a, RT_RMED, i);
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions (ApplyBoundaryCondition src/SideEuler.cu:31-41)
+
+// OpenBoundaryKernel src/Kernels.cu:482-495
+template <class T>
+__global__ void k_bc_open(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, nsec = a.P.nsec;
+  if (j >= nsec) return;
+  T *D = a.d.dens, *E = a.d.energy, *V = a.d.vrad;
+  D[j] = D[nsec + j];
+  E[j] = E[nsec + j];
+  if (V[2 * nsec + j] > (T)0.0 || (D[nsec + j] < RT(a, RT_SIGMAMED, 0))) V[nsec + j] = (T)0.0;
+  else V[nsec + j] = V[2 * nsec + j];
+}
+
+// NonReflectingBoundary src/SideEuler.cu:45-76 with kernels src/Kernels.cu:498-607,
+// in one CTA.  NonReflectingBoundaryKernel2 runs nsec2pot threads without a
+// j < nsec guard; its extra threads write Vrad ring 2 (from ring 3) and ring
+// nrad (from ring nrad-1 after its update), as a launch whose threads run in
+// increasing j would.  The sound-speed ring nrad read there is zero.
+template <class T>
+__global__ void __launch_bounds__(1024) k_bc_nonreflecting(KArgs<T> a) {
+  __shared__ double s_red[32];
+  __shared__ int s_angle[2];
+  const int nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x;
+  T *D = a.d.dens, *E = a.d.energy, *V = a.d.vrad;
+  const T *CS = a.d.cs;
+  auto cs_at = [&](int i, int j) -> double {
+    return CS ? (double)CS[(size_t)i * nsec + j] : (i < nrad ? (double)RT(a, RT_CS, i) : 0.0);
+  };
+  double m[4];
+  const int rings[4] = {0, 1, nrad - 1, nrad - 2};
+  for (int r = 0; r < 4; r++) {
+    double s = 0.0;
+    for (int j = tid; j < nsec; j += blockDim.x) s += cs_at(rings[r], j);
+    m[r] = block_sum_d(s, s_red) / nsec;
+  }
+  if (tid == 0) {
+    const double *Rinf = a.d.rt64 + (size_t)RT_RINF * (nrad + 1);
+    const double *Rmed = a.d.rt64 + (size_t)RT_RMED * (nrad + 1);
+    double dangle = (pow(Rinf[1], -1.5) - 1.0) / (.5 * (m[0] + m[1]));
+    dangle *= (Rmed[1] - Rmed[0]);
+    s_angle[0] = (int)(dangle / 2.0 / PI * (double)nsec + .5);
+    double dangle2 = (pow(Rinf[nrad - 2], -1.5) - 1.0) / (.5 * (m[2] + m[3]));
+    dangle2 *= (Rmed[nrad - 1] - Rmed[nrad - 2]);
+    s_angle[1] = (int)(dangle2 / 2.0 / PI * (double)nsec + .5);
+  }
+  __syncthreads();
+  const int ia = s_angle[0], ia2 = s_angle[1];
+  // NonReflectingBoundaryKernel: ring 0 from ring 1 (shifted), ring nrad-1 from ring nrad-2
+  for (int j = tid; j < nsec; j += blockDim.x) {
+    // the reference wraps a shift once (|shift| < nsec in practice); a full
+    // modulo keeps every index inside the ring for any shift
+    int t = ((j + ia) % nsec + nsec) % nsec;
+    D[t] = D[nsec + j];
+    E[t] = E[nsec + j];
+    const long ii = nrad - 1;
+    const long src = (ii - 1) * nsec + (((j - ia2) % nsec + nsec) % nsec);
+    D[ii * nsec + j] = D[src];
+    E[ii * nsec + j] = E[src];
+  }
+  __syncthreads();
+  const double sm1 = RT64(a, RT_SIGMAMED, 1), sm2 = RT64(a, RT_SIGMAMED, nrad - 2);
+  // NonReflectingBoundaryKernel2, threads j < nsec
+  for (int j = tid; j < nsec; j += blockDim.x) {
+    double vm = -cs_at(1, j) * ((double)D[nsec + j] - sm1) / sm1;
+    V[nsec + j] = (T)(2.0 * vm - (double)V[2 * nsec + j]);
+    long ii = nrad - 1;
+    vm = cs_at(ii, j) * ((double)D[(ii - 1) * nsec + j] - sm2) / sm2;
+    V[ii * nsec + j] = (T)(2. * vm - (double)V[(ii - 1) * nsec + j]);
+  }
+  __syncthreads();
+  // ... threads j in [nsec, nsec2pot): flat index past the ring
+  for (int jj = tid; jj < a.P.nsec2pot - nsec; jj += blockDim.x) {
+    double vm = -cs_at(2, jj) * ((double)D[2 * nsec + jj] - sm1) / sm1;
+    V[2 * nsec + jj] = (T)(2.0 * vm - (double)V[3 * nsec + jj]);
+    long ii = nrad;
+    vm = cs_at((int)ii, jj) * ((double)D[(ii - 1) * nsec + jj] - sm2) / sm2;
+    V[ii * nsec + jj] = (T)(2. * vm - (double)V[(ii - 1) * nsec + jj]);
+  }
+  __syncthreads();
+  // ReduceMean + MinusMeanKernel
+  double md[4];
+  const T *src4[4] = {D, D + (size_t)(nrad - 1) * nsec, E, E + (size_t)(nrad - 1) * nsec};
+  for (int r = 0; r < 4; r++) {
+    double s = 0.0;
+    for (int j = tid; j < nsec; j += blockDim.x) s += (double)src4[r][j];
+    md[r] = block_sum_d(s, s_red) / nsec;
+  }
+  const double s0 = RT64(a, RT_SIGMAMED, 0), s1 = RT64(a, RT_SIGMAMED, nrad - 1);
+  const double e0 = RT64(a, RT_ENERGYMED, 0), e1 = RT64(a, RT_ENERGYMED, nrad - 1);
+  for (int j = tid; j < nsec; j += blockDim.x) {
+    D[j] += (T)(s0 - md[0]);
+    E[j] += (T)(e0 - md[2]);
+    D[(size_t)(nrad - 1) * nsec + j] += (T)(s1 - md[1]);
+    E[(size_t)(nrad - 1) * nsec + j] += (T)(e1 - md[3]);
+  }
+}
+
+// EvanescentBoundary src/SideEuler.cu:104-123; kernel src/Kernels.cu:967-1015.
+// Its SG term reads GLOBAL_bufarray_d, which the reference never fills (zero).
+template <class T>
+__global__ void k_bc_evanescent(KArgs<T> a) {
+  const DevParams &P = a.P;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = P.nrad, nsec = P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const double rm = RT64(a, RT_RMED, i), r0 = RT64(a, RT_RMED, 0), rl = RT64(a, RT_RMED, nrad - 1);
+  const double DRMIN = r0 * 1.25, DRMAX = rl * 0.84;
+  if (!((rm < DRMIN) || (rm > DRMAX))) return;
+  const Ctl *c = a.d.ctl;
+  const double step = c->dt, t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
+  const double Tin = 2.0 * PI * pow(r0, 3. / 2), Tout = 2.0 * PI * pow(rl, 3. / 2);
+  double damping, lambda = 0.0;
+  if (rm < DRMIN) {
+    damping = (rm - DRMIN) / (r0 - DRMIN);
+    lambda = damping * damping * 10.0 * step / Tin;
+  }
+  if (rm > DRMAX) {
+    damping = (rm - DRMAX) / (rl - DRMAX);
+    lambda = damping * damping * 10.0 * step / Tout;
+  }
+  const double AR = fargo_aspect_ratio(P, rm, t, t0);
+  double vtheta0 = sqrt(1.0 * 1.0 / rm *
+                        (1.0 - (1.0 + P.sigmaslope - 2.0 * P.flaringindex) * pow(AR, 2.0) * pow(rm, 2.0 * P.flaringindex)));
+  vtheta0 -= rm * c->OmegaFrame;
+  const double vrad0 = -3.0 * (double)a.d.nu[i] / rm * (-P.sigmaslope + .5);
+  const double dens0 = RT64(a, RT_SIGMAMED, i), energy0 = RT64(a, RT_ENERGYMED, i);
+  const size_t q = (size_t)i * nsec + j;
+  a.d.vrad[q] = (T)(((double)a.d.vrad[q] + lambda * vrad0) / (1.0 + lambda));
+  a.d.vtheta[q] = (T)(((double)a.d.vtheta[q] + lambda * vtheta0) / (1.0 + lambda));
+  a.d.dens[q] = (T)(((double)a.d.dens[q] + lambda * dens0) / (1.0 + lambda));
+  if (P.adiabatic) a.d.energy[q] = (T)(((double)a.d.energy[q] + lambda * energy0) / (1.0 + lambda));
+}
+
+// ---------------------------------------------------------------------------
+// ComputePressureField (src/Kernels.cu:187-200) + Substep1Kernel (src/Kernels.cu:13-53)
+// + Update_sgvelocityKernel (src/Kernels.cu:915-932) applied to VradInt/VthetaInt.
+// The potential is the planet part written by k_cfl_forces plus the star term
+// (direct + indirect) evaluated here; with no planet there is no star term, as in
+// the reference (it is added inside the planet loop, src/Kernels.cu:1246).
+template <class T>
+__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
+  const DevParams &P = a.P;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = P.nrad, nsec = P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const Ctl *c = a.d.ctl;
+  const T dt = (T)c->dt, Om = (T)c->OmegaFrame;
+  const T ix = (T)c->ind_x, iy = (T)c->ind_y;
+  const int jm = jm1(j, nsec), jp = jp1(j, nsec);
+  const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
+  const T *D = a.d.dens, *E = a.d.energy, *PHI = a.d.potential;
+  auto press = [&](size_t k, int ring) -> T {
+    if (P.adiabatic) return (T)(P.adiabaticindex - 1.0) * E[k];
+    const T cs = a.d.cs ? a.d.cs[k] : RT(a, RT_CS, ring);
+    return D[k] * cs * cs;
+  };
+  auto phi = [&](size_t k, int ring, int jj) -> T {
+    if (P.nb == 0) return (T)0.0;
+    const T rm = RT(a, RT_RMED, ring);
+    const T x = rm * a.d.cosP[jj], y = rm * a.d.sinP[jj];
+    T pot = -RT(a, RT_INVRMED, ring);
+    pot -= ix * x + iy * y;
+    return PHI[k] + pot;
+  };
+  const T p0 = press(q, i), pm = press(qm, i);
+  const T f0 = phi(q, i, j), fm = phi(qm, i, jm);
+  if (i > 0) {
+    const T p1 = press(q - nsec, i - 1);
+    const T f1 = phi(q - nsec, i - 1, j);
+    const T idr = RT(a, RT_INVDIFFRMED, i);
+    T gradp = (p0 - p1) * (T)2.0 / (D[q] + D[q - nsec]) * idr;
+    T gradphi = (f0 - f1) * idr;
+    const T *V = a.d.vtheta;
+    T vt2 = V[q] + V[(size_t)i * nsec + jp] + V[q - nsec] + V[(size_t)(i - 1) * nsec + jp];
+    vt2 = vt2 / (T)4.0 + Om * RT(a, RT_RINF, i);
+    vt2 = vt2 * vt2;
+    T vradint = -gradp - gradphi;
+    T vradint2 = vradint + vt2 * RT(a, RT_INVRINF, i);
+    T vr = a.d.vrad[q] + dt * vradint2;
+    if (P.self_gravity) {
+      const T *A = a.d.sg_accr;
+      vr += dt * ((RT(a, RT_RINF, i) - RT(a, RT_RMED, i - 1)) * A[q] + (RT(a, RT_RMED, i) - RT(a, RT_RINF, i)) * A[q - nsec]) *
+            idr;
+    }
+    a.d.vradint[q] = vr;
+  }
+  const T idx = RT(a, RT_INVDXTHETA, i);
+  T gradp = (p0 - pm) * (T)2.0 / (D[q] + D[qm]) * idx;
+  T gradphi = (f0 - fm) * idx;
+  T vt = a.d.vtheta[q] - dt * (gradp + gradphi);
+  vt += dt * RT(a, RT_SUPPTORQUE, i);
+  if (P.self_gravity) {
+    // (j-1)%nsec is -1 at j = 0: the flat index i*nsec-1 (previous ring's last
+    // cell); before the array at i = 0, taken as zero.
+    const T prev = (q > 0) ? a.d.sg_acct[q - 1] : (T)0.0;
+    vt += (T)0.5 * dt * (a.d.sg_acct[q] + prev);
+  }
+  a.d.vthetaint[q] = vt;
+  a.d.pressure[q] = p0;
+}
+
+// ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
+template <class T>
+__global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restrict__ vr, const T *__restrict__ vt) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const int jm = jm1(j, nsec), jp = jp1(j, nsec);
+  const size_t q = (size_t)i * nsec + j, qp = (size_t)i * nsec + jp, qm = (size_t)i * nsec + jm;
+  const T *D = a.d.dens;
+  const T invdphi = (T)a.invdphi, onethird = (T)(1.0 / 3.0);
+  const T irm = RT(a, RT_INVRMED, i), idrs = RT(a, RT_INVDIFFRSUP, i);
+  const T drr = (vr[q + nsec] - vr[q]) * idrs;
+  const T dpp = (vt[qp] - vt[q]) * invdphi * irm + (T)0.5 * (vr[q + nsec] + vr[q]) * irm;
+  T divv = (vr[q + nsec] * RT(a, RT_RSUP, i) - vr[q] * RT(a, RT_RINF, i)) * idrs * irm;
+  divv += (vt[qp] - vt[q]) * invdphi * irm;
+  const T nu = a.d.nu[i];
+  a.d.divv[q] = divv;
+  a.d.taurr[q] = (T)2.0 * D[q] * nu * (drr - onethird * divv);
+  a.d.taupp[q] = (T)2.0 * D[q] * nu * (dpp - onethird * divv);
+  if (i > 0) {
+    const T drp = (T)0.5 * (RT(a, RT_RINF, i) * (vt[q] * irm - vt[q - nsec] * RT(a, RT_INVRMED, i - 1)) * RT(a, RT_INVDIFFRMED, i) +
+                            (vr[q] - vr[qm]) * invdphi * RT(a, RT_INVRINF, i));
+    a.d.taurp[q] = (T)(2.0 * 0.25) * (D[q] + D[q - nsec] + D[qm] + D[qm - nsec]) * nu * drp;
+  }
+}
+
+// UpdateVelocitiesKernel src/Kernels.cu:118-150 + ApplySubKeplerianBoundaryKernel
+// src/Kernels.cu:1416-1430 (skipped with the evanescent boundary, src/SourceEuler.cu:338).
+template <class T>
+__global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const Ctl *c = a.d.ctl;
+  const T dt = (T)c->dt;
+  const int jm = jm1(j, nsec), jp = jp1(j, nsec);
+  const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm, qp = (size_t)i * nsec + jp;
+  const T *D = a.d.dens, *TRR = a.d.taurr, *TRP = a.d.taurp, *TPP = a.d.taupp;
+  const T invdphi = (T)a.invdphi;
+  if (i > 0 && i < nrad - 1) {
+    a.d.vthetaint[q] += dt * RT(a, RT_INVRMED, i) *
+                        ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) * RT(a, RT_INVDIFFRSUP, i) +
+                         (TPP[q] - TPP[qm]) * invdphi + (T)0.5 * (TRP[q] + TRP[q + nsec])) /
+                        ((T)0.5 * (D[q] + D[qm]));
+  }
+  if (i > 0) {
+    a.d.vradint[q] += dt * RT(a, RT_INVRINF, i) *
+                      ((RT(a, RT_RMED, i) * TRR[q] - RT(a, RT_RMED, i - 1) * TRR[q - nsec]) * RT(a, RT_INVDIFFRMED, i) +
+                       (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])) /
+                      ((T)0.5 * (D[q] + D[q - nsec]));
+  }
+  if (!a.P.evanescent && (i == 0 || i == nrad - 1)) {
+    const double vk = (i == 0) ? c->vkep_in : c->vkep_out;
+    a.d.vthetaint[q] = (T)(vk - RT64(a, RT_RMED, i) * c->OmegaFrame);
+  }
+}
+
+// Substep2Kernel (src/Kernels.cu:409-434) + kernel (src/Kernels.cu:438-479) +
+// ActualiseGasVrad/Vtheta: the artificial-viscosity pressures are evaluated where
+// they are needed and the new velocities are written to Vrad/Vtheta directly.
+template <class T>
+__global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const T dt = (T)a.d.ctl->dt;
+  const int jm = jm1(j, nsec), jp = jp1(j, nsec);
+  const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm, qp = (size_t)i * nsec + jp;
+  const T *D = a.d.dens, *VR = a.d.vradint, *VT = a.d.vthetaint;
+  const T c2 = (T)(CVNR * CVNR);
+  auto qr = [&](size_t k) -> T {
+    T dv = VR[k + nsec] - VR[k];
+    return (dv < (T)0.0) ? c2 * D[k] * dv * dv : (T)0.0;
+  };
+  auto qt = [&](size_t k, size_t kp) -> T {
+    T dv = VT[kp] - VT[k];
+    return (dv < (T)0.0) ? c2 * D[k] * dv * dv : (T)0.0;
+  };
+  const T qr0 = qr(q), qt0 = qt(q, qp);
+  T vrnew = (T)0.0;
+  if (i > 0) {
+    const T qr1 = qr(q - nsec);
+    const T dens = D[q] + D[q - nsec];
+    const T densint = qr0 - qr1;
+    vrnew = VR[q] - dt * (T)2.0 / dens * densint * RT(a, RT_INVDIFFRMED, i);
+  }
+  const T qtm = qt(qm, q);
+  const T dens2 = D[q] + D[qm];
+  const T tempint = qt0 - qtm;
+  const T idx = RT(a, RT_INVDXTHETA, i);
+  const T vtnew = VT[q] - dt * (T)2.0 / dens2 * tempint * idx;
+  if (a.P.adiabatic) {
+    a.d.energyint[q] = a.d.energy[q] - dt * qr0 * (VR[q + nsec] - VR[q]) * RT(a, RT_INVDIFFRSUP, i) -
+                       dt * qt0 * (VT[qp] - VT[q]) * idx;
+  }
+  a.d.vrad[q] = vrnew;
+  a.d.vtheta[q] = vtnew;
+  if (i == nrad - 1) {  // ghost ring of VradNew/VthetaNew is never written (zero)
+    a.d.vrad[q + nsec] = (T)0.0;
+    a.d.vtheta[q + nsec] = (T)0.0;
+  }
+}
+
+// Substep3Kernel + Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
+template <class T>
+__global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const double g = a.P.adiabaticindex;
+  const T dt = (T)a.d.ctl->dt;
+  const T *D = a.d.dens;
+  auto qplus = [&](int ii) -> T {
+    const size_t k = (size_t)ii * nsec + j;
+    const T nu = a.d.nu[ii];
+    if (nu != (T)0.0) {
+      T qp = (T)0.5 / nu / D[k] * (a.d.taurr[k] * a.d.taurr[k] + a.d.taurp[k] * a.d.taurp[k] + a.d.taupp[k] * a.d.taupp[k]);
+      qp += (T)(2.0 / 9.0) * nu * D[k] * a.d.divv[k] * a.d.divv[k];
+      return qp;
+    }
+    return (T)0.0;
+  };
+  T qp;
+  if (i > 0) {
+    qp = qplus(i);
+  } else if (a.d.nu[nrad - 1] != (T)0.0) {
+    const T q1 = qplus(1), q2 = qplus(2);
+    qp = q1 * exp(log(q1 / q2) * (T)a.lr01 / (T)a.lr12);
+  } else {
+    qp = (T)0.0;
+  }
+  const size_t q = (size_t)i * nsec + j;
+  a.d.qplus[q] = qp;
+  const T ei = a.d.energyint[q], dv = a.d.divv[q];
+  T enew;
+  if (!a.P.cooling) {
+    T num = dt * qp + ei;
+    T den = (T)1.0 + (T)(g - 1.0) * dt * dv;
+    enew = num / den;
+  } else {
+    const T em = RT(a, RT_ENERGYMED, i), sm = RT(a, RT_SIGMAMED, i), ct = RT(a, RT_COOLTIME, i), qm = RT(a, RT_QPLUSMED, i);
+    T num = em * dt * D[q] / sm + ct * ei + dt * ct * (qp - qm * D[q] / sm);
+    T den = dt + ct + (T)(g - 1.0) * dt * ct * dv;
+    enew = num / den;
+  }
+  a.d.energy[q] = enew;
+}
+
+// ---------------------------------------------------------------------------
+// Radial transport: LRMomentaKernel (src/Kernels.cu:774-787) + OneWindRad
+// (src/TransportEuler.cu:60-156: StarRadKernel/2, DivisePolarGridKernel,
+// VanLeerRadialKernel for every conserved quantity, density last).  Each thread
+// rebuilds the quantities of rings i-2..i+2 of its column and writes the new
+// values of all of them at (i, j) -- no intermediate field goes to memory.
+namespace {
+
+template <class T>
+struct RadCol {
+  T q[5];  // rings i-2 .. i+2 (index k - i + 2)
+};
+
+// upwind interface value at ring interface m (StarRadKernel/StarRadKernel2)
+template <class T>
+__device__ __forceinline__ T qstar_rad(const KArgs<T> &a, const T *q, int i, int m, T v, T dt) {
+  const int nrad = a.P.nrad;
+  if (m <= 0 || m >= nrad) return (T)0.0;
+  auto dq = [&](int k) -> T {
+    if (k == 0 || k == nrad - 1) return (T)0.0;
+    const T dqm = (q[k - i + 2] - q[k - 1 - i + 2]) * RT(a, RT_INVDIFFRMED, k);
+    const T dqp = (q[k + 1 - i + 2] - q[k - i + 2]) * RT(a, RT_INVDIFFRMED, k + 1);
+    return (dqp * dqm > (T)0.0) ? (T)2.0 * dqp * dqm / (dqp + dqm) : (T)0.0;
+  };
+  if (v > (T)0.0)
+    return q[m - 1 - i + 2] + (RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt) * (T)0.5 * dq(m - 1);
+  return q[m - i + 2] - (RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt) * (T)0.5 * dq(m);
+}
+
+}  // namespace
+
+template <class T>
+__global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
+  const DevParams &P = a.P;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = P.nrad, nsec = P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const T dt = (T)a.d.ctl->dt, Om = (T)a.d.ctl->OmegaFrame;
+  const int jp = jp1(j, nsec);
+  const T *D = a.d.dens, *VR = a.d.vrad, *VT = a.d.vtheta, *E = a.d.energy;
+  T d[5], rmp[5], rmm[5], tmp[5], tmm[5], e[5], inv[5];
+#pragma unroll
+  for (int o = 0; o < 5; o++) {
+    const int k = i - 2 + o;
+    if (k < 0 || k >= nrad) {
+      d[o] = rmp[o] = rmm[o] = tmp[o] = tmm[o] = e[o] = inv[o] = (T)0.0;
+      continue;
+    }
+    const size_t qk = (size_t)k * nsec + j;
+    const T rm = RT(a, RT_RMED, k);
+    d[o] = D[qk];
+    rmp[o] = d[o] * VR[qk + nsec];
+    rmm[o] = d[o] * VR[qk];
+    tmp[o] = d[o] * (VT[(size_t)k * nsec + jp] + rm * Om) * rm;
+    tmm[o] = d[o] * (VT[qk] + rm * Om) * rm;
+    e[o] = P.adiabatic ? E[qk] : (T)0.0;
+    inv[o] = (T)1.0 / (d[o] + (T)1e-20);
+  }
+  const size_t q = (size_t)i * nsec + j;
+  const T v0 = VR[q], v1 = VR[q + nsec];
+  const T ds0 = qstar_rad(a, d, i, i, v0, dt), ds1 = qstar_rad(a, d, i, i + 1, v1, dt);
+  const T dtheta = (T)(2.0 * PI / (double)nsec);
+  const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
+  T varq_d = (T)0.0;
+  auto update = [&](const T *qq, bool keep_varq) -> T {
+    T w[5];
+#pragma unroll
+    for (int o = 0; o < 5; o++) w[o] = qq[o] * inv[o];
+    const T s0 = qstar_rad(a, w, i, i, v0, dt), s1 = qstar_rad(a, w, i, i + 1, v1, dt);
+    T varq = dt * dtheta * rinf * s0 * ds0 * v0;
+    varq -= dt * dtheta * rsup * s1 * ds1 * v1;
+    if (keep_varq) varq_d = varq;
+    return qq[2] + varq * isurf;
+  };
+  a.d.radmomp[q] = update(rmp, false);
+  a.d.radmomm[q] = update(rmm, false);
+  a.d.thetamomp[q] = update(tmp, false);
+  a.d.thetamomm[q] = update(tmm, false);
+  if (P.adiabatic) a.d.energyr[q] = update(e, false);
+  a.d.densr[q] = update(d, true);
+  if (i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq_d;
+}
+
+// ---------------------------------------------------------------------------
+// Azimuthal transport, one CTA per ring: OneWindTheta src/TransportEuler.cu:177-269
+// with ComputeAverageThetaVelocities, ComputeResiduals, ComputeConstantResidual,
+// QuantitiesAdvection (StarTheta/StarTheta2, DivisePolarGrid, VanLeerTheta) twice
+// and AdvectSHIFT (src/Kernels.cu:1049-1190).  The ring lives in shared memory
+// (or in global scratch when it does not fit); the FARGO shift is applied as an
+// index rotation when the ring is stored.
+#define AZ_NARR 11
+template <class T>
+__global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char az_smem[];
+  __shared__ double s_red[32];
+  __shared__ double s_vc;
+  __shared__ int s_shift;
+  const DevParams &P = a.P;
+  const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x, nt = blockDim.x;
+  T *base = a.az_smem ? (T *)az_smem : a.d.az_scratch + (size_t)i * AZ_NARR * nsec;
+  T *V = base, *Dn = base + nsec, *En = base + 2 * nsec, *M0 = base + 3 * nsec, *M1 = base + 4 * nsec,
+    *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *S = base + 9 * nsec,
+    *DS = base + 10 * nsec;
+  const Ctl *c = a.d.ctl;
+  const double dt = c->dt;
+  const size_t row = (size_t)i * nsec;
+  // ComputeAverageThetaVelocitiesKernel (FP64 ring mean)
+  double s = 0.0;
+  for (int j = tid; j < nsec; j += nt) s += (double)a.d.vtheta[row + j];
+  const double vmed = block_sum_d(s, s_red) / (double)nsec;
+  if (tid == 0) {
+    // ComputeConstantResidualKernel (FP64 split; Nshift is an integer decision)
+    const double invdt = 1.0 / dt;
+    const double dpinvns = 2.0 * PI / (double)nsec;
+    const double Ntilde = vmed * RT64(a, RT_INVRMED, i) * dt * (double)nsec / 2.0 / PI;
+    const double Nround = floor(Ntilde + 0.5);
+    s_shift = (int)(long)Nround;
+    s_vc = (Ntilde - Nround) * RT64(a, RT_RMED, i) * invdt * dpinvns;
+  }
+  __syncthreads();
+  const double vc = s_vc;
+  const bool split = P.fast_transport;  // NoSplitAdvection == NO
+  for (int j = tid; j < nsec; j += nt) {
+    const double vt = (double)a.d.vtheta[row + j];
+    V[j] = split ? (T)(vt - vmed) : (T)((vt - vmed) + vc);  // VthetaRes
+    Dn[j] = a.d.densr[row + j];
+    if (P.adiabatic) En[j] = a.d.energyr[row + j];
+    M0[j] = a.d.radmomp[row + j];
+    M1[j] = a.d.radmomm[row + j];
+    M2[j] = a.d.thetamomp[row + j];
+    M3[j] = a.d.thetamomm[row + j];
+  }
+  __syncthreads();
+  const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
+  const T dxrad = RT(a, RT_DRAD, i) * (T)dt, isurf = RT(a, RT_INVSURF, i);
+  const T tdt = (T)dt;
+  // StarThetaKernel: harmonic slope of q into dq
+  auto slope = [&](const T *q, T *dq) {
+    for (int j = tid; j < nsec; j += nt) {
+      const T dqm = q[j] - q[jm1(j, nsec)];
+      const T dqp = q[jp1(j, nsec)] - q[j];
+      dq[j] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+    }
+  };
+  // StarThetaKernel2: upwind interface value
+  auto star = [&](const T *q, const T *dq, T *qs, const T *vel, T vconst) {
+    for (int j = tid; j < nsec; j += nt) {
+      const T v = vel ? vel[j] : vconst;
+      const T ksi = v * tdt;
+      const int jm = jm1(j, nsec);
+      qs[j] = (ksi > (T)0.0) ? q[jm] + (dxtheta - ksi) * dq[jm] : q[j] - (dxtheta + ksi) * dq[j];
+    }
+  };
+  // QuantitiesAdvection with velocity vel[] (or the constant vconst)
+  auto advect = [&](const T *vel, T vconst) {
+    slope(Dn, B);
+    __syncthreads();
+    star(Dn, B, DS, vel, vconst);
+    __syncthreads();
+    T *qs[6] = {M0, M1, M2, M3, En, Dn};
+    for (int f = 0; f < 6; f++) {
+      if (f == 4 && !P.adiabatic) continue;
+      T *Q = qs[f];
+      for (int j = tid; j < nsec; j += nt) W[j] = Q[j] / (Dn[j] + (T)1e-20);
+      __syncthreads();
+      slope(W, B);
+      __syncthreads();
+      star(W, B, S, vel, vconst);
+      __syncthreads();
+      for (int j = tid; j < nsec; j += nt) {
+        const int jp = jp1(j, nsec);
+        const T v0 = vel ? vel[j] : vconst, v1 = vel ? vel[jp] : vconst;
+        T varq = dxrad * S[j] * DS[j] * v0;
+        varq -= dxrad * S[jp] * DS[jp] * v1;
+        Q[j] += varq * isurf;
+      }
+      __syncthreads();
+    }
+  };
+  advect(V, (T)0.0);
+  if (split) advect(nullptr, (T)vc);
+  // AdvectSHIFT: out[j] = q[(j - Nshift) mod nsec]
+  int sh = s_shift % nsec;
+  if (sh < 0) sh += nsec;
+  for (int j = tid; j < nsec; j += nt) {
+    int ji = j - sh;
+    if (ji < 0) ji += nsec;
+    a.d.dens[row + j] = Dn[ji];
+    if (P.adiabatic) a.d.energy[row + j] = En[ji];
+    a.d.radmomp[row + j] = M0[ji];
+    a.d.radmomm[row + j] = M1[ji];
+    a.d.thetamomp[row + j] = M2[ji];
+    a.d.thetamomm[row + j] = M3[ji];
+  }
+}
+
+// ComputeVelocitiesKernel src/Kernels.cu:1193-1210 (+ ComputeTemperatureFieldKernel
+// src/Kernels.cu:203-213 when no boundary runs in between).
+template <class T>
+__global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_temperature) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const T Om = (T)a.d.ctl->OmegaFrame;
+  const int jm = jm1(j, nsec);
+  const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
+  const T *D = a.d.dens;
+  if (i == 0) a.d.vrad[q] = (T)0.0;
+  else a.d.vrad[q] = (a.d.radmomp[q - nsec] + a.d.radmomm[q]) / (D[q] + D[q - nsec] + (T)1e-20);
+  const T rm = RT(a, RT_RMED, i);
+  a.d.vtheta[q] = (a.d.thetamomp[qm] + a.d.thetamomm[q]) / (D[q] + D[qm] + (T)1e-15) / rm - rm * Om;
+  if (with_temperature) {
+    if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / D[q];
+    else a.d.temperature[q] = (T)(a.P.adiabaticindex - 1.0) * a.d.energy[q] / D[q];
+  }
+  if (!isfinite((double)D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
+}
+
+// ComputeTemperatureFieldKernel src/Kernels.cu:203-213 (after a boundary condition)
+template <class T>
+__global__ void k_temperature(KArgs<T> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.P.nrad || j >= a.P.nsec) return;
+  const size_t q = (size_t)i * a.P.nsec + j;
+  if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / a.d.dens[q];
+  else a.d.temperature[q] = (T)(a.P.adiabaticindex - 1.0) * a.d.energy[q] / a.d.dens[q];
+}
+
+// End of a substep: LostMass (src/TransportEuler.cu:77), PhysicalTime += dt
+// (src/SourceEuler.cu:302) and the while-loop condition of AlgoGas (line 222).
+template <class T>
+__global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
+  __shared__ double s_red[32];
+  Ctl *c = a.d.ctl;
+  if (a.P.open_inner) {
+    double s = 0.0;
+    for (int j = threadIdx.x; j < a.P.nsec; j += blockDim.x) s += a.d.lostbydisk[j];
+    s = block_sum_d(s, s_red);
+    if (threadIdx.x == 0) c->LostMass += s;
+  }
+  if (threadIdx.x == 0) {
+    c->PhysicalTime += c->dt;
+    c->substeps += 1;
+    int done = !(c->dtemp < 0.999999999 * c->DT);
+    if (c->err) done = 1;
+    if (c->nsub_dt >= FARGO_MAX_SUBSTEPS_PER_DT) {
+      c->err |= FARGO_DEVERR_CAP;
+      done = 1;
+    }
+    c->done = done;
+    if (a.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_handle, done ? 0u : 1u);
+  }
+}
+
+// Start of a DT (AlgoGas entry, src/SourceEuler.cu:202-221).
+__global__ void k_dt_begin(Ctl *c) {
+  c->dtemp = 0.0;
+  c->nsub_dt = 0;
+  c->done = 0;
+  c->ticket = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+template <class T>
+void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes) {
+  KArgs<T> a = a0;
+  const DevParams &P = a.P;
+  const dim3 b2(64, 4);
+  const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
+  if (which_mask & SUBK_CFL_FORCES) {
+    // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
+    // 3 forces + potential only (no planet advance, no time update)
+    k_cfl_forces<T><<<P.nrad, 256, 0, s>>>(a);
+  }
+  if ((which_mask & SUBK_COROT) && P.corotating) k_correct_vtheta<T><<<g2, b2, 0, s>>>(a);
+  if (which_mask & SUBK_BC1) launch_boundaries(a, s);
+  if ((which_mask & SUBK_SG) && P.self_gravity) launch_selfgravity(a, s);
+  if (which_mask & SUBK_SOURCE) {
+    k_source<T><<<g2, b2, 0, s>>>(a);
+    k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vradint, a.d.vthetaint);
+    k_visc_update<T><<<g2, b2, 0, s>>>(a);
+    k_artvisc<T><<<g2, b2, 0, s>>>(a);
+  }
+  if (which_mask & SUBK_BC2) launch_boundaries(a, s);
+  if ((which_mask & SUBK_ENERGY) && P.adiabatic) {
+    k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vrad, a.d.vtheta);
+    k_energy<T><<<g2, b2, 0, s>>>(a);
+  }
+  const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
+  if (which_mask & SUBK_TRANSPORT) {
+    k_transport_radial<T><<<g2, b2, 0, s>>>(a);
+    int nt = P.nsec >= 1024 ? 512 : 256;
+    a.az_smem = az_smem_bytes > 0;
+    k_transport_azimuthal<T><<<P.nrad, nt, az_smem_bytes, s>>>(a);
+    a.az_smem = 0;
+    k_velocities<T><<<g2, b2, 0, s>>>(a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
+  }
+  if (which_mask & SUBK_BC3) launch_boundaries(a, s);
+  if ((which_mask & SUBK_TEMPERATURE) && (bc || !(which_mask & SUBK_TRANSPORT))) k_temperature<T><<<g2, b2, 0, s>>>(a);
+  if (which_mask & SUBK_END) k_end<T><<<1, 256, 0, s>>>(a);
+}
+
+template <class T>
+void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
+  const DevParams &P = a.P;
+  if (P.open_inner) k_bc_open<T><<<(P.nsec + 255) / 256, 256, 0, s>>>(a);
+  if (P.non_reflecting) {
+    if (P.adiabatic) k_soundspeed<T><<<P.nrad, 256, 0, s>>>(a);
+    k_bc_nonreflecting<T><<<1, 1024, 0, s>>>(a);
+  }
+  if (P.evanescent) {
+    const dim3 b2(64, 4);
+    const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
+    k_bc_evanescent<T><<<g2, b2, 0, s>>>(a);
+  }
+}
+
+template <class T>
+void launch_dt_prefix(const KArgs<T> &a0, cudaStream_t s) {
+  KArgs<T> a = a0;
+  k_dt_begin<<<1, 1, 0, s>>>(a.d.ctl);
+  if (a.P.adiabatic) k_soundspeed<T><<<a.P.nrad, 256, 0, s>>>(a);
+  if (a.P.sloppy_cfl) {
+    a.mode = 1;
+    k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+  }
+}
+
+template <class T>
+void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
+  KArgs<T> a = a0;
+  a.mode = 1;
+  k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+}
+
+template <class T>
+cudaError_t prepare_kernels(size_t az_smem_bytes) {
+  if (az_smem_bytes > 0)
+    return cudaFuncSetAttribute(k_transport_azimuthal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
+  return cudaSuccess;
+}
+
+#define INSTANTIATE(T)                                                                                  \
+  template void launch_substep_kernels<T>(const KArgs<T> &, cudaStream_t, unsigned, size_t);          \
+  template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
+  template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
+  template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \
+  template cudaError_t prepare_kernels<T>(size_t);
+INSTANTIATE(double)
+INSTANTIATE(float)

@@ -1,0 +1,40 @@
+// fargo_kernels.cuh -- launch interface of the step kernels (fargo_kernels.cu, fargo_sg.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fargo_device.cuh"
+
+// parts of one substep, in launch order
+#define SUBK_CFL_FORCES  0x001u  // ConditionCFL + ComputeAccel + FillForcesArrays (planets) + planets
+#define SUBK_COROT       0x002u  // CorrectVtheta (corotating frame)
+#define SUBK_BC1         0x004u  // ApplyBoundaryCondition before the source step
+#define SUBK_SG          0x008u  // compute_selfgravity
+#define SUBK_SOURCE      0x010u  // pressure, Substep1, viscosity, Substep2, host, Actualise
+#define SUBK_BC2         0x020u  // ApplyBoundaryCondition after the source step
+#define SUBK_ENERGY      0x040u  // ComputeViscousTerms + Substep3 (energy equation)
+#define SUBK_TRANSPORT   0x080u  // Transport
+#define SUBK_BC3         0x100u  // ApplyBoundaryCondition after transport
+#define SUBK_TEMPERATURE 0x200u  // ComputeTemperatureField
+#define SUBK_END         0x400u  // PhysicalTime, LostMass, loop condition
+#define SUBK_ALL         0x7ffu
+
+template <class T>
+void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes);
+template <class T>
+void launch_dt_prefix(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+void launch_cfl_only(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+void launch_boundaries(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+cudaError_t prepare_kernels(size_t az_smem_bytes);
+
+// self-gravity (fargo_sg.cu)
+template <class T>
+void launch_selfgravity(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+void launch_sg_kernel_spectra(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+cudaError_t prepare_sg_kernels(int nsec, int n0);
+int sg_radices(int n, int *rad);  // radix-4/2/3 plan; returns stage count, -1 if n has other factors

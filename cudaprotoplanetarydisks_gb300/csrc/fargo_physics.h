@@ -1,0 +1,269 @@
+// fargo_physics.h -- shared host/device definitions of the step's small FP64 parts.
+//
+// DevParams: the parameter set as kernels see it (by value).
+// Ctl: the per-context control block that lives in device memory; it carries
+// the time state, the CFL decision, the planetary system and the per-substep
+// scalars from kernel to kernel, so a whole DT runs without the host.
+// The FARGO_HD functions restate the reference's scalar host code (planet
+// integration, frame rotation, profiles) and run on the host at set-up and on
+// one device thread inside the step.  All FP64 in every precision mode.
+#pragma once
+
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define FARGO_HD __host__ __device__ inline
+#else
+#define FARGO_HD inline
+#endif
+
+#define FARGO_MAXPL 16
+#define FARGO_PI 3.14159265358979323844  /* include/Fondam.cuh:4 */
+#define FARGO_CFLSECURITY 0.5            /* include/Fondam.cuh:7 */
+#define FARGO_CVNR 1.41                  /* include/Fondam.cuh:10 */
+#define FARGO_MAX_SUBSTEPS_PER_DT 100000
+
+// error bits set on the device
+#define FARGO_DEVERR_CFL 1        // non-finite or non-positive CFL time step
+#define FARGO_DEVERR_CAP 2        // too many substeps in one DT
+#define FARGO_DEVERR_NAN 4        // non-finite density found
+
+struct DevParams {
+  int nrad, nsec, nb, nsec2pot;
+  int adiabatic, cooling, self_gravity, fast_transport;
+  int open_inner, non_reflecting, evanescent, corotating, guiding_center;
+  int indirect_term, exclude_hill, viscosity_alpha, roche_smoothing, forced_circular;
+  int sloppy_cfl, is_disk;
+  int nu_dynamic;   // recompute the viscosity profile on the device each substep
+  double DT;
+  double aspectratio, flaringindex, sigmaslope, sigma0, imposeddiskdrift;
+  double adiabaticindex, coolingtime0;
+  double thicknesssmoothing, rochesmoothing, masstaper, releaseradius, releasedate;
+  double transitionradius, transitionratio, transitionwidth, lambdadoubling;
+  double viscosity, alphaviscosity, cavityradius, cavityratio, cavitywidth;
+  double sgp_eps, sgp_rstep, sgp_tstep;
+};
+
+struct Ctl {
+  // time state (reference globals PhysicalTime, OmegaFrame, LostMass; AlgoGas locals)
+  double DT, dtemp, dt;
+  double PhysicalTime, PhysicalTimeInitial, OmegaFrame, MassTaper, domega;
+  double LostMass;
+  double ind_x, ind_y;        // IndirectTerm (Pframeforce.cu:24)
+  double vkep_in, vkep_out;   // ApplySubKeplerianBoundary values of this substep
+  double sloppy_dt;
+  int cfl, done, err, nsub_dt;
+  long long substeps;
+  unsigned int ticket;        // last-block-done counter of the CFL/force kernel
+  unsigned int pad0;
+  // planetary system (Types.cuh:2-12)
+  int nb;
+  int pad1;
+  double x[FARGO_MAXPL], y[FARGO_MAXPL], vx[FARGO_MAXPL], vy[FARGO_MAXPL];
+  double mass[FARGO_MAXPL], acc[FARGO_MAXPL];
+  int feeldisk[FARGO_MAXPL], feelothers[FARGO_MAXPL];
+  // GetPsysInfo statics (Psys.cu:79)
+  double xmark, ymark;
+};
+
+// AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392
+FARGO_HD double fargo_aspect_ratio(const DevParams &P, double r, double t, double t0) {
+  double aspectratio, rmin, rmax, scale;
+  aspectratio = P.aspectratio;
+  rmin = P.transitionradius - P.transitionwidth * P.aspectratio;
+  rmax = P.transitionradius + P.transitionwidth * P.aspectratio;
+  scale = 1.0 + (t - t0) * P.lambdadoubling;
+  rmin *= scale;
+  rmax *= scale;
+  if (r < rmin) aspectratio *= P.transitionratio;
+  if ((r >= rmin) && (r <= rmax)) aspectratio *= exp((rmax - r) / (rmax - rmin) * log(P.transitionratio));
+  return aspectratio;
+}
+
+// FViscosity  src/Viscosity.cu:33-50; csmean is GLOBAL_bufarray[i] for r = Rmed[i]
+FARGO_HD double fargo_fviscosity(const DevParams &P, double r, double csmean, double t, double t0) {
+  double viscosity, rmin, rmax, scale;
+  viscosity = P.viscosity;
+  if (P.viscosity_alpha) viscosity = P.alphaviscosity * csmean * csmean * pow(r, 1.5);
+  rmin = P.cavityradius - P.cavitywidth * P.aspectratio;
+  rmax = P.cavityradius + P.cavitywidth * P.aspectratio;
+  scale = 1.0 + (t - t0) * P.lambdadoubling;
+  rmin *= scale;
+  rmax *= scale;
+  if (r < rmin) viscosity *= P.cavityratio;
+  if ((r >= rmin) && (r <= rmax)) viscosity *= exp((rmax - r) / (rmax - rmin) * log(P.cavityratio));
+  return viscosity;
+}
+
+// Compute_smoothing  src/Force.cu:137-142
+FARGO_HD double fargo_smoothing(const DevParams &P, double r, double t, double t0) {
+  return P.thicknesssmoothing * fargo_aspect_ratio(P, r, t, t0) * pow(r, 1.0 + P.flaringindex);
+}
+
+// MassTaper  src/SourceEuler.cu:223-224
+FARGO_HD double fargo_mass_taper(const DevParams &P, double t) {
+  double m = t / (P.masstaper * 2.0 * M_PI);
+  return (m > 1.0 ? 1.0 : pow(sin(m * M_PI / 2.0), 2.0));
+}
+
+// GetPsysInfo  src/Psys.cu:249-319 (action 0 = GET, 1 = MARK, 2 = FREQUENCY)
+FARGO_HD double fargo_psys_info(Ctl &c, const DevParams &P, int action) {
+  double d1, d2, cross, x, y, vx, vy, m, h, d, Ax, Ay, e, a, E, M, xc, yc, omega, arg, PerihelionPA;
+  xc = x = c.x[0];
+  yc = y = c.y[0];
+  vx = c.vx[0];
+  vy = c.vy[0];
+  m = c.mass[0] + 1.;
+  h = x * vy - y * vx;
+  d = sqrt(x * x + y * y);
+  Ax = x * vy * vy - y * vx * vy - 1.0 * m * x / d;
+  Ay = y * vx * vx - x * vx * vy - 1.0 * m * y / d;
+  e = sqrt(Ax * Ax + Ay * Ay) / m;
+  a = h * h / 1.0 / m / (1. - e * e);
+  if (e == 0.0) arg = 1.0;
+  else arg = (1.0 - d / a) / e;
+  if (fabs(arg) >= 1.0) E = FARGO_PI * (1. - arg / fabs(arg)) / 2.;
+  else E = acos((1.0 - d / a) / e);
+  if ((x * y * (vy * vy - vx * vx) + vx * vy * (x * x - y * y)) < 0) E = -E;
+  M = E - e * sin(E);
+  PerihelionPA = atan2(Ay, Ax);
+  omega = sqrt(m / a / a / a);
+  if (P.guiding_center) {
+    xc = a * cos(M + PerihelionPA);
+    yc = a * sin(M + PerihelionPA);
+  }
+  if (e < 1e-08) {
+    xc = x;
+    yc = y;
+  }
+  switch (action) {
+    case 1:
+      c.xmark = xc;
+      c.ymark = yc;
+      return 0.;
+    case 0:
+      x = xc;
+      y = yc;
+      d2 = sqrt(x * x + y * y);
+      d1 = sqrt(c.xmark * c.xmark + c.ymark * c.ymark);
+      cross = c.xmark * y - x * c.ymark;
+      c.xmark = x;
+      c.ymark = y;
+      return asin(cross / (d1 * d2));
+    case 2:
+      return omega;
+  }
+  return 0.0;
+}
+
+// RotatePsys  src/Psys.cu:323-340 (rotate by -angle)
+FARGO_HD void fargo_rotate_psys(Ctl &c, double angle) {
+  double sint = sin(angle), cost = cos(angle);
+  for (int i = 0; i < c.nb; i++) {
+    double xt = c.x[i], yt = c.y[i];
+    c.x[i] = xt * cost + yt * sint;
+    c.y[i] = -xt * sint + yt * cost;
+    xt = c.vx[i];
+    yt = c.vy[i];
+    c.vx[i] = xt * cost + yt * sint;
+    c.vy[i] = -xt * sint + yt * cost;
+  }
+}
+
+// DerivMotionRK5  src/RungeKutta.cu:30-67 (the feel-others term divides by the
+// distance of body j to the star, as the reference does)
+FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, int nb, double dt,
+                              const int *feelothers, int indirect) {
+  const double *x = q, *y = x + nb, *vx = y + nb, *vy = vx + nb;
+  double *dx = deriv, *dy = dx + nb, *dvx = dy + nb, *dvy = dvx + nb;
+  double Dist[FARGO_MAXPL];
+  for (int i = 0; i < nb; i++) Dist[i] = sqrt(x[i] * x[i] + y[i] * y[i]);
+  for (int i = 0; i < nb; i++) {
+    dx[i] = vx[i];
+    dy[i] = vy[i];
+    dvx[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * x[i];
+    dvy[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * y[i];
+    for (int j = 0; j < nb; j++) {
+      if (indirect) {
+        dvx[i] -= 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * x[j];
+        dvy[i] -= 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * y[j];
+      }
+      if ((j != i) && (feelothers[i] == 1)) {
+        dvx[i] += 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * (x[j] - x[i]);
+        dvy[i] += 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * (y[j] - y[i]);
+      }
+    }
+  }
+  for (int i = 0; i < 4 * nb; i++) deriv[i] *= dt;
+}
+
+// RungeKutta + AdvanceSystemRK5  src/RungeKutta.cu:8-28, src/Pframeforce.cu:124-187
+FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt) {
+  const int nb = c.nb;
+  double q0[4 * FARGO_MAXPL], q1[4 * FARGO_MAXPL], pm[FARGO_MAXPL];
+  for (int i = 0; i < 4 * FARGO_MAXPL; i++) q0[i] = q1[i] = 0.0;
+  if (!P.forced_circular && nb > 0) {
+    double k[6][4 * FARGO_MAXPL];
+    for (int s = 0; s < 6; s++)
+      for (int i = 0; i < 4 * nb; i++) k[s][i] = 0.0;
+    for (int i = 0; i < nb; i++) {
+      q0[i] = c.x[i];
+      q0[i + nb] = c.y[i];
+      q0[i + 2 * nb] = c.vx[i];
+      q0[i + 3 * nb] = c.vy[i];
+      pm[i] = c.mass[i];
+    }
+    const double cf[5][5] = {{0.2, 0.0, 0.0, 0.0, 0.0},
+                             {0.075, 0.225, 0.0, 0.0, 0.0},
+                             {0.3, -0.9, 1.2, 0.0, 0.0},
+                             {-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0, 0.0},
+                             {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
+    fargo_deriv_rk5(q0, pm, k[0], nb, dt, c.feelothers, P.indirect_term);
+    for (int s = 0; s < 5; s++) {
+      for (int i = 0; i < 4 * nb; i++)
+        q1[i] = q0[i] + cf[s][0] * k[0][i] + cf[s][1] * k[1][i] + cf[s][2] * k[2][i] + cf[s][3] * k[3][i] +
+                cf[s][4] * k[4][i];
+      fargo_deriv_rk5(q1, pm, k[s + 1], nb, dt, c.feelothers, P.indirect_term);
+    }
+    for (int i = 0; i < 4 * nb; i++)
+      q1[i] = q0[i] + 37.0 / 378.0 * k[0][i] + 250.0 / 621.0 * k[2][i] + 125.0 / 594.0 * k[3][i] +
+              512.0 / 1771.0 * k[5][i];
+  }
+  for (int i = 1 - (c.PhysicalTime >= P.releasedate); i < nb; i++) {
+    if (!P.forced_circular) {
+      c.x[i] = q1[i];
+      c.y[i] = q1[i + nb];
+      c.vx[i] = q1[i + 2 * nb];
+      c.vy[i] = q1[i + 3 * nb];
+    } else {
+      double x = c.x[i], y = c.y[i];
+      double theta = atan2(y, x);
+      double vx = c.vx[i], vy = c.vy[i];
+      double r = sqrt(x * x + y * y);
+      double omega = (-y * vx + x * vy) / r / r;
+      double dtheta = omega * dt;
+      c.x[i] = r * cos(theta + dtheta);
+      c.y[i] = r * sin(theta + dtheta);
+      c.vx[i] = vx * cos(dtheta + theta) - vy * sin(dtheta + theta);
+      c.vy[i] = vx * sin(dtheta + theta) + vy * cos(dtheta + theta);
+    }
+  }
+  if (c.PhysicalTime < P.releasedate && nb > 0) {
+    double x = c.x[0], y = c.y[0];
+    double r = sqrt(x * x + y * y);
+    double theta = atan2(y, x);
+    double rdot = (P.releaseradius - r) / (P.releasedate - c.PhysicalTime);
+    double omega = sqrt((1. + c.mass[0]) / r / r / r);
+    double new_r = r + rdot * dt;
+    double denom = r - new_r;
+    double dtheta;
+    if (denom != 0.0) dtheta = 2. * dt * r * omega / denom * (sqrt(r / new_r) - 1.);
+    else dtheta = omega * dt;
+    double vx = rdot;
+    double vy = new_r * sqrt((1. + c.mass[0]) / new_r / new_r / new_r);
+    c.x[0] = new_r * cos(dtheta + theta);
+    c.y[0] = new_r * sin(dtheta + theta);
+    c.vx[0] = vx * cos(dtheta + theta) - vy * sin(dtheta + theta);
+    c.vy[0] = vx * sin(dtheta + theta) + vx * cos(dtheta + theta);
+  }
+}

@@ -1,0 +1,218 @@
+/*
+ * fargo_gb300.h -- C-ABI of the GB300-native FARGO-ADSG 2D polar-grid hydro step.
+ *
+ * Every entry point is plain C: opaque context handle, plain pointers and sizes,
+ * an int status (FARGO_OK == 0), never exit().  The reference exposes the same
+ * operations as C++ host functions working on file-scope globals; each function
+ * below names the reference interface it replaces (file:line in
+ * MatiasFloresS/CudaProtoplanetaryDisks).
+ *
+ * Field layout (host and device): row-major [i*nsec + j], i = ring (radial, 0..nrad),
+ * j = sector (azimuth, fastest).  Every field buffer holds (nrad+1)*nsec doubles;
+ * ring nrad is the ghost ring of staggered radial quantities
+ * (reference src/Main.cu:203 size_grid = (NRAD+1)*NSEC).
+ */
+#ifndef FARGO_GB300_H
+#define FARGO_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define FARGO_OK            0
+#define FARGO_ERR_INVALID   1   /* bad argument or parameter set            */
+#define FARGO_ERR_CUDA      2   /* CUDA runtime error (message in last_error) */
+#define FARGO_ERR_IO        3   /* file could not be read or written        */
+#define FARGO_ERR_NUMERIC   4   /* NaN/Inf in the CFL, CFL overflow, substep cap */
+#define FARGO_ERR_STATE     5   /* call out of order (e.g. no context)      */
+
+/* ---- precision modes ---------------------------------------------------- */
+#define FARGO_FP64        0   /* every field and every operation in FP64 (parity mode) */
+#define FARGO_FP32_BULK   1   /* fields, transport, source, viscosity in FP32; FP64 kept
+                                 for planet RK5, force/indirect-term sums, azimuthal means,
+                                 the FARGO mean/residual split and the SG convolution */
+
+/* ---- per-substep entry points (fargo_substep 'which') ------------------- */
+#define FARGO_SUB_BOUNDARY      1  /* ApplyBoundaryCondition   src/SideEuler.cu:31-41       */
+#define FARGO_SUB_SOURCE        2  /* ComputePressureField + Substep1 + Substep2 + host +
+                                      ActualiseGasVrad/Vtheta  src/SourceEuler.cu:278-284   */
+#define FARGO_SUB_ENERGY        3  /* ComputeViscousTerms + Substep3 + ActualiseGasEnergy
+                                      src/SourceEuler.cu:287-291                             */
+#define FARGO_SUB_TRANSPORT     4  /* Transport                src/TransportEuler.cu:30-41  */
+#define FARGO_SUB_TEMPERATURE   5  /* ComputeTemperatureField  src/SourceEuler.cu:484-489   */
+#define FARGO_SUB_SOUNDSPEED    6  /* ComputeSoundSpeed        src/SourceEuler.cu:475-481   */
+#define FARGO_SUB_POTENTIAL     7  /* ComputeAccel(star) + FillForcesArrays
+                                      src/SourceEuler.cu:241-244                             */
+
+/* ---- named fields for fargo_get_field ----------------------------------- */
+#define FARGO_FIELD_DENS         0
+#define FARGO_FIELD_VRAD         1
+#define FARGO_FIELD_VTHETA       2
+#define FARGO_FIELD_ENERGY       3
+#define FARGO_FIELD_TEMPERATURE  4
+#define FARGO_FIELD_PRESSURE     5
+#define FARGO_FIELD_SOUNDSPEED   6
+#define FARGO_FIELD_POTENTIAL    7
+#define FARGO_FIELD_QPLUS        8
+#define FARGO_FIELD_DIVERGENCE   9
+#define FARGO_FIELD_SG_ACCR     10
+#define FARGO_FIELD_SG_ACCT     11
+
+/*
+ * Parameter set: one member per global of include/Param.cuh:51-104 and the derived
+ * flags of src/Interpret.cu:22-31 / src/Interpret.cu:130-206, plus the CLI switches of
+ * src/Main.cu:115-179 that change the physics (-c, -b, -f).  The last block holds
+ * extensions with no counterpart in the reference (seeded initial noise).
+ */
+typedef struct fargo_params {
+  /* mesh */
+  int    nrad, nsec;
+  double rmin, rmax;
+  int    log_grid;              /* RadialSpacing LOGARITHM */
+  /* time */
+  double dt;                    /* DT */
+  int    ntot, ninterm;
+  /* disk */
+  double sigma0, sigmaslope, aspectratio, flaringindex;
+  double viscosity, alphaviscosity;
+  double imposeddiskdrift, eccentricity;
+  double cavityradius, cavityratio, cavitywidth;
+  double transitionradius, transitionratio, transitionwidth;
+  double lambdadoubling;
+  double adiabaticindex, coolingtime0;
+  /* planets */
+  double thicknesssmoothing, rochesmoothing;
+  double masstaper;
+  double releaseradius, releasedate;
+  double omegaframe;
+  /* derived flags (src/Interpret.cu:22-31) */
+  int    fast_transport;        /* Transport != STANDARD            */
+  int    open_inner;            /* InnerBoundary OPEN               */
+  int    non_reflecting;        /* InnerBoundary NONREFLECTING      */
+  int    evanescent;            /* InnerBoundary EVANESCENT         */
+  int    is_disk;               /* Disk != NO                       */
+  int    corotating;            /* Frame COROTATING / GUIDING-CENTER*/
+  int    guiding_center;        /* Frame GUIDING-CENTER             */
+  int    indirect_term;         /* IndirectTerm != NO               */
+  int    exclude_hill;
+  int    self_gravity, sg_zero_mode;
+  int    adiabatic, cooling;
+  int    cic_planet, forced_circular;
+  int    viscosity_alpha;       /* AlphaViscosity != 0              */
+  int    roche_smoothing;       /* RocheSmoothing != 0              */
+  int    advect_label;
+  int    outer_source_mass;
+  int    write_density, write_velocity, write_energy;
+  int    write_temperature, write_divv, write_qplus;
+  /* CLI switches (src/Main.cu:115-179) */
+  int    sloppy_cfl;            /* -c */
+  int    centrifugal_balance;   /* -b */
+  double scaling_factor;        /* -f */
+  /* strings */
+  char   outputdir[512];
+  char   planetconfig[512];
+  /* extensions (no counterpart in the reference): seeded uniform noise on the
+     initial surface density / energy, Sigma *= 1 + amp*U[-1,1] (splitmix64) */
+  double sigma_noise;
+  double energy_noise;
+  unsigned long long noise_seed;
+} fargo_params;
+
+/* One body of the planetary system (include/Types.cuh:2-12). */
+typedef struct fargo_planet {
+  double x, y, vx, vy, mass, acc;
+  int    feel_disk, feel_others;
+} fargo_planet;
+
+/* Run-time scalars of the reference globals kept across steps. */
+typedef struct fargo_scalars {
+  double physical_time;         /* PhysicalTime  src/Viscosity.cu:21      */
+  double omega_frame;           /* OmegaFrame    src/Main.cu:59           */
+  double lost_mass;             /* LostMass      src/TransportEuler.cu:23 */
+  double last_dt;               /* dt of the last hydro substep           */
+  long long substeps;           /* hydro substeps done since creation     */
+  int    last_cfl;              /* CFL integer of the last substep        */
+  int    nb;                    /* number of planets                      */
+} fargo_scalars;
+
+typedef struct fargo_ctx fargo_ctx;
+
+/* ---- parameter interface ------------------------------------------------ */
+/* Defaults of include/Param.cuh:51-104 and src/Interpret.cu:22-31. */
+void fargo_params_default(fargo_params *p);
+/* ReadVariables  src/Interpret.cu:100-212 (key/value .par file, '#' comments,
+   case-folded keys).  Returns FARGO_ERR_IO when the file cannot be opened and
+   FARGO_ERR_INVALID for the parameter conflicts the reference stops on
+   (src/Interpret.cu:177-201). */
+int  fargo_params_read(const char *parfile, fargo_params *p);
+/* CLI switch string such as "-c" or "-bc" (src/Main.cu:115-151): sets sloppy_cfl /
+   centrifugal_balance; returns FARGO_ERR_INVALID on characters the reference rejects. */
+int  fargo_params_apply_switches(const char *sw, fargo_params *p);
+/* InitPlanetarySystem  src/Psys.cu:168-217 (.cfg table: Name Distance Mass
+   Accretion FeelsDisk FeelsOthers).  CICPlanet placement needs the mesh and is
+   applied by fargo_ctx_create.  Writes at most cap bodies, *nb = bodies found. */
+int  fargo_planets_read(const char *cfgfile, const fargo_params *p,
+                        fargo_planet *out, int cap, int *nb);
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* Allocation + the initialisation sequence of main(), src/Main.cu:233-305:
+   FillPolar1DArrays, InitGasDensity/InitGasEnergy (+ optional noise), the
+   self-gravity set-up, Initialization (InitEuler, InitGasVelocities).
+   stream: a cudaStream_t to launch on, or NULL for a context-owned stream. */
+int  fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
+                      int precision, void *stream, fargo_ctx **out);
+void fargo_ctx_destroy(fargo_ctx *ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char *fargo_last_error(const fargo_ctx *ctx);
+
+/* ---- state -------------------------------------------------------------- */
+/* DeviceToHostcudaMemcpy  src/Main.cu:605-616: copies (nrad+1)*nsec doubles per
+   non-NULL buffer; temperature is the Temperature field of the last substep. */
+int  fargo_get_fields(fargo_ctx *ctx, double *dens, double *vrad, double *vtheta,
+                      double *energy, double *temperature);
+/* Overwrites the state fields (host -> device); NULL leaves a field unchanged. */
+int  fargo_set_fields(fargo_ctx *ctx, const double *dens, const double *vrad,
+                      const double *vtheta, const double *energy);
+/* One named field (FARGO_FIELD_*), (nrad+1)*nsec doubles. */
+int  fargo_get_field(fargo_ctx *ctx, int which, double *host);
+int  fargo_get_planets(fargo_ctx *ctx, fargo_planet *out, int cap, int *nb);
+int  fargo_get_scalars(fargo_ctx *ctx, fargo_scalars *s);
+/* 1D mesh arrays (FillPolar1DArrays src/SourceEuler.cu:66-162): Rinf, Rmed, Rsup,
+   Surf, each nrad+1 doubles (any may be NULL). */
+int  fargo_get_mesh(fargo_ctx *ctx, double *rinf, double *rmed, double *rsup, double *surf);
+
+/* ---- stepping ----------------------------------------------------------- */
+/* AlgoGas  src/SourceEuler.cu:199-307 (include/SourceEuler.cuh:10-11): one DT,
+   CFL-subcycled.  *nsub (may be NULL) = hydro substeps taken.  Synchronous. */
+int  fargo_step_DT(fargo_ctx *ctx, int *nsub);
+/* ndt consecutive AlgoGas calls, launched back to back (no host sync inside);
+   the main loop of src/Main.cu:309-333 without its output branch. */
+int  fargo_run(fargo_ctx *ctx, int ndt, long long *nsub);
+/* Asynchronous variant: enqueues ndt DT-steps on the context stream and returns. */
+int  fargo_run_async(fargo_ctx *ctx, int ndt);
+int  fargo_sync(fargo_ctx *ctx);
+/* One hydro substep of length dt (the body of the AlgoGas while loop,
+   src/SourceEuler.cu:223-302) with the CFL evaluation skipped. */
+int  fargo_substep_full(fargo_ctx *ctx, double dt);
+/* Per-substep entry points for parity harnesses (FARGO_SUB_*):
+   ApplyBoundaryCondition (include/SideEuler.cuh:1), Substep1/2/host
+   (include/SourceEuler.cuh:12-20), Substep3, Transport (include/TransportEuler.cuh:1),
+   ComputeTemperatureField, ComputeSoundSpeed, ComputeAccel + FillForcesArrays
+   (include/SideEuler.cuh:10, include/Pframeforce.cuh:4). */
+int  fargo_substep(fargo_ctx *ctx, int which, double dt);
+/* ConditionCFL  src/SourceEuler.cu:520-546 (include/SourceEuler.cuh:20). */
+int  fargo_condition_cfl(fargo_ctx *ctx, double deltaT, int *cfl);
+
+/* ---- output (src/Output.cu) ---------------------------------------------- */
+/* SendOutput + WritePlanetSystemFile  src/Output.cu:133-181 / 76-131:
+   OUTPUTDIR/<name>/<name><index>.dat raw FP64 nrad*nsec, names dens, vrad,
+   vtheta, energy, temperature, divergence, qplus; planet<k>.dat rows. */
+int  fargo_write_outputs(fargo_ctx *ctx, int index);
+/* WriteDim (src/Output.cu:19-35) + EmptyPlanetSystemFile (37-58). */
+int  fargo_write_dims(fargo_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FARGO_GB300_H */
