@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""Benchmark of the FARGO-ADSG hydro step on GB300.
+
+Workload (default): the self-gravitating disk, 256 x 768 log grid on
+[0.4, 4.0], Sigma ~ 1/r with disk mass 0.02, alpha = 1e-3, self-gravity through a
+2*Nrad zero-padded log-r FFT convolution (softening 0.3 h), one migrating
+planet q = 5e-4 from r = 1.5 with the indirect term, 1e-3 seeded noise
+(cudaprotoplanetarydisks_gb300/configs/c2_selfgravity.par).  A step is one DT
+(AlgoGas: CFL-subcycled hydro substeps); the metric counts cell updates,
+Nrad * Nsec per hydro substep.
+
+Own arm: the state stays in HBM; each timed step is one graph launch of a DT
+(CFL loop on the device), timed with CUDA events on the launching stream, with an
+L2 flush (a 256 MiB write) before every timed step.  The headline is the
+FP32-bulk mode; the FP64 mode is measured in the same run, and the FP32 fields
+are compared with the FP64 oracle after the same steps.  e2e: the same metric
+through the C-ABI with host buffers (pinned FP64 arrays copied in and out every
+step).
+
+--impl reference: the reference has no CPU implementation of this path (every
+substep is a CUDA kernel); its CPU restatement (the oracle, OpenMP over rings)
+is timed on all host cores.
+
+--gpus N (torchrun, one rank per GPU): replicas only -- every rank advances its
+own disk; value = all ranks' cell updates / the slowest rank's time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(cfg):
+    import cudaprotoplanetarydisks_gb300 as fg
+    params, planets = fg.load_config(cfg)
+    name = {"c1": "isothermal disk 128x384, 1 planet (fixed orbit)",
+            "c2": "self-gravitating disk 256x768, alpha viscosity, migrating planet",
+            "c3": "adiabatic disk with cooling 1024x3072, 1 planet"}.get(cfg, cfg)
+    return params, planets, name
+
+
+def config_obj(params, name, cfg, extra=None):
+    c = {"workload": name, "config_file": f"configs/{cfg}", "nrad": params.nrad, "nsec": params.nsec,
+         "cells": params.nrad * params.nsec, "self_gravity": bool(params.self_gravity),
+         "adiabatic": bool(params.adiabatic), "DT": params.dt, "step": "one DT (AlgoGas, CFL-subcycled)",
+         "l2": "flushed (256 MiB write) before every timed step"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            f = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+            self.path = f.name
+            f.close()
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path).read().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per launch (compulsory reads + writes of each kernel)
+def kernel_bytes(name, params, esize):
+    G = params.nrad * params.nsec
+    ad = 1 if params.adiabatic else 0
+    sg = 1 if params.self_gravity else 0
+    M = params.nsec // 2 + 1
+    spec = 2 * M * params.nrad * 16          # both work spectra, complex FP64
+    khat = 2 * M * 2 * params.nrad * 16      # both kernel spectra
+    fields = {
+        "k_cfl_forces": (3 + ad) + (1 if True else 0),
+        "k_source": (4 + ad + 2 * sg) + 3,
+        "k_visc_tau": 3 + 4,
+        "k_visc_update": 6 + 2,
+        "k_artvisc": (3 + ad) + (2 + ad),
+        "k_energy": 8 + 2,
+        "k_transport_radial": (3 + ad) + (5 + ad),
+        "k_transport_azimuthal": (6 + ad) + (5 + ad),
+        "k_velocities": (5 + 1) + 3,
+        "k_temperature": 3,
+    }
+    if name in fields:
+        return fields[name] * G * esize
+    if name == "k_sg_rows_fwd":
+        return G * esize + spec
+    if name == "k_sg_cols":
+        return spec + khat + spec
+    if name == "k_sg_rows_inv":
+        return spec + G * esize + 2 * G * esize
+    return 0
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def time_device(disk, stream, steps, flush):
+    import torch
+    times = []
+    s0 = disk.scalars().substeps
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        disk.run_async(1)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    disk.sync()
+    nsub = disk.scalars().substeps - s0
+    return sum(times), nsub
+
+
+def time_e2e(disk, stream, steps, params):
+    """Through the C-ABI with host buffers: pinned FP64 host arrays are copied in,
+    one DT runs, the fields are copied out, every step."""
+    import ctypes
+
+    import numpy as np
+    import torch
+    shape = (params.nrad + 1, params.nsec)
+    names = ["dens", "vrad", "vtheta"] + (["energy"] if params.adiabatic else [])
+    host = {n: torch.from_numpy(disk.field(n)).pin_memory() for n in names}
+    ptr = {n: ctypes.cast(host[n].data_ptr(), ctypes.POINTER(ctypes.c_double)) for n in names}
+    lib, h = disk.lib, disk.h
+    nbytes = int(np.prod(shape)) * 8
+    disk.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    s0 = disk.scalars().substeps
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        rc = lib.fargo_set_fields(h, ptr["dens"], ptr["vrad"], ptr["vtheta"], ptr.get("energy"))
+        assert rc == 0
+        n = ctypes.c_int(0)
+        rc = lib.fargo_step_DT(h, ctypes.byref(n))
+        assert rc == 0, lib.fargo_last_error(h)
+        rc = lib.fargo_get_fields(h, ptr["dens"], ptr["vrad"], ptr["vtheta"], ptr.get("energy"), None)
+        assert rc == 0
+    e1.record(stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    nsub = disk.scalars().substeps - s0
+    return wall, nsub, len(names) * nbytes, len(names) * nbytes
+
+
+def oracle_sample(params, planets, ndt, threads):
+    from oracle.oracle import OracleDisk
+    OracleDisk.set_threads(threads)
+    o = OracleDisk(params, planets)
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(ndt):
+        n += o.step_DT()
+    dt = time.perf_counter() - t0
+    return o, n, dt
+
+
+def run_own(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import cudaprotoplanetarydisks_gb300 as fg
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    params, planets, wname = workload(args.config)
+    cells = params.nrad * params.nsec
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    results = {}
+    for prec, key in ((fg.FARGO_FP32_BULK, "fp32"), (fg.FARGO_FP64, "fp64")):
+        disk = fg.Disk(params, planets, prec, stream=stream.cuda_stream)
+        for _ in range(args.warmup):
+            disk.run(1)
+        sampler = ClockSampler(local) if key == "fp32" else None
+        barrier()
+        if sampler:
+            sampler.start()
+        ms, nsub = time_device(disk, stream, args.steps, flush)
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        t = torch.tensor([ms, float(nsub)], dtype=torch.float64, device="cuda")
+        if world > 1:
+            import torch.distributed as dist
+            tmax = t.clone()
+            dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
+            dist.all_reduce(t[1:2], op=dist.ReduceOp.SUM)
+            ms_max, nsub_all = float(tmax[0]), float(t[1])
+        else:
+            ms_max, nsub_all = ms, float(nsub)
+        r = {"ms_total": ms_max, "substeps": nsub_all, "value": nsub_all * cells / (ms_max * 1e-3),
+             "ms_per_step": ms_max / args.steps, "substeps_per_step": nsub / args.steps}
+        sc = disk.scalars()
+        r["launches"] = int(args.steps * sc.launches_per_dt + nsub * sc.launches_per_substep)
+        if key == "fp32":
+            r["clocks"] = clocks
+            wall, n_e2e, bi, bo = time_e2e(disk, stream, args.steps, params)
+            r["e2e"] = {"value": n_e2e * cells * world / wall, "unit": METRIC,
+                        "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "ms_per_step": wall * 1e3 / args.steps}
+        # per-kernel device time (launch by launch, after the timed region)
+        ms_k = (ctypes.c_double * 96)()
+        nk = ctypes.c_int(0)
+        rc = disk.lib.fargo_time_substep_kernels(disk.h, 5, ms_k, 96, ctypes.byref(nk))
+        kern = []
+        if rc == 0:
+            for k in range(nk.value):
+                nm = disk.lib.fargo_substep_kernel_name(disk.h, k).decode()
+                kern.append((nm, ms_k[k]))
+        r["kernels"] = kern
+        disk.close()
+        results[key] = r
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    hbm_peak, peak_kind = measured_peaks()
+    f32 = results["fp32"]
+    # dominant kernel of the headline mode, with its algorithmic bytes
+    agg = {}
+    for nm, t in f32["kernels"]:
+        a = agg.setdefault(nm, [0.0, 0])
+        a[0] += t
+        a[1] += 1
+    dom = max(agg.items(), key=lambda kv: kv[1][0]) if agg else ("none", [1.0, 1])
+    dom_name, (dom_ms, dom_n) = dom
+    dom_avg_ms = dom_ms / dom_n
+    alg = kernel_bytes(dom_name, params, 4)
+    achieved = alg / (dom_avg_ms * 1e-3) / 1e9
+    step_alg = 24 + (128 if params.self_gravity else 0) + (8 if params.adiabatic else 0)
+    line = {
+        "metric": METRIC, "value": f32["value"], "unit": "cell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields; f64 CFL decision, force sums, planets, ring means, FARGO split, SG FFT",
+        "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
+        "config": config_obj(params, wname, args.config,
+                             {"precision": "FP32_BULK", "parallelism": f"replicas x{world}",
+                              "substeps_per_step": f32["substeps_per_step"]}),
+        "e2e": f32["e2e"],
+        "gpu_launches": f32["launches"],
+        "clocks": f32["clocks"],
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "alg_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms, "traffic": None},
+        "step_roofline": {"alg_bytes_per_cell_update": step_alg,
+                          "achieved_GBs": f32["value"] * step_alg / 1e9,
+                          "frac": f32["value"] * step_alg / 1e9 / hbm_peak},
+        "kernels_ms": {nm: round(t / n, 5) for nm, (t, n) in agg.items()},
+        "fp64": {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms_per_step"],
+                 "gpu_launches": results["fp64"]["launches"],
+                 "kernels_ms": {nm: round(t, 5) for nm, t in results["fp64"]["kernels"]}},
+    }
+    # CPU baseline (oracle, all host cores) on a bounded sample, and the FP32 error
+    # against the FP64 oracle after the same DTs
+    if not args.no_cpu_baseline:
+        import numpy as np
+        ndt = 2
+        cores = os.cpu_count() or 1
+        o, n_cpu, t_cpu = oracle_sample(params, planets, ndt, cores)
+        line["cpu_baseline"] = {"value": n_cpu * cells / t_cpu, "unit": METRIC, "cores": cores, "kind": "port",
+                                "sample": f"{ndt} DTs ({n_cpu} substeps) of the same disk from its initial state"}
+        disk = fg.Disk(params, planets, fg.FARGO_FP32_BULK, stream=stream.cuda_stream)
+        for _ in range(ndt):
+            disk.step_DT()
+        err = {}
+        for nm in ("dens", "vrad", "vtheta"):
+            a, b = disk.field(nm)[:-1], o.field(nm)[:-1]
+            err[nm] = {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                       "rel_linf": float(np.abs(a - b).max() / np.abs(b).max())}
+        line["fp32_error_vs_fp64_oracle"] = {"after": f"{ndt} DTs", "fields": err}
+        disk.close()
+        o.close()
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    params, planets, wname = workload(args.config)
+    cells = params.nrad * params.nsec
+    cores = os.cpu_count() or 1
+    from oracle.oracle import OracleDisk
+    OracleDisk.set_threads(cores)
+    o = OracleDisk(params, planets)
+    for _ in range(args.warmup):
+        o.step_DT()
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(args.steps):
+        n += o.step_DT()
+    dt = time.perf_counter() - t0
+    value = n * cells / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "impl": "reference", "dtype": "f64",
+        "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
+        "config": config_obj(params, wname, args.config, {"precision": "FP64", "parallelism": "host cores"}),
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} DTs ({n} substeps) after {args.warmup} warm-up DTs"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference runs every substep as a CUDA kernel and has no CPU path; "
+                "this arm times its CPU restatement (the oracle) with OpenMP over rings",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_own(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -72,7 +72,8 @@ class FargoPlanet(ctypes.Structure):
 
 class FargoScalars(ctypes.Structure):
     _fields_ = [("physical_time", _D), ("omega_frame", _D), ("lost_mass", _D),
-                ("last_dt", _D), ("substeps", ctypes.c_longlong), ("last_cfl", _I), ("nb", _I)]
+                ("last_dt", _D), ("substeps", ctypes.c_longlong), ("last_cfl", _I), ("nb", _I),
+                ("launches_per_substep", _I), ("launches_per_dt", _I)]
 
 
 _DP = ctypes.POINTER(_D)
@@ -104,6 +105,8 @@ SIGNATURES = [
     ("fargo_condition_cfl", _I, [_P, _D, ctypes.POINTER(_I)]),
     ("fargo_write_outputs", _I, [_P, _I]),
     ("fargo_write_dims", _I, [_P]),
+    ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
+    ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
 ]
 
 _lib = None

@@ -40,6 +40,7 @@ struct fargo_ctx {
   void *densr = nullptr, *energyr = nullptr, *radmomp = nullptr, *radmomm = nullptr;
   void *thetamomp = nullptr, *thetamomm = nullptr, *sg_accr = nullptr, *sg_acct = nullptr;
   void *az_scratch = nullptr, *rt = nullptr, *nu = nullptr, *cosP = nullptr, *sinP = nullptr;
+  void *cosFt = nullptr, *sinFt = nullptr;
   double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
   double *ring_vmoy = nullptr, *ring_newdt = nullptr, *ring_force = nullptr, *lostbydisk = nullptr;
   // self-gravity
@@ -47,6 +48,9 @@ struct fargo_ctx {
   double *kr = nullptr, *kt = nullptr;
   int rad1[16], nst1 = 0, rad0[16], nst0 = 0;
   size_t az_smem = 0;
+  double *staging = nullptr;   // FP64 staging buffer of host <-> device transfers
+  int launches_per_substep = 0, launches_per_dt = 0;
+  std::vector<std::string> kernel_names;
   // graph of one DT
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -106,6 +110,8 @@ KArgs<T> make_args(const fargo_ctx *c) {
   d.cosF = c->cosF;
   d.sinF = c->sinF;
   d.cosP = (const T *)c->cosP;
+  d.cosFt = (const T *)c->cosFt;
+  d.sinFt = (const T *)c->sinFt;
   d.sinP = (const T *)c->sinP;
   d.ring_vmoy = c->ring_vmoy;
   d.ring_newdt = c->ring_newdt;
@@ -149,29 +155,36 @@ int dev_alloc(fargo_ctx *c, void **p, size_t bytes) {
   return FARGO_OK;
 }
 
-// host double -> device T
+// host FP64 -> device T (FP32 fields are converted on the device from an FP64
+// staging buffer, so the host side always moves FP64 arrays)
 int upload(fargo_ctx *c, void *dst, const double *src, size_t n) {
-  if (c->esize == 8) {
-    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+  if (c->esize == 8 || !c->staging || n > c->h.size_grid) {
+    if (c->esize == 8) {
+      CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+    } else {
+      std::vector<float> tmp(n);
+      for (size_t k = 0; k < n; k++) tmp[k] = (float)src[k];
+      CK(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
   } else {
-    std::vector<float> tmp(n);
-    for (size_t k = 0; k < n; k++) tmp[k] = (float)src[k];
-    CK(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpyAsync(c->staging, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+    launch_convert_from_f64(c->staging, dst, n, (int)c->esize, c->stream);
+    CK(cudaGetLastError());
   }
+  CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 
 int download(fargo_ctx *c, double *dst, const void *src, size_t n) {
-  CK(cudaStreamSynchronize(c->stream));
   if (c->esize == 8) {
-    CK(cudaMemcpy(dst, src, n * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToHost, c->stream));
   } else {
-    std::vector<float> tmp(n);
-    CK(cudaMemcpy(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < n; k++) dst[k] = (double)tmp[k];
+    launch_convert_to_f64(src, c->staging, n, (int)c->esize, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, c->staging, n * 8, cudaMemcpyDeviceToHost, c->stream));
   }
+  CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 
@@ -208,9 +221,14 @@ int build_graph(fargo_ctx *c) {
   KArgs<T> a = make_args<T>(c);
   cudaGraph_t g = nullptr, gp = nullptr;
   CK(cudaGraphCreate(&g, 0));
+  LaunchProbe probe;
+  std::memset(&probe, 0, sizeof(probe));
+  g_probe = &probe;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   launch_dt_prefix<T>(a, c->stream);
+  g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &gp));
+  c->launches_per_dt = probe.count;
   cudaGraphNode_t np, nc;
   CK(cudaGraphAddChildGraphNode(&np, g, nullptr, 0, gp));
   CK(cudaGraphDestroy(gp));
@@ -225,8 +243,12 @@ int build_graph(fargo_ctx *c) {
   a.cond_handle = (unsigned long long)h;
   a.use_cond = 1;
   CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  probe.count = 0;
+  g_probe = &probe;
   launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+  g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &body));
+  c->launches_per_substep = probe.count;
   CK(cudaGraphInstantiate(&c->exec, g, 0));
   c->graph = g;
   c->cond_handle = a.cond_handle;
@@ -284,17 +306,22 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   if ((rc = dev_alloc(c, (void **)&c->sinF, (size_t)p.nsec * 8))) return rc;
   if ((rc = dev_alloc(c, &c->cosP, (size_t)p.nsec * E))) return rc;
   if ((rc = dev_alloc(c, &c->sinP, (size_t)p.nsec * E))) return rc;
+  if ((rc = dev_alloc(c, &c->cosFt, (size_t)p.nsec * E))) return rc;
+  if ((rc = dev_alloc(c, &c->sinFt, (size_t)p.nsec * E))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->ring_vmoy, n1 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->ring_newdt, n1 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->ring_force, n1 * (FARGO_MAXPL + 1) * 2 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->lostbydisk, (size_t)p.nsec * 8))) return rc;
+  if (c->esize == 4 && (rc = dev_alloc(c, (void **)&c->staging, sg * 8))) return rc;
   // azimuthal transport ring buffers: shared memory when they fit
   {
     int dev = 0, maxsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     size_t need = (size_t)11 * p.nsec * E;
-    if (need + 1024 <= (size_t)maxsm) {
+    const char *fg = std::getenv("FARGO_AZ_GLOBAL");  // force the global-memory ring buffers
+    const bool force_global = fg && fg[0] == '1';
+    if (!force_global && need + 1024 <= (size_t)maxsm) {
       c->az_smem = need;
       CK(prepare_kernels<T>(need));
     } else {
@@ -369,6 +396,8 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   CK(cudaMemcpy(c->sinF, h.sinF.data(), (size_t)p.nsec * 8, cudaMemcpyHostToDevice));
   if ((rc = upload(c, c->cosP, h.cosP.data(), p.nsec))) return rc;
   if ((rc = upload(c, c->sinP, h.sinP.data(), p.nsec))) return rc;
+  if ((rc = upload(c, c->cosFt, h.cosF.data(), p.nsec))) return rc;
+  if ((rc = upload(c, c->sinFt, h.sinF.data(), p.nsec))) return rc;
   if ((rc = upload(c, c->vrad, h.Vrad.data(), sg))) return rc;
   if ((rc = upload(c, c->vtheta, h.Vtheta.data(), sg))) return rc;
   if ((rc = upload(c, c->energy, h.Energy.data(), sg))) return rc;
@@ -467,6 +496,48 @@ int cfl_typed(fargo_ctx *c, double deltaT, int *cfl) {
   c->pin_ctl->err = 0;
   c->pin_ctl->done = 0;
   return write_ctl(c);
+}
+
+// Per-kernel device time of reps substeps, launched one by one with events.
+template <class T>
+int time_kernels_typed(fargo_ctx *c, int reps, std::vector<double> &ms) {
+  KArgs<T> a = make_args<T>(c);
+  LaunchProbe probe;
+  std::memset(&probe, 0, sizeof(probe));
+  probe.nev = 96;
+  for (int k = 0; k < probe.nev; k++) CK(cudaEventCreate(&probe.ev[k]));
+  cudaEvent_t start;
+  CK(cudaEventCreate(&start));
+  int rc = FARGO_OK;
+  for (int r = 0; r < reps && rc == FARGO_OK; r++) {
+    launch_dt_prefix<T>(a, c->stream);  // a fresh DT per repetition keeps dtemp < DT
+    CK(cudaEventRecord(start, c->stream));
+    probe.n = 0;
+    probe.count = 0;
+    g_probe = &probe;
+    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+    g_probe = nullptr;
+    rc = check_launch(c, "timed substep");
+    if (rc) break;
+    CK(cudaStreamSynchronize(c->stream));
+    if (ms.empty()) {
+      ms.assign(probe.n, 0.0);
+      c->kernel_names.assign(probe.name, probe.name + probe.n);
+    }
+    cudaEvent_t prev = start;
+    for (int k = 0; k < probe.n && k < (int)ms.size(); k++) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, prev, probe.ev[k]));
+      ms[k] += t / reps;
+      prev = probe.ev[k];
+    }
+  }
+  for (int k = 0; k < probe.nev; k++) cudaEventDestroy(probe.ev[k]);
+  cudaEventDestroy(start);
+  if (rc) return rc;
+  // the timed substeps moved the clock; keep the DT bookkeeping consistent
+  if ((rc = read_ctl(c))) return rc;
+  return device_error(c);
 }
 
 void *field_ptr(fargo_ctx *c, int which) {
@@ -583,7 +654,21 @@ int fargo_get_field(fargo_ctx *c, int which, double *host) {
     return FARGO_OK;
   }
   if (!p) return set_err(c, FARGO_ERR_INVALID, "field not available in this configuration");
-  return download(c, host, p, c->h.size_grid);
+  int rc = download(c, host, p, c->h.size_grid);
+  if (rc || which != FARGO_FIELD_POTENTIAL || c->nb == 0) return rc;
+  // the device array holds the planet part; the star term (direct + indirect,
+  // src/Kernels.cu:1246-1250) is evaluated by its consumer, and here on the host
+  if ((rc = read_ctl(c))) return rc;
+  const HostState &h = c->h;
+  const double ix = c->pin_ctl->ind_x, iy = c->pin_ctl->ind_y;
+  for (int i = 0; i < c->P.nrad; i++)
+    for (int j = 0; j < c->P.nsec; j++) {
+      const double x = h.Rmed[i] * h.cosP[j], y = h.Rmed[i] * h.sinP[j];
+      double pot = -h.invRmed[i];
+      pot -= ix * x + iy * y;
+      host[(size_t)i * c->P.nsec + j] += pot;
+    }
+  return FARGO_OK;
 }
 
 int fargo_get_planets(fargo_ctx *c, fargo_planet *out, int cap, int *nb) {
@@ -617,6 +702,8 @@ int fargo_get_scalars(fargo_ctx *c, fargo_scalars *s) {
   s->substeps = k.substeps;
   s->last_cfl = k.cfl;
   s->nb = k.nb;
+  s->launches_per_substep = c->launches_per_substep;
+  s->launches_per_dt = c->launches_per_dt;
   return FARGO_OK;
 }
 
@@ -713,6 +800,21 @@ int fargo_write_outputs(fargo_ctx *c, int index) {
     if ((rc = host_write_planet_row(dir, k, index, pl[k], s.lost_mass, s.physical_time, s.omega_frame)))
       return set_err(c, rc, "cannot write planet file");
   return FARGO_OK;
+}
+
+int fargo_time_substep_kernels(fargo_ctx *c, int reps, double *ms_per_kernel, int cap, int *nkernels) {
+  if (!c || reps < 1 || !nkernels) return FARGO_ERR_INVALID;
+  std::vector<double> ms;
+  int rc = DISPATCH(c, time_kernels_typed, c, reps, ms);
+  if (rc) return rc;
+  *nkernels = (int)ms.size();
+  for (int k = 0; k < (int)ms.size() && k < cap; k++) ms_per_kernel[k] = ms[k];
+  return FARGO_OK;
+}
+
+const char *fargo_substep_kernel_name(const fargo_ctx *c, int k) {
+  if (!c || k < 0 || k >= (int)c->kernel_names.size()) return nullptr;
+  return c->kernel_names[k].c_str();
 }
 
 int fargo_write_dims(fargo_ctx *c) {

@@ -25,6 +25,7 @@ struct DiskPtrs {
   T *nu;            // viscosity profile (may be refreshed on the device)
   double *csmean;   // ring means of the sound speed (energy equation)
   const double *cosF, *sinF;  // force angle table (FP64)
+  const T *cosFt, *sinFt;     // the same table in T
   const T *cosP, *sinP;       // potential angle table
   // per-ring partial results of the CFL/force kernel
   double *ring_vmoy, *ring_newdt, *ring_force;

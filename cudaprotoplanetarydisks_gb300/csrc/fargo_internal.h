@@ -25,6 +25,9 @@ enum RingTab {
   RT_CSMEAN,       // ring mean of SoundSpeed (GLOBAL_bufarray)
   RT_SGNORMR,      // normaccr of ComputeSgAccKernel (src/Kernels.cu:902-905)
   RT_SGNORMT,      // normacct
+  RT_INVDRAD,      // 1/(Rsup - Rinf)
+  RT_INVDXTHETA_CFL,  // 1/RT_DXTHETA_CFL
+  RT_INVMIND,      // 1/min(Rsup - Rinf, RT_DXTHETA_CFL)
   RT_COUNT
 };
 

@@ -95,52 +95,57 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     for (int j = tid; j < nsec; j += blockDim.x) s += (double)vth[j];
     const double vmoy = block_sum_d(s, s_red) / (double)nsec;
     if (tid == 0) a.d.ring_vmoy[i] = vmoy;
-    // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum (i >= 1)
+    // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum (i >= 1).
+    // min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
+    // monotonically), so only S_j is formed per cell; the per-ring divisions of the
+    // reference are products with per-ring reciprocals.
     double mn = 1e30;
     if (i > 0) {
-      const T dxrad = RT(a, RT_DRAD, i);
-      const T dxtheta = RT(a, RT_DXTHETA_CFL, i);
-      const T mind = (dxtheta < dxrad) ? dxtheta : dxrad;
+      const T invdrad = RT(a, RT_INVDRAD, i);
+      const T invdxt = RT(a, RT_INVDXTHETA_CFL, i);
+      const T invmind = RT(a, RT_INVMIND, i);
       const T *vr = a.d.vrad + (size_t)i * nsec;
+      T mx = (T)0.0;
       for (int j = tid; j < nsec; j += blockDim.x) {
         T vres = P.fast_transport ? (T)((double)vth[j] - vmoy) : vth[j];
         T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
-        T invdt1 = cs / mind;
-        T invdt2 = fabs(vr[j]) / dxrad;
-        T invdt3 = fabs(vres) / dxtheta;
+        T invdt1 = cs * invmind;
+        T invdt2 = fabs(vr[j]) * invdrad;
+        T invdt3 = fabs(vres) * invdxt;
         T dvr = vr[j + nsec] - vr[j];
         T dvt = vth[jp1(j, nsec)] - vth[j];
         if (dvr >= (T)0.0) dvr = (T)1e-10;
         else dvr = -dvr;
         if (dvt >= (T)0.0) dvt = (T)1e-10;
         else dvt = -dvt;
-        T a4 = dvr / dxrad, b4 = dvt / dxtheta;
+        T a4 = dvr * invdrad, b4 = dvt * invdxt;
         T invdt4 = (b4 > a4) ? b4 : a4;
         invdt4 *= (T)(4.0 * CVNR * CVNR);
-        T dt = (T)CFLSECURITY / sqrt(invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4);
-        mn = fmin(mn, (double)dt);
+        T S = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
+        mx = (S > mx) ? S : mx;
       }
+      const double smax = -block_min_d(-(double)mx, s_red);
+      mn = CFLSECURITY / sqrt(smax);
     }
-    mn = block_min_d(mn, s_red);
     if (tid == 0) a.d.ring_newdt[i] = mn;
   }
   const int nbody = s_nbody;
   if (do_forces) {
-    // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0)
-    const double surf = RT64(a, RT_SURF, i), rmed = RT64(a, RT_RMED, i);
+    // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0):
+    // per-cell term in T (1/d^3 from rsqrt), ring sums in FP64
+    const T surf = RT(a, RT_SURF, i), rmed = RT(a, RT_RMED, i);
     for (int b = 0; b < nbody; b++) {
-      const double x = s_body[b][0], y = s_body[b][1], rs2 = s_body[b][2];
+      const T x = (T)s_body[b][0], y = (T)s_body[b][1], rs2 = (T)s_body[b][2];
       double fx = 0.0, fy = 0.0;
       for (int j = tid; j < nsec; j += blockDim.x) {
-        double cellmass = surf * (double)dens[j];
-        double dx = __dmul_rn(rmed, a.d.cosF[j]) - x;
-        double dy = __dmul_rn(rmed, a.d.sinF[j]) - y;
-        double d2 = dx * dx + dy * dy;
-        double dist2 = d2 + rs2;
-        double distance = sqrt(dist2);
-        double InvDist3 = 1.0 / dist2 / distance;
-        fx += cellmass * dx * InvDist3;
-        fy += cellmass * dy * InvDist3;
+        const T cellmass = surf * dens[j];
+        const T dx = rmed * a.d.cosFt[j] - x;
+        const T dy = rmed * a.d.sinFt[j] - y;
+        const T dist2 = dx * dx + dy * dy + rs2;
+        const T ir = rsqrt(dist2);
+        const T InvDist3 = ir * ir * ir;
+        fx += (double)(cellmass * dx * InvDist3);
+        fy += (double)(cellmass * dy * InvDist3);
       }
       fx = block_sum_d(fx, s_red);
       fy = block_sum_d(fy, s_red);
@@ -190,12 +195,15 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     if (tid == 0) s_newdt = mn;
   }
   if (do_forces) {
-    if (tid < 2 * nbody) {
-      const int b = tid >> 1, comp = tid & 1;
-      double s = 0.0;
-      for (int k = 0; k < nrad; k++) s += __ldcg(a.d.ring_force + ((size_t)k * (FARGO_MAXPL + 1) + b) * 2 + comp);
-      s_acc[b][comp] = s;
-    }
+    // force totals: block-wide tree over the rings (fixed order, deterministic)
+    for (int b = 0; b < nbody; b++)
+      for (int comp = 0; comp < 2; comp++) {
+        double s = 0.0;
+        for (int k = tid; k < nrad; k += blockDim.x)
+          s += __ldcg(a.d.ring_force + ((size_t)k * (FARGO_MAXPL + 1) + b) * 2 + comp);
+        s = block_sum_d(s, s_red);
+        if (tid == 0) s_acc[b][comp] = s;
+      }
   }
   __syncthreads();
   if (tid == 0) {
@@ -251,20 +259,6 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       }
       fargo_rotate_psys(*c, c->OmegaFrame * dt);
     }
-    if (do_forces) {
-      // ApplySubKeplerianBoundary values (src/SideEuler.cu:296-320)
-      const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
-      const double r0 = RT64(a, RT_RMED, 0), r1 = RT64(a, RT_RMED, nrad - 1);
-      const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
-      double in = 1.0 * 1.0 / r0 * (1.0 - f * pow(fargo_aspect_ratio(P, r0, t, t0), 2.0) * pow(r0, 2.0 * P.flaringindex));
-      double out = 1.0 * 1.0 / r1 * (1.0 - f * pow(fargo_aspect_ratio(P, r1, t, t0), 2.0) * pow(r1, 2.0 * P.flaringindex));
-      if (P.self_gravity) {
-        in -= r0 * a.d.csmean[0];
-        out -= r1 * a.d.csmean[nrad - 1];
-      }
-      c->vkep_in = sqrt(in);
-      c->vkep_out = sqrt(out);
-    }
   }
   // FViscosity profile when it changes in time (alpha viscosity with an energy
   // equation, or a moving cavity)
@@ -291,7 +285,16 @@ __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
     s += (double)cs;
   }
   s = block_sum_d(s, s_red);
-  if (threadIdx.x == 0) a.d.csmean[i] = s / (double)nsec;
+  if (threadIdx.x == 0) {
+    const double m = s / (double)nsec;
+    a.d.csmean[i] = m;
+    // FViscosity reads this ring mean (alpha viscosity): refresh the profile here,
+    // where the sound speed changes
+    if (a.P.viscosity_alpha) {
+      const Ctl *c = a.d.ctl;
+      a.d.nu[i] = (T)fargo_fviscosity(a.P, RT64(a, RT_RMED, i), m, c->PhysicalTime, c->PhysicalTimeInitial);
+    }
+  }
 }
 
 // CorrectVthetaKernel src/Kernels.cu:1256-1263 (corotating frame)
@@ -558,8 +561,15 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
                       ((T)0.5 * (D[q] + D[q - nsec]));
   }
   if (!a.P.evanescent && (i == 0 || i == nrad - 1)) {
-    const double vk = (i == 0) ? c->vkep_in : c->vkep_out;
-    a.d.vthetaint[q] = (T)(vk - RT64(a, RT_RMED, i) * c->OmegaFrame);
+    // ApplySubKeplerianBoundary (src/SideEuler.cu:296-320), with the current ring
+    // mean of the sound speed in the self-gravity form (Make1Dprofile(1))
+    const DevParams &P = a.P;
+    const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
+    const double r = RT64(a, RT_RMED, i);
+    const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
+    double v2 = 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
+    if (P.self_gravity) v2 -= r * a.d.csmean[i];
+    a.d.vthetaint[q] = (T)(sqrt(v2) - r * c->OmegaFrame);
   }
 }
 
@@ -913,11 +923,16 @@ __global__ void k_dt_begin(Ctl *c) {
   c->dtemp = 0.0;
   c->nsub_dt = 0;
   c->done = 0;
+  c->err = 0;
   c->ticket = 0u;
 }
 
 // ---------------------------------------------------------------------------
-// host-side launchers
+// host-side launchers.  MARK records the launch in the optional probe (launch
+// counting, per-kernel CUDA-event timing); it never changes what runs.
+thread_local LaunchProbe *g_probe = nullptr;
+#define MARK(name) probe_mark(s, name)
+
 template <class T>
 void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes) {
   KArgs<T> a = a0;
@@ -928,47 +943,74 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
     // 3 forces + potential only (no planet advance, no time update)
     k_cfl_forces<T><<<P.nrad, 256, 0, s>>>(a);
+    MARK("k_cfl_forces");
   }
-  if ((which_mask & SUBK_COROT) && P.corotating) k_correct_vtheta<T><<<g2, b2, 0, s>>>(a);
+  if ((which_mask & SUBK_COROT) && P.corotating) {
+    k_correct_vtheta<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_correct_vtheta");
+  }
   if (which_mask & SUBK_BC1) launch_boundaries(a, s);
   if ((which_mask & SUBK_SG) && P.self_gravity) launch_selfgravity(a, s);
   if (which_mask & SUBK_SOURCE) {
     k_source<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_source");
     k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vradint, a.d.vthetaint);
+    MARK("k_visc_tau");
     k_visc_update<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_visc_update");
     k_artvisc<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_artvisc");
   }
   if (which_mask & SUBK_BC2) launch_boundaries(a, s);
   if ((which_mask & SUBK_ENERGY) && P.adiabatic) {
     k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vrad, a.d.vtheta);
+    MARK("k_visc_tau");
     k_energy<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_energy");
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
     k_transport_radial<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_transport_radial");
     int nt = P.nsec >= 1024 ? 512 : 256;
     a.az_smem = az_smem_bytes > 0;
     k_transport_azimuthal<T><<<P.nrad, nt, az_smem_bytes, s>>>(a);
+    MARK("k_transport_azimuthal");
     a.az_smem = 0;
     k_velocities<T><<<g2, b2, 0, s>>>(a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
+    MARK("k_velocities");
   }
   if (which_mask & SUBK_BC3) launch_boundaries(a, s);
-  if ((which_mask & SUBK_TEMPERATURE) && (bc || !(which_mask & SUBK_TRANSPORT))) k_temperature<T><<<g2, b2, 0, s>>>(a);
-  if (which_mask & SUBK_END) k_end<T><<<1, 256, 0, s>>>(a);
+  if ((which_mask & SUBK_TEMPERATURE) && (bc || !(which_mask & SUBK_TRANSPORT))) {
+    k_temperature<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_temperature");
+  }
+  if (which_mask & SUBK_END) {
+    k_end<T><<<1, 256, 0, s>>>(a);
+    MARK("k_end");
+  }
 }
 
 template <class T>
 void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
   const DevParams &P = a.P;
-  if (P.open_inner) k_bc_open<T><<<(P.nsec + 255) / 256, 256, 0, s>>>(a);
+  if (P.open_inner) {
+    k_bc_open<T><<<(P.nsec + 255) / 256, 256, 0, s>>>(a);
+    MARK("k_bc_open");
+  }
   if (P.non_reflecting) {
-    if (P.adiabatic) k_soundspeed<T><<<P.nrad, 256, 0, s>>>(a);
+    if (P.adiabatic) {
+      k_soundspeed<T><<<P.nrad, 256, 0, s>>>(a);
+      MARK("k_soundspeed");
+    }
     k_bc_nonreflecting<T><<<1, 1024, 0, s>>>(a);
+    MARK("k_bc_nonreflecting");
   }
   if (P.evanescent) {
     const dim3 b2(64, 4);
     const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
     k_bc_evanescent<T><<<g2, b2, 0, s>>>(a);
+    MARK("k_bc_evanescent");
   }
 }
 
@@ -976,10 +1018,15 @@ template <class T>
 void launch_dt_prefix(const KArgs<T> &a0, cudaStream_t s) {
   KArgs<T> a = a0;
   k_dt_begin<<<1, 1, 0, s>>>(a.d.ctl);
-  if (a.P.adiabatic) k_soundspeed<T><<<a.P.nrad, 256, 0, s>>>(a);
+  MARK("k_dt_begin");
+  if (a.P.adiabatic) {
+    k_soundspeed<T><<<a.P.nrad, 256, 0, s>>>(a);
+    MARK("k_soundspeed");
+  }
   if (a.P.sloppy_cfl) {
     a.mode = 1;
     k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+    MARK("k_cfl_forces");
   }
 }
 
@@ -988,6 +1035,7 @@ void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
   KArgs<T> a = a0;
   a.mode = 1;
   k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+  MARK("k_cfl_forces");
 }
 
 template <class T>
@@ -995,6 +1043,26 @@ cudaError_t prepare_kernels(size_t az_smem_bytes) {
   if (az_smem_bytes > 0)
     return cudaFuncSetAttribute(k_transport_azimuthal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
   return cudaSuccess;
+}
+
+// FP64 host data <-> device fields of type T through an FP64 staging buffer
+template <class T>
+__global__ void k_convert_from_f64(const double *__restrict__ in, T *__restrict__ out, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = (T)in[k];
+}
+template <class T>
+__global__ void k_convert_to_f64(const T *__restrict__ in, double *__restrict__ out, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    out[k] = (double)in[k];
+}
+void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s) {
+  if (esize == 4) k_convert_from_f64<float><<<608, 256, 0, s>>>(in, (float *)out, n);
+  else k_convert_from_f64<double><<<608, 256, 0, s>>>(in, (double *)out, n);
+}
+void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s) {
+  if (esize == 4) k_convert_to_f64<float><<<608, 256, 0, s>>>((const float *)in, out, n);
+  else k_convert_to_f64<double><<<608, 256, 0, s>>>((const double *)in, out, n);
 }
 
 #define INSTANTIATE(T)                                                                                  \

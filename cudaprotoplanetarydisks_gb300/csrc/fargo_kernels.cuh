@@ -19,6 +19,29 @@
 #define SUBK_END         0x400u  // PhysicalTime, LostMass, loop condition
 #define SUBK_ALL         0x7ffu
 
+// Optional launch probe: counts launches and, when events are given, records one
+// event after each kernel so the per-kernel device time can be read back.
+struct LaunchProbe {
+  cudaEvent_t ev[96];
+  const char *name[96];
+  int n;       // events recorded
+  int count;   // launches seen
+  int nev;     // events available (0: count only)
+};
+extern thread_local LaunchProbe *g_probe;
+inline void probe_mark(cudaStream_t s, const char *name) {
+  if (!g_probe) return;
+  if (g_probe->n < g_probe->nev) {
+    cudaEventRecord(g_probe->ev[g_probe->n], s);
+    g_probe->name[g_probe->n] = name;
+    g_probe->n++;
+  }
+  g_probe->count++;
+}
+
+void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s);
+void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s);
+
 template <class T>
 void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes);
 template <class T>

@@ -197,8 +197,11 @@ template <class T>
 void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, nrad = a.P.nrad;
   k_sg_rows_fwd<T><<<nrad, 256, 2 * nsec * sizeof(double2), s>>>(a, 0, a.sg.spec_r, a.sg.spec_t, nrad);
+  probe_mark(s, "k_sg_rows_fwd");
   k_sg_cols<T><<<a.sg.M, 256, 2 * 2 * nrad * sizeof(double2), s>>>(a, 0);
+  probe_mark(s, "k_sg_cols");
   k_sg_rows_inv<T><<<nrad, 256, 2 * nsec * sizeof(double2), s>>>(a);
+  probe_mark(s, "k_sg_rows_inv");
 }
 
 // Set-up: spectra of the constant kernels (compute_kernel src/SgMain.cu:49-81 is

@@ -356,6 +356,12 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
     T(RT_CS, i) = (i < p.nrad && !p.adiabatic) ? at(h.SoundSpeed, (size_t)i * NSEC) : 0.0;
     T(RT_NU, i) = at(h.nu, i);
     T(RT_DRAD, i) = h.Rsup[i] - h.Rinf[i];
+    if (i < p.nrad) {
+      const double dxr = h.Rsup[i] - h.Rinf[i], dxt = h.Rmed[i] * 2.0 * PI / (double)NSEC;
+      T(RT_INVDRAD, i) = 1.0 / dxr;
+      T(RT_INVDXTHETA_CFL, i) = 1.0 / dxt;
+      T(RT_INVMIND, i) = 1.0 / ((dxt < dxr) ? dxt : dxr);
+    }
     T(RT_SIGMAMED, i) = at(h.SigmaMed, i);
     T(RT_ENERGYMED, i) = at(h.EnergyMed, i);
     T(RT_COOLTIME, i) = at(h.CoolingTimeMed, i);

@@ -134,6 +134,8 @@ typedef struct fargo_scalars {
   long long substeps;           /* hydro substeps done since creation     */
   int    last_cfl;              /* CFL integer of the last substep        */
   int    nb;                    /* number of planets                      */
+  int    launches_per_substep;  /* kernels launched by one hydro substep  */
+  int    launches_per_dt;       /* kernels launched once per DT (prefix)  */
 } fargo_scalars;
 
 typedef struct fargo_ctx fargo_ctx;
@@ -211,6 +213,14 @@ int  fargo_condition_cfl(fargo_ctx *ctx, double deltaT, int *cfl);
 int  fargo_write_outputs(fargo_ctx *ctx, int index);
 /* WriteDim (src/Output.cu:19-35) + EmptyPlanetSystemFile (37-58). */
 int  fargo_write_dims(fargo_ctx *ctx);
+
+/* ---- measurement (no counterpart in the reference) ----------------------- */
+/* Runs reps hydro substeps launch by launch with a CUDA event after every kernel
+   and returns the mean device time (ms) of each kernel of one substep, in launch
+   order; *nkernels = kernels per substep.  Advances the state like reps substeps. */
+int  fargo_time_substep_kernels(fargo_ctx *ctx, int reps, double *ms_per_kernel, int cap, int *nkernels);
+/* Name of kernel k of the last fargo_time_substep_kernels call (NULL if none). */
+const char *fargo_substep_kernel_name(const fargo_ctx *ctx, int k);
 
 #ifdef __cplusplus
 }

@@ -73,7 +73,9 @@ static double device_reduce(const double *in, int N) {
       double mySum = 0.0;
       while (i < (unsigned)N) {
         mySum += in[i];
-        if (is_pow2 || i + threads < (unsigned)N) mySum += in[i + threads];
+        /* for N == 1 (IsPow2 true) the reference reads in[32], past the array;
+           that element counts as zero here */
+        if ((is_pow2 || i + threads < (unsigned)N) && i + threads < (unsigned)N) mySum += in[i + threads];
         i += gridSize;
       }
       s[t] = mySum;

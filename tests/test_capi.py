@@ -1,0 +1,64 @@
+"""C-ABI checks that need no GPU: the library loads, exports every entry point of
+include/fargo_gb300.h, and the ctypes layout matches the C layout."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+from cudaprotoplanetarydisks_gb300 import _capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fargo_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fargo_[a-z_A-Z0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _capi.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.missing_symbols == []
+
+
+def test_ctypes_signatures_cover_header():
+    assert sorted(n for n, _, _ in _capi.SIGNATURES) == declared_functions()
+
+
+def test_struct_layout_matches_c():
+    fields = [f for f, _ in _capi.FargoParams._fields_]
+    prog = ["#include <stdio.h>", "#include <stddef.h>", '#include "fargo_gb300.h"', "int main(void){",
+            'printf("%zu %zu %zu\\n", sizeof(fargo_params), sizeof(fargo_planet), sizeof(fargo_scalars));']
+    for f in fields:
+        prog.append(f'printf("%zu\\n", offsetof(fargo_params, {f}));')
+    prog.append("return 0;}")
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write("\n".join(prog))
+        exe = os.path.join(d, "t")
+        subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    sizes = [int(x) for x in out[:3]]
+    assert sizes == [ctypes.sizeof(_capi.FargoParams), ctypes.sizeof(_capi.FargoPlanet),
+                     ctypes.sizeof(_capi.FargoScalars)]
+    offs = [int(x) for x in out[3:]]
+    assert offs == [getattr(_capi.FargoParams, f).offset for f in fields]
+
+
+def test_invalid_create_is_rejected_without_gpu_work():
+    lib = _capi.load()
+    p = _capi.FargoParams()
+    lib.fargo_params_default(ctypes.byref(p))
+    p.nrad = 2  # too small: rejected before any device call
+    h = ctypes.c_void_p()
+    assert lib.fargo_ctx_create(ctypes.byref(p), None, 0, 0, None, ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
+    p.nrad = 64
+    assert lib.fargo_ctx_create(ctypes.byref(p), None, 0, 7, None, ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
+    assert lib.fargo_ctx_create(ctypes.byref(p), None, -1, 0, None, ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
+    assert lib.fargo_last_error(None) == b"no context"
