@@ -222,6 +222,21 @@ int  fargo_time_substep_kernels(fargo_ctx *ctx, int reps, double *ms_per_kernel,
 /* Name of kernel k of the last fargo_time_substep_kernels call (NULL if none). */
 const char *fargo_substep_kernel_name(const fargo_ctx *ctx, int k);
 
+/* ---- allocation-free CFL (no counterpart in the reference) --------------- */
+/* The CFL integer of fargo_condition_cfl for callers that cannot call cudaMalloc
+   (device memory owned by another allocator, or a loop that must not take
+   cudaMalloc's implicit synchronisation).  Inputs are the caller's FP64 device
+   arrays: vrad, vtheta, soundspeed ((nrad+1)*nsec each, ring-major) and rinf,
+   rmed, rsup (nrad+1 each); *cfl_out is a device int written on `stream`
+   (-1 when the time step is not finite).  Allocates nothing: its scratch is a
+   fixed array inside the library, at most 16384 rings (larger nrad:
+   FARGO_ERR_INVALID).  The first call on a device sets up that device (make it
+   before any stream capture); calls that overlap on the GPU race on the array. */
+int  fargo_condition_cfl_noalloc(const double *vrad, const double *vtheta, const double *soundspeed,
+                                 const double *rinf, const double *rmed, const double *rsup,
+                                 int nrad, int nsec, int fast_transport, double deltaT,
+                                 void *stream, int *cfl_out);
+
 #ifdef __cplusplus
 }
 #endif
