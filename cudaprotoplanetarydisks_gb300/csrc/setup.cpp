@@ -323,8 +323,10 @@ void host_init_euler(const fargo_params &p, HostState &h, const DevParams &dp, C
       if (i == NRAD) h.Vrad[q] = 0.0;
       else {
         h.Vrad[q] = p.imposeddiskdrift * p.sigma0 / h.SigmaInf[i] / ri;
-        if (p.viscosity_alpha) h.Vrad[q] -= 3.0 * h.nu[i] / r * (-p.sigmaslope + 2.0 * p.flaringindex + 1.0);
-        else h.Vrad[q] -= 3.0 * h.nu[i] / r * (-p.sigmaslope + .5);
+        // the kernel's alpha branch (src/Kernels.cu:681) is unreachable: its int
+        // flag receives `extern double ViscosityAlpha` (src/Pframeforce.cu:21), a
+        // tiny double made of the int flag's bits, which converts to 0
+        h.Vrad[q] -= 3.0 * h.nu[i] / r * (-p.sigmaslope + .5);
       }
     }
   }

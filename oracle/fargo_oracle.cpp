@@ -377,8 +377,11 @@ struct Oracle {
         if (i == NRAD) Vrad[c] = 0.0;
         else {
           Vrad[c] = P.imposeddiskdrift * P.sigma0 / SigmaInf[i] / ri;
-          if (P.viscosity_alpha) Vrad[c] -= 3.0 * viscosity_array[i] / r * (-P.sigmaslope + 2.0 * P.flaringindex + 1.0);
-          else Vrad[c] -= 3.0 * viscosity_array[i] / r * (-P.sigmaslope + .5);
+          /* The alpha branch of the kernel (src/Kernels.cu:681) is never taken: the
+             caller passes `extern double ViscosityAlpha` (src/Pframeforce.cu:21),
+             whose bits are the int flag and its neighbour, to the kernel's int
+             parameter, and that tiny double converts to 0. */
+          Vrad[c] -= 3.0 * viscosity_array[i] / r * (-P.sigmaslope + .5);
         }
       }
     }

@@ -1,0 +1,94 @@
+"""The oracle pinned to the reference itself.
+
+tests/golden/ref_*.npz were made by tests/golden/make_golden.py, which runs the
+reference's own sources (src/*.cu, compiled for the CPU by
+oracle/ref_emul/build_ref.py) on seven .par files.  Here the oracle reads the same
+.par text through the library's parser, runs the same DTs, and must reproduce
+the reference's dumps: bitwise (SHA-256 of each full field) on the machine type
+the fixtures were made on, and to 1e-12 (ring sums, full rings, planets) anywhere.
+"""
+import hashlib
+import os
+import platform
+
+import numpy as np
+import pytest
+
+import cudaprotoplanetarydisks_gb300 as fg
+from oracle.oracle import OracleDisk
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = sorted(f[4:-4] for f in os.listdir(GOLDEN) if f.startswith("ref_") and f.endswith(".npz"))
+FIELDS = ("dens", "vrad", "vtheta", "energy", "temperature")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, f"ref_{name}.npz")))
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    den = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / den)
+
+
+def oracle_for(rec, tmp_path):
+    cfg = tmp_path / "planet.cfg"
+    cfg.write_text("# Name Distance Mass Accretion FeelsDisk FeelsOthers\n" + str(rec["cfg"]))
+    text = str(rec["par"]).replace("@RUNDIR@", str(tmp_path))
+    text = "\n".join(line for line in text.splitlines() if not line.startswith("PlanetConfig"))
+    text += f"\nPlanetConfig {cfg}\n"
+    par = tmp_path / "run.par"
+    par.write_text(text)
+    params = fg.read_par(str(par))
+    planets = fg.read_planets(params, str(par))
+    return params, OracleDisk(params, planets)
+
+
+def test_fixtures_present():
+    assert len(CASES) >= 7, CASES
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_reproduces_reference(name, tmp_path):
+    rec = load(name)
+    if int(rec["returncode"]) != 0:
+        pytest.skip("the reference stops during set-up for this case (see test_selfgravity_setup_aborts)")
+    params, o = oracle_for(rec, tmp_path)
+    same_machine = str(rec["machine"]) == platform.machine()
+    rows = rec["planet_rows"]
+    for k in (1, 2):
+        o.step_DT()
+        for f in FIELDS:
+            if f"{f}{k}_ringsum" not in rec:
+                continue
+            mine = o.field(f)[:-1]
+            assert rel(mine.sum(axis=1), rec[f"{f}{k}_ringsum"]) <= 1e-12, (f, k)
+            for key in rec:
+                if key.startswith(f"{f}{k}_ring") and key[len(f"{f}{k}_ring"):].isdigit():
+                    i = int(key[len(f"{f}{k}_ring"):])
+                    assert rel(mine[i], rec[key]) <= 1e-12, (f, k, i)
+            if same_machine:
+                digest = hashlib.sha256(np.ascontiguousarray(mine).tobytes()).hexdigest()
+                assert digest == str(rec[f"{f}{k}_sha256"]), f"{f} after {k} DTs is not bitwise equal"
+        pl = o.planets()[0]
+        s = o.scalars()
+        row = rows[k]
+        assert int(row[0]) == k
+        for got, want in ((pl.x, row[1]), (pl.y, row[2]), (pl.vx, row[3]), (pl.vy, row[4]),
+                          (s.lost_mass, row[6]), (s.physical_time, row[7]), (s.omega_frame, row[8])):
+            assert abs(got - want) <= 1e-12 * max(1.0, abs(want)), (k, got, want)
+            if same_machine:
+                assert got == want
+
+
+def test_selfgravity_setup_aborts():
+    # The reference cannot start a self-gravitating run: Init_planetarysys_withSG
+    # (src/Main.cu:289) calls Make1Dprofile(1), which copies from SoundSpeed_d before
+    # InitEuler allocates it (src/Kernels.cu:631); the CUDA runtime rejects the null
+    # source and gpuErrchk exits.  The oracle and the GPU path replace that step
+    # (the planet's initial velocity uses the azimuthal mean of the radial SG acceleration).
+    rec = load("selfgravity")
+    assert int(rec["returncode"]) != 0
+    msg = str(rec["stderr"])
+    assert "invalid argument" in msg and "Kernels.cu 631" in msg
