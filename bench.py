@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
+                    help="profiling target: warm-up DTs, then --steps substeps launched kernel by kernel "
+                         "(kernels inside the DT graph's while loop are invisible to ncu)")
     return ap.parse_args()
 
 
@@ -397,9 +400,28 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    import cudaprotoplanetarydisks_gb300 as fg
+    params, planets, _ = workload(args.config)
+    prec = fg.FARGO_FP32_BULK if args.profile == "fp32" else fg.FARGO_FP64
+    disk = fg.Disk(params, planets, prec)
+    for _ in range(args.warmup):
+        disk.run(1)
+    ms = (ctypes.c_double * 96)()
+    nk = ctypes.c_int(0)
+    rc = disk.lib.fargo_time_substep_kernels(disk.h, args.steps, ms, 96, ctypes.byref(nk))
+    assert rc == 0, disk.lib.fargo_last_error(disk.h)
+    for k in range(nk.value):
+        print(f"{disk.lib.fargo_substep_kernel_name(disk.h, k).decode():28s} {ms[k] * 1e3:9.2f} us")
+    disk.close()
+
+
 def main():
     args = parse()
     world, rank, local = dist_env()
+    if args.profile:
+        run_profile(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

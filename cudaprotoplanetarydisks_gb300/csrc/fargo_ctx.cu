@@ -26,6 +26,7 @@ struct fargo_ctx {
   int nb = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  SideBranch side = {nullptr, nullptr, nullptr};  // planet update beside the hydro kernels
   HostState h;
   std::string err = "no error";
   Ctl *d_ctl = nullptr;
@@ -245,7 +246,7 @@ int build_graph(fargo_ctx *c) {
   CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   probe.count = 0;
   g_probe = &probe;
-  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side);
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &body));
   c->launches_per_substep = probe.count;
@@ -261,7 +262,7 @@ int run_dt_hostloop(fargo_ctx *c) {
   KArgs<T> a = make_args<T>(c);
   launch_dt_prefix<T>(a, c->stream);
   for (int n = 0; n < FARGO_MAX_SUBSTEPS_PER_DT + 1; n++) {
-    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem);
+    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side);
     int rc = check_launch(c, "substep");
     if (rc) return rc;
     if ((rc = read_ctl(c))) return rc;
@@ -407,6 +408,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   ctl.PhysicalTime = 0.0;
   ctl.PhysicalTimeInitial = 0.0;
   ctl.OmegaFrame = h.OmegaFrame;
+  fargo_planet_params(ctl, c->dp, ctl.PhysicalTime);
   if ((rc = write_ctl(c))) return rc;
   // the SG spectra are no longer needed on the host
   h.Kr.clear();
@@ -589,7 +591,10 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
     }
     c->own_stream = true;
   }
-  e = cudaMallocHost((void **)&c->pin_ctl, sizeof(Ctl));
+  e = cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&c->pin_ctl, sizeof(Ctl));
   if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_ctl, sizeof(Ctl));
   if (e != cudaSuccess) {
     fargo_ctx_destroy(c);
@@ -615,6 +620,10 @@ void fargo_ctx_destroy(fargo_ctx *c) {
   for (void *p : c->allocs) cudaFree(p);
   if (c->d_ctl) cudaFree(c->d_ctl);
   if (c->pin_ctl) cudaFreeHost(c->pin_ctl);
+  if (c->side.s) cudaStreamSynchronize(c->side.s);
+  if (c->side.fork) cudaEventDestroy(c->side.fork);
+  if (c->side.join) cudaEventDestroy(c->side.join);
+  if (c->side.s) cudaStreamDestroy(c->side.s);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

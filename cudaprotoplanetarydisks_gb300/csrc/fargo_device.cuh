@@ -51,6 +51,7 @@ struct KArgs {
   double lr01, lr12;   // log(Rmed[0]/Rmed[1]), log(Rmed[1]/Rmed[2]) for the Qplus extrapolation
   int mode;            // CFL/force kernel mode
   int az_smem;         // azimuthal kernel keeps its ring in shared memory
+  int vkep_inline;     // k_visc_update computes the sub-Keplerian edge speeds itself
   unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
   int use_cond;                    // 1: k_end sets the while-loop condition
   SgDev sg;

@@ -54,37 +54,25 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   __shared__ int s_nbody, s_last;
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
-  const bool do_planets = (a.mode == 0 || a.mode == 2);
-  if (tid == 0) {
-    const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
-    const double taper = fargo_mass_taper(P, t);
-    int nbody = 1;
-    s_body[0][0] = 0.0;
-    s_body[0][1] = 0.0;
-    s_body[0][2] = 0.0;
-    for (int k = 0; k < P.nb; k++) {
-      double x = c->x[k], y = c->y[k], m = c->mass[k];
-      if (c->feeldisk[k]) {  // AdvanceSystemFromDisk src/Pframeforce.cu:105-111
-        double r = sqrt(x * x + y * y);
-        double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing : fargo_smoothing(P, r, t, t0);
-        s_body[nbody][0] = x;
-        s_body[nbody][1] = y;
-        s_body[nbody][2] = sm * sm;
-        nbody++;
-      }
-      // FillForcesArrays src/Pframeforce.cu:68-77
-      double mp = m * taper;
-      double PD = sqrt(x * x + y * y);
-      double invd3 = 1.0 / PD / PD / PD;
-      double RRoche = PD * pow((1.0 / 3.0 * mp), 1.0 / 3.0);
-      double sm = P.roche_smoothing ? RRoche * P.rochesmoothing : fargo_smoothing(P, PD, t, t0);
-      s_pot[k][0] = x;
-      s_pot[k][1] = y;
-      s_pot[k][2] = mp;
-      s_pot[k][3] = sm * sm;
-      s_pot[k][4] = invd3;
+  const bool do_step = (a.mode == 0 || a.mode == 2);
+  // planet parameters of this substep, computed after the previous planet update
+  // (fargo_planet_params): bodies feeling the disk and the planets' potential terms
+  if (do_forces) {
+    const int nbody = c->nbody;
+    if (tid < nbody) {
+      s_body[tid][0] = c->bx[tid];
+      s_body[tid][1] = c->by[tid];
+      s_body[tid][2] = c->brs2[tid];
     }
-    s_nbody = nbody;
+    if (tid >= 32 && tid < 32 + P.nb) {
+      const int k = tid - 32;
+      s_pot[k][0] = c->px[k];
+      s_pot[k][1] = c->py[k];
+      s_pot[k][2] = c->pm[k];
+      s_pot[k][3] = c->ps2[k];
+      s_pot[k][4] = c->pinvd3[k];
+    }
+    if (tid == 0) s_nbody = nbody;
   }
   __syncthreads();
   const T *dens = a.d.dens + (size_t)i * nsec;
@@ -129,7 +117,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     }
     if (tid == 0) a.d.ring_newdt[i] = mn;
   }
-  const int nbody = s_nbody;
+  const int nbody = do_forces ? s_nbody : 0;
   if (do_forces) {
     // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0):
     // per-cell term in T (1/d^3 from rsqrt), ring sums in FP64
@@ -232,33 +220,28 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       // DiskOnPrimaryAcceleration, ComputeIndirectTerm (src/Pframeforce.cu:86-94)
       c->ind_x = P.indirect_term ? -s_acc[0][0] : 0.0;
       c->ind_y = P.indirect_term ? -s_acc[0][1] : 0.0;
+      for (int b = 0; b < nbody; b++) {
+        c->accx[b] = s_acc[b][0];
+        c->accy[b] = s_acc[b][1];
+      }
     }
-    if (do_planets) {
+    if (do_step) {
       if (c->err) dt = 0.0;
       c->dt = dt;
       c->dtemp += dt;
       c->nsub_dt += 1;
-      if (P.corotating) fargo_psys_info(*c, P, 1);
-      // AdvanceSystemFromDisk src/Pframeforce.cu:97-121
-      int b = 1;
-      for (int k = 0; k < P.nb; k++) {
-        if (c->feeldisk[k]) {
-          c->vx[k] += dt * s_acc[b][0];
-          c->vy[k] += dt * s_acc[b][1];
-          c->vx[k] += dt * c->ind_x;
-          c->vy[k] += dt * c->ind_y;
-          b++;
-        }
-      }
-      fargo_advance_rk5(*c, P, dt);
-      c->domega = 0.0;
-      if (P.corotating && dt > 0.0) {
-        double OmegaNew = fargo_psys_info(*c, P, 0) / dt;
-        c->domega = OmegaNew - c->OmegaFrame;
-        c->OmegaFrame = OmegaNew;
-      }
-      fargo_rotate_psys(*c, c->OmegaFrame * dt);
+      c->t_sub = c->PhysicalTime;
     }
+  }
+  // sub-Keplerian edge velocities of this substep (ApplySubKeplerianBoundary),
+  // one ring per warp; k_visc_update computes them itself when the sound-speed
+  // ring means change after this kernel (non-reflecting edge, energy equation)
+  if (do_forces && !P.evanescent && (tid == 0 || tid == 32)) {
+    const int ir = tid == 0 ? 0 : nrad - 1;
+    const double r = RT64(a, RT_RMED, ir);
+    const double v = fargo_vkep(P, r, c->PhysicalTime, c->PhysicalTimeInitial, a.d.csmean ? a.d.csmean[ir] : 0.0);
+    if (tid == 0) c->vkep_in = v;
+    else c->vkep_out = v;
   }
   // FViscosity profile when it changes in time (alpha viscosity with an energy
   // equation, or a moving cavity)
@@ -268,6 +251,17 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     for (int k = tid; k < nrad; k += blockDim.x)
       a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
   }
+}
+
+// The planetary part of a substep (AdvanceSystemFromDisk, AdvanceSystemRK5,
+// the corotating frame, RotatePsys; src/SourceEuler.cu:236-261) on one thread,
+// from the disk accelerations, indirect term, dt and start time that
+// k_cfl_forces left in the control block.  It writes only planet state and the
+// next substep's planet parameters, which no hydro kernel of the substep reads,
+// so it may run beside them; in a corotating frame the hydro kernels need the
+// new frame rate and it runs before them.
+__global__ void k_planets(DevParams P, Ctl *c) {
+  fargo_planets_substep(*c, P, c->dt, c->t_sub);
 }
 
 // ---------------------------------------------------------------------------
@@ -563,13 +557,11 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
   if (!a.P.evanescent && (i == 0 || i == nrad - 1)) {
     // ApplySubKeplerianBoundary (src/SideEuler.cu:296-320), with the current ring
     // mean of the sound speed in the self-gravity form (Make1Dprofile(1))
-    const DevParams &P = a.P;
-    const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
     const double r = RT64(a, RT_RMED, i);
-    const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
-    double v2 = 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
-    if (P.self_gravity) v2 -= r * a.d.csmean[i];
-    a.d.vthetaint[q] = (T)(sqrt(v2) - r * c->OmegaFrame);
+    const double v = a.vkep_inline
+                         ? fargo_vkep(a.P, r, c->PhysicalTime, c->PhysicalTimeInitial, a.d.csmean ? a.d.csmean[i] : 0.0)
+                         : (i == 0 ? c->vkep_in : c->vkep_out);
+    a.d.vthetaint[q] = (T)(v - r * c->OmegaFrame);
   }
 }
 
@@ -934,16 +926,35 @@ thread_local LaunchProbe *g_probe = nullptr;
 #define MARK(name) probe_mark(s, name)
 
 template <class T>
-void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes) {
+void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes,
+                            const SideBranch *side) {
   KArgs<T> a = a0;
   const DevParams &P = a.P;
   const dim3 b2(64, 4);
   const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
+  bool joined = true;
+  // the edge speeds precomputed by k_cfl_forces hold unless it does not run here,
+  // or the non-reflecting edge recomputes the sound speed (and its ring means,
+  // which the self-gravity form reads) after it
+  a.vkep_inline = !(which_mask & SUBK_CFL_FORCES) || (P.non_reflecting && P.adiabatic && P.self_gravity);
   if (which_mask & SUBK_CFL_FORCES) {
     // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
     // 3 forces + potential only (no planet advance, no time update)
     k_cfl_forces<T><<<P.nrad, 256, 0, s>>>(a);
     MARK("k_cfl_forces");
+    if (a.mode == 0 || a.mode == 2) {
+      if (side && !P.corotating) {
+        cudaEventRecord(side->fork, s);
+        cudaStreamWaitEvent(side->s, side->fork, 0);
+        k_planets<<<1, 1, 0, side->s>>>(P, a.d.ctl);
+        cudaEventRecord(side->join, side->s);
+        joined = false;
+        if (g_probe) g_probe->count++;
+      } else {
+        k_planets<<<1, 1, 0, s>>>(P, a.d.ctl);
+        MARK("k_planets");
+      }
+    }
   }
   if ((which_mask & SUBK_COROT) && P.corotating) {
     k_correct_vtheta<T><<<g2, b2, 0, s>>>(a);
@@ -989,6 +1000,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     k_end<T><<<1, 256, 0, s>>>(a);
     MARK("k_end");
   }
+  if (!joined) cudaStreamWaitEvent(s, side->join, 0);
 }
 
 template <class T>
@@ -1066,7 +1078,8 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
 }
 
 #define INSTANTIATE(T)                                                                                  \
-  template void launch_substep_kernels<T>(const KArgs<T> &, cudaStream_t, unsigned, size_t);          \
+  template void launch_substep_kernels<T>(const KArgs<T> &, cudaStream_t, unsigned, size_t,            \
+                                         const SideBranch *);                                          \
   template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
   template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \

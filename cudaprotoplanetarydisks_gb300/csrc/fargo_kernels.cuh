@@ -42,8 +42,17 @@ inline void probe_mark(cudaStream_t s, const char *name) {
 void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s);
 void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s);
 
+// A second stream for the planet update of a substep, which then runs beside the
+// hydro kernels (forked after k_cfl_forces, joined at the end of the substep).
+// Without one, or in a corotating frame, it runs in line.
+struct SideBranch {
+  cudaStream_t s;
+  cudaEvent_t fork, join;
+};
+
 template <class T>
-void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes);
+void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes,
+                            const SideBranch *side = nullptr);
 template <class T>
 void launch_dt_prefix(const KArgs<T> &a, cudaStream_t s);
 template <class T>

@@ -64,6 +64,15 @@ struct Ctl {
   int feeldisk[FARGO_MAXPL], feelothers[FARGO_MAXPL];
   // GetPsysInfo statics (Psys.cu:79)
   double xmark, ymark;
+  // per-substep planet parameters, computed once after each planet update:
+  // bodies feeling the disk (0 = the star) and the potential of every planet
+  int nbody;
+  int pad2;
+  double bx[FARGO_MAXPL + 1], by[FARGO_MAXPL + 1], brs2[FARGO_MAXPL + 1];
+  double px[FARGO_MAXPL], py[FARGO_MAXPL], pm[FARGO_MAXPL], ps2[FARGO_MAXPL], pinvd3[FARGO_MAXPL];
+  // disk accelerations of the bodies (ComputeAccel) and start time of the substep
+  double accx[FARGO_MAXPL + 1], accy[FARGO_MAXPL + 1];
+  double t_sub;
 };
 
 // AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392
@@ -198,7 +207,7 @@ FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, 
 }
 
 // RungeKutta + AdvanceSystemRK5  src/RungeKutta.cu:8-28, src/Pframeforce.cu:124-187
-FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt) {
+FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt, double t) {
   const int nb = c.nb;
   double q0[4 * FARGO_MAXPL], q1[4 * FARGO_MAXPL], pm[FARGO_MAXPL];
   for (int i = 0; i < 4 * FARGO_MAXPL; i++) q0[i] = q1[i] = 0.0;
@@ -229,7 +238,7 @@ FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt) {
       q1[i] = q0[i] + 37.0 / 378.0 * k[0][i] + 250.0 / 621.0 * k[2][i] + 125.0 / 594.0 * k[3][i] +
               512.0 / 1771.0 * k[5][i];
   }
-  for (int i = 1 - (c.PhysicalTime >= P.releasedate); i < nb; i++) {
+  for (int i = 1 - (t >= P.releasedate); i < nb; i++) {
     if (!P.forced_circular) {
       c.x[i] = q1[i];
       c.y[i] = q1[i + nb];
@@ -248,11 +257,11 @@ FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt) {
       c.vy[i] = vx * sin(dtheta + theta) + vy * cos(dtheta + theta);
     }
   }
-  if (c.PhysicalTime < P.releasedate && nb > 0) {
+  if (t < P.releasedate && nb > 0) {
     double x = c.x[0], y = c.y[0];
     double r = sqrt(x * x + y * y);
     double theta = atan2(y, x);
-    double rdot = (P.releaseradius - r) / (P.releasedate - c.PhysicalTime);
+    double rdot = (P.releaseradius - r) / (P.releasedate - t);
     double omega = sqrt((1. + c.mass[0]) / r / r / r);
     double new_r = r + rdot * dt;
     double denom = r - new_r;
@@ -266,4 +275,74 @@ FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt) {
     c.vx[0] = vx * cos(dtheta + theta) - vy * sin(dtheta + theta);
     c.vy[0] = vx * sin(dtheta + theta) + vx * cos(dtheta + theta);
   }
+}
+
+// Planet parameters of a substep starting at time t: the smoothing of the disk's
+// force on each FeelDisk body (AdvanceSystemFromDisk src/Pframeforce.cu:105-111;
+// body 0 is the star, ComputeAccel(0,0,0) src/SourceEuler.cu:241) and the
+// potential parameters of every planet (FillForcesArrays src/Pframeforce.cu:68-77).
+FARGO_HD void fargo_planet_params(Ctl &c, const DevParams &P, double t) {
+  const double t0 = c.PhysicalTimeInitial;
+  const double taper = fargo_mass_taper(P, t);
+  int nbody = 1;
+  c.bx[0] = c.by[0] = c.brs2[0] = 0.0;
+  for (int k = 0; k < c.nb; k++) {
+    const double x = c.x[k], y = c.y[k], m = c.mass[k];
+    if (c.feeldisk[k]) {
+      const double r = sqrt(x * x + y * y);
+      const double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing : fargo_smoothing(P, r, t, t0);
+      c.bx[nbody] = x;
+      c.by[nbody] = y;
+      c.brs2[nbody] = sm * sm;
+      nbody++;
+    }
+    const double mp = m * taper;
+    const double PD = sqrt(x * x + y * y);
+    const double RRoche = PD * pow((1.0 / 3.0 * mp), 1.0 / 3.0);
+    const double sm = P.roche_smoothing ? RRoche * P.rochesmoothing : fargo_smoothing(P, PD, t, t0);
+    c.px[k] = x;
+    c.py[k] = y;
+    c.pm[k] = mp;
+    c.ps2[k] = sm * sm;
+    c.pinvd3[k] = 1.0 / PD / PD / PD;
+  }
+  c.nbody = nbody;
+}
+
+// Keplerian speed of ApplySubKeplerianBoundary (src/SideEuler.cu:296-320) at ring
+// radius r, before the frame term; csmean is the ring's mean sound speed, which the
+// self-gravity form subtracts (Make1Dprofile(1)).
+FARGO_HD double fargo_vkep(const DevParams &P, double r, double t, double t0, double csmean) {
+  const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
+  double v2 = 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
+  if (P.self_gravity) v2 -= r * csmean;
+  return sqrt(v2);
+}
+
+// The planetary part of one substep of length dt that started at time t
+// (src/SourceEuler.cu:236-261): disk kicks with the indirect term
+// (AdvanceSystemFromDisk), RK5 (AdvanceSystemRK5), the corotating frame update
+// and RotatePsys; then the parameters of the next substep.  The disk
+// accelerations and the indirect term are those of this substep.
+FARGO_HD void fargo_planets_substep(Ctl &c, const DevParams &P, double dt, double t) {
+  if (P.corotating) fargo_psys_info(c, P, 1);
+  int b = 1;
+  for (int k = 0; k < c.nb; k++) {
+    if (c.feeldisk[k]) {
+      c.vx[k] += dt * c.accx[b];
+      c.vy[k] += dt * c.accy[b];
+      c.vx[k] += dt * c.ind_x;
+      c.vy[k] += dt * c.ind_y;
+      b++;
+    }
+  }
+  fargo_advance_rk5(c, P, dt, t);
+  c.domega = 0.0;
+  if (P.corotating && dt > 0.0) {
+    const double OmegaNew = fargo_psys_info(c, P, 0) / dt;
+    c.domega = OmegaNew - c.OmegaFrame;
+    c.OmegaFrame = OmegaNew;
+  }
+  fargo_rotate_psys(c, c.OmegaFrame * dt);
+  fargo_planet_params(c, P, t + dt);
 }
