@@ -28,7 +28,7 @@ struct DiskPtrs {
   const T *cosFt, *sinFt;     // the same table in T
   const T *cosP, *sinP;       // potential angle table
   // per-ring partial results of the CFL/force kernel
-  double *ring_vmoy, *ring_newdt, *ring_force;
+  double *ring_vmoy, *ring_smax, *ring_force;
   double *lostbydisk;
   Ctl *ctl;
 };
@@ -51,10 +51,89 @@ struct KArgs {
   double lr01, lr12;   // log(Rmed[0]/Rmed[1]), log(Rmed[1]/Rmed[2]) for the Qplus extrapolation
   int mode;            // CFL/force kernel mode
   int az_smem;         // azimuthal kernel keeps its ring in shared memory
-  int vkep_inline;     // k_visc_update computes the sub-Keplerian edge speeds itself
   unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
   int use_cond;                    // 1: k_end sets the while-loop condition
   SgDev sg;
+};
+
+// Sum accumulators of the reductions.  FP64 for T = double.  For T = float a
+// float-float pair (Knuth's TwoSum per term, renormalised when two partial sums
+// merge): about 44 significant bits from FP32 arithmetic, where this GPU issues
+// FP64 at 1/64 of the FP32 rate.
+template <class T>
+struct SumAcc;
+
+template <>
+struct SumAcc<double> {
+  double s;
+  __device__ __forceinline__ void zero() { s = 0.0; }
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void merge(const SumAcc &o) { s += o.s; }
+  __device__ __forceinline__ void merge_down(int o) { s += __shfl_down_sync(0xffffffffu, s, o); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct SumAcc<float> {
+  float hi, lo;
+  __device__ __forceinline__ void zero() { hi = lo = 0.0f; }
+  __device__ __forceinline__ void add(float x) {
+    const float t = hi + x, bb = t - hi;
+    lo += (hi - (t - bb)) + (x - bb);
+    hi = t;
+  }
+  __device__ __forceinline__ void merge(const SumAcc &o) {
+    const float t = hi + o.hi, bb = t - hi;
+    const float e = ((hi - (t - bb)) + (o.hi - bb)) + (lo + o.lo);
+    hi = t + e;
+    lo = e - (hi - t);
+  }
+  __device__ __forceinline__ void merge_down(int o) {
+    SumAcc p;
+    p.hi = __shfl_down_sync(0xffffffffu, hi, o);
+    p.lo = __shfl_down_sync(0xffffffffu, lo, o);
+    merge(p);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <class T>
+__device__ __forceinline__ void warp_sum(SumAcc<T> &v) {
+  for (int o = 16; o > 0; o >>= 1) v.merge_down(o);
+}
+
+// Block total of one SumAcc per thread; the result is valid in thread 0 only.
+// sh: one SumAcc per warp.
+template <class T>
+__device__ __forceinline__ double block_total(SumAcc<T> v, SumAcc<T> *sh) {
+  warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < nw; k++) v.merge(sh[k]);
+    return v.value();
+  }
+  return 0.0;
+}
+
+// The ring mean m as T arithmetic sees it: hi + lo with hi = (T)m (lo = 0 for FP64),
+// so that x - m is formed as (x - hi) - lo.
+template <class T>
+struct RingMean {
+  T hi, lo;
+  __device__ __forceinline__ void set(double m) {
+    hi = (T)m;
+    lo = (T)(m - (double)hi);
+  }
+  __device__ __forceinline__ T sub_from(T x) const { return (x - hi) - lo; }
+};
+template <>
+struct RingMean<double> {
+  double hi, lo;
+  __device__ __forceinline__ void set(double m) { hi = m; lo = 0.0; }
+  __device__ __forceinline__ double sub_from(double x) const { return x - hi; }
 };
 
 #define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])

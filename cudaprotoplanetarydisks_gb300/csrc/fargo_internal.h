@@ -28,6 +28,9 @@ enum RingTab {
   RT_INVDRAD,      // 1/(Rsup - Rinf)
   RT_INVDXTHETA_CFL,  // 1/RT_DXTHETA_CFL
   RT_INVMIND,      // 1/min(Rsup - Rinf, RT_DXTHETA_CFL)
+  RT_VKEP2,        // squared sub-Keplerian edge speed before the self-gravity term (t = t0)
+  RT_R15,          // pow(Rmed, 1.5) of the alpha viscosity
+  RT_CAVFAC,       // cavity factor of FViscosity (t = t0)
   RT_COUNT
 };
 

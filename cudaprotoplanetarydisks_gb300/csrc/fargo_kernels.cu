@@ -40,17 +40,27 @@ __device__ __forceinline__ int jp1(int j, int n) { return j == n - 1 ? 0 : j + 1
 // ConditionCFL (src/SourceEuler.cu:520-546, kernels src/Kernels.cu:1267-1359),
 // ComputeAccel / ComputeForce (src/SideEuler.cu:242-255, src/Force.cu:372-405,
 // ComputeForceKernel src/Kernels.cu:693-729) and the planet part of
-// FillForcesArraysKernel (src/Kernels.cu:1226-1253).  One CTA per ring.
+// FillForcesArraysKernel (src/Kernels.cu:1226-1253).  One CTA of 256 threads per
+// ring, one pass over the ring's cells for the CFL terms, the forces on the first
+// two bodies and the potential; per-warp partial results meet in shared memory
+// behind one barrier.  The last CTA to finish decides dt and totals the forces.
 // mode 0: full substep start.  mode 1: CFL only (sloppy CFL at the DT start, or
-// the ConditionCFL entry point).  mode 2: forces only, dt = sloppy_dt.
+// the ConditionCFL entry point).  mode 2: forces, dt = sloppy_dt.  mode 3: forces
+// and potential only.
 template <class T>
 __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
+  constexpr int NW = 8;                       // warps of the 256-thread CTA
+  constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
   const DevParams &P = a.P;
   const int i = blockIdx.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
+  const int lane = tid & 31, w = tid >> 5;
   Ctl *c = a.d.ctl;
-  __shared__ double s_red[32];
+  __shared__ SumAcc<T> s_part[NW][NV];
+  __shared__ SumAcc<T> s_vpart[NW];
+  __shared__ T s_mx[NW];
   __shared__ double s_body[FARGO_MAXPL + 1][3];
   __shared__ double s_pot[FARGO_MAXPL][5];
+  __shared__ double s_vmoy;
   __shared__ int s_nbody, s_last;
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
@@ -74,124 +84,190 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     }
     if (tid == 0) s_nbody = nbody;
   }
-  __syncthreads();
   const T *dens = a.d.dens + (size_t)i * nsec;
   const T *vth = a.d.vtheta + (size_t)i * nsec;
   if (do_cfl) {
     // ConditionCFLKernel1D: ring mean of Vtheta
-    double s = 0.0;
-    for (int j = tid; j < nsec; j += blockDim.x) s += (double)vth[j];
-    const double vmoy = block_sum_d(s, s_red) / (double)nsec;
-    if (tid == 0) a.d.ring_vmoy[i] = vmoy;
-    // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum (i >= 1).
-    // min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
-    // monotonically), so only S_j is formed per cell; the per-ring divisions of the
-    // reference are products with per-ring reciprocals.
-    double mn = 1e30;
-    if (i > 0) {
-      const T invdrad = RT(a, RT_INVDRAD, i);
-      const T invdxt = RT(a, RT_INVDXTHETA_CFL, i);
-      const T invmind = RT(a, RT_INVMIND, i);
-      const T *vr = a.d.vrad + (size_t)i * nsec;
-      T mx = (T)0.0;
-      for (int j = tid; j < nsec; j += blockDim.x) {
-        T vres = P.fast_transport ? (T)((double)vth[j] - vmoy) : vth[j];
-        T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
-        T invdt1 = cs * invmind;
-        T invdt2 = fabs(vr[j]) * invdrad;
-        T invdt3 = fabs(vres) * invdxt;
+    SumAcc<T> v;
+    v.zero();
+    for (int j = tid; j < nsec; j += blockDim.x) v.add(vth[j]);
+    warp_sum(v);
+    if (lane == 0) s_vpart[w] = v;
+  }
+  __syncthreads();
+  if (do_cfl) {
+    if (tid == 0) {
+      SumAcc<T> v = s_vpart[0];
+      for (int k = 1; k < NW; k++) v.merge(s_vpart[k]);
+      const double vmoy = v.value() / (double)nsec;
+      s_vmoy = vmoy;
+      a.d.ring_vmoy[i] = vmoy;
+    }
+    __syncthreads();
+  }
+  const int nbody = do_forces ? s_nbody : 0;
+  const bool cfl_ring = do_cfl && i > 0;
+  RingMean<T> vm;
+  vm.set(do_cfl ? s_vmoy : 0.0);
+  const T rm = RT(a, RT_RMED, i), surf = RT(a, RT_SURF, i);
+  T invdrad = (T)0, invdxt = (T)0, invmind = (T)0;
+  if (cfl_ring) {
+    invdrad = RT(a, RT_INVDRAD, i);
+    invdxt = RT(a, RT_INVDXTHETA_CFL, i);
+    invmind = RT(a, RT_INVMIND, i);
+  }
+  const T *vr = a.d.vrad + (size_t)i * nsec;
+  T *pot = a.d.potential + (size_t)i * nsec;
+  T mx = (T)0.0;
+  const int nchunk = do_forces ? (nbody + 1) >> 1 : 1;
+  for (int ch = 0; ch < nchunk; ch++) {
+    const bool first = (ch == 0);
+    const int b0 = 2 * ch;
+    const bool two = do_forces && b0 + 1 < nbody;
+    T x0 = (T)0, y0 = (T)0, r0 = (T)0, x1 = (T)0, y1 = (T)0, r1 = (T)0;
+    if (do_forces) {
+      x0 = (T)s_body[b0][0];
+      y0 = (T)s_body[b0][1];
+      r0 = (T)s_body[b0][2];
+    }
+    if (two) {
+      x1 = (T)s_body[b0 + 1][0];
+      y1 = (T)s_body[b0 + 1][1];
+      r1 = (T)s_body[b0 + 1][2];
+    }
+    SumAcc<T> fx0, fy0, fx1, fy1;
+    fx0.zero();
+    fy0.zero();
+    fx1.zero();
+    fy1.zero();
+    for (int j = tid; j < nsec; j += blockDim.x) {
+      if (first && cfl_ring) {
+        // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum.
+        // min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
+        // monotonically), so only S_j is formed per cell, with per-ring reciprocals.
+        const T vres = P.fast_transport ? vm.sub_from(vth[j]) : vth[j];
+        const T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
+        const T invdt1 = cs * invmind;
+        const T invdt2 = fabs(vr[j]) * invdrad;
+        const T invdt3 = fabs(vres) * invdxt;
         T dvr = vr[j + nsec] - vr[j];
         T dvt = vth[jp1(j, nsec)] - vth[j];
         if (dvr >= (T)0.0) dvr = (T)1e-10;
         else dvr = -dvr;
         if (dvt >= (T)0.0) dvt = (T)1e-10;
         else dvt = -dvt;
-        T a4 = dvr * invdrad, b4 = dvt * invdxt;
+        const T a4 = dvr * invdrad, b4 = dvt * invdxt;
         T invdt4 = (b4 > a4) ? b4 : a4;
         invdt4 *= (T)(4.0 * CVNR * CVNR);
-        T S = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
+        const T S = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
         mx = (S > mx) ? S : mx;
       }
-      const double smax = -block_min_d(-(double)mx, s_red);
-      mn = CFLSECURITY / sqrt(smax);
-    }
-    if (tid == 0) a.d.ring_newdt[i] = mn;
-  }
-  const int nbody = do_forces ? s_nbody : 0;
-  if (do_forces) {
-    // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0):
-    // per-cell term in T (1/d^3 from rsqrt), ring sums in FP64
-    const T surf = RT(a, RT_SURF, i), rmed = RT(a, RT_RMED, i);
-    for (int b = 0; b < nbody; b++) {
-      const T x = (T)s_body[b][0], y = (T)s_body[b][1], rs2 = (T)s_body[b][2];
-      double fx = 0.0, fy = 0.0;
-      for (int j = tid; j < nsec; j += blockDim.x) {
+      if (do_forces) {
+        // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0):
+        // per-cell terms in T (1/d^3 from rsqrt), compensated or FP64 ring sums
         const T cellmass = surf * dens[j];
-        const T dx = rmed * a.d.cosFt[j] - x;
-        const T dy = rmed * a.d.sinFt[j] - y;
-        const T dist2 = dx * dx + dy * dy + rs2;
-        const T ir = rsqrt(dist2);
-        const T InvDist3 = ir * ir * ir;
-        fx += (double)(cellmass * dx * InvDist3);
-        fy += (double)(cellmass * dy * InvDist3);
-      }
-      fx = block_sum_d(fx, s_red);
-      fy = block_sum_d(fy, s_red);
-      if (tid == 0) {
-        a.d.ring_force[((size_t)i * (FARGO_MAXPL + 1) + b) * 2 + 0] = fx;
-        a.d.ring_force[((size_t)i * (FARGO_MAXPL + 1) + b) * 2 + 1] = fy;
+        const T xc = rm * a.d.cosFt[j], yc = rm * a.d.sinFt[j];
+        {
+          const T dx = xc - x0, dy = yc - y0;
+          const T ir = rsqrt(dx * dx + dy * dy + r0);
+          const T InvDist3 = ir * ir * ir;
+          fx0.add(cellmass * dx * InvDist3);
+          fy0.add(cellmass * dy * InvDist3);
+        }
+        if (two) {
+          const T dx = xc - x1, dy = yc - y1;
+          const T ir = rsqrt(dx * dx + dy * dy + r1);
+          const T InvDist3 = ir * ir * ir;
+          fx1.add(cellmass * dx * InvDist3);
+          fy1.add(cellmass * dy * InvDist3);
+        }
+        if (first && P.nb > 0) {
+          // planet part of the potential (positions at the start of the substep)
+          const T x = rm * a.d.cosP[j], y = rm * a.d.sinP[j];
+          T phi = (T)0.0;
+          for (int k = 0; k < P.nb; k++) {
+            const T xp = (T)s_pot[k][0], yp = (T)s_pot[k][1], mp = (T)s_pot[k][2];
+            const T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
+            const T distancesmooth = sqrt(distance + (T)s_pot[k][3]);
+            T pt = -mp / distancesmooth;
+            if (P.indirect_term) pt += mp * (T)s_pot[k][4] * (x * xp + y * yp);
+            phi += pt;
+          }
+          pot[j] = phi;
+        }
       }
     }
-    // planet part of the potential (positions at the start of the substep)
-    if (P.nb > 0) {
-      const T rm = RT(a, RT_RMED, i);
-      T *pot = a.d.potential + (size_t)i * nsec;
-      for (int j = tid; j < nsec; j += blockDim.x) {
-        const T x = rm * a.d.cosP[j], y = rm * a.d.sinP[j];
-        T phi = (T)0.0;
-        for (int k = 0; k < P.nb; k++) {
-          const T xp = (T)s_pot[k][0], yp = (T)s_pot[k][1], mp = (T)s_pot[k][2];
-          T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
-          T distancesmooth = sqrt(distance + (T)s_pot[k][3]);
-          T pt = -mp / distancesmooth;
-          if (P.indirect_term) pt += mp * (T)s_pot[k][4] * (x * xp + y * yp);
-          phi += pt;
+    if (do_forces) {
+      warp_sum(fx0);
+      warp_sum(fy0);
+      if (two) {
+        warp_sum(fx1);
+        warp_sum(fy1);
+      }
+      if (lane == 0) {
+        s_part[w][2 * b0] = fx0;
+        s_part[w][2 * b0 + 1] = fy0;
+        if (two) {
+          s_part[w][2 * b0 + 2] = fx1;
+          s_part[w][2 * b0 + 3] = fy1;
         }
-        pot[j] = phi;
       }
     }
   }
-  // last block: CFL decision, force totals, planets
+  if (cfl_ring) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const T m2 = __shfl_down_sync(0xffffffffu, mx, o);
+      mx = (m2 > mx) ? m2 : mx;
+    }
+    if (lane == 0) s_mx[w] = mx;
+  }
+  __syncthreads();
+  if (tid < 2 * nbody) {
+    SumAcc<T> f = s_part[0][tid];
+    for (int k = 1; k < NW; k++) f.merge(s_part[k][tid]);
+    a.d.ring_force[(size_t)i * NV + tid] = f.value();
+  }
+  if (cfl_ring && tid == 32) {
+    T m = s_mx[0];
+    for (int k = 1; k < NW; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
+    a.d.ring_smax[i] = (double)m;
+  }
+  // last block: CFL decision, force totals
   __threadfence();
   __syncthreads();
   if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  __shared__ double s_acc[FARGO_MAXPL + 1][2];
-  __shared__ double s_newdt;
-  if (do_cfl) {
-    double mn = 1e30;
-    for (int k = 1 + tid; k < nrad; k += blockDim.x) mn = fmin(mn, __ldcg(a.d.ring_newdt + k));
-    for (int k = tid; k < nrad - 1; k += blockDim.x) {
-      double v0 = __ldcg(a.d.ring_vmoy + k), v1 = __ldcg(a.d.ring_vmoy + k + 1);
-      double d1 = 2.0 * PI * CFLSECURITY / (double)nsec /
-                  fabs(v0 * RT64(a, RT_INVRMED, k) - v1 * RT64(a, RT_INVRMED, k + 1));
-      mn = fmin(mn, d1);
+  __shared__ double s_acc[NV];
+  __shared__ double s_dtc[2];
+  if (do_forces && w < 4) {
+    // force totals, one warp per component; fixed order, deterministic
+    for (int v = w; v < 2 * nbody; v += 4) {
+      double s = 0.0;
+      for (int k = lane; k < nrad; k += 32) s += __ldcg(a.d.ring_force + (size_t)k * NV + v);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) s_acc[v] = s;
     }
-    mn = block_min_d(mn, s_red);
-    if (tid == 0) s_newdt = mn;
   }
-  if (do_forces) {
-    // force totals: block-wide tree over the rings (fixed order, deterministic)
-    for (int b = 0; b < nbody; b++)
-      for (int comp = 0; comp < 2; comp++) {
-        double s = 0.0;
-        for (int k = tid; k < nrad; k += blockDim.x)
-          s += __ldcg(a.d.ring_force + ((size_t)k * (FARGO_MAXPL + 1) + b) * 2 + comp);
-        s = block_sum_d(s, s_red);
-        if (tid == 0) s_acc[b][comp] = s;
-      }
+  if (do_cfl && w == 4) {
+    // largest S over the rings i >= 1, compared as integers (non-negative doubles)
+    long long m = 0;
+    for (int k = 1 + lane; k < nrad; k += 32) m = max(m, __double_as_longlong(__ldcg(a.d.ring_smax + k)));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0) s_dtc[0] = (m > 0) ? CFLSECURITY / sqrt(__longlong_as_double(m)) : 1e30;
+  }
+  if (do_cfl && w == 5) {
+    // shear limit 2 pi C / nsec / |Omega_k - Omega_k+1|: the largest difference
+    // gives the smallest step (NaN differences are skipped, as fmin skips them)
+    long long m = 0;
+    for (int k = lane; k < nrad - 1; k += 32) {
+      const double v0 = __ldcg(a.d.ring_vmoy + k), v1 = __ldcg(a.d.ring_vmoy + k + 1);
+      const double d = fabs(v0 * RT64(a, RT_INVRMED, k) - v1 * RT64(a, RT_INVRMED, k + 1));
+      if (d == d) m = max(m, __double_as_longlong(d));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0) s_dtc[1] = (m > 0) ? 2.0 * PI * CFLSECURITY / (double)nsec / __longlong_as_double(m) : 1e30;
   }
   __syncthreads();
   if (tid == 0) {
@@ -199,7 +275,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     double dt;
     if (do_cfl) {
       const double DeltaT = (a.mode == 1) ? c->DT : c->DT - c->dtemp;
-      double newdt = s_newdt;
+      double newdt = fmin(s_dtc[0], s_dtc[1]);
       if (DeltaT < newdt) newdt = DeltaT;
       double q = DeltaT / newdt;
       int cfl;
@@ -218,11 +294,11 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     }
     if (do_forces) {
       // DiskOnPrimaryAcceleration, ComputeIndirectTerm (src/Pframeforce.cu:86-94)
-      c->ind_x = P.indirect_term ? -s_acc[0][0] : 0.0;
-      c->ind_y = P.indirect_term ? -s_acc[0][1] : 0.0;
+      c->ind_x = P.indirect_term ? -s_acc[0] : 0.0;
+      c->ind_y = P.indirect_term ? -s_acc[1] : 0.0;
       for (int b = 0; b < nbody; b++) {
-        c->accx[b] = s_acc[b][0];
-        c->accy[b] = s_acc[b][1];
+        c->accx[b] = s_acc[2 * b];
+        c->accy[b] = s_acc[2 * b + 1];
       }
     }
     if (do_step) {
@@ -233,20 +309,8 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       c->t_sub = c->PhysicalTime;
     }
   }
-  // sub-Keplerian edge velocities of this substep (ApplySubKeplerianBoundary),
-  // one ring per warp; k_visc_update computes them itself when the sound-speed
-  // ring means change after this kernel (non-reflecting edge, energy equation)
-  if (do_forces && !P.evanescent && (tid == 0 || tid == 32)) {
-    const int ir = tid == 0 ? 0 : nrad - 1;
-    const double r = RT64(a, RT_RMED, ir);
-    const double v = fargo_vkep(P, r, c->PhysicalTime, c->PhysicalTimeInitial, a.d.csmean ? a.d.csmean[ir] : 0.0);
-    if (tid == 0) c->vkep_in = v;
-    else c->vkep_out = v;
-  }
-  // FViscosity profile when it changes in time (alpha viscosity with an energy
-  // equation, or a moving cavity)
+  // FViscosity profile when it changes in time (a moving cavity)
   if (do_forces && P.nu_dynamic) {
-    __syncthreads();
     const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
     for (int k = tid; k < nrad; k += blockDim.x)
       a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
@@ -268,25 +332,29 @@ __global__ void k_planets(DevParams P, Ctl *c) {
 // ComputeSoundSpeed (energy equation) + Make1Dprofile(1) ring means; one CTA per ring.
 template <class T>
 __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
-  __shared__ double s_red[32];
+  __shared__ SumAcc<T> s_red[8];
   const int i = blockIdx.x, nsec = a.P.nsec;
   const double g = a.P.adiabaticindex;
-  double s = 0.0;
+  SumAcc<T> s;
+  s.zero();
   for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
     size_t q = (size_t)i * nsec + j;
     T cs = sqrt((T)(g * (g - 1.0)) * a.d.energy[q] / a.d.dens[q]);
     a.d.cs[q] = cs;
-    s += (double)cs;
+    s.add(cs);
   }
-  s = block_sum_d(s, s_red);
+  const double tot = block_total(s, s_red);
   if (threadIdx.x == 0) {
-    const double m = s / (double)nsec;
+    const double m = tot / (double)nsec;
     a.d.csmean[i] = m;
     // FViscosity reads this ring mean (alpha viscosity): refresh the profile here,
     // where the sound speed changes
     if (a.P.viscosity_alpha) {
+      const DevParams &P = a.P;
       const Ctl *c = a.d.ctl;
-      a.d.nu[i] = (T)fargo_fviscosity(a.P, RT64(a, RT_RMED, i), m, c->PhysicalTime, c->PhysicalTimeInitial);
+      a.d.nu[i] = (T)(P.lambdadoubling == 0.0
+                          ? P.alphaviscosity * m * m * RT64(a, RT_R15, i) * RT64(a, RT_CAVFAC, i)
+                          : fargo_fviscosity(P, RT64(a, RT_RMED, i), m, c->PhysicalTime, c->PhysicalTimeInitial));
     }
   }
 }
@@ -557,10 +625,11 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
   if (!a.P.evanescent && (i == 0 || i == nrad - 1)) {
     // ApplySubKeplerianBoundary (src/SideEuler.cu:296-320), with the current ring
     // mean of the sound speed in the self-gravity form (Make1Dprofile(1))
+    const DevParams &P = a.P;
     const double r = RT64(a, RT_RMED, i);
-    const double v = a.vkep_inline
-                         ? fargo_vkep(a.P, r, c->PhysicalTime, c->PhysicalTimeInitial, a.d.csmean ? a.d.csmean[i] : 0.0)
-                         : (i == 0 ? c->vkep_in : c->vkep_out);
+    const double cm = P.self_gravity ? a.d.csmean[i] : 0.0;
+    const double v = P.lambdadoubling == 0.0 ? sqrt(RT64(a, RT_VKEP2, i) - (P.self_gravity ? r * cm : 0.0))
+                                             : fargo_vkep(P, r, c->PhysicalTime, c->PhysicalTimeInitial, cm);
     a.d.vthetaint[q] = (T)(v - r * c->OmegaFrame);
   }
 }
@@ -933,10 +1002,6 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   const dim3 b2(64, 4);
   const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
   bool joined = true;
-  // the edge speeds precomputed by k_cfl_forces hold unless it does not run here,
-  // or the non-reflecting edge recomputes the sound speed (and its ring means,
-  // which the self-gravity form reads) after it
-  a.vkep_inline = !(which_mask & SUBK_CFL_FORCES) || (P.non_reflecting && P.adiabatic && P.self_gravity);
   if (which_mask & SUBK_CFL_FORCES) {
     // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
     // 3 forces + potential only (no planet advance, no time update)

@@ -50,7 +50,6 @@ struct Ctl {
   double PhysicalTime, PhysicalTimeInitial, OmegaFrame, MassTaper, domega;
   double LostMass;
   double ind_x, ind_y;        // IndirectTerm (Pframeforce.cu:24)
-  double vkep_in, vkep_out;   // ApplySubKeplerianBoundary values of this substep
   double sloppy_dt;
   int cfl, done, err, nsub_dt;
   long long substeps;
@@ -89,19 +88,26 @@ FARGO_HD double fargo_aspect_ratio(const DevParams &P, double r, double t, doubl
   return aspectratio;
 }
 
-// FViscosity  src/Viscosity.cu:33-50; csmean is GLOBAL_bufarray[i] for r = Rmed[i]
-FARGO_HD double fargo_fviscosity(const DevParams &P, double r, double csmean, double t, double t0) {
-  double viscosity, rmin, rmax, scale;
-  viscosity = P.viscosity;
-  if (P.viscosity_alpha) viscosity = P.alphaviscosity * csmean * csmean * pow(r, 1.5);
+// The cavity factor of FViscosity (src/Viscosity.cu:40-48): cavityratio inside the
+// cavity, an exponential ramp across its edge, 1 outside.
+FARGO_HD double fargo_cavity_factor(const DevParams &P, double r, double t, double t0) {
+  double rmin, rmax, scale;
   rmin = P.cavityradius - P.cavitywidth * P.aspectratio;
   rmax = P.cavityradius + P.cavitywidth * P.aspectratio;
   scale = 1.0 + (t - t0) * P.lambdadoubling;
   rmin *= scale;
   rmax *= scale;
-  if (r < rmin) viscosity *= P.cavityratio;
-  if ((r >= rmin) && (r <= rmax)) viscosity *= exp((rmax - r) / (rmax - rmin) * log(P.cavityratio));
-  return viscosity;
+  if (r < rmin) return P.cavityratio;
+  if ((r >= rmin) && (r <= rmax)) return exp((rmax - r) / (rmax - rmin) * log(P.cavityratio));
+  return 1.0;
+}
+
+// FViscosity  src/Viscosity.cu:33-50; csmean is GLOBAL_bufarray[i] for r = Rmed[i].
+// The cavity branches multiply once (by the factor above; a factor 1 is exact).
+FARGO_HD double fargo_fviscosity(const DevParams &P, double r, double csmean, double t, double t0) {
+  double viscosity = P.viscosity;
+  if (P.viscosity_alpha) viscosity = P.alphaviscosity * csmean * csmean * pow(r, 1.5);
+  return viscosity * fargo_cavity_factor(P, r, t, t0);
 }
 
 // Compute_smoothing  src/Force.cu:137-142
@@ -309,12 +315,17 @@ FARGO_HD void fargo_planet_params(Ctl &c, const DevParams &P, double t) {
   c.nbody = nbody;
 }
 
-// Keplerian speed of ApplySubKeplerianBoundary (src/SideEuler.cu:296-320) at ring
-// radius r, before the frame term; csmean is the ring's mean sound speed, which the
-// self-gravity form subtracts (Make1Dprofile(1)).
-FARGO_HD double fargo_vkep(const DevParams &P, double r, double t, double t0, double csmean) {
+// Squared Keplerian speed of ApplySubKeplerianBoundary (src/SideEuler.cu:296-320)
+// at ring radius r, before the self-gravity term.
+FARGO_HD double fargo_vkep2(const DevParams &P, double r, double t, double t0) {
   const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
-  double v2 = 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
+  return 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
+}
+
+// The Keplerian speed itself, before the frame term; csmean is the ring's mean
+// sound speed, which the self-gravity form subtracts (Make1Dprofile(1)).
+FARGO_HD double fargo_vkep(const DevParams &P, double r, double t, double t0, double csmean) {
+  double v2 = fargo_vkep2(P, r, t, t0);
   if (P.self_gravity) v2 -= r * csmean;
   return sqrt(v2);
 }

@@ -45,7 +45,7 @@ DevParams host_dev_params(const fargo_params &p, int nb) {
   d.forced_circular = p.forced_circular;
   d.sloppy_cfl = p.sloppy_cfl;
   d.is_disk = p.is_disk;
-  d.nu_dynamic = (p.viscosity_alpha && p.adiabatic) || p.lambdadoubling != 0.0;
+  d.nu_dynamic = p.lambdadoubling != 0.0;
   d.DT = p.dt;
   d.aspectratio = p.aspectratio;
   d.flaringindex = p.flaringindex;
@@ -364,6 +364,11 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
       T(RT_INVDXTHETA_CFL, i) = 1.0 / dxt;
       T(RT_INVMIND, i) = 1.0 / ((dxt < dxr) ? dxt : dxr);
     }
+    // time-independent parts of the edge speed and of the viscosity profile (the
+    // device evaluates them in full when the aspect ratio changes in time)
+    T(RT_VKEP2, i) = fargo_vkep2(dp, h.Rmed[i], 0.0, 0.0);
+    T(RT_R15, i) = pow(h.Rmed[i], 1.5);
+    T(RT_CAVFAC, i) = fargo_cavity_factor(dp, h.Rmed[i], 0.0, 0.0);
     T(RT_SIGMAMED, i) = at(h.SigmaMed, i);
     T(RT_ENERGYMED, i) = at(h.EnergyMed, i);
     T(RT_COOLTIME, i) = at(h.CoolingTimeMed, i);
