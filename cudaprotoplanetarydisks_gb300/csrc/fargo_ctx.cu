@@ -45,7 +45,8 @@ struct fargo_ctx {
   double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
   double *ring_vmoy = nullptr, *ring_smax = nullptr, *ring_force = nullptr, *lostbydisk = nullptr;
   // self-gravity
-  double2 *spec_r = nullptr, *spec_t = nullptr, *khat_r = nullptr, *khat_t = nullptr, *tw1 = nullptr, *tw0 = nullptr;
+  void *spec_r = nullptr, *spec_t = nullptr, *khat_r = nullptr, *khat_t = nullptr, *tw1 = nullptr, *tw0 = nullptr;
+  double2 *khat64_r = nullptr, *khat64_t = nullptr, *tw1_64 = nullptr, *tw0_64 = nullptr;  // FP64 set-up
   double *kr = nullptr, *kt = nullptr;
   int rad1[16], nst1 = 0, rad0[16], nst0 = 0;
   size_t az_smem = 0;
@@ -134,6 +135,10 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.sg.khat_t = c->khat_t;
   a.sg.tw1 = c->tw1;
   a.sg.tw0 = c->tw0;
+  a.sg.khat64_r = c->khat64_r;
+  a.sg.khat64_t = c->khat64_t;
+  a.sg.tw1_64 = c->tw1_64;
+  a.sg.tw0_64 = c->tw0_64;
   a.sg.kr = c->kr;
   a.sg.kt = c->kt;
   for (int k = 0; k < 16; k++) {
@@ -341,12 +346,26 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     if (c->nst1 < 0 || c->nst0 < 0)
       return set_err(c, FARGO_ERR_INVALID, "self-gravity needs NSEC and 2*NRAD of the form 2^a 3^b");
     host_sg_kernel(p, h, c->dp);
-    if ((rc = dev_alloc(c, (void **)&c->spec_r, (size_t)M * p.nrad * 16))) return rc;
-    if ((rc = dev_alloc(c, (void **)&c->spec_t, (size_t)M * p.nrad * 16))) return rc;
-    if ((rc = dev_alloc(c, (void **)&c->khat_r, (size_t)M * n0 * 16))) return rc;
-    if ((rc = dev_alloc(c, (void **)&c->khat_t, (size_t)M * n0 * 16))) return rc;
-    if ((rc = dev_alloc(c, (void **)&c->tw1, (size_t)p.nsec * 16))) return rc;
-    if ((rc = dev_alloc(c, (void **)&c->tw0, (size_t)n0 * 16))) return rc;
+    // per-step spectra and twiddles in the field type; the FP64 set-up buffers
+    // are the same ones in the FP64 mode
+    const size_t cx = 2 * E;
+    if ((rc = dev_alloc(c, &c->spec_r, (size_t)M * p.nrad * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->spec_t, (size_t)M * p.nrad * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->khat_r, (size_t)M * n0 * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->khat_t, (size_t)M * n0 * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->tw1, (size_t)p.nsec * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->tw0, (size_t)n0 * cx))) return rc;
+    if (E == 8) {
+      c->khat64_r = (double2 *)c->khat_r;
+      c->khat64_t = (double2 *)c->khat_t;
+      c->tw1_64 = (double2 *)c->tw1;
+      c->tw0_64 = (double2 *)c->tw0;
+    } else {
+      if ((rc = dev_alloc(c, (void **)&c->khat64_r, (size_t)M * n0 * 16))) return rc;
+      if ((rc = dev_alloc(c, (void **)&c->khat64_t, (size_t)M * n0 * 16))) return rc;
+      if ((rc = dev_alloc(c, (void **)&c->tw1_64, (size_t)p.nsec * 16))) return rc;
+      if ((rc = dev_alloc(c, (void **)&c->tw0_64, (size_t)n0 * 16))) return rc;
+    }
     if ((rc = dev_alloc(c, (void **)&c->kr, (size_t)n0 * p.nsec * 8))) return rc;
     if ((rc = dev_alloc(c, (void **)&c->kt, (size_t)n0 * p.nsec * 8))) return rc;
     if ((rc = dev_alloc(c, &c->sg_accr, sg * E))) return rc;
@@ -361,8 +380,13 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
       return t;
     };
     std::vector<double> t1 = twiddles(p.nsec), t0 = twiddles(n0);
-    CK(cudaMemcpy(c->tw1, t1.data(), t1.size() * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->tw0, t0.data(), t0.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->tw1_64, t1.data(), t1.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->tw0_64, t0.data(), t0.size() * 8, cudaMemcpyHostToDevice));
+    if (E == 4) {
+      std::vector<float> f1(t1.begin(), t1.end()), f0(t0.begin(), t0.end());
+      CK(cudaMemcpy(c->tw1, f1.data(), f1.size() * 4, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(c->tw0, f0.data(), f0.size() * 4, cudaMemcpyHostToDevice));
+    }
     CK(cudaMemcpy(c->kr, h.Kr.data(), h.Kr.size() * 8, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(c->kt, h.Kt.data(), h.Kt.size() * 8, cudaMemcpyHostToDevice));
     CK(prepare_sg_kernels<T>(p.nsec, n0));

@@ -35,12 +35,16 @@ struct DiskPtrs {
 
 // Self-gravity FFT plan and buffers (fargo_sg.cu)
 struct SgDev {
-  double2 *spec_r, *spec_t;   // work spectra, [m][i], M x nrad
-  double2 *khat_r, *khat_t;   // kernel spectra, [m][k], M x 2 nrad
-  const double2 *tw1, *tw0;   // exp(-2 pi i t / N) for N = nsec and N = 2 nrad
-  const double *kr, *kt;      // real kernel tables, 2 nrad x nsec (set-up only)
+  // per-step buffers, complex of the field type (double2 or float2)
+  void *spec_r, *spec_t;        // work spectra, [m][i], M x nrad
+  void *khat_r, *khat_t;        // kernel spectra, [m][k], M x 2 nrad
+  const void *tw1, *tw0;        // exp(-2 pi i t / N) for N = nsec and N = 2 nrad
+  // set-up, FP64 (the same buffers as above in the FP64 mode)
+  double2 *khat64_r, *khat64_t;
+  const double2 *tw1_64, *tw0_64;
+  const double *kr, *kt;        // real kernel tables, 2 nrad x nsec
   int rad1[16], nst1, rad0[16], nst0;
-  int M;                      // nsec / 2 + 1
+  int M;                        // nsec / 2 + 1
 };
 
 template <class T>
