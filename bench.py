@@ -45,7 +45,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2")
@@ -104,6 +104,13 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the timed region starts once the sampler has written its first line
+        t0 = time.time()
+        while time.time() - t0 < 5.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if not self.proc:
@@ -313,7 +320,10 @@ def run_own(args, world, rank, local):
         a = agg.setdefault(nm, [0.0, 0])
         a[0] += t
         a[1] += 1
-    dom = max(agg.items(), key=lambda kv: kv[1][0]) if agg else ("none", [1.0, 1])
+    # k_planets runs on a second stream beside the hydro kernels (outside a
+    # corotating frame), off the substep's critical path
+    crit = {k: v for k, v in agg.items() if not (k == "k_planets" and not params.corotating)}
+    dom = max(crit.items(), key=lambda kv: kv[1][0]) if crit else ("none", [1.0, 1])
     dom_name, (dom_ms, dom_n) = dom
     dom_avg_ms = dom_ms / dom_n
     alg = kernel_bytes(dom_name, params, 4)
@@ -323,7 +333,8 @@ def run_own(args, world, rank, local):
         "metric": METRIC, "value": f32["value"], "unit": "cell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 fields; f64 CFL decision, force sums, planets, ring means, FARGO split, SG FFT",
+        "dtype": "f32 fields and self-gravity FFT; f64 CFL decision, planets, ring means, FARGO split; "
+                 "compensated f32 (float-float) force and ring sums",
         "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
         "config": config_obj(params, wname, args.config,
                              {"precision": "FP32_BULK", "parallelism": f"replicas x{world}",

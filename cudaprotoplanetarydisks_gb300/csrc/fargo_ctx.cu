@@ -50,6 +50,7 @@ struct fargo_ctx {
   double *kr = nullptr, *kt = nullptr;
   int rad1[16], nst1 = 0, rad0[16], nst0 = 0;
   size_t az_smem = 0;
+  int az_regs = 0;
   double *staging = nullptr;   // FP64 staging buffer of host <-> device transfers
   int launches_per_substep = 0, launches_per_dt = 0;
   std::vector<std::string> kernel_names;
@@ -121,12 +122,22 @@ KArgs<T> make_args(const fargo_ctx *c) {
   d.lostbydisk = c->lostbydisk;
   d.ctl = c->d_ctl;
   a.invdphi = 1.0 / (2.0 * M_PI / (double)c->P.nsec);
+  a.dtheta = 2.0 * FARGO_PI / (double)c->P.nsec;
+  {
+    const double g = c->P.adiabaticindex;
+    a.k64[KC_GM1] = g - 1.0;
+    a.k64[KC_GGM1] = g * (g - 1.0);
+    a.k64[KC_INVDPHI] = a.invdphi;
+    a.k64[KC_SGSELF] = 1.0 * c->dp.sgp_rstep * c->dp.sgp_tstep / c->dp.sgp_eps;
+    for (int k = 0; k < KC_COUNT; k++) a.k32[k] = (float)a.k64[k];
+  }
   if (c->P.nrad >= 3) {
     a.lr01 = log(c->h.Rmed[0] / c->h.Rmed[1]);
     a.lr12 = log(c->h.Rmed[1] / c->h.Rmed[2]);
   }
   a.mode = c->P.sloppy_cfl ? 2 : 0;
   a.az_smem = 0;
+  a.az_regs = c->az_regs;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -201,6 +212,7 @@ int read_ctl(fargo_ctx *c) {
 }
 
 int write_ctl(fargo_ctx *c) {
+  fargo_ctl_mirror(*c->pin_ctl);
   CK(cudaMemcpyAsync(c->d_ctl, c->pin_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
@@ -324,12 +336,20 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     int dev = 0, maxsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    size_t need = (size_t)11 * p.nsec * E;
+    size_t need = (size_t)11 * p.nsec * E, need4 = (size_t)13 * p.nsec * E;
     const char *fg = std::getenv("FARGO_AZ_GLOBAL");  // force the global-memory ring buffers
     const bool force_global = fg && fg[0] == '1';
-    if (!force_global && need + 1024 <= (size_t)maxsm) {
+    const char *fs = std::getenv("FARGO_AZ_GENERIC");  // force the barrier-per-phase kernel
+    const bool force_generic = force_global || (fs && fs[0] == '1');
+    // FP32 fields only: in FP64 the halo recomputation doubles the divisions on
+    // the (narrow) FP64 pipe, and the barrier-per-phase kernel is faster
+    if (!force_generic && E == 4 && p.nsec % 4 == 0 && p.nsec / 4 <= 768 && need4 + 1024 <= (size_t)maxsm) {
+      c->az_smem = need4;
+      c->az_regs = 1;
+      CK(prepare_kernels<T>(need4, 1));
+    } else if (!force_global && need + 1024 <= (size_t)maxsm) {
       c->az_smem = need;
-      CK(prepare_kernels<T>(need));
+      CK(prepare_kernels<T>(need, 0));
     } else {
       c->az_smem = 0;
       if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * 11 * p.nsec * E))) return rc;
@@ -394,6 +414,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     std::vector<double> tab;
     host_ring_table(p, h, c->dp, tab);  // uses only mesh rows at this point
     CK(cudaMemcpy(c->rt64, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
+    if ((rc = upload(c, c->rt, tab.data(), tab.size()))) return rc;
     KArgs<T> a = make_args<T>(c);
     a.P = c->dp;
     launch_sg_kernel_spectra<T>(a, c->stream);

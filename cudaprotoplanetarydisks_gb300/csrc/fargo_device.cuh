@@ -52,9 +52,14 @@ struct KArgs {
   DevParams P;
   DiskPtrs<T> d;
   double invdphi;      // 1.0/(2.0*M_PI/(double)nsec)
+  double dtheta;       // 2.0*PI/(double)nsec
+  // per-launch constants in both precisions (KC_*), read through KC()
+  double k64[8];
+  float k32[8];
   double lr01, lr12;   // log(Rmed[0]/Rmed[1]), log(Rmed[1]/Rmed[2]) for the Qplus extrapolation
   int mode;            // CFL/force kernel mode
   int az_smem;         // azimuthal kernel keeps its ring in shared memory
+  int az_regs;         // register-blocked azimuthal kernel (nsec % 4 == 0)
   unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
   int use_cond;                    // 1: k_end sets the while-loop condition
   SgDev sg;
@@ -139,6 +144,13 @@ struct RingMean<double> {
   __device__ __forceinline__ void set(double m) { hi = m; lo = 0.0; }
   __device__ __forceinline__ double sub_from(double x) const { return x - hi; }
 };
+
+enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_COUNT };
+
+// control-block scalar in T: the FP32 copy for float kernels, the FP64 value otherwise
+#define CTL_T(T, c, field, idx) (sizeof(T) == 4 ? (T)(c)->f32[idx] : (T)(c)->field)
+// launch constant in T
+#define KC(T, a, k) (sizeof(T) == 4 ? (T)(a).k32[k] : (T)(a).k64[k])
 
 #define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 #define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])

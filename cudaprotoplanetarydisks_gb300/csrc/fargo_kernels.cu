@@ -58,9 +58,10 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   __shared__ SumAcc<T> s_part[NW][NV];
   __shared__ SumAcc<T> s_vpart[NW];
   __shared__ T s_mx[NW];
-  __shared__ double s_body[FARGO_MAXPL + 1][3];
-  __shared__ double s_pot[FARGO_MAXPL][5];
+  __shared__ T s_body[FARGO_MAXPL + 1][3];
+  __shared__ T s_pot[FARGO_MAXPL][5];
   __shared__ double s_vmoy;
+  __shared__ RingMean<T> s_vm;
   __shared__ int s_nbody, s_last;
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
@@ -70,17 +71,17 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   if (do_forces) {
     const int nbody = c->nbody;
     if (tid < nbody) {
-      s_body[tid][0] = c->bx[tid];
-      s_body[tid][1] = c->by[tid];
-      s_body[tid][2] = c->brs2[tid];
+      s_body[tid][0] = (T)c->bx[tid];
+      s_body[tid][1] = (T)c->by[tid];
+      s_body[tid][2] = (T)c->brs2[tid];
     }
     if (tid >= 32 && tid < 32 + P.nb) {
       const int k = tid - 32;
-      s_pot[k][0] = c->px[k];
-      s_pot[k][1] = c->py[k];
-      s_pot[k][2] = c->pm[k];
-      s_pot[k][3] = c->ps2[k];
-      s_pot[k][4] = c->pinvd3[k];
+      s_pot[k][0] = (T)c->px[k];
+      s_pot[k][1] = (T)c->py[k];
+      s_pot[k][2] = (T)c->pm[k];
+      s_pot[k][3] = (T)c->ps2[k];
+      s_pot[k][4] = (T)c->pinvd3[k];
     }
     if (tid == 0) s_nbody = nbody;
   }
@@ -101,14 +102,13 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       for (int k = 1; k < NW; k++) v.merge(s_vpart[k]);
       const double vmoy = v.value() / (double)nsec;
       s_vmoy = vmoy;
+      s_vm.set(vmoy);
       a.d.ring_vmoy[i] = vmoy;
     }
     __syncthreads();
   }
   const int nbody = do_forces ? s_nbody : 0;
   const bool cfl_ring = do_cfl && i > 0;
-  RingMean<T> vm;
-  vm.set(do_cfl ? s_vmoy : 0.0);
   const T rm = RT(a, RT_RMED, i), surf = RT(a, RT_SURF, i);
   T invdrad = (T)0, invdxt = (T)0, invmind = (T)0;
   if (cfl_ring) {
@@ -126,14 +126,14 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     const bool two = do_forces && b0 + 1 < nbody;
     T x0 = (T)0, y0 = (T)0, r0 = (T)0, x1 = (T)0, y1 = (T)0, r1 = (T)0;
     if (do_forces) {
-      x0 = (T)s_body[b0][0];
-      y0 = (T)s_body[b0][1];
-      r0 = (T)s_body[b0][2];
+      x0 = s_body[b0][0];
+      y0 = s_body[b0][1];
+      r0 = s_body[b0][2];
     }
     if (two) {
-      x1 = (T)s_body[b0 + 1][0];
-      y1 = (T)s_body[b0 + 1][1];
-      r1 = (T)s_body[b0 + 1][2];
+      x1 = s_body[b0 + 1][0];
+      y1 = s_body[b0 + 1][1];
+      r1 = s_body[b0 + 1][2];
     }
     SumAcc<T> fx0, fy0, fx1, fy1;
     fx0.zero();
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
         // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum.
         // min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
         // monotonically), so only S_j is formed per cell, with per-ring reciprocals.
-        const T vres = P.fast_transport ? vm.sub_from(vth[j]) : vth[j];
+        const T vres = P.fast_transport ? s_vm.sub_from(vth[j]) : vth[j];
         const T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
         const T invdt1 = cs * invmind;
         const T invdt2 = fabs(vr[j]) * invdrad;
@@ -186,11 +186,11 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
           const T x = rm * a.d.cosP[j], y = rm * a.d.sinP[j];
           T phi = (T)0.0;
           for (int k = 0; k < P.nb; k++) {
-            const T xp = (T)s_pot[k][0], yp = (T)s_pot[k][1], mp = (T)s_pot[k][2];
+            const T xp = s_pot[k][0], yp = s_pot[k][1], mp = s_pot[k][2];
             const T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
-            const T distancesmooth = sqrt(distance + (T)s_pot[k][3]);
+            const T distancesmooth = sqrt(distance + s_pot[k][3]);
             T pt = -mp / distancesmooth;
-            if (P.indirect_term) pt += mp * (T)s_pot[k][4] * (x * xp + y * yp);
+            if (P.indirect_term) pt += mp * s_pot[k][4] * (x * xp + y * yp);
             phi += pt;
           }
           pot[j] = phi;
@@ -296,6 +296,8 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       // DiskOnPrimaryAcceleration, ComputeIndirectTerm (src/Pframeforce.cu:86-94)
       c->ind_x = P.indirect_term ? -s_acc[0] : 0.0;
       c->ind_y = P.indirect_term ? -s_acc[1] : 0.0;
+      c->f32[CTL_F_INDX] = (float)c->ind_x;
+      c->f32[CTL_F_INDY] = (float)c->ind_y;
       for (int b = 0; b < nbody; b++) {
         c->accx[b] = s_acc[2 * b];
         c->accy[b] = s_acc[2 * b + 1];
@@ -304,6 +306,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     if (do_step) {
       if (c->err) dt = 0.0;
       c->dt = dt;
+      c->f32[CTL_F_DT] = (float)dt;
       c->dtemp += dt;
       c->nsub_dt += 1;
       c->t_sub = c->PhysicalTime;
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
   s.zero();
   for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
     size_t q = (size_t)i * nsec + j;
-    T cs = sqrt((T)(g * (g - 1.0)) * a.d.energy[q] / a.d.dens[q]);
+    T cs = sqrt(KC(T, a, KC_GGM1) * a.d.energy[q] / a.d.dens[q]);
     a.d.cs[q] = cs;
     s.add(cs);
   }
@@ -365,7 +368,7 @@ __global__ void k_correct_vtheta(KArgs<T> a) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const size_t q = (size_t)i * a.P.nsec + j;
-  a.d.vtheta[q] = a.d.vtheta[q] - (T)a.d.ctl->domega * RT(a, RT_RMED, i);
+  a.d.vtheta[q] = a.d.vtheta[q] - CTL_T(T, a.d.ctl, domega, CTL_F_DOMEGA) * RT(a, RT_RMED, i);
 }
 
 // ---------------------------------------------------------------------------
@@ -516,13 +519,13 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
   const int nrad = P.nrad, nsec = P.nsec;
   if (i >= nrad || j >= nsec) return;
   const Ctl *c = a.d.ctl;
-  const T dt = (T)c->dt, Om = (T)c->OmegaFrame;
-  const T ix = (T)c->ind_x, iy = (T)c->ind_y;
+  const T dt = CTL_T(T, c, dt, CTL_F_DT), Om = CTL_T(T, c, OmegaFrame, CTL_F_OMEGA);
+  const T ix = CTL_T(T, c, ind_x, CTL_F_INDX), iy = CTL_T(T, c, ind_y, CTL_F_INDY);
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens, *E = a.d.energy, *PHI = a.d.potential;
   auto press = [&](size_t k, int ring) -> T {
-    if (P.adiabatic) return (T)(P.adiabaticindex - 1.0) * E[k];
+    if (P.adiabatic) return KC(T, a, KC_GM1) * E[k];
     const T cs = a.d.cs ? a.d.cs[k] : RT(a, RT_CS, ring);
     return D[k] * cs * cs;
   };
@@ -580,7 +583,7 @@ __global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restric
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qp = (size_t)i * nsec + jp, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens;
-  const T invdphi = (T)a.invdphi, onethird = (T)(1.0 / 3.0);
+  const T invdphi = KC(T, a, KC_INVDPHI), onethird = (T)(1.0 / 3.0);
   const T irm = RT(a, RT_INVRMED, i), idrs = RT(a, RT_INVDIFFRSUP, i);
   const T drr = (vr[q + nsec] - vr[q]) * idrs;
   const T dpp = (vt[qp] - vt[q]) * invdphi * irm + (T)0.5 * (vr[q + nsec] + vr[q]) * irm;
@@ -605,11 +608,11 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const Ctl *c = a.d.ctl;
-  const T dt = (T)c->dt;
+  const T dt = CTL_T(T, c, dt, CTL_F_DT);
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm, qp = (size_t)i * nsec + jp;
   const T *D = a.d.dens, *TRR = a.d.taurr, *TRP = a.d.taurp, *TPP = a.d.taupp;
-  const T invdphi = (T)a.invdphi;
+  const T invdphi = KC(T, a, KC_INVDPHI);
   if (i > 0 && i < nrad - 1) {
     a.d.vthetaint[q] += dt * RT(a, RT_INVRMED, i) *
                         ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) * RT(a, RT_INVDIFFRSUP, i) +
@@ -642,7 +645,7 @@ __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
-  const T dt = (T)a.d.ctl->dt;
+  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm, qp = (size_t)i * nsec + jp;
   const T *D = a.d.dens, *VR = a.d.vradint, *VT = a.d.vthetaint;
@@ -687,7 +690,7 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const double g = a.P.adiabaticindex;
-  const T dt = (T)a.d.ctl->dt;
+  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
   const T *D = a.d.dens;
   auto qplus = [&](int ii) -> T {
     const size_t k = (size_t)ii * nsec + j;
@@ -714,12 +717,12 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
   T enew;
   if (!a.P.cooling) {
     T num = dt * qp + ei;
-    T den = (T)1.0 + (T)(g - 1.0) * dt * dv;
+    T den = (T)1.0 + KC(T, a, KC_GM1) * dt * dv;
     enew = num / den;
   } else {
     const T em = RT(a, RT_ENERGYMED, i), sm = RT(a, RT_SIGMAMED, i), ct = RT(a, RT_COOLTIME, i), qm = RT(a, RT_QPLUSMED, i);
     T num = em * dt * D[q] / sm + ct * ei + dt * ct * (qp - qm * D[q] / sm);
-    T den = dt + ct + (T)(g - 1.0) * dt * ct * dv;
+    T den = dt + ct + KC(T, a, KC_GM1) * dt * ct * dv;
     enew = num / den;
   }
   a.d.energy[q] = enew;
@@ -762,7 +765,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = P.nrad, nsec = P.nsec;
   if (i >= nrad || j >= nsec) return;
-  const T dt = (T)a.d.ctl->dt, Om = (T)a.d.ctl->OmegaFrame;
+  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT), Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
   const int jp = jp1(j, nsec);
   const T *D = a.d.dens, *VR = a.d.vrad, *VT = a.d.vtheta, *E = a.d.energy;
   T d[5], rmp[5], rmm[5], tmp[5], tmm[5], e[5], inv[5];
@@ -786,7 +789,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
   const size_t q = (size_t)i * nsec + j;
   const T v0 = VR[q], v1 = VR[q + nsec];
   const T ds0 = qstar_rad(a, d, i, i, v0, dt), ds1 = qstar_rad(a, d, i, i + 1, v1, dt);
-  const T dtheta = (T)(2.0 * PI / (double)nsec);
+  const T dtheta = (T)a.dtheta;
   const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
   T varq_d = (T)0.0;
   auto update = [&](const T *qq, bool keep_varq) -> T {
@@ -921,6 +924,174 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   }
 }
 
+// The same transport in registers, for nsec % 4 == 0: thread t owns cells
+// 4t..4t+3 of the ring and reads halos of two cells on either side from shared
+// memory, so each sweep (slopes, upwind interface values and the update of all
+// transported quantities, which depend only on themselves and on the old density)
+// is one pass without barriers.  The first sweep writes a second copy of the
+// ring, the second sweep (or the only one) stores to global memory at the
+// shifted index.  Same per-cell arithmetic as k_transport_azimuthal.
+namespace {
+template <class T>
+__device__ __forceinline__ void az_load4(const T *__restrict__ p, T *out);
+template <>
+__device__ __forceinline__ void az_load4<float>(const float *__restrict__ p, float *out) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  out[0] = v.x;
+  out[1] = v.y;
+  out[2] = v.z;
+  out[3] = v.w;
+}
+template <>
+__device__ __forceinline__ void az_load4<double>(const double *__restrict__ p, double *out) {
+  const double2 v0 = *reinterpret_cast<const double2 *>(p), v1 = *reinterpret_cast<const double2 *>(p + 2);
+  out[0] = v0.x;
+  out[1] = v0.y;
+  out[2] = v1.x;
+  out[3] = v1.y;
+}
+__device__ __forceinline__ int az_wrap(int j, int n) { return j < 0 ? j + n : (j >= n ? j - n : j); }
+}  // namespace
+
+#define AZ4_NARR 13
+template <class T>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char az_smem[];
+  __shared__ SumAcc<T> s_part[32];
+  __shared__ double s_vc;
+  __shared__ RingMean<T> s_vm;
+  __shared__ T s_vct;
+  __shared__ int s_shift;
+  const DevParams &P = a.P;
+  const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x;
+  const int lane = tid & 31, w = tid >> 5, nw = (blockDim.x + 31) >> 5;
+  const bool own = tid < (nsec >> 2);
+  const int j0 = 4 * tid;
+  T *VT = (T *)az_smem;
+  T *QA = VT + nsec;           // M0 M1 M2 M3 En Dn, nsec each
+  T *QB = QA + 6 * nsec;       // the same after the first sweep
+  const size_t row = (size_t)i * nsec;
+  const T *src[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
+  // ring to shared memory; ComputeAverageThetaVelocitiesKernel
+  SumAcc<T> vs;
+  vs.zero();
+  if (own) {
+    T x[4];
+    az_load4(a.d.vtheta + row + j0, x);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      VT[j0 + c] = x[c];
+      vs.add(x[c]);
+    }
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      if (f == 4 && !P.adiabatic) continue;
+      az_load4(src[f] + row + j0, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) QA[f * nsec + j0 + c] = x[c];
+    }
+  }
+  warp_sum(vs);
+  if (lane == 0) s_part[w] = vs;
+  __syncthreads();
+  if (tid == 0) {
+    SumAcc<T> v = s_part[0];
+    for (int k = 1; k < nw; k++) v.merge(s_part[k]);
+    const double vmed = v.value() / (double)nsec;
+    const double dt = a.d.ctl->dt;
+    // ComputeConstantResidualKernel (FP64 split; Nshift is an integer decision)
+    const double invdt = 1.0 / dt;
+    const double dpinvns = 2.0 * PI / (double)nsec;
+    const double Ntilde = vmed * RT64(a, RT_INVRMED, i) * dt * (double)nsec / 2.0 / PI;
+    const double Nround = floor(Ntilde + 0.5);
+    s_shift = (int)(long)Nround;
+    s_vc = (Ntilde - Nround) * RT64(a, RT_RMED, i) * invdt * dpinvns;
+    s_vct = (T)s_vc;
+    s_vm.set(vmed);
+  }
+  __syncthreads();
+  const T vct = s_vct;
+  const bool split = P.fast_transport;  // NoSplitAdvection == NO
+  const T tdt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
+  const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
+  const T dxrad = RT(a, RT_DRAD, i) * tdt, isurf = RT(a, RT_INVSURF, i);
+  int sh = s_shift % nsec;
+  if (sh < 0) sh += nsec;
+  // VthetaRes at cells j0 .. j0+4
+  T vel[5];
+#pragma unroll
+  for (int c = 0; c < 5; c++) {
+    const T vt = own ? VT[az_wrap(j0 + c, nsec)] : (T)0;
+    T vr = s_vm.sub_from(vt);
+    if (!split) vr = vr + vct;
+    vel[c] = vr;
+  }
+  // one sweep (QuantitiesAdvection) from ring Q; out == nullptr: store to global
+  auto sweep = [&](const T *Q, T *out, bool const_vel) {
+    T v[5];
+#pragma unroll
+    for (int c = 0; c < 5; c++) v[c] = const_vel ? vct : vel[c];
+    // StarThetaKernel / StarThetaKernel2 on the density
+    T d[8], dq[6], ds[5];
+#pragma unroll
+    for (int c = 0; c < 8; c++) d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
+      dq[k] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+    }
+#pragma unroll
+    for (int c = 0; c < 5; c++) {
+      const T ksi = v[c] * tdt;
+      ds[c] = (ksi > (T)0.0) ? d[c + 1] + (dxtheta - ksi) * dq[c] : d[c + 2] - (dxtheta + ksi) * dq[c + 1];
+    }
+    for (int f = 0; f < 6; f++) {
+      if (f == 4 && !P.adiabatic) continue;
+      const T *q = Q + f * nsec;
+      T *dst = f == 0 ? a.d.radmomp
+             : f == 1 ? a.d.radmomm
+             : f == 2 ? a.d.thetamomp
+             : f == 3 ? a.d.thetamomm
+             : f == 4 ? a.d.energy
+                      : a.d.dens;
+      T wv[8], dw[6], sw[5];
+#pragma unroll
+      for (int c = 0; c < 8; c++) wv[c] = q[az_wrap(j0 - 2 + c, nsec)] / (d[c] + (T)1e-20);
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const T dqm = wv[k + 1] - wv[k], dqp = wv[k + 2] - wv[k + 1];
+        dw[k] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+      }
+#pragma unroll
+      for (int c = 0; c < 5; c++) {
+        const T ksi = v[c] * tdt;
+        sw[c] = (ksi > (T)0.0) ? wv[c + 1] + (dxtheta - ksi) * dw[c] : wv[c + 2] - (dxtheta + ksi) * dw[c + 1];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        T varq = dxrad * sw[c] * ds[c] * v[c];
+        varq -= dxrad * sw[c + 1] * ds[c + 1] * v[c + 1];
+        const T nq = q[j0 + c] + varq * isurf;
+        if (out) {
+          out[f * nsec + j0 + c] = nq;
+        } else {
+          // AdvectSHIFT: out[j] = q[(j - Nshift) mod nsec]
+          int jo = j0 + c + sh;
+          if (jo >= nsec) jo -= nsec;
+          dst[row + jo] = nq;
+        }
+      }
+    }
+  };
+  if (split) {
+    if (own) sweep(QA, QB, false);
+    __syncthreads();
+    if (own) sweep(QB, nullptr, true);
+  } else {
+    if (own) sweep(QA, nullptr, false);
+  }
+}
+
 // ComputeVelocitiesKernel src/Kernels.cu:1193-1210 (+ ComputeTemperatureFieldKernel
 // src/Kernels.cu:203-213 when no boundary runs in between).
 template <class T>
@@ -928,7 +1099,7 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
-  const T Om = (T)a.d.ctl->OmegaFrame;
+  const T Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
   const int jm = jm1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens;
@@ -938,9 +1109,9 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
   a.d.vtheta[q] = (a.d.thetamomp[qm] + a.d.thetamomm[q]) / (D[q] + D[qm] + (T)1e-15) / rm - rm * Om;
   if (with_temperature) {
     if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / D[q];
-    else a.d.temperature[q] = (T)(a.P.adiabaticindex - 1.0) * a.d.energy[q] / D[q];
+    else a.d.temperature[q] = KC(T, a, KC_GM1) * a.d.energy[q] / D[q];
   }
-  if (!isfinite((double)D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
+  if (!isfinite(D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
 }
 
 // ComputeTemperatureFieldKernel src/Kernels.cu:203-213 (after a boundary condition)
@@ -950,7 +1121,7 @@ __global__ void k_temperature(KArgs<T> a) {
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const size_t q = (size_t)i * a.P.nsec + j;
   if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / a.d.dens[q];
-  else a.d.temperature[q] = (T)(a.P.adiabaticindex - 1.0) * a.d.energy[q] / a.d.dens[q];
+  else a.d.temperature[q] = KC(T, a, KC_GM1) * a.d.energy[q] / a.d.dens[q];
 }
 
 // End of a substep: LostMass (src/TransportEuler.cu:77), PhysicalTime += dt
@@ -1048,11 +1219,15 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   if (which_mask & SUBK_TRANSPORT) {
     k_transport_radial<T><<<g2, b2, 0, s>>>(a);
     MARK("k_transport_radial");
-    int nt = P.nsec >= 1024 ? 512 : 256;
-    a.az_smem = az_smem_bytes > 0;
-    k_transport_azimuthal<T><<<P.nrad, nt, az_smem_bytes, s>>>(a);
+    if (a.az_regs) {
+      k_transport_azimuthal4<T><<<P.nrad, (P.nsec / 4 + 31) / 32 * 32, az_smem_bytes, s>>>(a);
+    } else {
+      int nt = P.nsec >= 1024 ? 512 : 256;
+      a.az_smem = az_smem_bytes > 0;
+      k_transport_azimuthal<T><<<P.nrad, nt, az_smem_bytes, s>>>(a);
+      a.az_smem = 0;
+    }
     MARK("k_transport_azimuthal");
-    a.az_smem = 0;
     k_velocities<T><<<g2, b2, 0, s>>>(a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
     MARK("k_velocities");
   }
@@ -1116,10 +1291,11 @@ void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
 }
 
 template <class T>
-cudaError_t prepare_kernels(size_t az_smem_bytes) {
-  if (az_smem_bytes > 0)
-    return cudaFuncSetAttribute(k_transport_azimuthal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
-  return cudaSuccess;
+cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
+  if (az_smem_bytes == 0) return cudaSuccess;
+  if (az_regs)
+    return cudaFuncSetAttribute(k_transport_azimuthal4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
+  return cudaFuncSetAttribute(k_transport_azimuthal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
 }
 
 // FP64 host data <-> device fields of type T through an FP64 staging buffer
@@ -1148,6 +1324,6 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
   template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
   template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \
-  template cudaError_t prepare_kernels<T>(size_t);
+  template cudaError_t prepare_kernels<T>(size_t, int);
 INSTANTIATE(double)
 INSTANTIATE(float)

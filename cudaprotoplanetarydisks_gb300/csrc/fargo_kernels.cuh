@@ -60,7 +60,7 @@ void launch_cfl_only(const KArgs<T> &a, cudaStream_t s);
 template <class T>
 void launch_boundaries(const KArgs<T> &a, cudaStream_t s);
 template <class T>
-cudaError_t prepare_kernels(size_t az_smem_bytes);
+cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
 
 // self-gravity (fargo_sg.cu)
 template <class T>

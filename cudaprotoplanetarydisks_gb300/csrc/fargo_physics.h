@@ -72,7 +72,21 @@ struct Ctl {
   // disk accelerations of the bodies (ComputeAccel) and start time of the substep
   double accx[FARGO_MAXPL + 1], accy[FARGO_MAXPL + 1];
   double t_sub;
+  // FP32 copies of the per-substep scalars the field kernels read (CTL_F_*), so
+  // that FP32 kernels convert nothing per thread; refreshed with their FP64 values
+  float f32[8];
 };
+
+enum { CTL_F_DT = 0, CTL_F_OMEGA, CTL_F_INDX, CTL_F_INDY, CTL_F_DOMEGA, CTL_F_COUNT };
+
+// refresh every FP32 copy from its FP64 value
+FARGO_HD void fargo_ctl_mirror(Ctl &c) {
+  c.f32[CTL_F_DT] = (float)c.dt;
+  c.f32[CTL_F_OMEGA] = (float)c.OmegaFrame;
+  c.f32[CTL_F_INDX] = (float)c.ind_x;
+  c.f32[CTL_F_INDY] = (float)c.ind_y;
+  c.f32[CTL_F_DOMEGA] = (float)c.domega;
+}
 
 // AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392
 FARGO_HD double fargo_aspect_ratio(const DevParams &P, double r, double t, double t0) {
@@ -356,4 +370,6 @@ FARGO_HD void fargo_planets_substep(Ctl &c, const DevParams &P, double dt, doubl
   }
   fargo_rotate_psys(c, c.OmegaFrame * dt);
   fargo_planet_params(c, P, t + dt);
+  c.f32[CTL_F_OMEGA] = (float)c.OmegaFrame;
+  c.f32[CTL_F_DOMEGA] = (float)c.domega;
 }

@@ -54,58 +54,105 @@ __device__ __forceinline__ V cconj(V a) {
   return mk2(a.x, -a.y);
 }
 
-// Forward Stockham FFT of length N on shared buffers d0 -> (d0|d1); returns the
-// buffer holding the result.  tw[t] = exp(-2 pi i t / N).
-template <class R>
-__device__ typename Vec2<R>::t *fft_fwd(typename Vec2<R>::t *d0, typename Vec2<R>::t *d1, int N, const int *rad,
-                                        int nst, const typename Vec2<R>::t *__restrict__ tw) {
-  using V = typename Vec2<R>::t;
+// DFT of length RAD in registers (forward, exp(-2 pi i / RAD)).
+template <int RAD, class V>
+__device__ __forceinline__ void butterfly(V *v) {
+  using R = decltype(v[0].x);
+  if (RAD == 2) {
+    const V a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if (RAD == 3) {
+    const R h = (R)0.86602540378443864676;  // sqrt(3)/2
+    const V t1 = cadd(v[1], v[2]);
+    const V t2 = mk2(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
+    const V t3 = csub(v[1], v[2]);
+    v[0] = cadd(v[0], t1);
+    v[1] = mk2(t2.x + h * t3.y, t2.y - h * t3.x);  // t2 - i h t3
+    v[2] = mk2(t2.x - h * t3.y, t2.y + h * t3.x);  // t2 + i h t3
+  } else if (RAD == 4) {
+    const V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    const V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = mk2(d02.x + d13.y, d02.y - d13.x);  // d02 - i d13
+    v[3] = mk2(d02.x - d13.y, d02.y + d13.x);  // d02 + i d13
+  } else {  // RAD == 8: two DFT4 of the even and odd points, then W8^k
+    V e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    butterfly<4>(e);
+    butterfly<4>(o);
+    const R h = (R)0.70710678118654752440;  // 1/sqrt(2)
+    const V w1 = mk2((o[1].x + o[1].y) * h, (o[1].y - o[1].x) * h);    // (1 - i)/sqrt2 o1
+    const V w2 = mk2(o[2].y, -o[2].x);                                  // -i o2
+    const V w3 = mk2((o[3].y - o[3].x) * h, -(o[3].y + o[3].x) * h);   // -(1 + i)/sqrt2 o3
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], w1);
+    v[5] = csub(e[1], w1);
+    v[2] = cadd(e[2], w2);
+    v[6] = csub(e[2], w2);
+    v[3] = cadd(e[3], w3);
+    v[7] = csub(e[3], w3);
+  }
+}
+
+// One Stockham stage of radix RAD over src (length N, Ns = product of the
+// earlier radices): butterflies j = lt, lt + G, ...; out(index, value) stores.
+template <int RAD, class V, class Out>
+__device__ __forceinline__ void fft_stage(const V *src, int N, int Ns, const V *tw, int lt, int G, Out out) {
+  const int NR = N / RAD, tws = N / (Ns * RAD);
+  for (int j = lt; j < NR; j += G) {
+    const int jj = j % Ns;
+    V v[RAD];
+#pragma unroll
+    for (int r = 0; r < RAD; r++) {
+      v[r] = src[j + r * NR];
+      if (r > 0) v[r] = cmul(v[r], tw[r * jj * tws]);
+    }
+    butterfly<RAD>(v);
+    const int idxD = (j / Ns) * Ns * RAD + jj;
+#pragma unroll
+    for (int r = 0; r < RAD; r++) out(idxD + r * Ns, v[r]);
+  }
+}
+
+// Forward Stockham FFT of length N from d0, ping-ponging with d1, by the G
+// threads lt = 0..G-1 of a group (every thread of the CTA calls it: one barrier
+// per stage).  tw[t] = exp(-2 pi i t / N).  The last stage hands its outputs to
+// last(index, value, free buffer); the default stores them there.  Returns the
+// buffer the last stage wrote to when last stores into the free buffer.
+template <class V, class Last>
+__device__ V *fft_run(V *d0, V *d1, int N, const int *rad, int nst, const V *tw, int lt, int G, Last last) {
   int Ns = 1;
   for (int s = 0; s < nst; s++) {
-    const int R_ = rad[s], NR = N / R_, tws = N / (Ns * R_);
-    for (int j = threadIdx.x; j < NR; j += blockDim.x) {
-      const int jj = j % Ns;
-      V v[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) {
-        if (r < R_) {
-          v[r] = d0[j + r * NR];
-          if (r > 0) v[r] = cmul(v[r], __ldg(tw + r * jj * tws));
-        }
-      }
-      if (R_ == 2) {
-        V a = v[0], b = v[1];
-        v[0] = cadd(a, b);
-        v[1] = csub(a, b);
-      } else if (R_ == 4) {
-        V s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-        V s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
-        v[0] = cadd(s02, s13);
-        v[2] = csub(s02, s13);
-        v[1] = mk2(d02.x + d13.y, d02.y - d13.x);  // d02 - i d13
-        v[3] = mk2(d02.x - d13.y, d02.y + d13.x);  // d02 + i d13
-      } else {  // R_ == 3
-        const R h = (R)0.86602540378443864676;  // sqrt(3)/2
-        V t1 = cadd(v[1], v[2]);
-        V t2 = mk2(v[0].x - (R)0.5 * t1.x, v[0].y - (R)0.5 * t1.y);
-        V t3 = csub(v[1], v[2]);
-        v[0] = cadd(v[0], t1);
-        v[1] = mk2(t2.x + h * t3.y, t2.y - h * t3.x);  // t2 - i h t3
-        v[2] = mk2(t2.x - h * t3.y, t2.y + h * t3.x);  // t2 + i h t3
-      }
-      const int idxD = (j / Ns) * Ns * R_ + jj;
-#pragma unroll
-      for (int r = 0; r < 4; r++)
-        if (r < R_) d1[idxD + r * Ns] = v[r];
+    const int R = rad[s];
+    V *dst = d1;
+    if (s == nst - 1) {
+      auto out = [&](int k, V v) { last(k, v, dst); };
+      if (R == 8) fft_stage<8>(d0, N, Ns, tw, lt, G, out);
+      else if (R == 4) fft_stage<4>(d0, N, Ns, tw, lt, G, out);
+      else if (R == 2) fft_stage<2>(d0, N, Ns, tw, lt, G, out);
+      else fft_stage<3>(d0, N, Ns, tw, lt, G, out);
+    } else {
+      auto out = [&](int k, V v) { dst[k] = v; };
+      if (R == 8) fft_stage<8>(d0, N, Ns, tw, lt, G, out);
+      else if (R == 4) fft_stage<4>(d0, N, Ns, tw, lt, G, out);
+      else if (R == 2) fft_stage<2>(d0, N, Ns, tw, lt, G, out);
+      else fft_stage<3>(d0, N, Ns, tw, lt, G, out);
     }
     __syncthreads();
     V *t = d0;
     d0 = d1;
     d1 = t;
-    Ns *= R_;
+    Ns *= R;
   }
   return d0;
 }
+
+template <class V>
+struct StoreFree {
+  __device__ __forceinline__ void operator()(int k, V v, V *dst) const { dst[k] = v; }
+};
 
 // Splits the FFT Z of two packed real rows into the modes m < M of each:
 // X_r = (Z[m] + conj Z[N-m]) / 2, X_t = (Z[m] - conj Z[N-m]) / (2i)
@@ -121,11 +168,18 @@ __device__ __forceinline__ void unpack_pair(const V *Z, int m, int N, V &xr, V &
 
 int sg_radices(int n, int *rad) {
   int k = 0;
-  while (n % 4 == 0) { rad[k++] = 4; n /= 4; }
-  while (n % 2 == 0) { rad[k++] = 2; n /= 2; }
-  while (n % 3 == 0) { rad[k++] = 3; n /= 3; }
-  if (n != 1 || k > 16) return -1;
+  while (n % 8 == 0 && k < 16) { rad[k++] = 8; n /= 8; }
+  while (n % 4 == 0 && k < 16) { rad[k++] = 4; n /= 4; }
+  while (n % 2 == 0 && k < 16) { rad[k++] = 2; n /= 2; }
+  while (n % 3 == 0 && k < 16) { rad[k++] = 3; n /= 3; }
+  if (n != 1) return -1;
   return k;
+}
+
+// threads per FFT group for length n: one radix-8 butterfly per thread and stage
+static inline int sg_group(int n) {
+  int g = (n / 8 + 31) / 32 * 32;
+  return g < 32 ? 32 : (g > 256 ? 256 : g);
 }
 
 // Azimuthal forward transform of each ring with the ComputeFFTKernel packing
@@ -135,17 +189,20 @@ template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  V *b0 = (V *)sg_raw, *b1 = b0 + a.P.nsec;
-  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad;
-  const T f = (T)RT64(a, RT_SGSQRT, i), rm = (T)RT64(a, RT_RMED, i), r0 = (T)RT64(a, RT_RMED, 0);
-  for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
+  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x, G = blockDim.x;
+  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + nsec;
+  const V *twg = (const V *)a.sg.tw1;
+  const T f = RT(a, RT_SGSQRT, i), rm = RT(a, RT_RMED, i), r0 = RT(a, RT_RMED, 0);
+#pragma unroll 4
+  for (int j = tid; j < nsec; j += G) {
+    tw[j] = twg[j];
     const T var = a.d.dens[(size_t)i * nsec + j] * f;
     b0[j] = mk2(var, var * rm / r0);
   }
   __syncthreads();
-  V *Z = fft_fwd<T>(b0, b1, nsec, a.sg.rad1, a.sg.nst1, (const V *)a.sg.tw1);
+  V *Z = fft_run(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, G, StoreFree<V>());
   V *out_r = (V *)a.sg.spec_r, *out_t = (V *)a.sg.spec_t;
-  for (int m = threadIdx.x; m < a.sg.M; m += blockDim.x) {
+  for (int m = tid; m < a.sg.M; m += G) {
     V xr, xt;
     unpack_pair(Z, m, nsec, xr, xt);
     out_r[(size_t)m * nrad + i] = xr;
@@ -153,47 +210,55 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
   }
 }
 
-// Radial transforms, one CTA per azimuthal mode m: for (S_r, K^r) and
-// (S_theta, K^theta), forward transform of the zero-padded column, product
-// -G K^ S^ (ComputeConvolutionKernel src/Kernels.cu:871-890), inverse transform,
-// rows < nrad stored back in place.
+// Radial transforms, one CTA per azimuthal mode m, one thread group per field:
+// (S_r, K^r) and (S_theta, K^theta) side by side.  Forward transform of the
+// zero-padded column; its last stage forms -G K^ S^ (ComputeConvolutionKernel
+// src/Kernels.cu:871-890), conjugated so that the forward routine runs the
+// inverse; the inverse's last stage stores rows < nrad back in place.
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int m = blockIdx.x, n0 = 2 * a.P.nrad, nrad = a.P.nrad;
-  V *b0 = (V *)sg_raw, *b1 = b0 + n0;
-  const V *tw = (const V *)a.sg.tw0;
-  for (int f = 0; f < 2; f++) {
-    const V *kh = (const V *)(f == 0 ? a.sg.khat_r : a.sg.khat_t) + (size_t)m * n0;
-    V *col = (V *)(f == 0 ? a.sg.spec_r : a.sg.spec_t) + (size_t)m * nrad;
-    for (int k = threadIdx.x; k < n0; k += blockDim.x) b0[k] = (k < nrad) ? col[k] : mk2((T)0, (T)0);
-    __syncthreads();
-    V *X = fft_fwd<T>(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw);
-    V *Y = (X == b0) ? b1 : b0;
-    for (int k = threadIdx.x; k < n0; k += blockDim.x) {
-      const V K = kh[k], S = X[k];
-      // -G*(K S); stored conjugated so that the forward routine runs the inverse
-      const T gx = (T)-1.0 * (K.x * S.x - K.y * S.y);
-      const T gy = (T)-1.0 * (K.x * S.y + K.y * S.x);
-      Y[k] = mk2(gx, -gy);
-    }
-    __syncthreads();
-    V *Z = fft_fwd<T>(Y, X, n0, a.sg.rad0, a.sg.nst0, tw);
-    for (int k = threadIdx.x; k < nrad; k += blockDim.x) col[k] = cconj(Z[k]);
-    __syncthreads();
+  const int G = blockDim.x >> 1, g = threadIdx.x >= G ? 1 : 0, lt = threadIdx.x - g * G;
+  V *tw = (V *)sg_raw;
+  V *b0 = tw + n0 + g * 3 * n0, *b1 = b0 + n0, *K = b1 + n0;
+  const V *twg = (const V *)a.sg.tw0;
+  const V *kh = (const V *)(g == 0 ? a.sg.khat_r : a.sg.khat_t) + (size_t)m * n0;
+  V *col = (V *)(g == 0 ? a.sg.spec_r : a.sg.spec_t) + (size_t)m * nrad;
+#pragma unroll 4
+  for (int k = threadIdx.x; k < n0; k += blockDim.x) tw[k] = twg[k];
+#pragma unroll 4
+  for (int k = lt; k < n0; k += G) {
+    K[k] = kh[k];
+    b0[k] = (k < nrad) ? col[k] : mk2((T)0, (T)0);
   }
+  __syncthreads();
+  V *X = fft_run(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V S, V *dst) {
+    const V Kk = K[k];
+    const T gx = (T)-1.0 * (Kk.x * S.x - Kk.y * S.y);
+    const T gy = (T)-1.0 * (Kk.x * S.y + Kk.y * S.x);
+    dst[k] = mk2(gx, -gy);
+  });
+  V *Y = (X == b0) ? b1 : b0;
+  fft_run(X, Y, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V z, V *) {
+    if (k < nrad) col[k] = cconj(z);
+  });
 }
 
-// Inverse azimuthal transform of each ring + ComputeSgAccKernel (src/Kernels.cu:893-912).
+// Inverse azimuthal transform of each ring; its last stage applies
+// ComputeSgAccKernel (src/Kernels.cu:893-912).
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M;
-  V *b0 = (V *)sg_raw, *b1 = b0 + nsec;
+  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
+  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + nsec;
+  const V *twg = (const V *)a.sg.tw1;
   const V *spr = (const V *)a.sg.spec_r, *spt = (const V *)a.sg.spec_t;
-  for (int m = threadIdx.x; m < nsec; m += blockDim.x) {
+#pragma unroll 4
+  for (int m = tid; m < nsec; m += G) {
+    tw[m] = twg[m];
     V hr, ht;
     if (m < M) {
       hr = spr[(size_t)m * nrad + i];
@@ -206,28 +271,30 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
     b0[m] = mk2(hr.x - ht.y, -(hr.y + ht.x));
   }
   __syncthreads();
-  V *Z = fft_fwd<T>(b0, b1, nsec, a.sg.rad1, a.sg.nst1, (const V *)a.sg.tw1);
-  const T normr = (T)RT64(a, RT_SGNORMR, i), normt = (T)RT64(a, RT_SGNORMT, i);
-  const T selfc = (T)a.P.sgp_rstep, tstep = (T)a.P.sgp_tstep, eps = (T)a.P.sgp_eps;
-  for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
-    const V z = cconj(Z[j]);
-    const size_t q = (size_t)i * nsec + j;
+  const T normr = RT(a, RT_SGNORMR, i), normt = RT(a, RT_SGNORMT, i);
+  const T selfc = (T)a.P.sgp_rstep, tstep = (T)a.P.sgp_tstep, eps = (T)a.P.sgp_eps, sgself = KC(T, a, KC_SGSELF);
+  const size_t row = (size_t)i * nsec;
+  fft_run(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, G, [&](int j, V v, V *) {
+    const V z = cconj(v);
+    const size_t q = row + j;
     a.d.sg_acct[q] = z.y * normt;
     T accr = z.x * normr;
-    accr += (T)1.0 * a.d.dens[q] * selfc * tstep / eps;
+    // FP64: the reference's expression; FP32: its constant factor folded once
+    accr += sizeof(T) == 8 ? (T)1.0 * a.d.dens[q] * selfc * tstep / eps : a.d.dens[q] * sgself;
     a.d.sg_accr[q] = accr;
-  }
+  });
 }
 
 template <class T>
 void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
-  const int nsec = a.P.nsec, nrad = a.P.nrad;
+  const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
   const size_t vs = 2 * sizeof(T);
-  k_sg_rows_fwd<T><<<nrad, 256, 2 * nsec * vs, s>>>(a);
+  k_sg_rows_fwd<T><<<nrad, 256, 3 * nsec * vs, s>>>(a);
   probe_mark(s, "k_sg_rows_fwd");
-  k_sg_cols<T><<<a.sg.M, 256, 2 * 2 * nrad * vs, s>>>(a);
+  const int gc = sg_group(n0) < 128 ? sg_group(n0) : 128;
+  k_sg_cols<T><<<a.sg.M, 2 * gc, 7 * n0 * vs, s>>>(a);
   probe_mark(s, "k_sg_cols");
-  k_sg_rows_inv<T><<<nrad, 256, 2 * nsec * vs, s>>>(a);
+  k_sg_rows_inv<T><<<nrad, 256, 3 * nsec * vs, s>>>(a);
   probe_mark(s, "k_sg_rows_inv");
 }
 
@@ -241,7 +308,8 @@ __global__ void __launch_bounds__(256) k_sg_setup_rows(SgDev sg, int nsec, int n
   for (int j = threadIdx.x; j < nsec; j += blockDim.x)
     b0[j] = make_double2(sg.kr[(size_t)i * nsec + j], sg.kt[(size_t)i * nsec + j]);
   __syncthreads();
-  double2 *Z = fft_fwd<double>(b0, b1, nsec, sg.rad1, sg.nst1, sg.tw1_64);
+  double2 *Z = fft_run(b0, b1, nsec, sg.rad1, sg.nst1, sg.tw1_64, (int)threadIdx.x, (int)blockDim.x,
+                       StoreFree<double2>());
   for (int m = threadIdx.x; m < sg.M; m += blockDim.x) {
     double2 xr, xt;
     unpack_pair(Z, m, nsec, xr, xt);
@@ -259,7 +327,8 @@ __global__ void __launch_bounds__(256) k_sg_setup_cols(SgDev sg, int n0) {
     double2 *kh = (f == 0 ? sg.khat64_r : sg.khat64_t) + (size_t)m * n0;
     for (int k = threadIdx.x; k < n0; k += blockDim.x) b0[k] = kh[k];
     __syncthreads();
-    double2 *X = fft_fwd<double>(b0, b1, n0, sg.rad0, sg.nst0, sg.tw0_64);
+    double2 *X = fft_run(b0, b1, n0, sg.rad0, sg.nst0, sg.tw0_64, (int)threadIdx.x, (int)blockDim.x,
+                         StoreFree<double2>());
     for (int k = threadIdx.x; k < n0; k += blockDim.x) kh[k] = X[k];
     __syncthreads();
   }
@@ -287,7 +356,7 @@ template <class T>
 cudaError_t prepare_sg_kernels(int nsec, int n0) {
   cudaError_t e;
   const int vs = 2 * sizeof(T);
-  const int rows = 2 * nsec * vs, cols = 2 * n0 * vs;
+  const int rows = 3 * nsec * vs, cols = 7 * n0 * vs;
   const int rows64 = 2 * nsec * (int)sizeof(double2), cols64 = 2 * n0 * (int)sizeof(double2);
   if ((e = cudaFuncSetAttribute(k_sg_rows_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sg_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;

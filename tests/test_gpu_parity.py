@@ -121,20 +121,48 @@ def test_no_planet():
     disk.close()
 
 
+def _disk_with_env(params, planets, prec, env):
+    saved = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return fg.Disk(params, planets, prec)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
 @pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_AZ_GLOBAL"])
 def test_code_paths_are_bitwise_identical(env):
-    # the conditional-graph DT loop vs the host loop, and the shared-memory vs
-    # global-memory azimuthal ring buffers run the same arithmetic
+    # the conditional-graph DT loop vs the host loop; the shared-memory vs the
+    # global-memory ring buffers of the barrier-per-phase azimuthal kernel
     params, planets = small("c2")
-    a = fg.Disk(params, planets, fg.FARGO_FP64)
-    os.environ[env] = "1"
-    try:
-        b = fg.Disk(params, planets, fg.FARGO_FP64)
-    finally:
-        del os.environ[env]
+    base = {} if env == "FARGO_NO_GRAPH" else {"FARGO_AZ_GENERIC": "1"}
+    a = _disk_with_env(params, planets, fg.FARGO_FP64, base)
+    b = _disk_with_env(params, planets, fg.FARGO_FP64, {**base, env: "1"})
     for _ in range(2):
         assert a.step_DT() == b.step_DT()
     for name in ("dens", "vrad", "vtheta"):
         assert np.array_equal(a.field(name), b.field(name))
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2", "c3"])
+def test_register_azimuthal_kernel_matches_barrier_kernel(cfg):
+    # the register-blocked azimuthal transport (nsec % 4 == 0) runs the per-cell
+    # arithmetic of the barrier-per-phase kernel; only the ring-mean summation
+    # order differs, so the FP64 fields agree to a few ulps per substep
+    params, planets = small(cfg)
+    assert params.nsec % 4 == 0
+    a = fg.Disk(params, planets, fg.FARGO_FP64)
+    b = _disk_with_env(params, planets, fg.FARGO_FP64, {"FARGO_AZ_GENERIC": "1"})
+    for _ in range(2):
+        assert a.step_DT() == b.step_DT()
+    names = ("dens", "vrad", "vtheta") + (("energy",) if params.adiabatic else ())
+    for name in names:
+        assert rel_linf(a.field(name), b.field(name)) < 1e-11, name
     a.close()
     b.close()
