@@ -123,12 +123,14 @@ KArgs<T> make_args(const fargo_ctx *c) {
   d.ctl = c->d_ctl;
   a.invdphi = 1.0 / (2.0 * M_PI / (double)c->P.nsec);
   a.dtheta = 2.0 * FARGO_PI / (double)c->P.nsec;
+  a.inv_nsec = 1.0 / (double)c->P.nsec;
   {
     const double g = c->P.adiabaticindex;
     a.k64[KC_GM1] = g - 1.0;
     a.k64[KC_GGM1] = g * (g - 1.0);
     a.k64[KC_INVDPHI] = a.invdphi;
     a.k64[KC_SGSELF] = 1.0 * c->dp.sgp_rstep * c->dp.sgp_tstep / c->dp.sgp_eps;
+    a.k64[KC_DTHETA] = a.dtheta;
     for (int k = 0; k < KC_COUNT; k++) a.k32[k] = (float)a.k64[k];
   }
   if (c->P.nrad >= 3) {
@@ -352,6 +354,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
       CK(prepare_kernels<T>(need, 0));
     } else {
       c->az_smem = 0;
+      CK(prepare_kernels<T>(0, 0));
       if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * 11 * p.nsec * E))) return rc;
     }
   }

@@ -53,6 +53,7 @@ struct KArgs {
   DiskPtrs<T> d;
   double invdphi;      // 1.0/(2.0*M_PI/(double)nsec)
   double dtheta;       // 2.0*PI/(double)nsec
+  double inv_nsec;     // 1.0/nsec
   // per-launch constants in both precisions (KC_*), read through KC()
   double k64[8];
   float k32[8];
@@ -145,7 +146,7 @@ struct RingMean<double> {
   __device__ __forceinline__ double sub_from(double x) const { return x - hi; }
 };
 
-enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_COUNT };
+enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_DTHETA, KC_COUNT };
 
 // control-block scalar in T: the FP32 copy for float kernels, the FP64 value otherwise
 #define CTL_T(T, c, field, idx) (sizeof(T) == 4 ? (T)(c)->f32[idx] : (T)(c)->field)

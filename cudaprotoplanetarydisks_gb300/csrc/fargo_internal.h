@@ -31,6 +31,7 @@ enum RingTab {
   RT_VKEP2,        // squared sub-Keplerian edge speed before the self-gravity term (t = t0)
   RT_R15,          // pow(Rmed, 1.5) of the alpha viscosity
   RT_CAVFAC,       // cavity factor of FViscosity (t = t0)
+  RT_AZSHIFT,      // nsec/(2 pi Rmed): the FARGO shift per unit (Vtheta mean x dt)
   RT_COUNT
 };
 

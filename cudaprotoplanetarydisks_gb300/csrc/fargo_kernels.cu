@@ -47,6 +47,24 @@ __device__ __forceinline__ int jp1(int j, int n) { return j == n - 1 ? 0 : j + 1
 // mode 0: full substep start.  mode 1: CFL only (sloppy CFL at the DT start, or
 // the ConditionCFL entry point).  mode 2: forces, dt = sloppy_dt.  mode 3: forces
 // and potential only.
+// Total over the rings of component v of the per-ring force partials (SumAcc<T>
+// stored in 8 bytes), summed by one warp in a fixed order; valid in lane 0.
+template <class T>
+__device__ __forceinline__ double ring_total(const double *ring_force, int nrad, int nv, int v, int lane) {
+  static_assert(sizeof(SumAcc<T>) == 8, "8-byte ring partials");
+  SumAcc<T> s;
+  s.zero();
+#pragma unroll 8
+  for (int k = lane; k < nrad; k += 32) {
+    const double d = __ldcg(ring_force + (size_t)k * nv + v);
+    SumAcc<T> x;
+    memcpy(&x, &d, 8);
+    s.merge(x);
+  }
+  warp_sum(s);
+  return s.value();
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   constexpr int NW = 8;                       // warps of the 256-thread CTA
@@ -63,14 +81,20 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   __shared__ double s_vmoy;
   __shared__ RingMean<T> s_vm;
   __shared__ int s_nbody, s_last;
+  __shared__ double s_ctl[5];  // DT, dtemp, sloppy_dt, PhysicalTime, err (read before any write)
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
   const bool do_step = (a.mode == 0 || a.mode == 2);
+  // the control scalars the last block's decision reads, fetched up front by
+  // every block so that the last one has them at hand
+  if (tid >= 64 && tid < 69) {
+    const int k = tid - 64;
+    s_ctl[k] = k == 0 ? c->DT : k == 1 ? c->dtemp : k == 2 ? c->sloppy_dt : k == 3 ? c->PhysicalTime : (double)c->err;
+  }
   // planet parameters of this substep, computed after the previous planet update
   // (fargo_planet_params): bodies feeling the disk and the planets' potential terms
   if (do_forces) {
-    const int nbody = c->nbody;
-    if (tid < nbody) {
+    if (tid <= FARGO_MAXPL) {
       s_body[tid][0] = (T)c->bx[tid];
       s_body[tid][1] = (T)c->by[tid];
       s_body[tid][2] = (T)c->brs2[tid];
@@ -83,7 +107,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       s_pot[k][3] = (T)c->ps2[k];
       s_pot[k][4] = (T)c->pinvd3[k];
     }
-    if (tid == 0) s_nbody = nbody;
+    if (tid == 0) s_nbody = c->nbody;
   }
   const T *dens = a.d.dens + (size_t)i * nsec;
   const T *vth = a.d.vtheta + (size_t)i * nsec;
@@ -100,10 +124,11 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     if (tid == 0) {
       SumAcc<T> v = s_vpart[0];
       for (int k = 1; k < NW; k++) v.merge(s_vpart[k]);
-      const double vmoy = v.value() / (double)nsec;
+      const double vmoy = sizeof(T) == 8 ? v.value() / (double)nsec : v.value() * a.inv_nsec;
       s_vmoy = vmoy;
       s_vm.set(vmoy);
-      a.d.ring_vmoy[i] = vmoy;
+      // ring angular velocity of the shear limit (ConditionCFLKernel2D2)
+      a.d.ring_vmoy[i] = vmoy * RT64(a, RT_INVRMED, i);
     }
     __syncthreads();
   }
@@ -223,9 +248,10 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   }
   __syncthreads();
   if (tid < 2 * nbody) {
+    // ring partial sums stay SumAcc<T> (8 bytes either way) until the totals
     SumAcc<T> f = s_part[0][tid];
     for (int k = 1; k < NW; k++) f.merge(s_part[k][tid]);
-    a.d.ring_force[(size_t)i * NV + tid] = f.value();
+    reinterpret_cast<SumAcc<T> *>(a.d.ring_force)[(size_t)i * NV + tid] = f;
   }
   if (cfl_ring && tid == 32) {
     T m = s_mx[0];
@@ -241,18 +267,16 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   __threadfence();
   __shared__ double s_acc[NV];
   __shared__ double s_dtc[2];
-  if (do_forces && w < 4) {
-    // force totals, one warp per component; fixed order, deterministic
-    for (int v = w; v < 2 * nbody; v += 4) {
-      double s = 0.0;
-      for (int k = lane; k < nrad; k += 32) s += __ldcg(a.d.ring_force + (size_t)k * NV + v);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-      if (lane == 0) s_acc[v] = s;
-    }
+  if (do_forces && w < 2) {
+    // the disk's force on the star, one warp per component (fixed order,
+    // deterministic); the planets' totals are formed by k_planets
+    const double tot = ring_total<T>(a.d.ring_force, nrad, NV, w, lane);  // valid in lane 0
+    if (lane == 0) s_acc[w] = tot;
   }
   if (do_cfl && w == 4) {
     // largest S over the rings i >= 1, compared as integers (non-negative doubles)
     long long m = 0;
+#pragma unroll 8
     for (int k = 1 + lane; k < nrad; k += 32) m = max(m, __double_as_longlong(__ldcg(a.d.ring_smax + k)));
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
     if (lane == 0) s_dtc[0] = (m > 0) ? CFLSECURITY / sqrt(__longlong_as_double(m)) : 1e30;
@@ -261,9 +285,9 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     // shear limit 2 pi C / nsec / |Omega_k - Omega_k+1|: the largest difference
     // gives the smallest step (NaN differences are skipped, as fmin skips them)
     long long m = 0;
+#pragma unroll 8
     for (int k = lane; k < nrad - 1; k += 32) {
-      const double v0 = __ldcg(a.d.ring_vmoy + k), v1 = __ldcg(a.d.ring_vmoy + k + 1);
-      const double d = fabs(v0 * RT64(a, RT_INVRMED, k) - v1 * RT64(a, RT_INVRMED, k + 1));
+      const double d = fabs(__ldcg(a.d.ring_vmoy + k) - __ldcg(a.d.ring_vmoy + k + 1));
       if (d == d) m = max(m, __double_as_longlong(d));
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
@@ -273,14 +297,16 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   if (tid == 0) {
     c->ticket = 0u;
     double dt;
+    bool cfl_err = false;
     if (do_cfl) {
-      const double DeltaT = (a.mode == 1) ? c->DT : c->DT - c->dtemp;
+      const double DeltaT = (a.mode == 1) ? s_ctl[0] : s_ctl[0] - s_ctl[1];
       double newdt = fmin(s_dtc[0], s_dtc[1]);
       if (DeltaT < newdt) newdt = DeltaT;
       double q = DeltaT / newdt;
       int cfl;
       if (!(q > 0.0) || !(q < 1.0e8)) {
         c->err |= FARGO_DEVERR_CFL;
+        cfl_err = true;
         cfl = 1;
         c->done = 1;
       } else {
@@ -290,7 +316,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       dt = DeltaT / (double)cfl;
       if (a.mode == 1) c->sloppy_dt = dt;
     } else {
-      dt = c->sloppy_dt;
+      dt = s_ctl[2];
     }
     if (do_forces) {
       // DiskOnPrimaryAcceleration, ComputeIndirectTerm (src/Pframeforce.cu:86-94)
@@ -298,18 +324,17 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       c->ind_y = P.indirect_term ? -s_acc[1] : 0.0;
       c->f32[CTL_F_INDX] = (float)c->ind_x;
       c->f32[CTL_F_INDY] = (float)c->ind_y;
-      for (int b = 0; b < nbody; b++) {
-        c->accx[b] = s_acc[2 * b];
-        c->accy[b] = s_acc[2 * b + 1];
-      }
+      c->accx[0] = s_acc[0];
+      c->accy[0] = s_acc[1];
     }
     if (do_step) {
-      if (c->err) dt = 0.0;
+      if (s_ctl[4] != 0.0 || cfl_err) dt = 0.0;
       c->dt = dt;
       c->f32[CTL_F_DT] = (float)dt;
-      c->dtemp += dt;
+      c->f32[CTL_F_INVDT] = 1.0f / (float)dt;
+      c->dtemp = s_ctl[1] + dt;
       c->nsub_dt += 1;
-      c->t_sub = c->PhysicalTime;
+      c->t_sub = s_ctl[3];
     }
   }
   // FViscosity profile when it changes in time (a moving cavity)
@@ -327,8 +352,20 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
 // next substep's planet parameters, which no hydro kernel of the substep reads,
 // so it may run beside them; in a corotating frame the hydro kernels need the
 // new frame rate and it runs before them.
-__global__ void k_planets(DevParams P, Ctl *c) {
-  fargo_planets_substep(*c, P, c->dt, c->t_sub);
+__global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const double *__restrict__ ring_force, int fp32) {
+  constexpr int NV = 2 * (FARGO_MAXPL + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nrad = P.nrad;
+  // the disk's force on each planet feeling it (bodies 1.. of k_cfl_forces)
+  for (int v = 2 + w; v < 2 * c->nbody; v += 2) {
+    const double s = fp32 ? ring_total<float>(ring_force, nrad, NV, v, lane)
+                          : ring_total<double>(ring_force, nrad, NV, v, lane);
+    if (lane == 0) {
+      if (v & 1) c->accy[v >> 1] = s;
+      else c->accx[v >> 1] = s;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) fargo_planets_substep(*c, P, c->dt, c->t_sub);
 }
 
 // ---------------------------------------------------------------------------
@@ -731,84 +768,108 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
 // ---------------------------------------------------------------------------
 // Radial transport: LRMomentaKernel (src/Kernels.cu:774-787) + OneWindRad
 // (src/TransportEuler.cu:60-156: StarRadKernel/2, DivisePolarGridKernel,
-// VanLeerRadialKernel for every conserved quantity, density last).  Each thread
-// rebuilds the quantities of rings i-2..i+2 of its column and writes the new
-// values of all of them at (i, j) -- no intermediate field goes to memory.
-namespace {
-
-template <class T>
-struct RadCol {
-  T q[5];  // rings i-2 .. i+2 (index k - i + 2)
-};
-
-// upwind interface value at ring interface m (StarRadKernel/StarRadKernel2)
-template <class T>
-__device__ __forceinline__ T qstar_rad(const KArgs<T> &a, const T *q, int i, int m, T v, T dt) {
-  const int nrad = a.P.nrad;
-  if (m <= 0 || m >= nrad) return (T)0.0;
-  auto dq = [&](int k) -> T {
-    if (k == 0 || k == nrad - 1) return (T)0.0;
-    const T dqm = (q[k - i + 2] - q[k - 1 - i + 2]) * RT(a, RT_INVDIFFRMED, k);
-    const T dqp = (q[k + 1 - i + 2] - q[k - i + 2]) * RT(a, RT_INVDIFFRMED, k + 1);
-    return (dqp * dqm > (T)0.0) ? (T)2.0 * dqp * dqm / (dqp + dqm) : (T)0.0;
-  };
-  if (v > (T)0.0)
-    return q[m - 1 - i + 2] + (RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt) * (T)0.5 * dq(m - 1);
-  return q[m - i + 2] - (RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt) * (T)0.5 * dq(m);
-}
-
-}  // namespace
-
+// VanLeerRadialKernel for every conserved quantity, density last), with no
+// intermediate field in memory.  One CTA per 32 sectors x RAD_TR rings: the
+// transported quantities of the tile and a halo of two rings go to shared
+// memory, then the slopes dq(k) of the rings, the upwind values at the
+// interfaces and the cell updates are each formed once, one barrier between
+// the phases.
+#define RAD_TR 16
+#define RAD_NS 7   // streams: rmp, rmm, tmp, tmm, energy, density (as q/rho), raw density
+#define RAD_SMEM(T) \
+  (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 2) + RAD_NS * (RAD_TR + 1)))
 template <class T>
 __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
+  constexpr int TW = 32, TR = RAD_TR, NS = RAD_NS;
+  extern __shared__ __align__(16) unsigned char rad_smem[];
+  T(*sW)[TR + 4][TW] = reinterpret_cast<T(*)[TR + 4][TW]>(rad_smem);    // q/rho, rings i0-2 .. i0+TR+1
+  T(*sQ)[TR][TW] = reinterpret_cast<T(*)[TR][TW]>(sW + NS);              // raw quantities of the tile's rings
+  T(*sV)[TW] = reinterpret_cast<T(*)[TW]>(sQ + 6);                       // Vrad at interfaces i0 .. i0+TR
+  T(*sD)[TR + 2][TW] = reinterpret_cast<T(*)[TR + 2][TW]>(sV + TR + 1);  // slopes of rings i0-1 .. i0+TR
+  T(*sS)[TR + 1][TW] = reinterpret_cast<T(*)[TR + 1][TW]>(sD + NS);      // interface values at i0 .. i0+TR
   const DevParams &P = a.P;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = P.nrad, nsec = P.nsec;
-  if (i >= nrad || j >= nsec) return;
+  const int x = threadIdx.x, y = threadIdx.y, ny = blockDim.y;
+  const int j = blockIdx.x * TW + x, i0 = blockIdx.y * TR;
+  const bool col = j < nsec;
+  const int jp = col ? jp1(j, nsec) : 0;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT), Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
-  const int jp = jp1(j, nsec);
-  const T *D = a.d.dens, *VR = a.d.vrad, *VT = a.d.vtheta, *E = a.d.energy;
-  T d[5], rmp[5], rmm[5], tmp[5], tmm[5], e[5], inv[5];
-#pragma unroll
-  for (int o = 0; o < 5; o++) {
-    const int k = i - 2 + o;
-    if (k < 0 || k >= nrad) {
-      d[o] = rmp[o] = rmm[o] = tmp[o] = tmm[o] = e[o] = inv[o] = (T)0.0;
-      continue;
+  // LRMomenta and DivisePolarGrid over the tile and its halo (zero outside the grid)
+  for (int rr = y; rr < TR + 4; rr += ny) {
+    const int k = i0 - 2 + rr;
+    T q[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0}, inv = (T)0.0, vr = (T)0.0;
+    if (col && k >= 0 && k < nrad) {
+      const size_t qk = (size_t)k * nsec + j;
+      const T rm = RT(a, RT_RMED, k);
+      const T d = a.d.dens[qk], v0 = a.d.vrad[qk], v1 = a.d.vrad[qk + nsec];
+      q[0] = d * v1;
+      q[1] = d * v0;
+      q[2] = d * (a.d.vtheta[(size_t)k * nsec + jp] + rm * Om) * rm;
+      q[3] = d * (a.d.vtheta[qk] + rm * Om) * rm;
+      q[4] = P.adiabatic ? a.d.energy[qk] : (T)0.0;
+      q[5] = d;
+      inv = (T)1.0 / (d + (T)1e-20);
+      vr = v0;
+    } else if (col && k == nrad) {
+      vr = a.d.vrad[(size_t)k * nsec + j];
     }
-    const size_t qk = (size_t)k * nsec + j;
-    const T rm = RT(a, RT_RMED, k);
-    d[o] = D[qk];
-    rmp[o] = d[o] * VR[qk + nsec];
-    rmm[o] = d[o] * VR[qk];
-    tmp[o] = d[o] * (VT[(size_t)k * nsec + jp] + rm * Om) * rm;
-    tmm[o] = d[o] * (VT[qk] + rm * Om) * rm;
-    e[o] = P.adiabatic ? E[qk] : (T)0.0;
-    inv[o] = (T)1.0 / (d[o] + (T)1e-20);
-  }
-  const size_t q = (size_t)i * nsec + j;
-  const T v0 = VR[q], v1 = VR[q + nsec];
-  const T ds0 = qstar_rad(a, d, i, i, v0, dt), ds1 = qstar_rad(a, d, i, i + 1, v1, dt);
-  const T dtheta = (T)a.dtheta;
-  const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
-  T varq_d = (T)0.0;
-  auto update = [&](const T *qq, bool keep_varq) -> T {
-    T w[5];
 #pragma unroll
-    for (int o = 0; o < 5; o++) w[o] = qq[o] * inv[o];
-    const T s0 = qstar_rad(a, w, i, i, v0, dt), s1 = qstar_rad(a, w, i, i + 1, v1, dt);
-    T varq = dt * dtheta * rinf * s0 * ds0 * v0;
-    varq -= dt * dtheta * rsup * s1 * ds1 * v1;
-    if (keep_varq) varq_d = varq;
-    return qq[2] + varq * isurf;
-  };
-  a.d.radmomp[q] = update(rmp, false);
-  a.d.radmomm[q] = update(rmm, false);
-  a.d.thetamomp[q] = update(tmp, false);
-  a.d.thetamomm[q] = update(tmm, false);
-  if (P.adiabatic) a.d.energyr[q] = update(e, false);
-  a.d.densr[q] = update(d, true);
-  if (i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq_d;
+    for (int f = 0; f < 6; f++) sW[f][rr][x] = q[f] * inv;
+    sW[6][rr][x] = q[5];
+    if (rr >= 2 && rr < TR + 2) {
+#pragma unroll
+      for (int f = 0; f < 6; f++) sQ[f][rr - 2][x] = q[f];
+    }
+    if (rr >= 2 && rr <= TR + 2) sV[rr - 2][x] = vr;
+  }
+  __syncthreads();
+  // StarRadKernel: slopes of rings k = i0-1 .. i0+TR (zero at the first and last ring)
+  for (int e = y; e < NS * (TR + 2); e += ny) {
+    const int f = e / (TR + 2), dd = e - f * (TR + 2), k = i0 - 1 + dd;
+    T v = (T)0.0;
+    if (k > 0 && k < nrad - 1) {
+      const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
+      const T dqm = (w0 - wm) * RT(a, RT_INVDIFFRMED, k);
+      const T dqp = (wp - w0) * RT(a, RT_INVDIFFRMED, k + 1);
+      v = (dqp * dqm > (T)0.0) ? (T)2.0 * dqp * dqm / (dqp + dqm) : (T)0.0;
+    }
+    sD[f][dd][x] = v;
+  }
+  __syncthreads();
+  // StarRadKernel2: upwind values at the interfaces m = i0 .. i0+TR
+  for (int e = y; e < NS * (TR + 1); e += ny) {
+    const int f = e / (TR + 1), ss = e - f * (TR + 1), m = i0 + ss;
+    T st = (T)0.0;
+    if (m > 0 && m < nrad) {
+      const T v = sV[ss][x];
+      if (v > (T)0.0)
+        st = sW[f][ss + 1][x] + (RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt) * (T)0.5 * sD[f][ss][x];
+      else
+        st = sW[f][ss + 2][x] - (RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt) * (T)0.5 * sD[f][ss + 1][x];
+    }
+    sS[f][ss][x] = st;
+  }
+  __syncthreads();
+  if (!col) return;
+  // VanLeerRadialKernel
+  const T dtheta = KC(T, a, KC_DTHETA);
+  for (int t = y; t < TR; t += ny) {
+    const int i = i0 + t;
+    if (i >= nrad) break;
+    const size_t q = (size_t)i * nsec + j;
+    const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
+    const T v0 = sV[t][x], v1 = sV[t + 1][x];
+    const T ds0 = sS[6][t][x], ds1 = sS[6][t + 1][x];
+    T *out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      if (f == 4 && !P.adiabatic) continue;
+      T varq = dt * dtheta * rinf * sS[f][t][x] * ds0 * v0;
+      varq -= dt * dtheta * rsup * sS[f][t + 1][x] * ds1 * v1;
+      out[f][q] = sQ[f][t][x] + varq * isurf;
+      if (f == 5 && i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -958,7 +1019,6 @@ template <class T>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
   extern __shared__ __align__(16) unsigned char az_smem[];
   __shared__ SumAcc<T> s_part[32];
-  __shared__ double s_vc;
   __shared__ RingMean<T> s_vm;
   __shared__ T s_vct;
   __shared__ int s_shift;
@@ -997,16 +1057,15 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   if (tid == 0) {
     SumAcc<T> v = s_part[0];
     for (int k = 1; k < nw; k++) v.merge(s_part[k]);
-    const double vmed = v.value() / (double)nsec;
-    const double dt = a.d.ctl->dt;
-    // ComputeConstantResidualKernel (FP64 split; Nshift is an integer decision)
-    const double invdt = 1.0 / dt;
-    const double dpinvns = 2.0 * PI / (double)nsec;
-    const double Ntilde = vmed * RT64(a, RT_INVRMED, i) * dt * (double)nsec / 2.0 / PI;
+    // ComputeAverageThetaVelocities + ComputeConstantResidual: the shift Nshift
+    // is an FP64 integer decision; the constant residual velocity is a field
+    // value, formed in T from the per-ring factor rm 2pi/nsec and 1/dt
+    const double vmed = v.value() * a.inv_nsec;
+    const double Ntilde = vmed * RT64(a, RT_AZSHIFT, i) * a.d.ctl->dt;
     const double Nround = floor(Ntilde + 0.5);
     s_shift = (int)(long)Nround;
-    s_vc = (Ntilde - Nround) * RT64(a, RT_RMED, i) * invdt * dpinvns;
-    s_vct = (T)s_vc;
+    const T invdt = sizeof(T) == 4 ? (T)a.d.ctl->f32[CTL_F_INVDT] : (T)(1.0 / a.d.ctl->dt);
+    s_vct = (T)(Ntilde - Nround) * RT(a, RT_DXTHETA, i) * invdt;
     s_vm.set(vmed);
   }
   __syncthreads();
@@ -1182,12 +1241,12 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
       if (side && !P.corotating) {
         cudaEventRecord(side->fork, s);
         cudaStreamWaitEvent(side->s, side->fork, 0);
-        k_planets<<<1, 1, 0, side->s>>>(P, a.d.ctl);
+        k_planets<<<1, 64, 0, side->s>>>(P, a.d.ctl, a.d.ring_force, sizeof(T) == 4);
         cudaEventRecord(side->join, side->s);
         joined = false;
         if (g_probe) g_probe->count++;
       } else {
-        k_planets<<<1, 1, 0, s>>>(P, a.d.ctl);
+        k_planets<<<1, 64, 0, s>>>(P, a.d.ctl, a.d.ring_force, sizeof(T) == 4);
         MARK("k_planets");
       }
     }
@@ -1217,7 +1276,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
-    k_transport_radial<T><<<g2, b2, 0, s>>>(a);
+    k_transport_radial<T><<<dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, 8), RAD_SMEM(T), s>>>(a);
     MARK("k_transport_radial");
     if (a.az_regs) {
       k_transport_azimuthal4<T><<<P.nrad, (P.nsec / 4 + 31) / 32 * 32, az_smem_bytes, s>>>(a);
@@ -1292,6 +1351,8 @@ void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
 
 template <class T>
 cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
+  cudaError_t e = cudaFuncSetAttribute(k_transport_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM(T));
+  if (e != cudaSuccess) return e;
   if (az_smem_bytes == 0) return cudaSuccess;
   if (az_regs)
     return cudaFuncSetAttribute(k_transport_azimuthal4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);

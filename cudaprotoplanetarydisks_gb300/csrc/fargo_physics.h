@@ -77,7 +77,7 @@ struct Ctl {
   float f32[8];
 };
 
-enum { CTL_F_DT = 0, CTL_F_OMEGA, CTL_F_INDX, CTL_F_INDY, CTL_F_DOMEGA, CTL_F_COUNT };
+enum { CTL_F_DT = 0, CTL_F_OMEGA, CTL_F_INDX, CTL_F_INDY, CTL_F_DOMEGA, CTL_F_INVDT, CTL_F_COUNT };
 
 // refresh every FP32 copy from its FP64 value
 FARGO_HD void fargo_ctl_mirror(Ctl &c) {
@@ -86,6 +86,7 @@ FARGO_HD void fargo_ctl_mirror(Ctl &c) {
   c.f32[CTL_F_INDX] = (float)c.ind_x;
   c.f32[CTL_F_INDY] = (float)c.ind_y;
   c.f32[CTL_F_DOMEGA] = (float)c.domega;
+  c.f32[CTL_F_INVDT] = 1.0f / (float)c.dt;
 }
 
 // AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392
@@ -124,15 +125,25 @@ FARGO_HD double fargo_fviscosity(const DevParams &P, double r, double csmean, do
   return viscosity * fargo_cavity_factor(P, r, t, t0);
 }
 
+// pow with the exponents 0, 1 and 2 of the usual disk set-ups (flat flaring,
+// squares) taken exactly: x^0 = 1, x^1 = x, x^2 = x*x are the correctly rounded
+// powers, and an FP64 pow costs thousands of cycles on this GPU.
+FARGO_HD double fargo_pow(double x, double e) {
+  if (e == 1.0) return x;
+  if (e == 2.0) return x * x;
+  if (e == 0.0) return 1.0;
+  return pow(x, e);
+}
+
 // Compute_smoothing  src/Force.cu:137-142
 FARGO_HD double fargo_smoothing(const DevParams &P, double r, double t, double t0) {
-  return P.thicknesssmoothing * fargo_aspect_ratio(P, r, t, t0) * pow(r, 1.0 + P.flaringindex);
+  return P.thicknesssmoothing * fargo_aspect_ratio(P, r, t, t0) * fargo_pow(r, 1.0 + P.flaringindex);
 }
 
 // MassTaper  src/SourceEuler.cu:223-224
 FARGO_HD double fargo_mass_taper(const DevParams &P, double t) {
   double m = t / (P.masstaper * 2.0 * M_PI);
-  return (m > 1.0 ? 1.0 : pow(sin(m * M_PI / 2.0), 2.0));
+  return (m > 1.0 ? 1.0 : fargo_pow(sin(m * M_PI / 2.0), 2.0));
 }
 
 // GetPsysInfo  src/Psys.cu:249-319 (action 0 = GET, 1 = MARK, 2 = FREQUENCY)
@@ -308,18 +319,19 @@ FARGO_HD void fargo_planet_params(Ctl &c, const DevParams &P, double t) {
   c.bx[0] = c.by[0] = c.brs2[0] = 0.0;
   for (int k = 0; k < c.nb; k++) {
     const double x = c.x[k], y = c.y[k], m = c.mass[k];
+    // the distance to the star, and the thickness smoothing at it, serve both uses
+    const double r = sqrt(x * x + y * y);
+    const double smt = P.roche_smoothing ? 0.0 : fargo_smoothing(P, r, t, t0);
     if (c.feeldisk[k]) {
-      const double r = sqrt(x * x + y * y);
-      const double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing : fargo_smoothing(P, r, t, t0);
+      const double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing : smt;
       c.bx[nbody] = x;
       c.by[nbody] = y;
       c.brs2[nbody] = sm * sm;
       nbody++;
     }
     const double mp = m * taper;
-    const double PD = sqrt(x * x + y * y);
-    const double RRoche = PD * pow((1.0 / 3.0 * mp), 1.0 / 3.0);
-    const double sm = P.roche_smoothing ? RRoche * P.rochesmoothing : fargo_smoothing(P, PD, t, t0);
+    const double PD = r;
+    const double sm = P.roche_smoothing ? PD * pow((1.0 / 3.0 * mp), 1.0 / 3.0) * P.rochesmoothing : smt;
     c.px[k] = x;
     c.py[k] = y;
     c.pm[k] = mp;
@@ -333,7 +345,7 @@ FARGO_HD void fargo_planet_params(Ctl &c, const DevParams &P, double t) {
 // at ring radius r, before the self-gravity term.
 FARGO_HD double fargo_vkep2(const DevParams &P, double r, double t, double t0) {
   const double f = 1.0 + P.sigmaslope - 2.0 * P.flaringindex;
-  return 1.0 * 1.0 / r * (1.0 - f * pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * pow(r, 2.0 * P.flaringindex));
+  return 1.0 * 1.0 / r * (1.0 - f * fargo_pow(fargo_aspect_ratio(P, r, t, t0), 2.0) * fargo_pow(r, 2.0 * P.flaringindex));
 }
 
 // The Keplerian speed itself, before the frame term; csmean is the ring's mean

@@ -369,6 +369,7 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
     T(RT_VKEP2, i) = fargo_vkep2(dp, h.Rmed[i], 0.0, 0.0);
     T(RT_R15, i) = pow(h.Rmed[i], 1.5);
     T(RT_CAVFAC, i) = fargo_cavity_factor(dp, h.Rmed[i], 0.0, 0.0);
+    T(RT_AZSHIFT, i) = (i < p.nrad) ? h.invRmed[i] * (double)NSEC / 2.0 / PI : 0.0;
     T(RT_SIGMAMED, i) = at(h.SigmaMed, i);
     T(RT_ENERGYMED, i) = at(h.EnergyMed, i);
     T(RT_COOLTIME, i) = at(h.CoolingTimeMed, i);
