@@ -59,6 +59,7 @@ struct fargo_ctx {
   cudaGraphExec_t exec = nullptr;
   unsigned long long cond_handle = 0;
   bool use_graph = true;
+  bool use_pdl = true;   // programmatic dependent launch between the step kernels
 };
 
 namespace {
@@ -140,6 +141,7 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.mode = c->P.sloppy_cfl ? 2 : 0;
   a.az_smem = 0;
   a.az_regs = c->az_regs;
+  a.pdl = c->use_pdl ? 1 : 0;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -627,6 +629,8 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   c->dp = host_dev_params(*p, nb);
   const char *ng = std::getenv("FARGO_NO_GRAPH");
   if (ng && ng[0] == '1') c->use_graph = false;
+  const char *np = std::getenv("FARGO_NO_PDL");
+  if (np && np[0] == '1') c->use_pdl = false;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

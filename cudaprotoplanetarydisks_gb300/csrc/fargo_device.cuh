@@ -63,6 +63,7 @@ struct KArgs {
   int az_regs;         // register-blocked azimuthal kernel (nsec % 4 == 0)
   unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
   int use_cond;                    // 1: k_end sets the while-loop condition
+  int pdl;                         // launch with programmatic dependent launch
   SgDev sg;
 };
 
@@ -152,6 +153,14 @@ enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_DTHETA, KC_COUNT };
 #define CTL_T(T, c, field, idx) (sizeof(T) == 4 ? (T)(c)->f32[idx] : (T)(c)->field)
 // launch constant in T
 #define KC(T, a, k) (sizeof(T) == 4 ? (T)(a).k32[k] : (T)(a).k64[k])
+
+// Programmatic dependent launch: a step kernel launched with the attribute may
+// be scheduled before the kernel ahead of it in the stream has finished; it
+// first waits until that kernel has completed and its writes are visible.  The
+// earlier kernel lets it launch only at its own exit (no explicit trigger: an
+// early trigger parks waiting blocks on the SMs and slows the running kernel).
+// A no-op for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 #define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 #define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])

@@ -67,6 +67,7 @@ __device__ __forceinline__ double ring_total(const double *ring_force, int nrad,
 
 template <class T>
 __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
+  pdl_enter();
   constexpr int NW = 8;                       // warps of the 256-thread CTA
   constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
   const DevParams &P = a.P;
@@ -353,6 +354,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
 // so it may run beside them; in a corotating frame the hydro kernels need the
 // new frame rate and it runs before them.
 __global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const double *__restrict__ ring_force, int fp32) {
+  pdl_enter();
   constexpr int NV = 2 * (FARGO_MAXPL + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nrad = P.nrad;
   // the disk's force on each planet feeling it (bodies 1.. of k_cfl_forces)
@@ -372,6 +374,7 @@ __global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const doubl
 // ComputeSoundSpeed (energy equation) + Make1Dprofile(1) ring means; one CTA per ring.
 template <class T>
 __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
+  pdl_enter();
   __shared__ SumAcc<T> s_red[8];
   const int i = blockIdx.x, nsec = a.P.nsec;
   const double g = a.P.adiabaticindex;
@@ -402,6 +405,7 @@ __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
 // CorrectVthetaKernel src/Kernels.cu:1256-1263 (corotating frame)
 template <class T>
 __global__ void k_correct_vtheta(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const size_t q = (size_t)i * a.P.nsec + j;
@@ -414,6 +418,7 @@ __global__ void k_correct_vtheta(KArgs<T> a) {
 // OpenBoundaryKernel src/Kernels.cu:482-495
 template <class T>
 __global__ void k_bc_open(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, nsec = a.P.nsec;
   if (j >= nsec) return;
   T *D = a.d.dens, *E = a.d.energy, *V = a.d.vrad;
@@ -430,6 +435,7 @@ __global__ void k_bc_open(KArgs<T> a) {
 // increasing j would.  The sound-speed ring nrad read there is zero.
 template <class T>
 __global__ void __launch_bounds__(1024) k_bc_nonreflecting(KArgs<T> a) {
+  pdl_enter();
   __shared__ double s_red[32];
   __shared__ int s_angle[2];
   const int nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x;
@@ -511,6 +517,7 @@ __global__ void __launch_bounds__(1024) k_bc_nonreflecting(KArgs<T> a) {
 // Its SG term reads GLOBAL_bufarray_d, which the reference never fills (zero).
 template <class T>
 __global__ void k_bc_evanescent(KArgs<T> a) {
+  pdl_enter();
   const DevParams &P = a.P;
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = P.nrad, nsec = P.nsec;
@@ -551,6 +558,7 @@ __global__ void k_bc_evanescent(KArgs<T> a) {
 // the reference (it is added inside the planet loop, src/Kernels.cu:1246).
 template <class T>
 __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
+  pdl_enter();
   const DevParams &P = a.P;
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = P.nrad, nsec = P.nsec;
@@ -614,6 +622,7 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
 // ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
 template <class T>
 __global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restrict__ vr, const T *__restrict__ vt) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
@@ -641,6 +650,7 @@ __global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restric
 // src/Kernels.cu:1416-1430 (skipped with the evanescent boundary, src/SourceEuler.cu:338).
 template <class T>
 __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
@@ -679,6 +689,7 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
 // they are needed and the new velocities are written to Vrad/Vtheta directly.
 template <class T>
 __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
@@ -723,6 +734,7 @@ __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
 // Substep3Kernel + Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
 template <class T>
 __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
@@ -780,6 +792,7 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
   (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 2) + RAD_NS * (RAD_TR + 1)))
 template <class T>
 __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
+  pdl_enter();
   constexpr int TW = 32, TR = RAD_TR, NS = RAD_NS;
   extern __shared__ __align__(16) unsigned char rad_smem[];
   T(*sW)[TR + 4][TW] = reinterpret_cast<T(*)[TR + 4][TW]>(rad_smem);    // q/rho, rings i0-2 .. i0+TR+1
@@ -882,6 +895,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
 #define AZ_NARR 11
 template <class T>
 __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char az_smem[];
   __shared__ double s_red[32];
   __shared__ double s_vc;
@@ -1017,6 +1031,7 @@ __device__ __forceinline__ int az_wrap(int j, int n) { return j < 0 ? j + n : (j
 #define AZ4_NARR 13
 template <class T>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char az_smem[];
   __shared__ SumAcc<T> s_part[32];
   __shared__ RingMean<T> s_vm;
@@ -1155,6 +1170,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 // src/Kernels.cu:203-213 when no boundary runs in between).
 template <class T>
 __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_temperature) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
@@ -1176,6 +1192,7 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
 // ComputeTemperatureFieldKernel src/Kernels.cu:203-213 (after a boundary condition)
 template <class T>
 __global__ void k_temperature(KArgs<T> a) {
+  pdl_enter();
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const size_t q = (size_t)i * a.P.nsec + j;
@@ -1187,6 +1204,7 @@ __global__ void k_temperature(KArgs<T> a) {
 // (src/SourceEuler.cu:302) and the while-loop condition of AlgoGas (line 222).
 template <class T>
 __global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
+  pdl_enter();
   __shared__ double s_red[32];
   Ctl *c = a.d.ctl;
   if (a.P.open_inner) {
@@ -1211,6 +1229,7 @@ __global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
 
 // Start of a DT (AlgoGas entry, src/SourceEuler.cu:202-221).
 __global__ void k_dt_begin(Ctl *c) {
+  pdl_enter();
   c->dtemp = 0.0;
   c->nsub_dt = 0;
   c->done = 0;
@@ -1235,7 +1254,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   if (which_mask & SUBK_CFL_FORCES) {
     // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
     // 3 forces + potential only (no planet advance, no time update)
-    k_cfl_forces<T><<<P.nrad, 256, 0, s>>>(a);
+    launch_k(a.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, a);
     MARK("k_cfl_forces");
     if (a.mode == 0 || a.mode == 2) {
       if (side && !P.corotating) {
@@ -1252,51 +1271,51 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     }
   }
   if ((which_mask & SUBK_COROT) && P.corotating) {
-    k_correct_vtheta<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_correct_vtheta<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_correct_vtheta");
   }
   if (which_mask & SUBK_BC1) launch_boundaries(a, s);
   if ((which_mask & SUBK_SG) && P.self_gravity) launch_selfgravity(a, s);
   if (which_mask & SUBK_SOURCE) {
-    k_source<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_source<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_source");
-    k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vradint, a.d.vthetaint);
+    launch_k(a.pdl, k_visc_tau<T>, dim3(g2), dim3(b2), 0, s, a, a.d.vradint, a.d.vthetaint);
     MARK("k_visc_tau");
-    k_visc_update<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_visc_update<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_visc_update");
-    k_artvisc<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_artvisc<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_artvisc");
   }
   if (which_mask & SUBK_BC2) launch_boundaries(a, s);
   if ((which_mask & SUBK_ENERGY) && P.adiabatic) {
-    k_visc_tau<T><<<g2, b2, 0, s>>>(a, a.d.vrad, a.d.vtheta);
+    launch_k(a.pdl, k_visc_tau<T>, dim3(g2), dim3(b2), 0, s, a, a.d.vrad, a.d.vtheta);
     MARK("k_visc_tau");
-    k_energy<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_energy<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_energy");
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
-    k_transport_radial<T><<<dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, 8), RAD_SMEM(T), s>>>(a);
+    launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, 8), RAD_SMEM(T), s, a);
     MARK("k_transport_radial");
     if (a.az_regs) {
-      k_transport_azimuthal4<T><<<P.nrad, (P.nsec / 4 + 31) / 32 * 32, az_smem_bytes, s>>>(a);
+      launch_k(a.pdl, k_transport_azimuthal4<T>, dim3(P.nrad), dim3((P.nsec / 4 + 31) / 32 * 32), az_smem_bytes, s, a);
     } else {
       int nt = P.nsec >= 1024 ? 512 : 256;
       a.az_smem = az_smem_bytes > 0;
-      k_transport_azimuthal<T><<<P.nrad, nt, az_smem_bytes, s>>>(a);
+      launch_k(a.pdl, k_transport_azimuthal<T>, dim3(P.nrad), dim3(nt), az_smem_bytes, s, a);
       a.az_smem = 0;
     }
     MARK("k_transport_azimuthal");
-    k_velocities<T><<<g2, b2, 0, s>>>(a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
+    launch_k(a.pdl, k_velocities<T>, dim3(g2), dim3(b2), 0, s, a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
     MARK("k_velocities");
   }
   if (which_mask & SUBK_BC3) launch_boundaries(a, s);
   if ((which_mask & SUBK_TEMPERATURE) && (bc || !(which_mask & SUBK_TRANSPORT))) {
-    k_temperature<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_temperature<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_temperature");
   }
   if (which_mask & SUBK_END) {
-    k_end<T><<<1, 256, 0, s>>>(a);
+    launch_k(a.pdl, k_end<T>, dim3(1), dim3(256), 0, s, a);
     MARK("k_end");
   }
   if (!joined) cudaStreamWaitEvent(s, side->join, 0);
@@ -1306,21 +1325,21 @@ template <class T>
 void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
   const DevParams &P = a.P;
   if (P.open_inner) {
-    k_bc_open<T><<<(P.nsec + 255) / 256, 256, 0, s>>>(a);
+    launch_k(a.pdl, k_bc_open<T>, dim3((P.nsec + 255) / 256), dim3(256), 0, s, a);
     MARK("k_bc_open");
   }
   if (P.non_reflecting) {
     if (P.adiabatic) {
-      k_soundspeed<T><<<P.nrad, 256, 0, s>>>(a);
+      launch_k(a.pdl, k_soundspeed<T>, dim3(P.nrad), dim3(256), 0, s, a);
       MARK("k_soundspeed");
     }
-    k_bc_nonreflecting<T><<<1, 1024, 0, s>>>(a);
+    launch_k(a.pdl, k_bc_nonreflecting<T>, dim3(1), dim3(1024), 0, s, a);
     MARK("k_bc_nonreflecting");
   }
   if (P.evanescent) {
     const dim3 b2(64, 4);
     const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
-    k_bc_evanescent<T><<<g2, b2, 0, s>>>(a);
+    launch_k(a.pdl, k_bc_evanescent<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_bc_evanescent");
   }
 }
@@ -1328,15 +1347,15 @@ void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
 template <class T>
 void launch_dt_prefix(const KArgs<T> &a0, cudaStream_t s) {
   KArgs<T> a = a0;
-  k_dt_begin<<<1, 1, 0, s>>>(a.d.ctl);
+  launch_k(a.pdl, k_dt_begin, dim3(1), dim3(1), 0, s, a.d.ctl);
   MARK("k_dt_begin");
   if (a.P.adiabatic) {
-    k_soundspeed<T><<<a.P.nrad, 256, 0, s>>>(a);
+    launch_k(a.pdl, k_soundspeed<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
     MARK("k_soundspeed");
   }
   if (a.P.sloppy_cfl) {
     a.mode = 1;
-    k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+    launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
     MARK("k_cfl_forces");
   }
 }
@@ -1345,7 +1364,7 @@ template <class T>
 void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
   KArgs<T> a = a0;
   a.mode = 1;
-  k_cfl_forces<T><<<a.P.nrad, 256, 0, s>>>(a);
+  launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
   MARK("k_cfl_forces");
 }
 
@@ -1362,11 +1381,13 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
 // FP64 host data <-> device fields of type T through an FP64 staging buffer
 template <class T>
 __global__ void k_convert_from_f64(const double *__restrict__ in, T *__restrict__ out, size_t n) {
+  pdl_enter();
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     out[k] = (T)in[k];
 }
 template <class T>
 __global__ void k_convert_to_f64(const T *__restrict__ in, double *__restrict__ out, size_t n) {
+  pdl_enter();
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     out[k] = (double)in[k];
 }

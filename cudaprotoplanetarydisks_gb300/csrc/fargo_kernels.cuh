@@ -39,6 +39,24 @@ inline void probe_mark(cudaStream_t s, const char *name) {
   g_probe->count++;
 }
 
+// Kernel launch, with the programmatic-stream-serialization attribute when pdl
+// is set (the kernel begins with pdl_enter()).
+template <typename... Exp, typename... Act>
+inline void launch_k(int pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     Act &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<Exp>(args)...);
+}
+
 void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s);
 void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s);
 

@@ -187,6 +187,7 @@ static inline int sg_group(int n) {
 // modes m < M of each real field, column-major [m][ring].
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
+  pdl_enter();
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x, G = blockDim.x;
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
 // inverse; the inverse's last stage stores rows < nrad back in place.
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
+  pdl_enter();
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int m = blockIdx.x, n0 = 2 * a.P.nrad, nrad = a.P.nrad;
@@ -250,6 +252,7 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
 // ComputeSgAccKernel (src/Kernels.cu:893-912).
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
+  pdl_enter();
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
@@ -289,12 +292,12 @@ template <class T>
 void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
   const size_t vs = 2 * sizeof(T);
-  k_sg_rows_fwd<T><<<nrad, 256, 3 * nsec * vs, s>>>(a);
+  launch_k(a.pdl, k_sg_rows_fwd<T>, dim3(nrad), dim3(256), 3 * nsec * vs, s, a);
   probe_mark(s, "k_sg_rows_fwd");
   const int gc = sg_group(n0) < 128 ? sg_group(n0) : 128;
-  k_sg_cols<T><<<a.sg.M, 2 * gc, 7 * n0 * vs, s>>>(a);
+  launch_k(a.pdl, k_sg_cols<T>, dim3(a.sg.M), dim3(2 * gc), 7 * n0 * vs, s, a);
   probe_mark(s, "k_sg_cols");
-  k_sg_rows_inv<T><<<nrad, 256, 3 * nsec * vs, s>>>(a);
+  launch_k(a.pdl, k_sg_rows_inv<T>, dim3(nrad), dim3(256), 3 * nsec * vs, s, a);
   probe_mark(s, "k_sg_rows_inv");
 }
 
@@ -302,6 +305,7 @@ void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
 // src/SgMain.cu:49-81 is evaluated on the host; its transforms are done once
 // here).  Azimuthal transforms of the 2 nrad rows of K^r, K^theta ...
 __global__ void __launch_bounds__(256) k_sg_setup_rows(SgDev sg, int nsec, int n0) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char sg_raw[];
   double2 *b0 = (double2 *)sg_raw, *b1 = b0 + nsec;
   const int i = blockIdx.x;
@@ -320,6 +324,7 @@ __global__ void __launch_bounds__(256) k_sg_setup_rows(SgDev sg, int nsec, int n
 
 // ... then the radial transform of each mode column, in place.
 __global__ void __launch_bounds__(256) k_sg_setup_cols(SgDev sg, int n0) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char sg_raw[];
   double2 *b0 = (double2 *)sg_raw, *b1 = b0 + n0;
   const int m = blockIdx.x;
@@ -336,6 +341,7 @@ __global__ void __launch_bounds__(256) k_sg_setup_cols(SgDev sg, int n0) {
 
 // FP64 kernel spectra rounded to the per-step FFT type (FP32-bulk mode)
 __global__ void k_sg_round_spectra(const double2 *__restrict__ in, float2 *__restrict__ out, size_t n) {
+  pdl_enter();
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     out[k] = make_float2((float)in[k].x, (float)in[k].y);
 }

@@ -134,12 +134,13 @@ def _disk_with_env(params, planets, prec, env):
                 os.environ[k] = v
 
 
-@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_AZ_GLOBAL"])
+@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_AZ_GLOBAL"])
 def test_code_paths_are_bitwise_identical(env):
-    # the conditional-graph DT loop vs the host loop; the shared-memory vs the
-    # global-memory ring buffers of the barrier-per-phase azimuthal kernel
+    # the conditional-graph DT loop vs the host loop; programmatic dependent
+    # launch vs plain launches; the shared-memory vs the global-memory ring
+    # buffers of the barrier-per-phase azimuthal kernel
     params, planets = small("c2")
-    base = {} if env == "FARGO_NO_GRAPH" else {"FARGO_AZ_GENERIC": "1"}
+    base = {"FARGO_AZ_GENERIC": "1"} if env == "FARGO_AZ_GLOBAL" else {}
     a = _disk_with_env(params, planets, fg.FARGO_FP64, base)
     b = _disk_with_env(params, planets, fg.FARGO_FP64, {**base, env: "1"})
     for _ in range(2):
