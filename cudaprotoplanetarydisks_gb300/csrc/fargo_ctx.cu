@@ -26,7 +26,7 @@ struct fargo_ctx {
   int nb = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  SideBranch side = {nullptr, nullptr, nullptr};  // planet update beside the hydro kernels
+  SideBranch side = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // side streams of a substep
   HostState h;
   std::string err = "no error";
   Ctl *d_ctl = nullptr;
@@ -646,6 +646,9 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   e = cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side.s2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.fork2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.join2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&c->pin_ctl, sizeof(Ctl));
   if (e == cudaSuccess) e = cudaMalloc((void **)&c->d_ctl, sizeof(Ctl));
   if (e != cudaSuccess) {
@@ -676,6 +679,10 @@ void fargo_ctx_destroy(fargo_ctx *c) {
   if (c->side.fork) cudaEventDestroy(c->side.fork);
   if (c->side.join) cudaEventDestroy(c->side.join);
   if (c->side.s) cudaStreamDestroy(c->side.s);
+  if (c->side.s2) cudaStreamSynchronize(c->side.s2);
+  if (c->side.fork2) cudaEventDestroy(c->side.fork2);
+  if (c->side.join2) cudaEventDestroy(c->side.join2);
+  if (c->side.s2) cudaStreamDestroy(c->side.s2);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

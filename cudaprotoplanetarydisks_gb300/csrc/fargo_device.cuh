@@ -162,6 +162,11 @@ enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_DTHETA, KC_COUNT };
 // A no-op for a kernel launched without the attribute.
 __device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Division in the transport sweeps: the fast reciprocal-based divide for float
+// fields (within 2 ulp; the FP32-bulk mode), IEEE division for double fields.
+__device__ __forceinline__ float bulk_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double bulk_div(double a, double b) { return a / b; }
+
 #define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 #define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 

@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
       const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
       const T dqm = (w0 - wm) * RT(a, RT_INVDIFFRMED, k);
       const T dqp = (wp - w0) * RT(a, RT_INVDIFFRMED, k + 1);
-      v = (dqp * dqm > (T)0.0) ? (T)2.0 * dqp * dqm / (dqp + dqm) : (T)0.0;
+      v = (dqp * dqm > (T)0.0) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
     }
     sD[f][dd][x] = v;
   }
@@ -1106,13 +1106,16 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
     for (int c = 0; c < 5; c++) v[c] = const_vel ? vct : vel[c];
     // StarThetaKernel / StarThetaKernel2 on the density
-    T d[8], dq[6], ds[5];
+    T d[8], id[8], dq[6], ds[5];
 #pragma unroll
-    for (int c = 0; c < 8; c++) d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
+    for (int c = 0; c < 8; c++) {
+      d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
+      id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell (FP32)
+    }
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
-      dq[k] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+      dq[k] = (dqp * dqm > (T)0.0) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
     }
 #pragma unroll
     for (int c = 0; c < 5; c++) {
@@ -1130,11 +1133,14 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
                       : a.d.dens;
       T wv[8], dw[6], sw[5];
 #pragma unroll
-      for (int c = 0; c < 8; c++) wv[c] = q[az_wrap(j0 - 2 + c, nsec)] / (d[c] + (T)1e-20);
+      for (int c = 0; c < 8; c++) {
+        const T qc = q[az_wrap(j0 - 2 + c, nsec)];
+        wv[c] = sizeof(T) == 4 ? qc * id[c] : qc / (d[c] + (T)1e-20);
+      }
 #pragma unroll
       for (int k = 0; k < 6; k++) {
         const T dqm = wv[k + 1] - wv[k], dqp = wv[k + 2] - wv[k + 1];
-        dw[k] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+        dw[k] = (dqp * dqm > (T)0.0) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
       }
 #pragma unroll
       for (int c = 0; c < 5; c++) {
@@ -1251,11 +1257,23 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   const dim3 b2(64, 4);
   const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
   bool joined = true;
+  const bool bc1 = (which_mask & SUBK_BC1) && (P.open_inner || P.non_reflecting || P.evanescent);
+  const bool sg_side = side && (which_mask & SUBK_SG) && P.self_gravity && (which_mask & SUBK_CFL_FORCES) && !bc1;
+  // the fork point precedes k_cfl_forces; the transforms are issued after it (the
+  // earlier-issued grid is scheduled first, and the CFL kernel is the longer)
+  if (sg_side) cudaEventRecord(side->fork2, s);
   if (which_mask & SUBK_CFL_FORCES) {
     // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
     // 3 forces + potential only (no planet advance, no time update)
     launch_k(a.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, a);
     MARK("k_cfl_forces");
+  }
+  if (sg_side) {
+    cudaStreamWaitEvent(side->s2, side->fork2, 0);
+    launch_selfgravity(a, side->s2);
+    cudaEventRecord(side->join2, side->s2);
+  }
+  if (which_mask & SUBK_CFL_FORCES) {
     if (a.mode == 0 || a.mode == 2) {
       if (side && !P.corotating) {
         cudaEventRecord(side->fork, s);
@@ -1275,7 +1293,10 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     MARK("k_correct_vtheta");
   }
   if (which_mask & SUBK_BC1) launch_boundaries(a, s);
-  if ((which_mask & SUBK_SG) && P.self_gravity) launch_selfgravity(a, s);
+  if ((which_mask & SUBK_SG) && P.self_gravity) {
+    if (sg_side) cudaStreamWaitEvent(s, side->join2, 0);
+    else launch_selfgravity(a, s);
+  }
   if (which_mask & SUBK_SOURCE) {
     launch_k(a.pdl, k_source<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_source");

@@ -60,12 +60,18 @@ inline void launch_k(int pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_
 void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s);
 void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s);
 
-// A second stream for the planet update of a substep, which then runs beside the
-// hydro kernels (forked after k_cfl_forces, joined at the end of the substep).
-// Without one, or in a corotating frame, it runs in line.
+// Second and third streams: the planet update of a substep runs beside the hydro
+// kernels (forked after k_cfl_forces, joined at the end of the substep); the
+// self-gravity transforms run beside k_cfl_forces.  Without them, or in a
+// corotating frame (for the planets), everything runs in line.
 struct SideBranch {
   cudaStream_t s;
   cudaEvent_t fork, join;
+  // self-gravity beside the CFL/force kernel: both read the density at the start
+  // of the substep and share no other data (used when no boundary kernel
+  // changes the density in between)
+  cudaStream_t s2;
+  cudaEvent_t fork2, join2;
 };
 
 template <class T>

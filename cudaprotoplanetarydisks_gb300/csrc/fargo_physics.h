@@ -198,7 +198,12 @@ FARGO_HD double fargo_psys_info(Ctl &c, const DevParams &P, int action) {
 
 // RotatePsys  src/Psys.cu:323-340 (rotate by -angle)
 FARGO_HD void fargo_rotate_psys(Ctl &c, double angle) {
-  double sint = sin(angle), cost = cos(angle);
+  // sin 0 = 0 and cos 0 = 1 exactly: a fixed frame skips the two FP64 calls
+  double sint = 0.0, cost = 1.0;
+  if (angle != 0.0) {
+    sint = sin(angle);
+    cost = cos(angle);
+  }
   for (int i = 0; i < c.nb; i++) {
     double xt = c.x[i], yt = c.y[i];
     c.x[i] = xt * cost + yt * sint;
@@ -211,18 +216,24 @@ FARGO_HD void fargo_rotate_psys(Ctl &c, double angle) {
 }
 
 // DerivMotionRK5  src/RungeKutta.cu:30-67 (the feel-others term divides by the
-// distance of body j to the star, as the reference does)
-FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, int nb, double dt,
+// distance of body j to the star, as the reference does).  NB > 0: NB bodies,
+// a compile-time count that keeps every array in registers; NB == 0: nb bodies.
+template <int NB>
+FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, int nb_rt, double dt,
                               const int *feelothers, int indirect) {
+  const int nb = NB > 0 ? NB : nb_rt;
   const double *x = q, *y = x + nb, *vx = y + nb, *vy = vx + nb;
   double *dx = deriv, *dy = dx + nb, *dvx = dy + nb, *dvy = dvx + nb;
-  double Dist[FARGO_MAXPL];
+  double Dist[NB > 0 ? NB : FARGO_MAXPL];
+#pragma unroll
   for (int i = 0; i < nb; i++) Dist[i] = sqrt(x[i] * x[i] + y[i] * y[i]);
+#pragma unroll
   for (int i = 0; i < nb; i++) {
     dx[i] = vx[i];
     dy[i] = vy[i];
     dvx[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * x[i];
     dvy[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * y[i];
+#pragma unroll
     for (int j = 0; j < nb; j++) {
       if (indirect) {
         dvx[i] -= 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * x[j];
@@ -234,40 +245,80 @@ FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, 
       }
     }
   }
+#pragma unroll
   for (int i = 0; i < 4 * nb; i++) deriv[i] *= dt;
 }
 
-// RungeKutta + AdvanceSystemRK5  src/RungeKutta.cu:8-28, src/Pframeforce.cu:124-187
+// AdvanceSystemRK5's Cash-Karp step (src/RungeKutta.cu:70-130) from the state q0,
+// result in q1; NB as for fargo_deriv_rk5.
+template <int NB>
+FARGO_HD void fargo_rk5_step(const double *q0, const double *pm, double *q1, int nb_rt, double dt,
+                             const int *feelothers, int indirect) {
+  constexpr int CAP = 4 * (NB > 0 ? NB : FARGO_MAXPL);
+  const int nb = NB > 0 ? NB : nb_rt;
+  double k[6][CAP];
+#pragma unroll
+  for (int s = 0; s < 6; s++)
+#pragma unroll
+    for (int i = 0; i < 4 * nb; i++) k[s][i] = 0.0;
+  const double cf[5][5] = {{0.2, 0.0, 0.0, 0.0, 0.0},
+                           {0.075, 0.225, 0.0, 0.0, 0.0},
+                           {0.3, -0.9, 1.2, 0.0, 0.0},
+                           {-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0, 0.0},
+                           {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
+  fargo_deriv_rk5<NB>(q0, pm, k[0], nb, dt, feelothers, indirect);
+#pragma unroll
+  for (int s = 0; s < 5; s++) {
+#pragma unroll
+    for (int i = 0; i < 4 * nb; i++)
+      q1[i] = q0[i] + cf[s][0] * k[0][i] + cf[s][1] * k[1][i] + cf[s][2] * k[2][i] + cf[s][3] * k[3][i] +
+              cf[s][4] * k[4][i];
+    fargo_deriv_rk5<NB>(q1, pm, k[s + 1], nb, dt, feelothers, indirect);
+  }
+#pragma unroll
+  for (int i = 0; i < 4 * nb; i++)
+    q1[i] = q0[i] + 37.0 / 378.0 * k[0][i] + 250.0 / 621.0 * k[2][i] + 125.0 / 594.0 * k[3][i] +
+            512.0 / 1771.0 * k[5][i];
+}
+
+// the step for nb bodies: one or two bodies (the usual set-ups) run a variant
+// whose arrays live in registers, the same arithmetic
+template <int NB>
+FARGO_HD void fargo_rk5_fixed(const Ctl &c, const DevParams &P, double dt, double *q1) {
+  double q0[4 * NB], pm[NB];
+#pragma unroll
+  for (int i = 0; i < NB; i++) {
+    q0[i] = c.x[i];
+    q0[i + NB] = c.y[i];
+    q0[i + 2 * NB] = c.vx[i];
+    q0[i + 3 * NB] = c.vy[i];
+    pm[i] = c.mass[i];
+  }
+  double r[4 * NB];
+  fargo_rk5_step<NB>(q0, pm, r, NB, dt, c.feelothers, P.indirect_term);
+#pragma unroll
+  for (int i = 0; i < 4 * NB; i++) q1[i] = r[i];
+}
+
 FARGO_HD void fargo_advance_rk5(Ctl &c, const DevParams &P, double dt, double t) {
   const int nb = c.nb;
   double q0[4 * FARGO_MAXPL], q1[4 * FARGO_MAXPL], pm[FARGO_MAXPL];
-  for (int i = 0; i < 4 * FARGO_MAXPL; i++) q0[i] = q1[i] = 0.0;
+  for (int i = 0; i < 4 * nb; i++) q0[i] = q1[i] = 0.0;
   if (!P.forced_circular && nb > 0) {
-    double k[6][4 * FARGO_MAXPL];
-    for (int s = 0; s < 6; s++)
-      for (int i = 0; i < 4 * nb; i++) k[s][i] = 0.0;
-    for (int i = 0; i < nb; i++) {
-      q0[i] = c.x[i];
-      q0[i + nb] = c.y[i];
-      q0[i + 2 * nb] = c.vx[i];
-      q0[i + 3 * nb] = c.vy[i];
-      pm[i] = c.mass[i];
+    if (nb == 1) {
+      fargo_rk5_fixed<1>(c, P, dt, q1);
+    } else if (nb == 2) {
+      fargo_rk5_fixed<2>(c, P, dt, q1);
+    } else {
+      for (int i = 0; i < nb; i++) {
+        q0[i] = c.x[i];
+        q0[i + nb] = c.y[i];
+        q0[i + 2 * nb] = c.vx[i];
+        q0[i + 3 * nb] = c.vy[i];
+        pm[i] = c.mass[i];
+      }
+      fargo_rk5_step<0>(q0, pm, q1, nb, dt, c.feelothers, P.indirect_term);
     }
-    const double cf[5][5] = {{0.2, 0.0, 0.0, 0.0, 0.0},
-                             {0.075, 0.225, 0.0, 0.0, 0.0},
-                             {0.3, -0.9, 1.2, 0.0, 0.0},
-                             {-11.0 / 54.0, 2.5, -70.0 / 27.0, 35.0 / 27.0, 0.0},
-                             {1631.0 / 55296.0, 175.0 / 512.0, 575.0 / 13824.0, 44275.0 / 110592.0, 253.0 / 4096.0}};
-    fargo_deriv_rk5(q0, pm, k[0], nb, dt, c.feelothers, P.indirect_term);
-    for (int s = 0; s < 5; s++) {
-      for (int i = 0; i < 4 * nb; i++)
-        q1[i] = q0[i] + cf[s][0] * k[0][i] + cf[s][1] * k[1][i] + cf[s][2] * k[2][i] + cf[s][3] * k[3][i] +
-                cf[s][4] * k[4][i];
-      fargo_deriv_rk5(q1, pm, k[s + 1], nb, dt, c.feelothers, P.indirect_term);
-    }
-    for (int i = 0; i < 4 * nb; i++)
-      q1[i] = q0[i] + 37.0 / 378.0 * k[0][i] + 250.0 / 621.0 * k[2][i] + 125.0 / 594.0 * k[3][i] +
-              512.0 / 1771.0 * k[5][i];
   }
   for (int i = 1 - (t >= P.releasedate); i < nb; i++) {
     if (!P.forced_circular) {
