@@ -167,6 +167,9 @@ __device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;
 __device__ __forceinline__ float bulk_div(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double bulk_div(double a, double b) { return a / b; }
 
+// preferred shared-memory carveout (percent) of every step kernel
+#define FARGO_SMEM_CARVEOUT 100
+
 #define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 #define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])
 

@@ -1391,7 +1391,23 @@ void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
 
 template <class T>
 cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
-  cudaError_t e = cudaFuncSetAttribute(k_transport_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM(T));
+  // One shared-memory carveout for every step kernel: an SM changes its L1 /
+  // shared split only when idle, so kernels that run side by side (the CFL/force
+  // kernel, the self-gravity transforms, the planet update) and successive
+  // kernels under programmatic launch can share SMs only with the same split.
+  const void *all[] = {(const void *)k_cfl_forces<T>, (const void *)k_planets, (const void *)k_soundspeed<T>,
+                       (const void *)k_correct_vtheta<T>, (const void *)k_bc_open<T>,
+                       (const void *)k_bc_nonreflecting<T>, (const void *)k_bc_evanescent<T>,
+                       (const void *)k_source<T>, (const void *)k_visc_tau<T>, (const void *)k_visc_update<T>,
+                       (const void *)k_artvisc<T>, (const void *)k_energy<T>, (const void *)k_transport_radial<T>,
+                       (const void *)k_transport_azimuthal<T>, (const void *)k_transport_azimuthal4<T>,
+                       (const void *)k_velocities<T>, (const void *)k_temperature<T>, (const void *)k_end<T>,
+                       (const void *)k_dt_begin};
+  cudaError_t e;
+  for (const void *f : all)
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
+      return e;
+  e = cudaFuncSetAttribute(k_transport_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM(T));
   if (e != cudaSuccess) return e;
   if (az_smem_bytes == 0) return cudaSuccess;
   if (az_regs)

@@ -19,6 +19,8 @@
 // FP64 FFT would run on a pipe 64 times narrower than the FP32 one.
 #include <cuda_runtime.h>
 
+#include <initializer_list>
+
 #include "fargo_device.cuh"
 #include "fargo_kernels.cuh"
 
@@ -53,6 +55,11 @@ template <class V>
 __device__ __forceinline__ V cconj(V a) {
   return mk2(a.x, -a.y);
 }
+
+// Shared-memory FFT buffers hold element i at fpad(i) = i + i/8: the stride-8
+// stores of a radix-8 stage then spread over the banks instead of hitting two.
+__host__ __device__ __forceinline__ int fpad(int i) { return i + (i >> 3); }
+__host__ __device__ __forceinline__ int fpadn(int n) { return n + (n >> 3) + 1; }
 
 // DFT of length RAD in registers (forward, exp(-2 pi i / RAD)).
 template <int RAD, class V>
@@ -106,7 +113,7 @@ __device__ __forceinline__ void fft_stage(const V *src, int N, int Ns, const V *
     V v[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; r++) {
-      v[r] = src[j + r * NR];
+      v[r] = src[fpad(j + r * NR)];
       if (r > 0) v[r] = cmul(v[r], tw[r * jj * tws]);
     }
     butterfly<RAD>(v);
@@ -134,7 +141,7 @@ __device__ V *fft_run(V *d0, V *d1, int N, const int *rad, int nst, const V *tw,
       else if (R == 2) fft_stage<2>(d0, N, Ns, tw, lt, G, out);
       else fft_stage<3>(d0, N, Ns, tw, lt, G, out);
     } else {
-      auto out = [&](int k, V v) { dst[k] = v; };
+      auto out = [&](int k, V v) { dst[fpad(k)] = v; };
       if (R == 8) fft_stage<8>(d0, N, Ns, tw, lt, G, out);
       else if (R == 4) fft_stage<4>(d0, N, Ns, tw, lt, G, out);
       else if (R == 2) fft_stage<2>(d0, N, Ns, tw, lt, G, out);
@@ -151,14 +158,14 @@ __device__ V *fft_run(V *d0, V *d1, int N, const int *rad, int nst, const V *tw,
 
 template <class V>
 struct StoreFree {
-  __device__ __forceinline__ void operator()(int k, V v, V *dst) const { dst[k] = v; }
+  __device__ __forceinline__ void operator()(int k, V v, V *dst) const { dst[fpad(k)] = v; }
 };
 
 // Splits the FFT Z of two packed real rows into the modes m < M of each:
 // X_r = (Z[m] + conj Z[N-m]) / 2, X_t = (Z[m] - conj Z[N-m]) / (2i)
 template <class V>
 __device__ __forceinline__ void unpack_pair(const V *Z, int m, int N, V &xr, V &xt) {
-  const V z = Z[m], zc = cconj(Z[m == 0 ? 0 : N - m]);
+  const V z = Z[fpad(m)], zc = cconj(Z[fpad(m == 0 ? 0 : N - m)]);
   xr = mk2((decltype(z.x))0.5 * (z.x + zc.x), (decltype(z.x))0.5 * (z.y + zc.y));
   const V d = csub(z, zc);
   xt = mk2((decltype(z.x))0.5 * d.y, (decltype(z.x))-0.5 * d.x);
@@ -191,14 +198,14 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x, G = blockDim.x;
-  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + nsec;
+  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
   const V *twg = (const V *)a.sg.tw1;
   const T f = RT(a, RT_SGSQRT, i), rm = RT(a, RT_RMED, i), r0 = RT(a, RT_RMED, 0);
 #pragma unroll 4
   for (int j = tid; j < nsec; j += G) {
     tw[j] = twg[j];
     const T var = a.d.dens[(size_t)i * nsec + j] * f;
-    b0[j] = mk2(var, var * rm / r0);
+    b0[fpad(j)] = mk2(var, var * rm / r0);
   }
   __syncthreads();
   V *Z = fft_run(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, G, StoreFree<V>());
@@ -224,7 +231,7 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   const int m = blockIdx.x, n0 = 2 * a.P.nrad, nrad = a.P.nrad;
   const int G = blockDim.x >> 1, g = threadIdx.x >= G ? 1 : 0, lt = threadIdx.x - g * G;
   V *tw = (V *)sg_raw;
-  V *b0 = tw + n0 + g * 3 * n0, *b1 = b0 + n0, *K = b1 + n0;
+  V *b0 = tw + n0 + g * 3 * fpadn(n0), *b1 = b0 + fpadn(n0), *K = b1 + fpadn(n0);
   const V *twg = (const V *)a.sg.tw0;
   const V *kh = (const V *)(g == 0 ? a.sg.khat_r : a.sg.khat_t) + (size_t)m * n0;
   V *col = (V *)(g == 0 ? a.sg.spec_r : a.sg.spec_t) + (size_t)m * nrad;
@@ -232,15 +239,15 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   for (int k = threadIdx.x; k < n0; k += blockDim.x) tw[k] = twg[k];
 #pragma unroll 4
   for (int k = lt; k < n0; k += G) {
-    K[k] = kh[k];
-    b0[k] = (k < nrad) ? col[k] : mk2((T)0, (T)0);
+    K[fpad(k)] = kh[k];
+    b0[fpad(k)] = (k < nrad) ? col[k] : mk2((T)0, (T)0);
   }
   __syncthreads();
   V *X = fft_run(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V S, V *dst) {
-    const V Kk = K[k];
+    const V Kk = K[fpad(k)];
     const T gx = (T)-1.0 * (Kk.x * S.x - Kk.y * S.y);
     const T gy = (T)-1.0 * (Kk.x * S.y + Kk.y * S.x);
-    dst[k] = mk2(gx, -gy);
+    dst[fpad(k)] = mk2(gx, -gy);
   });
   V *Y = (X == b0) ? b1 : b0;
   fft_run(X, Y, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V z, V *) {
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
-  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + nsec;
+  V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
   const V *twg = (const V *)a.sg.tw1;
   const V *spr = (const V *)a.sg.spec_r, *spt = (const V *)a.sg.spec_t;
 #pragma unroll 4
@@ -271,7 +278,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
       ht = cconj(spt[(size_t)(nsec - m) * nrad + i]);
     }
     // Z = H_r + i H_t, conjugated for the inverse
-    b0[m] = mk2(hr.x - ht.y, -(hr.y + ht.x));
+    b0[fpad(m)] = mk2(hr.x - ht.y, -(hr.y + ht.x));
   }
   __syncthreads();
   const T normr = RT(a, RT_SGNORMR, i), normt = RT(a, RT_SGNORMT, i);
@@ -292,12 +299,12 @@ template <class T>
 void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
   const size_t vs = 2 * sizeof(T);
-  launch_k(a.pdl, k_sg_rows_fwd<T>, dim3(nrad), dim3(256), 3 * nsec * vs, s, a);
+  launch_k(a.pdl, k_sg_rows_fwd<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_fwd");
   const int gc = sg_group(n0) < 128 ? sg_group(n0) : 128;
-  launch_k(a.pdl, k_sg_cols<T>, dim3(a.sg.M), dim3(2 * gc), 7 * n0 * vs, s, a);
+  launch_k(a.pdl, k_sg_cols<T>, dim3(a.sg.M), dim3(2 * gc), (n0 + 6 * fpadn(n0)) * vs, s, a);
   probe_mark(s, "k_sg_cols");
-  launch_k(a.pdl, k_sg_rows_inv<T>, dim3(nrad), dim3(256), 3 * nsec * vs, s, a);
+  launch_k(a.pdl, k_sg_rows_inv<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_inv");
 }
 
@@ -307,10 +314,10 @@ void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
 __global__ void __launch_bounds__(256) k_sg_setup_rows(SgDev sg, int nsec, int n0) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  double2 *b0 = (double2 *)sg_raw, *b1 = b0 + nsec;
+  double2 *b0 = (double2 *)sg_raw, *b1 = b0 + fpadn(nsec);
   const int i = blockIdx.x;
   for (int j = threadIdx.x; j < nsec; j += blockDim.x)
-    b0[j] = make_double2(sg.kr[(size_t)i * nsec + j], sg.kt[(size_t)i * nsec + j]);
+    b0[fpad(j)] = make_double2(sg.kr[(size_t)i * nsec + j], sg.kt[(size_t)i * nsec + j]);
   __syncthreads();
   double2 *Z = fft_run(b0, b1, nsec, sg.rad1, sg.nst1, sg.tw1_64, (int)threadIdx.x, (int)blockDim.x,
                        StoreFree<double2>());
@@ -326,15 +333,15 @@ __global__ void __launch_bounds__(256) k_sg_setup_rows(SgDev sg, int nsec, int n
 __global__ void __launch_bounds__(256) k_sg_setup_cols(SgDev sg, int n0) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  double2 *b0 = (double2 *)sg_raw, *b1 = b0 + n0;
+  double2 *b0 = (double2 *)sg_raw, *b1 = b0 + fpadn(n0);
   const int m = blockIdx.x;
   for (int f = 0; f < 2; f++) {
     double2 *kh = (f == 0 ? sg.khat64_r : sg.khat64_t) + (size_t)m * n0;
-    for (int k = threadIdx.x; k < n0; k += blockDim.x) b0[k] = kh[k];
+    for (int k = threadIdx.x; k < n0; k += blockDim.x) b0[fpad(k)] = kh[k];
     __syncthreads();
     double2 *X = fft_run(b0, b1, n0, sg.rad0, sg.nst0, sg.tw0_64, (int)threadIdx.x, (int)blockDim.x,
                          StoreFree<double2>());
-    for (int k = threadIdx.x; k < n0; k += blockDim.x) kh[k] = X[k];
+    for (int k = threadIdx.x; k < n0; k += blockDim.x) kh[k] = X[fpad(k)];
     __syncthreads();
   }
 }
@@ -349,8 +356,8 @@ __global__ void k_sg_round_spectra(const double2 *__restrict__ in, float2 *__res
 template <class T>
 void launch_sg_kernel_spectra(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, n0 = 2 * a.P.nrad;
-  k_sg_setup_rows<<<n0, 256, 2 * nsec * sizeof(double2), s>>>(a.sg, nsec, n0);
-  k_sg_setup_cols<<<a.sg.M, 256, 2 * n0 * sizeof(double2), s>>>(a.sg, n0);
+  k_sg_setup_rows<<<n0, 256, 2 * fpadn(nsec) * sizeof(double2), s>>>(a.sg, nsec, n0);
+  k_sg_setup_cols<<<a.sg.M, 256, 2 * fpadn(n0) * sizeof(double2), s>>>(a.sg, n0);
   if (sizeof(T) == 4) {
     const size_t n = (size_t)a.sg.M * n0;
     k_sg_round_spectra<<<608, 256, 0, s>>>(a.sg.khat64_r, (float2 *)a.sg.khat_r, n);
@@ -362,8 +369,11 @@ template <class T>
 cudaError_t prepare_sg_kernels(int nsec, int n0) {
   cudaError_t e;
   const int vs = 2 * sizeof(T);
-  const int rows = 3 * nsec * vs, cols = 7 * n0 * vs;
-  const int rows64 = 2 * nsec * (int)sizeof(double2), cols64 = 2 * n0 * (int)sizeof(double2);
+  const int rows = (nsec + 2 * fpadn(nsec)) * vs, cols = (n0 + 6 * fpadn(n0)) * vs;
+  const int rows64 = 2 * fpadn(nsec) * (int)sizeof(double2), cols64 = 2 * fpadn(n0) * (int)sizeof(double2);
+  for (const void *f : {(const void *)k_sg_rows_fwd<T>, (const void *)k_sg_cols<T>, (const void *)k_sg_rows_inv<T>})
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
+      return e;
   if ((e = cudaFuncSetAttribute(k_sg_rows_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sg_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
   if ((e = cudaFuncSetAttribute(k_sg_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols)) != cudaSuccess) return e;
