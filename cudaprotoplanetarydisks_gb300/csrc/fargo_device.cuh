@@ -170,8 +170,8 @@ __device__ __forceinline__ double bulk_div(double a, double b) { return a / b; }
 // preferred shared-memory carveout (percent) of every step kernel
 #define FARGO_SMEM_CARVEOUT 100
 
-#define RT(a, row, i) ((a).d.rt[(size_t)(row) * ((a).P.nrad + 1) + (i)])
-#define RT64(a, row, i) ((a).d.rt64[(size_t)(row) * ((a).P.nrad + 1) + (i)])
+#define RT(a, row, i) ((a).d.rt[(i) * RT_COUNT + (row)])
+#define RT64(a, row, i) ((a).d.rt64[(i) * RT_COUNT + (row)])
 
 __device__ __forceinline__ double block_sum_d(double v, double *sh) {
   // sh: >= 32 doubles of shared memory; every thread gets the block sum

@@ -8,7 +8,8 @@
 #include "fargo_gb300.h"
 #include "fargo_physics.h"
 
-// Per-ring table rows (device arrays of (nrad+1) values each, stored row after row).
+// Per-ring table rows: RT_COUNT values per ring for rings 0..nrad, stored ring after
+// ring (the rows of one ring adjacent).
 enum RingTab {
   RT_RINF = 0, RT_RMED, RT_RSUP, RT_SURF, RT_INVRINF, RT_INVSURF, RT_INVRMED,
   RT_INVDIFFRSUP, RT_INVDIFFRMED,

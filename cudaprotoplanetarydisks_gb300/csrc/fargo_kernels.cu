@@ -452,13 +452,13 @@ __global__ void __launch_bounds__(1024) k_bc_nonreflecting(KArgs<T> a) {
     m[r] = block_sum_d(s, s_red) / nsec;
   }
   if (tid == 0) {
-    const double *Rinf = a.d.rt64 + (size_t)RT_RINF * (nrad + 1);
-    const double *Rmed = a.d.rt64 + (size_t)RT_RMED * (nrad + 1);
-    double dangle = (pow(Rinf[1], -1.5) - 1.0) / (.5 * (m[0] + m[1]));
-    dangle *= (Rmed[1] - Rmed[0]);
+    auto Rinf = [&](int k) { return RT64(a, RT_RINF, k); };
+    auto Rmed = [&](int k) { return RT64(a, RT_RMED, k); };
+    double dangle = (pow(Rinf(1), -1.5) - 1.0) / (.5 * (m[0] + m[1]));
+    dangle *= (Rmed(1) - Rmed(0));
     s_angle[0] = (int)(dangle / 2.0 / PI * (double)nsec + .5);
-    double dangle2 = (pow(Rinf[nrad - 2], -1.5) - 1.0) / (.5 * (m[2] + m[3]));
-    dangle2 *= (Rmed[nrad - 1] - Rmed[nrad - 2]);
+    double dangle2 = (pow(Rinf(nrad - 2), -1.5) - 1.0) / (.5 * (m[2] + m[3]));
+    dangle2 *= (Rmed(nrad - 1) - Rmed(nrad - 2));
     s_angle[1] = (int)(dangle2 / 2.0 / PI * (double)nsec + .5);
   }
   __syncthreads();
@@ -556,13 +556,16 @@ __global__ void k_bc_evanescent(KArgs<T> a) {
 // The potential is the planet part written by k_cfl_forces plus the star term
 // (direct + indirect) evaluated here; with no planet there is no star term, as in
 // the reference (it is added inside the planet loop, src/Kernels.cu:1246).
+// One cell of the source step: the new VradInt (ring > 0; zero on ring 0, which
+// the reference never writes), VthetaInt and the pressure.
 template <class T>
-__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
-  pdl_enter();
+struct SrcCell {
+  T vr, vt, p;
+};
+template <class T>
+__device__ __forceinline__ SrcCell<T> source_cell(const KArgs<T> &a, int i, int j) {
   const DevParams &P = a.P;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
-  const int nrad = P.nrad, nsec = P.nsec;
-  if (i >= nrad || j >= nsec) return;
+  const int nsec = P.nsec;
   const Ctl *c = a.d.ctl;
   const T dt = CTL_T(T, c, dt, CTL_F_DT), Om = CTL_T(T, c, OmegaFrame, CTL_F_OMEGA);
   const T ix = CTL_T(T, c, ind_x, CTL_F_INDX), iy = CTL_T(T, c, ind_y, CTL_F_INDY);
@@ -582,8 +585,10 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
     pot -= ix * x + iy * y;
     return PHI[k] + pot;
   };
+  SrcCell<T> o;
   const T p0 = press(q, i), pm = press(qm, i);
   const T f0 = phi(q, i, j), fm = phi(qm, i, jm);
+  o.vr = (T)0.0;
   if (i > 0) {
     const T p1 = press(q - nsec, i - 1);
     const T f1 = phi(q - nsec, i - 1, j);
@@ -602,7 +607,7 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
       vr += dt * ((RT(a, RT_RINF, i) - RT(a, RT_RMED, i - 1)) * A[q] + (RT(a, RT_RMED, i) - RT(a, RT_RINF, i)) * A[q - nsec]) *
             idr;
     }
-    a.d.vradint[q] = vr;
+    o.vr = vr;
   }
   const T idx = RT(a, RT_INVDXTHETA, i);
   T gradp = (p0 - pm) * (T)2.0 / (D[q] + D[qm]) * idx;
@@ -615,8 +620,34 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
     const T prev = (q > 0) ? a.d.sg_acct[q - 1] : (T)0.0;
     vt += (T)0.5 * dt * (a.d.sg_acct[q] + prev);
   }
-  a.d.vthetaint[q] = vt;
-  a.d.pressure[q] = p0;
+  o.vt = vt;
+  o.p = p0;
+  return o;
+}
+
+// ApplySubKeplerianBoundary (src/SideEuler.cu:296-320) at edge ring i, with the
+// current ring mean of the sound speed in the self-gravity form (Make1Dprofile(1))
+template <class T>
+__device__ __forceinline__ T subkeplerian_edge(const KArgs<T> &a, int i) {
+  const DevParams &P = a.P;
+  const Ctl *c = a.d.ctl;
+  const double r = RT64(a, RT_RMED, i);
+  const double cm = P.self_gravity ? a.d.csmean[i] : 0.0;
+  const double v = P.lambdadoubling == 0.0 ? sqrt(RT64(a, RT_VKEP2, i) - (P.self_gravity ? r * cm : 0.0))
+                                           : fargo_vkep(P, r, c->PhysicalTime, c->PhysicalTimeInitial, cm);
+  return (T)(v - r * c->OmegaFrame);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
+  pdl_enter();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.P.nrad || j >= a.P.nsec) return;
+  const SrcCell<T> o = source_cell(a, i, j);
+  const size_t q = (size_t)i * a.P.nsec + j;
+  if (i > 0) a.d.vradint[q] = o.vr;
+  a.d.vthetaint[q] = o.vt;
+  a.d.pressure[q] = o.p;
 }
 
 // ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
@@ -672,16 +703,7 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
                        (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])) /
                       ((T)0.5 * (D[q] + D[q - nsec]));
   }
-  if (!a.P.evanescent && (i == 0 || i == nrad - 1)) {
-    // ApplySubKeplerianBoundary (src/SideEuler.cu:296-320), with the current ring
-    // mean of the sound speed in the self-gravity form (Make1Dprofile(1))
-    const DevParams &P = a.P;
-    const double r = RT64(a, RT_RMED, i);
-    const double cm = P.self_gravity ? a.d.csmean[i] : 0.0;
-    const double v = P.lambdadoubling == 0.0 ? sqrt(RT64(a, RT_VKEP2, i) - (P.self_gravity ? r * cm : 0.0))
-                                             : fargo_vkep(P, r, c->PhysicalTime, c->PhysicalTimeInitial, cm);
-    a.d.vthetaint[q] = (T)(v - r * c->OmegaFrame);
-  }
+  if (!a.P.evanescent && (i == 0 || i == nrad - 1)) a.d.vthetaint[q] = subkeplerian_edge(a, i);
 }
 
 // Substep2Kernel (src/Kernels.cu:409-434) + kernel (src/Kernels.cu:438-479) +

@@ -108,8 +108,13 @@ __device__ __forceinline__ void butterfly(V *v) {
 template <int RAD, class V, class Out>
 __device__ __forceinline__ void fft_stage(const V *src, int N, int Ns, const V *tw, int lt, int G, Out out) {
   const int NR = N / RAD, tws = N / (Ns * RAD);
+  // Ns is a power of two in every stage before a radix-3 one (radices run 8, 4,
+  // 2, then 3): shift and mask instead of integer division there
+  const bool p2 = (Ns & (Ns - 1)) == 0;
+  const int lg = __ffs(Ns) - 1;
   for (int j = lt; j < NR; j += G) {
-    const int jj = j % Ns;
+    const int jj = p2 ? (j & (Ns - 1)) : j % Ns;
+    const int jb = p2 ? (j >> lg) : j / Ns;
     V v[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; r++) {
@@ -117,7 +122,7 @@ __device__ __forceinline__ void fft_stage(const V *src, int N, int Ns, const V *
       if (r > 0) v[r] = cmul(v[r], tw[r * jj * tws]);
     }
     butterfly<RAD>(v);
-    const int idxD = (j / Ns) * Ns * RAD + jj;
+    const int idxD = jb * Ns * RAD + jj;
 #pragma unroll
     for (int r = 0; r < RAD; r++) out(idxD + r * Ns, v[r]);
   }

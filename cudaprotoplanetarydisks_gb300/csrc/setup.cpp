@@ -338,7 +338,8 @@ void host_init_euler(const fargo_params &p, HostState &h, const DevParams &dp, C
 void host_ring_table(const fargo_params &p, const HostState &h, const DevParams &dp, std::vector<double> &tab) {
   const int n1 = p.nrad + 1, NSEC = p.nsec;
   tab.assign((size_t)RT_COUNT * n1, 0.0);
-  auto T = [&](int row, int i) -> double & { return tab[(size_t)row * n1 + i]; };
+  // ring-major: the rows of one ring are adjacent (one base address per ring on the device)
+  auto T = [&](int row, int i) -> double & { return tab[(size_t)i * RT_COUNT + row]; };
   auto at = [](const std::vector<double> &v, size_t i) { return i < v.size() ? v[i] : 0.0; };
   for (int i = 0; i < n1; i++) {
     T(RT_RINF, i) = h.Rinf[i];
