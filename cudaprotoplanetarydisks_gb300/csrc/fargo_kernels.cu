@@ -858,31 +858,46 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
     if (rr >= 2 && rr <= TR + 2) sV[rr - 2][x] = vr;
   }
   __syncthreads();
-  // StarRadKernel: slopes of rings k = i0-1 .. i0+TR (zero at the first and last ring)
-  for (int e = y; e < NS * (TR + 2); e += ny) {
-    const int f = e / (TR + 2), dd = e - f * (TR + 2), k = i0 - 1 + dd;
-    T v = (T)0.0;
-    if (k > 0 && k < nrad - 1) {
-      const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
-      const T dqm = (w0 - wm) * RT(a, RT_INVDIFFRMED, k);
-      const T dqp = (wp - w0) * RT(a, RT_INVDIFFRMED, k + 1);
-      v = (dqp * dqm > (T)0.0) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+  // StarRadKernel: slopes of rings k = i0-1 .. i0+TR (zero at the first and last
+  // ring), the seven streams of a ring together
+  for (int dd = y; dd < TR + 2; dd += ny) {
+    const int k = i0 - 1 + dd;
+    const bool in = k > 0 && k < nrad - 1;
+    const T idm0 = in ? RT(a, RT_INVDIFFRMED, k) : (T)0.0, idm1 = in ? RT(a, RT_INVDIFFRMED, k + 1) : (T)0.0;
+#pragma unroll
+    for (int f = 0; f < NS; f++) {
+      T v = (T)0.0;
+      if (in) {
+        const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
+        const T dqm = (w0 - wm) * idm0;
+        const T dqp = (wp - w0) * idm1;
+        v = (dqp * dqm > (T)0.0) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+      }
+      sD[f][dd][x] = v;
     }
-    sD[f][dd][x] = v;
   }
   __syncthreads();
   // StarRadKernel2: upwind values at the interfaces m = i0 .. i0+TR
-  for (int e = y; e < NS * (TR + 1); e += ny) {
-    const int f = e / (TR + 1), ss = e - f * (TR + 1), m = i0 + ss;
-    T st = (T)0.0;
-    if (m > 0 && m < nrad) {
-      const T v = sV[ss][x];
-      if (v > (T)0.0)
-        st = sW[f][ss + 1][x] + (RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt) * (T)0.5 * sD[f][ss][x];
-      else
-        st = sW[f][ss + 2][x] - (RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt) * (T)0.5 * sD[f][ss + 1][x];
+  for (int ss = y; ss < TR + 1; ss += ny) {
+    const int m = i0 + ss;
+    const bool in = m > 0 && m < nrad;
+    const T v = sV[ss][x];
+    T lo = (T)0.0, hi = (T)0.0;
+    if (in) {
+      lo = RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt;
+      hi = RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt;
     }
-    sS[f][ss][x] = st;
+#pragma unroll
+    for (int f = 0; f < NS; f++) {
+      T st = (T)0.0;
+      if (in) {
+        if (v > (T)0.0)
+          st = sW[f][ss + 1][x] + lo * (T)0.5 * sD[f][ss][x];
+        else
+          st = sW[f][ss + 2][x] - hi * (T)0.5 * sD[f][ss + 1][x];
+      }
+      sS[f][ss][x] = st;
+    }
   }
   __syncthreads();
   if (!col) return;
