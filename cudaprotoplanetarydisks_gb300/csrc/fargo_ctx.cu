@@ -60,6 +60,7 @@ struct fargo_ctx {
   unsigned long long cond_handle = 0;
   bool use_graph = true;
   bool use_pdl = true;   // programmatic dependent launch between the step kernels
+  bool use_rotation = true;  // rotated DT loop (self-gravity ahead of each substep)
 };
 
 namespace {
@@ -246,8 +247,12 @@ int build_graph(fargo_ctx *c) {
   LaunchProbe probe;
   std::memset(&probe, 0, sizeof(probe));
   g_probe = &probe;
+  // with self-gravity the loop runs rotated: the prefix also runs the first
+  // substep's CFL/force kernel and transforms, each substep the next one's
+  const bool rot = c->use_rotation && rotation_allowed<T>(a, &c->side);
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   launch_dt_prefix<T>(a, c->stream);
+  if (rot) launch_dt_head<T>(a, c->stream, &c->side);
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &gp));
   c->launches_per_dt = probe.count;
@@ -267,7 +272,7 @@ int build_graph(fargo_ctx *c) {
   CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   probe.count = 0;
   g_probe = &probe;
-  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side);
+  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side, rot ? ROT_HEAD_DONE | ROT_NEXT_HEAD : 0u);
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &body));
   c->launches_per_substep = probe.count;
@@ -631,6 +636,8 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   if (ng && ng[0] == '1') c->use_graph = false;
   const char *np = std::getenv("FARGO_NO_PDL");
   if (np && np[0] == '1') c->use_pdl = false;
+  const char *nr = std::getenv("FARGO_NO_ROTATE");
+  if (nr && nr[0] == '1') c->use_rotation = false;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

@@ -64,6 +64,7 @@ struct KArgs {
   unsigned long long cond_handle;  // cudaGraphConditionalHandle of the DT while-loop
   int use_cond;                    // 1: k_end sets the while-loop condition
   int pdl;                         // launch with programmatic dependent launch
+  int guard;                       // 1: return at once when the DT loop is done (a next substep's kernels)
   SgDev sg;
 };
 

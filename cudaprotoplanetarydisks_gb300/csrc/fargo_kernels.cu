@@ -68,6 +68,7 @@ __device__ __forceinline__ double ring_total(const double *ring_force, int nrad,
 template <class T>
 __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   pdl_enter();
+  if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   constexpr int NW = 8;                       // warps of the 256-thread CTA
   constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
   const DevParams &P = a.P;
@@ -1288,27 +1289,31 @@ thread_local LaunchProbe *g_probe = nullptr;
 
 template <class T>
 void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes,
-                            const SideBranch *side) {
+                            const SideBranch *side, unsigned rot) {
   KArgs<T> a = a0;
   const DevParams &P = a.P;
   const dim3 b2(64, 4);
   const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
   bool joined = true;
+  const bool head_done = rot & ROT_HEAD_DONE;
   const bool bc1 = (which_mask & SUBK_BC1) && (P.open_inner || P.non_reflecting || P.evanescent);
-  const bool sg_side = side && (which_mask & SUBK_SG) && P.self_gravity && (which_mask & SUBK_CFL_FORCES) && !bc1;
-  // the fork point precedes k_cfl_forces; the transforms are issued after it (the
-  // earlier-issued grid is scheduled first, and the CFL kernel is the longer)
-  if (sg_side) cudaEventRecord(side->fork2, s);
-  if (which_mask & SUBK_CFL_FORCES) {
-    // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
-    // 3 forces + potential only (no planet advance, no time update)
-    launch_k(a.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, a);
-    MARK("k_cfl_forces");
-  }
-  if (sg_side) {
-    cudaStreamWaitEvent(side->s2, side->fork2, 0);
-    launch_selfgravity(a, side->s2);
-    cudaEventRecord(side->join2, side->s2);
+  const bool sg_side =
+      !head_done && side && (which_mask & SUBK_SG) && P.self_gravity && (which_mask & SUBK_CFL_FORCES) && !bc1;
+  if (!head_done) {
+    // the fork point precedes k_cfl_forces; the transforms are issued after it
+    // (the earlier-issued grid is scheduled first, and the CFL kernel is the longer)
+    if (sg_side) cudaEventRecord(side->fork2, s);
+    if (which_mask & SUBK_CFL_FORCES) {
+      // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
+      // 3 forces + potential only (no planet advance, no time update)
+      launch_k(a.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, a);
+      MARK("k_cfl_forces");
+    }
+    if (sg_side) {
+      cudaStreamWaitEvent(side->s2, side->fork2, 0);
+      launch_selfgravity(a, side->s2);
+      cudaEventRecord(side->join2, side->s2);
+    }
   }
   if (which_mask & SUBK_CFL_FORCES) {
     if (a.mode == 0 || a.mode == 2) {
@@ -1330,7 +1335,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     MARK("k_correct_vtheta");
   }
   if (which_mask & SUBK_BC1) launch_boundaries(a, s);
-  if ((which_mask & SUBK_SG) && P.self_gravity) {
+  if ((which_mask & SUBK_SG) && P.self_gravity && !head_done) {
     if (sg_side) cudaStreamWaitEvent(s, side->join2, 0);
     else launch_selfgravity(a, s);
   }
@@ -1376,7 +1381,50 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     launch_k(a.pdl, k_end<T>, dim3(1), dim3(256), 0, s, a);
     MARK("k_end");
   }
+  if (rot & ROT_NEXT_HEAD) {
+    // the next substep's transforms (they read only the density, final now) beside
+    // its CFL/force kernel; both return at once when this substep ended the DT
+    // (the loop flag k_end just set, which nothing else writes before the next k_end)
+    cudaEventRecord(side->fork2, s);
+    cudaStreamWaitEvent(side->s2, side->fork2, 0);
+    KArgs<T> g2s = a;
+    g2s.guard = 1;
+    launch_selfgravity(g2s, side->s2);
+    cudaEventRecord(side->join2, side->s2);
+    // the next substep's CFL/force kernel, after this substep's planet update
+    // (it reads the planet parameters that update leaves)
+    if (!joined) {
+      cudaStreamWaitEvent(s, side->join, 0);
+      joined = true;
+    }
+    KArgs<T> g = a;
+    g.guard = 1;
+    launch_k(g.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, g);
+    MARK("k_cfl_forces");
+    cudaStreamWaitEvent(s, side->join2, 0);
+  }
   if (!joined) cudaStreamWaitEvent(s, side->join, 0);
+}
+
+// The first substep's CFL/force kernel and self-gravity transforms, side by side,
+// ahead of a DT loop whose substeps launch the next substep's (ROT_NEXT_HEAD).
+template <class T>
+void launch_dt_head(const KArgs<T> &a, cudaStream_t s, const SideBranch *side) {
+  cudaEventRecord(side->fork2, s);
+  launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
+  MARK("k_cfl_forces");
+  cudaStreamWaitEvent(side->s2, side->fork2, 0);
+  launch_selfgravity(a, side->s2);
+  cudaEventRecord(side->join2, side->s2);
+  cudaStreamWaitEvent(s, side->join2, 0);
+}
+
+// whether a DT loop may run rotated: self-gravity, no boundary kernel that
+// changes the density, side streams available
+template <class T>
+bool rotation_allowed(const KArgs<T> &a, const SideBranch *side) {
+  const DevParams &P = a.P;
+  return side && P.self_gravity && !(P.open_inner || P.non_reflecting || P.evanescent);
 }
 
 template <class T>
@@ -1476,7 +1524,9 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
 
 #define INSTANTIATE(T)                                                                                  \
   template void launch_substep_kernels<T>(const KArgs<T> &, cudaStream_t, unsigned, size_t,            \
-                                         const SideBranch *);                                          \
+                                         const SideBranch *, unsigned);                                \
+  template void launch_dt_head<T>(const KArgs<T> &, cudaStream_t, const SideBranch *);                  \
+  template bool rotation_allowed<T>(const KArgs<T> &, const SideBranch *);                              \
   template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
   template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \

@@ -74,9 +74,19 @@ struct SideBranch {
   cudaEvent_t fork2, join2;
 };
 
+// DT loop rotation (the DT graph with self-gravity): a substep whose CFL/force
+// kernel and self-gravity transforms ran ahead (ROT_HEAD_DONE) launches the next
+// substep's after its k_end (ROT_NEXT_HEAD), guarded so that they do nothing once
+// the DT is done; launch_dt_head runs the first substep's in the DT prefix.
+#define ROT_HEAD_DONE 0x1u
+#define ROT_NEXT_HEAD 0x2u
 template <class T>
 void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes,
-                            const SideBranch *side = nullptr);
+                            const SideBranch *side = nullptr, unsigned rot = 0);
+template <class T>
+void launch_dt_head(const KArgs<T> &a, cudaStream_t s, const SideBranch *side);
+template <class T>
+bool rotation_allowed(const KArgs<T> &a, const SideBranch *side);
 template <class T>
 void launch_dt_prefix(const KArgs<T> &a, cudaStream_t s);
 template <class T>

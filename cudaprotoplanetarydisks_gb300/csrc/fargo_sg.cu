@@ -200,6 +200,7 @@ static inline int sg_group(int n) {
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
   pdl_enter();
+  if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x, G = blockDim.x;
@@ -231,6 +232,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   pdl_enter();
+  if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int m = blockIdx.x, n0 = 2 * a.P.nrad, nrad = a.P.nrad;
@@ -265,6 +267,7 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   pdl_enter();
+  if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
