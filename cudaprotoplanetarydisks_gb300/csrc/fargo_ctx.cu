@@ -45,6 +45,7 @@ struct fargo_ctx {
   double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
   double *ring_vmoy = nullptr, *ring_smax = nullptr, *ring_force = nullptr, *lostbydisk = nullptr;
   // self-gravity
+  void *spec2_r = nullptr, *spec2_t = nullptr;
   void *spec_r = nullptr, *spec_t = nullptr, *khat_r = nullptr, *khat_t = nullptr, *tw1 = nullptr, *tw0 = nullptr;
   double2 *khat64_r = nullptr, *khat64_t = nullptr, *tw1_64 = nullptr, *tw0_64 = nullptr;  // FP64 set-up
   double *kr = nullptr, *kt = nullptr;
@@ -147,6 +148,8 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
   a.sg.spec_t = c->spec_t;
+  a.sg.spec2_r = c->spec2_r;
+  a.sg.spec2_t = c->spec2_t;
   a.sg.khat_r = c->khat_r;
   a.sg.khat_t = c->khat_t;
   a.sg.tw1 = c->tw1;
@@ -381,6 +384,8 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     const size_t cx = 2 * E;
     if ((rc = dev_alloc(c, &c->spec_r, (size_t)M * p.nrad * cx))) return rc;
     if ((rc = dev_alloc(c, &c->spec_t, (size_t)M * p.nrad * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->spec2_r, (size_t)M * p.nrad * cx))) return rc;
+    if ((rc = dev_alloc(c, &c->spec2_t, (size_t)M * p.nrad * cx))) return rc;
     if ((rc = dev_alloc(c, &c->khat_r, (size_t)M * n0 * cx))) return rc;
     if ((rc = dev_alloc(c, &c->khat_t, (size_t)M * n0 * cx))) return rc;
     if ((rc = dev_alloc(c, &c->tw1, (size_t)p.nsec * cx))) return rc;

@@ -37,6 +37,7 @@ struct DiskPtrs {
 struct SgDev {
   // per-step buffers, complex of the field type (double2 or float2)
   void *spec_r, *spec_t;        // work spectra, [m][i], M x nrad
+  void *spec2_r, *spec2_t;      // convolved spectra, [i][m], nrad x M
   void *khat_r, *khat_t;        // kernel spectra, [m][k], M x 2 nrad
   const void *tw1, *tw0;        // exp(-2 pi i t / N) for N = nsec and N = 2 nrad
   // set-up, FP64 (the same buffers as above in the FP64 mode)

@@ -215,7 +215,7 @@ FARGO_HD void fargo_rotate_psys(Ctl &c, double angle) {
   }
 }
 
-// DerivMotionRK5  src/RungeKutta.cu:30-67 (the feel-others term divides by the
+// DerivMotionRK5  src/RungeKutta.cu:30-67 (the feel-others term uses the
 // distance of body j to the star, as the reference does).  NB > 0: NB bodies,
 // a compile-time count that keeps every array in registers; NB == 0: nb bodies.
 template <int NB>
@@ -224,24 +224,29 @@ FARGO_HD void fargo_deriv_rk5(const double *q, const double *pm, double *deriv, 
   const int nb = NB > 0 ? NB : nb_rt;
   const double *x = q, *y = x + nb, *vx = y + nb, *vy = vx + nb;
   double *dx = deriv, *dy = dx + nb, *dvx = dy + nb, *dvy = dvx + nb;
-  double Dist[NB > 0 ? NB : FARGO_MAXPL];
+  // 1/d^3 of each body with one divide (the reference divides three times; an
+  // FP64 divide is a long dependent sequence on this GPU's FP64 pipe)
+  double Inv3[NB > 0 ? NB : FARGO_MAXPL];
 #pragma unroll
-  for (int i = 0; i < nb; i++) Dist[i] = sqrt(x[i] * x[i] + y[i] * y[i]);
+  for (int i = 0; i < nb; i++) {
+    const double d = sqrt(x[i] * x[i] + y[i] * y[i]);
+    Inv3[i] = 1.0 / (d * d * d);
+  }
 #pragma unroll
   for (int i = 0; i < nb; i++) {
     dx[i] = vx[i];
     dy[i] = vy[i];
-    dvx[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * x[i];
-    dvy[i] = -1.0 * 1.0 / Dist[i] / Dist[i] / Dist[i] * y[i];
+    dvx[i] = -1.0 * Inv3[i] * x[i];
+    dvy[i] = -1.0 * Inv3[i] * y[i];
 #pragma unroll
     for (int j = 0; j < nb; j++) {
       if (indirect) {
-        dvx[i] -= 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * x[j];
-        dvy[i] -= 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * y[j];
+        dvx[i] -= 1.0 * pm[j] * Inv3[j] * x[j];
+        dvy[i] -= 1.0 * pm[j] * Inv3[j] * y[j];
       }
       if ((j != i) && (feelothers[i] == 1)) {
-        dvx[i] += 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * (x[j] - x[i]);
-        dvy[i] += 1.0 * pm[j] / Dist[j] / Dist[j] / Dist[j] * (y[j] - y[i]);
+        dvx[i] += 1.0 * pm[j] * Inv3[j] * (x[j] - x[i]);
+        dvy[i] += 1.0 * pm[j] * Inv3[j] * (y[j] - y[i]);
       }
     }
   }
@@ -387,7 +392,7 @@ FARGO_HD void fargo_planet_params(Ctl &c, const DevParams &P, double t) {
     c.py[k] = y;
     c.pm[k] = mp;
     c.ps2[k] = sm * sm;
-    c.pinvd3[k] = 1.0 / PD / PD / PD;
+    c.pinvd3[k] = 1.0 / (PD * PD * PD);  // one divide (the reference divides three times)
   }
   c.nbody = nbody;
 }

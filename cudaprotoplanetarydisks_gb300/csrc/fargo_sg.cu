@@ -228,7 +228,8 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
 // (S_r, K^r) and (S_theta, K^theta) side by side.  Forward transform of the
 // zero-padded column; its last stage forms -G K^ S^ (ComputeConvolutionKernel
 // src/Kernels.cu:871-890), conjugated so that the forward routine runs the
-// inverse; the inverse's last stage stores rows < nrad back in place.
+// inverse; the inverse's last stage stores rows < nrad ring-major (the
+// scattered side of the transpose is a store here, a contiguous load after).
 template <class T>
 __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   pdl_enter();
@@ -242,6 +243,7 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   const V *twg = (const V *)a.sg.tw0;
   const V *kh = (const V *)(g == 0 ? a.sg.khat_r : a.sg.khat_t) + (size_t)m * n0;
   V *col = (V *)(g == 0 ? a.sg.spec_r : a.sg.spec_t) + (size_t)m * nrad;
+  V *row = (V *)(g == 0 ? a.sg.spec2_r : a.sg.spec2_t) + m;  // ring-major output, stride M
 #pragma unroll 4
   for (int k = threadIdx.x; k < n0; k += blockDim.x) tw[k] = twg[k];
 #pragma unroll 4
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   });
   V *Y = (X == b0) ? b1 : b0;
   fft_run(X, Y, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V z, V *) {
-    if (k < nrad) col[k] = cconj(z);
+    if (k < nrad) row[(size_t)k * a.sg.M] = cconj(z);
   });
 }
 
@@ -273,17 +275,18 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
   V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
   const V *twg = (const V *)a.sg.tw1;
-  const V *spr = (const V *)a.sg.spec_r, *spt = (const V *)a.sg.spec_t;
+  // this ring's row of the ring-major spectra that k_sg_cols left
+  const V *spr = (const V *)a.sg.spec2_r + (size_t)i * M, *spt = (const V *)a.sg.spec2_t + (size_t)i * M;
 #pragma unroll 4
   for (int m = tid; m < nsec; m += G) {
     tw[m] = twg[m];
     V hr, ht;
     if (m < M) {
-      hr = spr[(size_t)m * nrad + i];
-      ht = spt[(size_t)m * nrad + i];
+      hr = spr[m];
+      ht = spt[m];
     } else {
-      hr = cconj(spr[(size_t)(nsec - m) * nrad + i]);
-      ht = cconj(spt[(size_t)(nsec - m) * nrad + i]);
+      hr = cconj(spr[nsec - m]);
+      ht = cconj(spt[nsec - m]);
     }
     // Z = H_r + i H_t, conjugated for the inverse
     b0[fpad(m)] = mk2(hr.x - ht.y, -(hr.y + ht.x));
