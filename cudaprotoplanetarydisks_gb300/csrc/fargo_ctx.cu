@@ -127,6 +127,7 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.invdphi = 1.0 / (2.0 * M_PI / (double)c->P.nsec);
   a.dtheta = 2.0 * FARGO_PI / (double)c->P.nsec;
   a.inv_nsec = 1.0 / (double)c->P.nsec;
+  a.shear_k = 2.0 * FARGO_PI * FARGO_CFLSECURITY / (double)c->P.nsec;
   {
     const double g = c->P.adiabaticindex;
     a.k64[KC_GM1] = g - 1.0;

@@ -55,6 +55,7 @@ struct KArgs {
   double invdphi;      // 1.0/(2.0*M_PI/(double)nsec)
   double dtheta;       // 2.0*PI/(double)nsec
   double inv_nsec;     // 1.0/nsec
+  double shear_k;      // 2.0*PI*CFLSECURITY/(double)nsec of the CFL shear limit
   // per-launch constants in both precisions (KC_*), read through KC()
   double k64[8];
   float k32[8];

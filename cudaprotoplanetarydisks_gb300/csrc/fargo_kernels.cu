@@ -47,6 +47,13 @@ __device__ __forceinline__ int jp1(int j, int n) { return j == n - 1 ? 0 : j + 1
 // mode 0: full substep start.  mode 1: CFL only (sloppy CFL at the DT start, or
 // the ConditionCFL entry point).  mode 2: forces, dt = sloppy_dt.  mode 3: forces
 // and potential only.
+// FP64 divide and square root for the single-thread decisions at the end of a
+// kernel: not inlined, so that the several calls share one copy of the code (run
+// once per launch by the one CTA that finishes last, it is fetched cold, and
+// instruction fetch, not arithmetic, sets its cost).  Same IEEE results.
+__device__ __noinline__ double div_once(double a, double b) { return a / b; }
+__device__ __noinline__ double sqrt_once(double x) { return sqrt(x); }
+
 // Total over the rings of component v of the per-ring force partials (SumAcc<T>
 // stored in 8 bytes), summed by one warp in a fixed order; valid in lane 0.
 template <class T>
@@ -281,7 +288,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
 #pragma unroll 8
     for (int k = 1 + lane; k < nrad; k += 32) m = max(m, __double_as_longlong(__ldcg(a.d.ring_smax + k)));
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) s_dtc[0] = (m > 0) ? CFLSECURITY / sqrt(__longlong_as_double(m)) : 1e30;
+    if (lane == 0) s_dtc[0] = (m > 0) ? div_once(CFLSECURITY, sqrt_once(__longlong_as_double(m))) : 1e30;
   }
   if (do_cfl && w == 5) {
     // shear limit 2 pi C / nsec / |Omega_k - Omega_k+1|: the largest difference
@@ -293,7 +300,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       if (d == d) m = max(m, __double_as_longlong(d));
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) s_dtc[1] = (m > 0) ? 2.0 * PI * CFLSECURITY / (double)nsec / __longlong_as_double(m) : 1e30;
+    if (lane == 0) s_dtc[1] = (m > 0) ? div_once(a.shear_k, __longlong_as_double(m)) : 1e30;
   }
   __syncthreads();
   if (tid == 0) {
@@ -304,7 +311,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
       const double DeltaT = (a.mode == 1) ? s_ctl[0] : s_ctl[0] - s_ctl[1];
       double newdt = fmin(s_dtc[0], s_dtc[1]);
       if (DeltaT < newdt) newdt = DeltaT;
-      double q = DeltaT / newdt;
+      double q = div_once(DeltaT, newdt);
       int cfl;
       if (!(q > 0.0) || !(q < 1.0e8)) {
         c->err |= FARGO_DEVERR_CFL;
@@ -315,7 +322,7 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
         cfl = (int)ceil(q);
       }
       c->cfl = cfl;
-      dt = DeltaT / (double)cfl;
+      dt = div_once(DeltaT, (double)cfl);
       if (a.mode == 1) c->sloppy_dt = dt;
     } else {
       dt = s_ctl[2];
