@@ -171,6 +171,25 @@ def kernel_bytes(name, params, esize):
     return 0
 
 
+def ncu_traffic(kernel, cfg, mode="fp32"):
+    """DRAM bytes (read + write) of one launch of `kernel` from the committed ncu
+    summary profiles/kernels_<cfg>_<mode>.md (one cold-cache capture), or None."""
+    path = os.path.join(ROOT, "profiles", f"kernels_{cfg}_{mode}.md")
+    if not os.path.exists(path):
+        return None
+    scale = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
+    for line in open(path):
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) > 4 and cells[0] == kernel:
+            try:
+                rd, ru = cells[2].split()
+                wr, wu = cells[3].split()
+                return float(rd) * scale[ru] + float(wr) * scale[wu]
+            except (ValueError, KeyError):
+                return None
+    return None
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -344,7 +363,9 @@ def run_own(args, world, rank, local):
         "clocks": f32["clocks"],
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "alg_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms, "traffic": None},
+                     "alg_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms,
+                     "traffic": ncu_traffic(dom_name, args.config),
+                     "traffic_source": f"profiles/kernels_{args.config}_fp32.md (ncu, one cold-cache launch)"},
         "step_roofline": {"alg_bytes_per_cell_update": step_alg,
                           "achieved_GBs": f32["value"] * step_alg / 1e9,
                           "frac": f32["value"] * step_alg / 1e9 / hbm_peak},
