@@ -61,7 +61,7 @@ struct fargo_ctx {
   unsigned long long cond_handle = 0;
   bool use_graph = true;
   bool use_pdl = true;   // programmatic dependent launch between the step kernels
-  bool use_rotation = true;  // rotated DT loop (self-gravity ahead of each substep)
+  bool use_rotation = false;  // rotated DT loop (self-gravity ahead of each substep)
 };
 
 namespace {
@@ -642,8 +642,8 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   if (ng && ng[0] == '1') c->use_graph = false;
   const char *np = std::getenv("FARGO_NO_PDL");
   if (np && np[0] == '1') c->use_pdl = false;
-  const char *nr = std::getenv("FARGO_NO_ROTATE");
-  if (nr && nr[0] == '1') c->use_rotation = false;
+  const char *nr = std::getenv("FARGO_ROTATE");
+  if (nr && nr[0] == '1') c->use_rotation = true;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

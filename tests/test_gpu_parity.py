@@ -134,7 +134,7 @@ def _disk_with_env(params, planets, prec, env):
                 os.environ[k] = v
 
 
-@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_NO_ROTATE", "FARGO_AZ_GLOBAL"])
+@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_AZ_GLOBAL"])
 def test_code_paths_are_bitwise_identical(env):
     # the conditional-graph DT loop vs the host loop; programmatic dependent
     # launch vs plain launches; the rotated DT loop (each substep launches the
