@@ -72,28 +72,117 @@ __device__ __forceinline__ double ring_total(const double *ring_force, int nrad,
   return s.value();
 }
 
+// "No limit" of a per-ring time step: a NaN bit pattern, above every non-negative
+// double (+inf included) when compared as a signed 64-bit integer.
+#define RING_NO_LIMIT 0x7ff8000000000000LL
+
+// Inputs of one cell of the CFL/force pass.
 template <class T>
-__global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
+struct CflCell {
+  T vt, vtn, vr0, vr1, cs, dn, cf, sf, cp, sp;
+};
+
+// Per-ring values of the CFL/force pass.
+template <class T>
+struct CflRing {
+  T rm, surf, invdrad, invdxt, invmind, cs;
+  RingMean<T> vm;
+};
+
+template <class T>
+__device__ __forceinline__ void cfl_cell_load(const KArgs<T> &a, int i, int j, bool cfl_ring, bool do_forces,
+                                              CflCell<T> &q) {
+  const int nsec = a.P.nsec;
+  const size_t o = (size_t)i * nsec + j;
+  q.vt = a.d.vtheta[o];
+  q.vtn = q.vr0 = q.vr1 = q.cs = q.dn = q.cf = q.sf = q.cp = q.sp = (T)0;
+  if (cfl_ring) {
+    q.vtn = a.d.vtheta[(size_t)i * nsec + jp1(j, nsec)];
+    q.vr0 = a.d.vrad[o];
+    q.vr1 = a.d.vrad[o + nsec];
+    if (a.d.cs) q.cs = a.d.cs[o];
+  }
+  if (do_forces) {
+    q.dn = a.d.dens[o];
+    q.cf = a.d.cosFt[j];
+    q.sf = a.d.sinFt[j];
+    if (a.P.nb > 0) {
+      q.cp = a.d.cosP[j];
+      q.sp = a.d.sinP[j];
+    }
+  }
+}
+
+// ConditionCFLKernel2D1 + 2D2 for one cell: the sum S of the squared inverse time
+// steps.  min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
+// monotonically), so only S_j is formed per cell, with per-ring reciprocals.
+template <class T>
+__device__ __forceinline__ T cfl_cell_S(const KArgs<T> &a, const CflCell<T> &q, const CflRing<T> &r) {
+  const T vres = a.P.fast_transport ? r.vm.sub_from(q.vt) : q.vt;
+  const T cs = a.d.cs ? q.cs : r.cs;
+  const T invdt1 = cs * r.invmind;
+  const T invdt2 = fabs(q.vr0) * r.invdrad;
+  const T invdt3 = fabs(vres) * r.invdxt;
+  T dvr = q.vr1 - q.vr0;
+  T dvt = q.vtn - q.vt;
+  if (dvr >= (T)0.0) dvr = (T)1e-10;
+  else dvr = -dvr;
+  if (dvt >= (T)0.0) dvt = (T)1e-10;
+  else dvt = -dvt;
+  const T a4 = dvr * r.invdrad, b4 = dvt * r.invdxt;
+  T invdt4 = (b4 > a4) ? b4 : a4;
+  invdt4 *= (T)(4.0 * CVNR * CVNR);
+  return invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
+}
+
+// ComputeForceKernel term of one cell on one body (k = 0; all Hill-cut levels
+// coincide since a = rh = 0): 1/d^3 from rsqrt, compensated or FP64 ring sums.
+template <class T>
+__device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T rs2, SumAcc<T> &fx, SumAcc<T> &fy) {
+  const T dx = xc - x, dy = yc - y;
+  const T ir = rsqrt(dx * dx + dy * dy + rs2);
+  const T InvDist3 = ir * ir * ir;
+  fx.add(cellmass * dx * InvDist3);
+  fy.add(cellmass * dy * InvDist3);
+}
+
+// CPT > 0: nsec <= 256 * CPT, and every thread holds the inputs of its CPT cells
+// in registers, loaded in one batch ahead of the ring mean (one memory latency
+// instead of one per pass and per cell).  CPT = 0: any nsec, cells streamed.
+// Each thread visits its cells in the same order either way (j = tid, tid + 256,
+// ...), so both give the same sums.
+// Per ring the CTA also forms the two time-step limits that the last CTA takes
+// the minimum of: C/sqrt(max S) of its cells (rings >= 1) and the shear limit
+// 2 pi C / nsec / |Omega_i - Omega_i+1| (rings < nrad - 1), with Omega_i+1 from the
+// mean of ring i+1 summed in the same order as ring i+1's own CTA sums it.  The
+// minimum over rings of these correctly rounded, monotone maps equals the map of
+// the extreme S or difference, so the result is that of one sqrt and one divide
+// of the maxima, while the last CTA's serial tail holds integer minima only.
+template <class T, int CPT>
+__global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   pdl_enter();
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   constexpr int NW = 8;                       // warps of the 256-thread CTA
   constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
+  constexpr int NC = CPT > 0 ? CPT : 1;
   const DevParams &P = a.P;
   const int i = blockIdx.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
   const int lane = tid & 31, w = tid >> 5;
   Ctl *c = a.d.ctl;
   __shared__ SumAcc<T> s_part[NW][NV];
-  __shared__ SumAcc<T> s_vpart[NW];
+  __shared__ SumAcc<T> s_vpart[2][NW];
   __shared__ T s_mx[NW];
   __shared__ T s_body[FARGO_MAXPL + 1][3];
   __shared__ T s_pot[FARGO_MAXPL][5];
-  __shared__ double s_vmoy;
+  __shared__ double s_om[2];
   __shared__ RingMean<T> s_vm;
   __shared__ int s_nbody, s_last;
   __shared__ double s_ctl[5];  // DT, dtemp, sloppy_dt, PhysicalTime, err (read before any write)
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
   const bool do_step = (a.mode == 0 || a.mode == 2);
+  const bool cfl_ring = do_cfl && i > 0;
+  const bool shear_ring = do_cfl && i < nrad - 1;
   // the control scalars the last block's decision reads, fetched up front by
   // every block so that the last one has them at hand
   if (tid >= 64 && tid < 69) {
@@ -118,39 +207,68 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     }
     if (tid == 0) s_nbody = c->nbody;
   }
-  const T *dens = a.d.dens + (size_t)i * nsec;
   const T *vth = a.d.vtheta + (size_t)i * nsec;
+  const T *vth1 = vth + nsec;
+  CflCell<T> q[NC];
+  T vn[NC];
+  if (CPT > 0) {
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+      const int j = tid + k * 256;
+      if (j < nsec) {
+        cfl_cell_load(a, i, j, cfl_ring, do_forces, q[k]);
+        vn[k] = shear_ring ? vth1[j] : (T)0;
+      }
+    }
+  }
   if (do_cfl) {
-    // ConditionCFLKernel1D: ring mean of Vtheta
-    SumAcc<T> v;
+    // ConditionCFLKernel1D: ring means of Vtheta (ring i, and ring i+1 for the shear)
+    SumAcc<T> v, v1;
     v.zero();
-    for (int j = tid; j < nsec; j += blockDim.x) v.add(vth[j]);
+    v1.zero();
+    if (CPT > 0) {
+#pragma unroll
+      for (int k = 0; k < NC; k++)
+        if (tid + k * 256 < nsec) {
+          v.add(q[k].vt);
+          v1.add(vn[k]);
+        }
+    } else {
+      for (int j = tid; j < nsec; j += 256) v.add(vth[j]);
+      if (shear_ring)
+        for (int j = tid; j < nsec; j += 256) v1.add(vth1[j]);
+    }
     warp_sum(v);
-    if (lane == 0) s_vpart[w] = v;
+    if (lane == 0) s_vpart[0][w] = v;
+    if (shear_ring) {
+      warp_sum(v1);
+      if (lane == 0) s_vpart[1][w] = v1;
+    }
   }
   __syncthreads();
-  if (do_cfl) {
-    if (tid == 0) {
-      SumAcc<T> v = s_vpart[0];
-      for (int k = 1; k < NW; k++) v.merge(s_vpart[k]);
-      const double vmoy = sizeof(T) == 8 ? v.value() / (double)nsec : v.value() * a.inv_nsec;
-      s_vmoy = vmoy;
-      s_vm.set(vmoy);
-      // ring angular velocity of the shear limit (ConditionCFLKernel2D2)
-      a.d.ring_vmoy[i] = vmoy * RT64(a, RT_INVRMED, i);
-    }
-    __syncthreads();
+  if (do_cfl && (tid == 0 || (tid == 32 && shear_ring))) {
+    const int h = tid >> 5;
+    SumAcc<T> v = s_vpart[h][0];
+    for (int k = 1; k < NW; k++) v.merge(s_vpart[h][k]);
+    const double vmoy = sizeof(T) == 8 ? v.value() / (double)nsec : v.value() * a.inv_nsec;
+    if (h == 0) s_vm.set(vmoy);
+    // ring angular velocity of the shear limit (ConditionCFLKernel2D2)
+    s_om[h] = vmoy * RT64(a, RT_INVRMED, i + h);
   }
+  if (do_cfl) __syncthreads();
   const int nbody = do_forces ? s_nbody : 0;
-  const bool cfl_ring = do_cfl && i > 0;
-  const T rm = RT(a, RT_RMED, i), surf = RT(a, RT_SURF, i);
-  T invdrad = (T)0, invdxt = (T)0, invmind = (T)0;
+  CflRing<T> r;
+  r.rm = RT(a, RT_RMED, i);
+  r.surf = RT(a, RT_SURF, i);
+  r.invdrad = r.invdxt = r.invmind = r.cs = (T)0;
+  r.vm.hi = r.vm.lo = (T)0;
   if (cfl_ring) {
-    invdrad = RT(a, RT_INVDRAD, i);
-    invdxt = RT(a, RT_INVDXTHETA_CFL, i);
-    invmind = RT(a, RT_INVMIND, i);
+    r.invdrad = RT(a, RT_INVDRAD, i);
+    r.invdxt = RT(a, RT_INVDXTHETA_CFL, i);
+    r.invmind = RT(a, RT_INVMIND, i);
+    r.cs = a.d.cs ? (T)0 : RT(a, RT_CS, i);
+    r.vm = s_vm;
   }
-  const T *vr = a.d.vrad + (size_t)i * nsec;
   T *pot = a.d.potential + (size_t)i * nsec;
   T mx = (T)0.0;
   const int nchunk = do_forces ? (nbody + 1) >> 1 : 1;
@@ -174,50 +292,19 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     fy0.zero();
     fx1.zero();
     fy1.zero();
-    for (int j = tid; j < nsec; j += blockDim.x) {
+    auto cell = [&](int j, const CflCell<T> &e) {
       if (first && cfl_ring) {
-        // ConditionCFLKernel2D1 + 2D2: per-cell time step, ring minimum.
-        // min_j C/sqrt(S_j) = C/sqrt(max_j S_j) exactly (sqrt and division round
-        // monotonically), so only S_j is formed per cell, with per-ring reciprocals.
-        const T vres = P.fast_transport ? s_vm.sub_from(vth[j]) : vth[j];
-        const T cs = a.d.cs ? a.d.cs[(size_t)i * nsec + j] : RT(a, RT_CS, i);
-        const T invdt1 = cs * invmind;
-        const T invdt2 = fabs(vr[j]) * invdrad;
-        const T invdt3 = fabs(vres) * invdxt;
-        T dvr = vr[j + nsec] - vr[j];
-        T dvt = vth[jp1(j, nsec)] - vth[j];
-        if (dvr >= (T)0.0) dvr = (T)1e-10;
-        else dvr = -dvr;
-        if (dvt >= (T)0.0) dvt = (T)1e-10;
-        else dvt = -dvt;
-        const T a4 = dvr * invdrad, b4 = dvt * invdxt;
-        T invdt4 = (b4 > a4) ? b4 : a4;
-        invdt4 *= (T)(4.0 * CVNR * CVNR);
-        const T S = invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
+        const T S = cfl_cell_S(a, e, r);
         mx = (S > mx) ? S : mx;
       }
       if (do_forces) {
-        // ComputeForceKernel (k = 0; all Hill-cut levels coincide since a = rh = 0):
-        // per-cell terms in T (1/d^3 from rsqrt), compensated or FP64 ring sums
-        const T cellmass = surf * dens[j];
-        const T xc = rm * a.d.cosFt[j], yc = rm * a.d.sinFt[j];
-        {
-          const T dx = xc - x0, dy = yc - y0;
-          const T ir = rsqrt(dx * dx + dy * dy + r0);
-          const T InvDist3 = ir * ir * ir;
-          fx0.add(cellmass * dx * InvDist3);
-          fy0.add(cellmass * dy * InvDist3);
-        }
-        if (two) {
-          const T dx = xc - x1, dy = yc - y1;
-          const T ir = rsqrt(dx * dx + dy * dy + r1);
-          const T InvDist3 = ir * ir * ir;
-          fx1.add(cellmass * dx * InvDist3);
-          fy1.add(cellmass * dy * InvDist3);
-        }
+        const T cellmass = r.surf * e.dn;
+        const T xc = r.rm * e.cf, yc = r.rm * e.sf;
+        cell_force(xc, yc, cellmass, x0, y0, r0, fx0, fy0);
+        if (two) cell_force(xc, yc, cellmass, x1, y1, r1, fx1, fy1);
         if (first && P.nb > 0) {
           // planet part of the potential (positions at the start of the substep)
-          const T x = rm * a.d.cosP[j], y = rm * a.d.sinP[j];
+          const T x = r.rm * e.cp, y = r.rm * e.sp;
           T phi = (T)0.0;
           for (int k = 0; k < P.nb; k++) {
             const T xp = s_pot[k][0], yp = s_pot[k][1], mp = s_pot[k][2];
@@ -229,6 +316,17 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
           }
           pot[j] = phi;
         }
+      }
+    };
+    if (CPT > 0) {
+#pragma unroll
+      for (int k = 0; k < NC; k++)
+        if (tid + k * 256 < nsec) cell(tid + k * 256, q[k]);
+    } else {
+      for (int j = tid; j < nsec; j += 256) {
+        CflCell<T> e;
+        cfl_cell_load(a, i, j, cfl_ring, do_forces, e);
+        cell(j, e);
       }
     }
     if (do_forces) {
@@ -265,7 +363,13 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
   if (cfl_ring && tid == 32) {
     T m = s_mx[0];
     for (int k = 1; k < NW; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
-    a.d.ring_smax[i] = (double)m;
+    const double S = (double)m;
+    a.d.ring_dtc[i] = S > 0.0 ? div_once(CFLSECURITY, sqrt_once(S)) : __longlong_as_double(RING_NO_LIMIT);
+  }
+  if (shear_ring && tid == 64) {
+    // NaN differences are skipped (d > 0 is false), as fmin skips them
+    const double d = fabs(s_om[0] - s_om[1]);
+    a.d.ring_dts[i] = d > 0.0 ? div_once(a.shear_k, d) : __longlong_as_double(RING_NO_LIMIT);
   }
   // last block: CFL decision, force totals
   __threadfence();
@@ -282,25 +386,16 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     const double tot = ring_total<T>(a.d.ring_force, nrad, NV, w, lane);  // valid in lane 0
     if (lane == 0) s_acc[w] = tot;
   }
-  if (do_cfl && w == 4) {
-    // largest S over the rings i >= 1, compared as integers (non-negative doubles)
-    long long m = 0;
+  if (do_cfl && (w == 4 || w == 5)) {
+    // smallest per-ring step (CFL over the rings i >= 1, shear over i < nrad - 1),
+    // compared as integers (non-negative doubles and the no-limit pattern)
+    const double *src = (w == 4) ? a.d.ring_dtc : a.d.ring_dts;
+    const int k0 = (w == 4) ? 1 : 0, k1 = (w == 4) ? nrad : nrad - 1;
+    long long m = RING_NO_LIMIT;
 #pragma unroll 8
-    for (int k = 1 + lane; k < nrad; k += 32) m = max(m, __double_as_longlong(__ldcg(a.d.ring_smax + k)));
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) s_dtc[0] = (m > 0) ? div_once(CFLSECURITY, sqrt_once(__longlong_as_double(m))) : 1e30;
-  }
-  if (do_cfl && w == 5) {
-    // shear limit 2 pi C / nsec / |Omega_k - Omega_k+1|: the largest difference
-    // gives the smallest step (NaN differences are skipped, as fmin skips them)
-    long long m = 0;
-#pragma unroll 8
-    for (int k = lane; k < nrad - 1; k += 32) {
-      const double d = fabs(__ldcg(a.d.ring_vmoy + k) - __ldcg(a.d.ring_vmoy + k + 1));
-      if (d == d) m = max(m, __double_as_longlong(d));
-    }
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) s_dtc[1] = (m > 0) ? div_once(a.shear_k, __longlong_as_double(m)) : 1e30;
+    for (int k = k0 + lane; k < k1; k += 32) m = min(m, __double_as_longlong(__ldcg(src + k)));
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0) s_dtc[w - 4] = (m == RING_NO_LIMIT) ? 1e30 : __longlong_as_double(m);
   }
   __syncthreads();
   if (tid == 0) {
@@ -352,6 +447,18 @@ __global__ void __launch_bounds__(256) k_cfl_forces(KArgs<T> a) {
     for (int k = tid; k < nrad; k += blockDim.x)
       a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
   }
+}
+
+// The CFL/force kernel for a ring of nsec cells: register-resident cells up to
+// 1024 per ring
+template <class T>
+void launch_cfl_forces(const KArgs<T> &a, cudaStream_t s) {
+  const int n = (a.P.nsec + 255) / 256;
+  const dim3 g(a.P.nrad), b(256);
+  if (n <= 2) launch_k(a.pdl, k_cfl_forces<T, 2>, g, b, 0, s, a);
+  else if (n == 3) launch_k(a.pdl, k_cfl_forces<T, 3>, g, b, 0, s, a);
+  else if (n == 4) launch_k(a.pdl, k_cfl_forces<T, 4>, g, b, 0, s, a);
+  else launch_k(a.pdl, k_cfl_forces<T, 0>, g, b, 0, s, a);
 }
 
 // The planetary part of a substep (AdvanceSystemFromDisk, AdvanceSystemRK5,
@@ -1313,7 +1420,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     if (which_mask & SUBK_CFL_FORCES) {
       // a.mode: 0 CFL + forces + planets, 2 forces + planets with dt = sloppy_dt,
       // 3 forces + potential only (no planet advance, no time update)
-      launch_k(a.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, a);
+      launch_cfl_forces(a, s);
       MARK("k_cfl_forces");
     }
     if (sg_side) {
@@ -1406,7 +1513,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     }
     KArgs<T> g = a;
     g.guard = 1;
-    launch_k(g.pdl, k_cfl_forces<T>, dim3(P.nrad), dim3(256), 0, s, g);
+    launch_cfl_forces(g, s);
     MARK("k_cfl_forces");
     cudaStreamWaitEvent(s, side->join2, 0);
   }
@@ -1418,7 +1525,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
 template <class T>
 void launch_dt_head(const KArgs<T> &a, cudaStream_t s, const SideBranch *side) {
   cudaEventRecord(side->fork2, s);
-  launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
+  launch_cfl_forces(a, s);
   MARK("k_cfl_forces");
   cudaStreamWaitEvent(side->s2, side->fork2, 0);
   launch_selfgravity(a, side->s2);
@@ -1468,7 +1575,7 @@ void launch_dt_prefix(const KArgs<T> &a0, cudaStream_t s) {
   }
   if (a.P.sloppy_cfl) {
     a.mode = 1;
-    launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
+    launch_cfl_forces(a, s);
     MARK("k_cfl_forces");
   }
 }
@@ -1477,7 +1584,7 @@ template <class T>
 void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
   KArgs<T> a = a0;
   a.mode = 1;
-  launch_k(a.pdl, k_cfl_forces<T>, dim3(a.P.nrad), dim3(256), 0, s, a);
+  launch_cfl_forces(a, s);
   MARK("k_cfl_forces");
 }
 
@@ -1487,7 +1594,8 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
   // shared split only when idle, so kernels that run side by side (the CFL/force
   // kernel, the self-gravity transforms, the planet update) and successive
   // kernels under programmatic launch can share SMs only with the same split.
-  const void *all[] = {(const void *)k_cfl_forces<T>, (const void *)k_planets, (const void *)k_soundspeed<T>,
+  const void *all[] = {(const void *)k_cfl_forces<T, 0>, (const void *)k_cfl_forces<T, 2>,
+                       (const void *)k_cfl_forces<T, 3>, (const void *)k_cfl_forces<T, 4>, (const void *)k_planets, (const void *)k_soundspeed<T>,
                        (const void *)k_correct_vtheta<T>, (const void *)k_bc_open<T>,
                        (const void *)k_bc_nonreflecting<T>, (const void *)k_bc_evanescent<T>,
                        (const void *)k_source<T>, (const void *)k_visc_tau<T>, (const void *)k_visc_update<T>,
