@@ -62,6 +62,7 @@ struct fargo_ctx {
   bool use_graph = true;
   bool use_pdl = true;   // programmatic dependent launch between the step kernels
   bool use_rotation = false;  // rotated DT loop (self-gravity ahead of each substep)
+  bool use_sg_ahead = true;   // ring transforms of the next substep beside the end of this one
 };
 
 namespace {
@@ -254,9 +255,11 @@ int build_graph(fargo_ctx *c) {
   // with self-gravity the loop runs rotated: the prefix also runs the first
   // substep's CFL/force kernel and transforms, each substep the next one's
   const bool rot = c->use_rotation && rotation_allowed<T>(a, &c->side);
+  const bool ahead = !rot && c->use_sg_ahead && sg_ahead_allowed<T>(a, &c->side);
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   launch_dt_prefix<T>(a, c->stream);
   if (rot) launch_dt_head<T>(a, c->stream, &c->side);
+  if (ahead) launch_sg_rows_fwd<T>(a, c->stream);
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &gp));
   c->launches_per_dt = probe.count;
@@ -276,7 +279,8 @@ int build_graph(fargo_ctx *c) {
   CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
   probe.count = 0;
   g_probe = &probe;
-  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side, rot ? ROT_HEAD_DONE | ROT_NEXT_HEAD : 0u);
+  launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side,
+                            rot ? ROT_HEAD_DONE | ROT_NEXT_HEAD : ahead ? SG_AHEAD : 0u);
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &body));
   c->launches_per_substep = probe.count;
@@ -290,9 +294,11 @@ int build_graph(fargo_ctx *c) {
 template <class T>
 int run_dt_hostloop(fargo_ctx *c) {
   KArgs<T> a = make_args<T>(c);
+  const bool ahead = c->use_sg_ahead && sg_ahead_allowed<T>(a, &c->side);
   launch_dt_prefix<T>(a, c->stream);
+  if (ahead) launch_sg_rows_fwd<T>(a, c->stream);
   for (int n = 0; n < FARGO_MAX_SUBSTEPS_PER_DT + 1; n++) {
-    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side);
+    launch_substep_kernels<T>(a, c->stream, SUBK_ALL, c->az_smem, &c->side, ahead ? SG_AHEAD : 0u);
     int rc = check_launch(c, "substep");
     if (rc) return rc;
     if ((rc = read_ctl(c))) return rc;
@@ -644,6 +650,8 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   if (np && np[0] == '1') c->use_pdl = false;
   const char *nr = std::getenv("FARGO_ROTATE");
   if (nr && nr[0] == '1') c->use_rotation = true;
+  const char *na = std::getenv("FARGO_NO_SG_AHEAD");
+  if (na && na[0] == '1') c->use_sg_ahead = false;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

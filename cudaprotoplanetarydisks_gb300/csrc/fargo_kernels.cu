@@ -1413,6 +1413,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   const bool bc1 = (which_mask & SUBK_BC1) && (P.open_inner || P.non_reflecting || P.evanescent);
   const bool sg_side =
       !head_done && side && (which_mask & SUBK_SG) && P.self_gravity && (which_mask & SUBK_CFL_FORCES) && !bc1;
+  const bool sg_ahead = sg_side && (rot & SG_AHEAD) && (which_mask & SUBK_TRANSPORT);
   if (!head_done) {
     // the fork point precedes k_cfl_forces; the transforms are issued after it
     // (the earlier-issued grid is scheduled first, and the CFL kernel is the longer)
@@ -1425,7 +1426,8 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     }
     if (sg_side) {
       cudaStreamWaitEvent(side->s2, side->fork2, 0);
-      launch_selfgravity(a, side->s2);
+      if (sg_ahead) launch_sg_cols_inv(a, side->s2);
+      else launch_selfgravity(a, side->s2);
       cudaEventRecord(side->join2, side->s2);
     }
   }
@@ -1483,6 +1485,15 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
       a.az_smem = 0;
     }
     MARK("k_transport_azimuthal");
+    if (sg_ahead) {
+      // the next substep's ring transforms, from the final density, beside the
+      // velocities and k_end (the DT's last substep's are unused: the DT prefix
+      // transforms the density it starts from)
+      cudaEventRecord(side->fork2, s);
+      cudaStreamWaitEvent(side->s2, side->fork2, 0);
+      launch_sg_rows_fwd(a, side->s2);
+      cudaEventRecord(side->join2, side->s2);
+    }
     launch_k(a.pdl, k_velocities<T>, dim3(g2), dim3(b2), 0, s, a, (!bc && (which_mask & SUBK_TEMPERATURE)) ? 1 : 0);
     MARK("k_velocities");
   }
@@ -1518,6 +1529,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     cudaStreamWaitEvent(s, side->join2, 0);
   }
   if (!joined) cudaStreamWaitEvent(s, side->join, 0);
+  if (sg_ahead) cudaStreamWaitEvent(s, side->join2, 0);
 }
 
 // The first substep's CFL/force kernel and self-gravity transforms, side by side,
@@ -1539,6 +1551,13 @@ template <class T>
 bool rotation_allowed(const KArgs<T> &a, const SideBranch *side) {
   const DevParams &P = a.P;
   return side && P.self_gravity && !(P.open_inner || P.non_reflecting || P.evanescent);
+}
+
+// whether a DT loop may run its ring transforms ahead (SG_AHEAD): the same
+// conditions as the rotated loop
+template <class T>
+bool sg_ahead_allowed(const KArgs<T> &a, const SideBranch *side) {
+  return rotation_allowed(a, side);
 }
 
 template <class T>
@@ -1641,6 +1660,7 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
   template void launch_substep_kernels<T>(const KArgs<T> &, cudaStream_t, unsigned, size_t,            \
                                          const SideBranch *, unsigned);                                \
   template void launch_dt_head<T>(const KArgs<T> &, cudaStream_t, const SideBranch *);                  \
+  template bool sg_ahead_allowed<T>(const KArgs<T> &, const SideBranch *);                            \
   template bool rotation_allowed<T>(const KArgs<T> &, const SideBranch *);                              \
   template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \

@@ -80,6 +80,12 @@ struct SideBranch {
 // the DT is done; launch_dt_head runs the first substep's in the DT prefix.
 #define ROT_HEAD_DONE 0x1u
 #define ROT_NEXT_HEAD 0x2u
+// Ring transforms ahead (the DT loop with self-gravity, not rotated): the
+// azimuthal forward transforms of a substep's density ran before the substep (in
+// the DT prefix, or at the end of the previous substep, beside its k_velocities
+// and k_end, since the density is final after the azimuthal transport); the
+// substep launches the next substep's after its own azimuthal transport.
+#define SG_AHEAD 0x8u
 template <class T>
 void launch_substep_kernels(const KArgs<T> &a, cudaStream_t s, unsigned which_mask, size_t az_smem_bytes,
                             const SideBranch *side = nullptr, unsigned rot = 0);
@@ -87,6 +93,8 @@ template <class T>
 void launch_dt_head(const KArgs<T> &a, cudaStream_t s, const SideBranch *side);
 template <class T>
 bool rotation_allowed(const KArgs<T> &a, const SideBranch *side);
+template <class T>
+bool sg_ahead_allowed(const KArgs<T> &a, const SideBranch *side);
 template <class T>
 void launch_dt_prefix(const KArgs<T> &a, cudaStream_t s);
 template <class T>
@@ -99,6 +107,10 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
 // self-gravity (fargo_sg.cu)
 template <class T>
 void launch_selfgravity(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+void launch_sg_rows_fwd(const KArgs<T> &a, cudaStream_t s);
+template <class T>
+void launch_sg_cols_inv(const KArgs<T> &a, cudaStream_t s);
 template <class T>
 void launch_sg_kernel_spectra(const KArgs<T> &a, cudaStream_t s);
 template <class T>

@@ -306,17 +306,31 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   });
 }
 
+// The azimuthal forward transforms of the rings (they read only the density).
 template <class T>
-void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
-  const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
+void launch_sg_rows_fwd(const KArgs<T> &a, cudaStream_t s) {
+  const int nsec = a.P.nsec, nrad = a.P.nrad;
   const size_t vs = 2 * sizeof(T);
   launch_k(a.pdl, k_sg_rows_fwd<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_fwd");
+}
+
+// The radial convolution and the inverse azimuthal transforms (accelerations).
+template <class T>
+void launch_sg_cols_inv(const KArgs<T> &a, cudaStream_t s) {
+  const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
+  const size_t vs = 2 * sizeof(T);
   const int gc = sg_group(n0) < 128 ? sg_group(n0) : 128;
   launch_k(a.pdl, k_sg_cols<T>, dim3(a.sg.M), dim3(2 * gc), (n0 + 6 * fpadn(n0)) * vs, s, a);
   probe_mark(s, "k_sg_cols");
   launch_k(a.pdl, k_sg_rows_inv<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_inv");
+}
+
+template <class T>
+void launch_selfgravity(const KArgs<T> &a, cudaStream_t s) {
+  launch_sg_rows_fwd(a, s);
+  launch_sg_cols_inv(a, s);
 }
 
 // Set-up, FP64 in both modes: spectra of the constant kernels (compute_kernel
@@ -394,6 +408,8 @@ cudaError_t prepare_sg_kernels(int nsec, int n0) {
 
 #define INSTANTIATE_SG(T)                                                      \
   template void launch_selfgravity<T>(const KArgs<T> &, cudaStream_t);         \
+  template void launch_sg_rows_fwd<T>(const KArgs<T> &, cudaStream_t);         \
+  template void launch_sg_cols_inv<T>(const KArgs<T> &, cudaStream_t);         \
   template void launch_sg_kernel_spectra<T>(const KArgs<T> &, cudaStream_t);   \
   template cudaError_t prepare_sg_kernels<T>(int, int);
 INSTANTIATE_SG(double)

@@ -134,12 +134,13 @@ def _disk_with_env(params, planets, prec, env):
                 os.environ[k] = v
 
 
-@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_AZ_GLOBAL"])
+@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_NO_SG_AHEAD", "FARGO_AZ_GLOBAL"])
 def test_code_paths_are_bitwise_identical(env):
     # the conditional-graph DT loop vs the host loop; programmatic dependent
     # launch vs plain launches; the rotated DT loop (each substep launches the
     # next one's CFL/force kernel and self-gravity transforms) vs the plain
-    # one; the shared-memory vs the global-memory ring
+    # one; the next substep's ring transforms launched after the azimuthal
+    # transport vs at the substep start; the shared-memory vs the global-memory ring
     # buffers of the barrier-per-phase azimuthal kernel
     params, planets = small("c2")
     base = {"FARGO_AZ_GENERIC": "1"} if env == "FARGO_AZ_GLOBAL" else {}
