@@ -43,7 +43,7 @@ struct fargo_ctx {
   void *az_scratch = nullptr, *rt = nullptr, *nu = nullptr, *cosP = nullptr, *sinP = nullptr;
   void *cosFt = nullptr, *sinFt = nullptr;
   double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
-  double *ring_dtc = nullptr, *ring_dts = nullptr, *ring_force = nullptr, *lostbydisk = nullptr;
+  double *ring_force = nullptr, *lostbydisk = nullptr;
   // self-gravity
   void *spec2_r = nullptr, *spec2_t = nullptr;
   void *spec_r = nullptr, *spec_t = nullptr, *khat_r = nullptr, *khat_t = nullptr, *tw1 = nullptr, *tw0 = nullptr;
@@ -120,8 +120,6 @@ KArgs<T> make_args(const fargo_ctx *c) {
   d.cosFt = (const T *)c->cosFt;
   d.sinFt = (const T *)c->sinFt;
   d.sinP = (const T *)c->sinP;
-  d.ring_dtc = c->ring_dtc;
-  d.ring_dts = c->ring_dts;
   d.ring_force = c->ring_force;
   d.lostbydisk = c->lostbydisk;
   d.ctl = c->d_ctl;
@@ -345,8 +343,6 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   if ((rc = dev_alloc(c, &c->sinP, (size_t)p.nsec * E))) return rc;
   if ((rc = dev_alloc(c, &c->cosFt, (size_t)p.nsec * E))) return rc;
   if ((rc = dev_alloc(c, &c->sinFt, (size_t)p.nsec * E))) return rc;
-  if ((rc = dev_alloc(c, (void **)&c->ring_dtc, n1 * 8))) return rc;
-  if ((rc = dev_alloc(c, (void **)&c->ring_dts, n1 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->ring_force, n1 * (FARGO_MAXPL + 1) * 2 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->lostbydisk, (size_t)p.nsec * 8))) return rc;
   if (c->esize == 4 && (rc = dev_alloc(c, (void **)&c->staging, sg * 8))) return rc;

@@ -28,7 +28,6 @@ struct DiskPtrs {
   const T *cosFt, *sinFt;     // the same table in T
   const T *cosP, *sinP;       // potential angle table
   // per-ring partial results of the CFL/force kernel
-  double *ring_dtc, *ring_dts;  // per-ring CFL and shear time-step limits
   double *ring_force;
   double *lostbydisk;
   Ctl *ctl;

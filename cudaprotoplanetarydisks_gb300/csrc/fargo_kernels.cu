@@ -72,10 +72,6 @@ __device__ __forceinline__ double ring_total(const double *ring_force, int nrad,
   return s.value();
 }
 
-// "No limit" of a per-ring time step: a NaN bit pattern, above every non-negative
-// double (+inf included) when compared as a signed 64-bit integer.
-#define RING_NO_LIMIT 0x7ff8000000000000LL
-
 // Inputs of one cell of the CFL/force pass.
 template <class T>
 struct CflCell {
@@ -151,13 +147,14 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
 // instead of one per pass and per cell).  CPT = 0: any nsec, cells streamed.
 // Each thread visits its cells in the same order either way (j = tid, tid + 256,
 // ...), so both give the same sums.
-// Per ring the CTA also forms the two time-step limits that the last CTA takes
-// the minimum of: C/sqrt(max S) of its cells (rings >= 1) and the shear limit
-// 2 pi C / nsec / |Omega_i - Omega_i+1| (rings < nrad - 1), with Omega_i+1 from the
-// mean of ring i+1 summed in the same order as ring i+1's own CTA sums it.  The
-// minimum over rings of these correctly rounded, monotone maps equals the map of
-// the extreme S or difference, so the result is that of one sqrt and one divide
-// of the maxima, while the last CTA's serial tail holds integer minima only.
+// Per ring the CTA also forms the two time-step limits and folds them into the
+// control block's minima (64-bit integer atomicMin on the bit patterns of
+// non-negative doubles: order-free, so deterministic): C/sqrt(max S) of its cells
+// (rings >= 1) and the shear limit 2 pi C / nsec / |Omega_i - Omega_i+1| (rings <
+// nrad - 1), with Omega_i+1 from the mean of ring i+1 summed in the same order as
+// ring i+1's own CTA sums it.  The minimum over rings of these correctly rounded,
+// monotone maps equals the map of the extreme S or difference, so the result is
+// that of one sqrt and one divide of the maxima, and the last CTA reads two words.
 template <class T, int CPT>
 __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   pdl_enter();
@@ -207,6 +204,19 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     }
     if (tid == 0) s_nbody = c->nbody;
   }
+  // per-ring table values, loaded with the cells (no load after a barrier)
+  CflRing<T> r;
+  r.rm = RT(a, RT_RMED, i);
+  r.surf = RT(a, RT_SURF, i);
+  r.invdrad = r.invdxt = r.invmind = r.cs = (T)0;
+  r.vm.hi = r.vm.lo = (T)0;
+  if (cfl_ring) {
+    r.invdrad = RT(a, RT_INVDRAD, i);
+    r.invdxt = RT(a, RT_INVDXTHETA_CFL, i);
+    r.invmind = RT(a, RT_INVMIND, i);
+    r.cs = a.d.cs ? (T)0 : RT(a, RT_CS, i);
+  }
+  const double inv_rm = (do_cfl && (tid == 0 || tid == 32)) ? RT64(a, RT_INVRMED, i + (tid >> 5)) : 0.0;
   const T *vth = a.d.vtheta + (size_t)i * nsec;
   const T *vth1 = vth + nsec;
   CflCell<T> q[NC];
@@ -253,22 +263,11 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     const double vmoy = sizeof(T) == 8 ? v.value() / (double)nsec : v.value() * a.inv_nsec;
     if (h == 0) s_vm.set(vmoy);
     // ring angular velocity of the shear limit (ConditionCFLKernel2D2)
-    s_om[h] = vmoy * RT64(a, RT_INVRMED, i + h);
+    s_om[h] = vmoy * inv_rm;
   }
   if (do_cfl) __syncthreads();
   const int nbody = do_forces ? s_nbody : 0;
-  CflRing<T> r;
-  r.rm = RT(a, RT_RMED, i);
-  r.surf = RT(a, RT_SURF, i);
-  r.invdrad = r.invdxt = r.invmind = r.cs = (T)0;
-  r.vm.hi = r.vm.lo = (T)0;
-  if (cfl_ring) {
-    r.invdrad = RT(a, RT_INVDRAD, i);
-    r.invdxt = RT(a, RT_INVDXTHETA_CFL, i);
-    r.invmind = RT(a, RT_INVMIND, i);
-    r.cs = a.d.cs ? (T)0 : RT(a, RT_CS, i);
-    r.vm = s_vm;
-  }
+  if (cfl_ring) r.vm = s_vm;
   T *pot = a.d.potential + (size_t)i * nsec;
   T mx = (T)0.0;
   const int nchunk = do_forces ? (nbody + 1) >> 1 : 1;
@@ -364,12 +363,12 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     T m = s_mx[0];
     for (int k = 1; k < NW; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
     const double S = (double)m;
-    a.d.ring_dtc[i] = S > 0.0 ? div_once(CFLSECURITY, sqrt_once(S)) : __longlong_as_double(RING_NO_LIMIT);
+    if (S > 0.0) atomicMin(&c->ring_min[0], __double_as_longlong(div_once(CFLSECURITY, sqrt_once(S))));
   }
   if (shear_ring && tid == 64) {
     // NaN differences are skipped (d > 0 is false), as fmin skips them
     const double d = fabs(s_om[0] - s_om[1]);
-    a.d.ring_dts[i] = d > 0.0 ? div_once(a.shear_k, d) : __longlong_as_double(RING_NO_LIMIT);
+    if (d > 0.0) atomicMin(&c->ring_min[1], __double_as_longlong(div_once(a.shear_k, d)));
   }
   // last block: CFL decision, force totals
   __threadfence();
@@ -386,16 +385,13 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     const double tot = ring_total<T>(a.d.ring_force, nrad, NV, w, lane);  // valid in lane 0
     if (lane == 0) s_acc[w] = tot;
   }
-  if (do_cfl && (w == 4 || w == 5)) {
+  if (do_cfl && (tid == 128 || tid == 160)) {
     // smallest per-ring step (CFL over the rings i >= 1, shear over i < nrad - 1),
-    // compared as integers (non-negative doubles and the no-limit pattern)
-    const double *src = (w == 4) ? a.d.ring_dtc : a.d.ring_dts;
-    const int k0 = (w == 4) ? 1 : 0, k1 = (w == 4) ? nrad : nrad - 1;
-    long long m = RING_NO_LIMIT;
-#pragma unroll 8
-    for (int k = k0 + lane; k < k1; k += 32) m = min(m, __double_as_longlong(__ldcg(src + k)));
-    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_down_sync(0xffffffffu, m, o));
-    if (lane == 0) s_dtc[w - 4] = (m == RING_NO_LIMIT) ? 1e30 : __longlong_as_double(m);
+    // reset for the next launch
+    const int k = (tid - 128) >> 5;
+    const long long m = __ldcg(&c->ring_min[k]);
+    c->ring_min[k] = FARGO_RING_NO_LIMIT;
+    s_dtc[k] = (m == FARGO_RING_NO_LIMIT) ? 1e30 : __longlong_as_double(m);
   }
   __syncthreads();
   if (tid == 0) {
@@ -1393,6 +1389,7 @@ __global__ void k_dt_begin(Ctl *c) {
   c->done = 0;
   c->err = 0;
   c->ticket = 0u;
+  c->ring_min[0] = c->ring_min[1] = FARGO_RING_NO_LIMIT;
 }
 
 // ---------------------------------------------------------------------------

@@ -44,6 +44,10 @@ struct DevParams {
   double sgp_eps, sgp_rstep, sgp_tstep;
 };
 
+// "No limit" of a per-ring time step: a NaN bit pattern, above every non-negative
+// double (+inf included) when compared as a signed 64-bit integer.
+#define FARGO_RING_NO_LIMIT 0x7ff8000000000000LL
+
 struct Ctl {
   // time state (reference globals PhysicalTime, OmegaFrame, LostMass; AlgoGas locals)
   double DT, dtemp, dt;
@@ -55,6 +59,9 @@ struct Ctl {
   long long substeps;
   unsigned int ticket;        // last-block-done counter of the CFL/force kernel
   unsigned int pad0;
+  // smallest per-ring CFL and shear time steps of the CFL/force kernel, as the
+  // integers of their (non-negative) bit patterns; FARGO_RING_NO_LIMIT between launches
+  long long ring_min[2];
   // planetary system (Types.cuh:2-12)
   int nb;
   int pad1;
@@ -87,6 +94,7 @@ FARGO_HD void fargo_ctl_mirror(Ctl &c) {
   c.f32[CTL_F_INDY] = (float)c.ind_y;
   c.f32[CTL_F_DOMEGA] = (float)c.domega;
   c.f32[CTL_F_INVDT] = 1.0f / (float)c.dt;
+  c.ring_min[0] = c.ring_min[1] = FARGO_RING_NO_LIMIT;
 }
 
 // AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392
