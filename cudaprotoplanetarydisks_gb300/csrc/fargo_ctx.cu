@@ -63,6 +63,7 @@ struct fargo_ctx {
   bool use_pdl = true;   // programmatic dependent launch between the step kernels
   bool use_rotation = false;  // rotated DT loop (self-gravity ahead of each substep)
   bool use_sg_ahead = true;   // ring transforms of the next substep beside the end of this one
+  bool sg_generic = false;    // run-time FFT plans only (the compile-time ones compared in the tests)
 };
 
 namespace {
@@ -144,6 +145,7 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.az_smem = 0;
   a.az_regs = c->az_regs;
   a.pdl = c->use_pdl ? 1 : 0;
+  a.sg_generic = c->sg_generic ? 1 : 0;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -648,6 +650,8 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   if (nr && nr[0] == '1') c->use_rotation = true;
   const char *na = std::getenv("FARGO_NO_SG_AHEAD");
   if (na && na[0] == '1') c->use_sg_ahead = false;
+  const char *sgg = std::getenv("FARGO_SG_GENERIC");
+  if (sgg && sgg[0] == '1') c->sg_generic = true;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

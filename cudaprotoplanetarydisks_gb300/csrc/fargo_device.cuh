@@ -67,6 +67,7 @@ struct KArgs {
   int use_cond;                    // 1: k_end sets the while-loop condition
   int pdl;                         // launch with programmatic dependent launch
   int guard;                       // 1: return at once when the DT loop is done (a next substep's kernels)
+  int sg_generic;                  // self-gravity FFTs with the run-time plan at every length
   SgDev sg;
 };
 

@@ -166,6 +166,77 @@ struct StoreFree {
   __device__ __forceinline__ void operator()(int k, V v, V *dst) const { dst[fpad(k)] = v; }
 };
 
+// Compile-time plans for the common lengths: the radices in the order
+// sg_radices gives (8s, then 4s, 2s, 3s), every stage's stride, butterfly count
+// and buffer offsets constants, so that a stage is its loads, butterflies and
+// stores.  Same arithmetic as fft_run (a stage with Ns = 1 skips the unit
+// twiddle, which changes no finite value).
+__host__ __device__ constexpr int plan_radix_of(int n) { return n % 8 == 0 ? 8 : n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : 3; }
+__host__ __device__ constexpr int plan_nst(int n) {
+  int k = 0;
+  while (n > 1) {
+    n /= plan_radix_of(n);
+    k++;
+  }
+  return k;
+}
+__host__ __device__ constexpr int plan_rad(int n, int s) {
+  for (int k = 0; k < s; k++) n /= plan_radix_of(n);
+  return plan_radix_of(n);
+}
+__host__ __device__ constexpr int plan_ns(int n, int s) {
+  int ns = 1;
+  for (int k = 0; k < s; k++) {
+    const int r = plan_radix_of(n);
+    ns *= r;
+    n /= r;
+  }
+  return ns;
+}
+
+template <int N, int RAD, int NS, int G, class V, class Out>
+__device__ __forceinline__ void fft_stage_c(const V *src, const V *tw, int lt, Out out) {
+  constexpr int NR = N / RAD, TWS = N / (NS * RAD);
+#pragma unroll
+  for (int k = 0; k < (NR + G - 1) / G; k++) {
+    const int j = lt + k * G;
+    if (NR % G == 0 || j < NR) {
+      const int jj = j % NS, jb = j / NS;
+      V v[RAD];
+#pragma unroll
+      for (int r = 0; r < RAD; r++) {
+        v[r] = src[fpad(j + r * NR)];
+        if (r > 0 && NS > 1) v[r] = cmul(v[r], tw[r * jj * TWS]);
+      }
+      butterfly<RAD>(v);
+      const int idxD = jb * NS * RAD + jj;
+#pragma unroll
+      for (int r = 0; r < RAD; r++) out(idxD + r * NS, v[r]);
+    }
+  }
+}
+
+template <int N, int S, int G, class V, class Last>
+__device__ __forceinline__ V *fft_run_c(V *d0, V *d1, const V *tw, int lt, Last last) {
+  constexpr int R = plan_rad(N, S), NS = plan_ns(N, S), NST = plan_nst(N);
+  if constexpr (S == NST - 1) {
+    fft_stage_c<N, R, NS, G>(d0, tw, lt, [&](int k, V v) { last(k, v, d1); });
+    __syncthreads();
+    return d1;
+  } else {
+    fft_stage_c<N, R, NS, G>(d0, tw, lt, [&](int k, V v) { d1[fpad(k)] = v; });
+    __syncthreads();
+    return fft_run_c<N, S + 1, G>(d1, d0, tw, lt, last);
+  }
+}
+
+// The compile-time plan for N > 0, the run-time one (rad, nst) for N = 0.
+template <int N, int G, class V, class Last>
+__device__ __forceinline__ V *fft_any(V *d0, V *d1, int n, const int *rad, int nst, const V *tw, int lt, Last last) {
+  if constexpr (N > 0) return fft_run_c<N, 0, G>(d0, d1, tw, lt, last);
+  else return fft_run(d0, d1, n, rad, nst, tw, lt, G, last);
+}
+
 // Splits the FFT Z of two packed real rows into the modes m < M of each:
 // X_r = (Z[m] + conj Z[N-m]) / 2, X_t = (Z[m] - conj Z[N-m]) / (2i)
 template <class V>
@@ -189,21 +260,23 @@ int sg_radices(int n, int *rad) {
 }
 
 // threads per FFT group for length n: one radix-8 butterfly per thread and stage
-static inline int sg_group(int n) {
-  int g = (n / 8 + 31) / 32 * 32;
-  return g < 32 ? 32 : (g > 256 ? 256 : g);
+__host__ __device__ constexpr int sg_group(int n) {
+  return (n / 8 + 31) / 32 * 32 < 32 ? 32 : ((n / 8 + 31) / 32 * 32 > 256 ? 256 : (n / 8 + 31) / 32 * 32);
 }
+// threads per field group of the radial kernel (two groups per CTA)
+__host__ __device__ constexpr int sg_col_group(int n0) { return sg_group(n0) < 128 ? sg_group(n0) : 128; }
 
 // Azimuthal forward transform of each ring with the ComputeFFTKernel packing
 // (S_r = Sigma sqrt(r/r0), S_theta = S_r r/r0, src/Kernels.cu:858-861).  Output:
 // modes m < M of each real field, column-major [m][ring].
-template <class T>
+template <class T, int NSEC>
 __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
   pdl_enter();
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x, G = blockDim.x;
+  constexpr int G = 256;
+  const int i = blockIdx.x, nsec = NSEC > 0 ? NSEC : a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x;
   V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
   const V *twg = (const V *)a.sg.tw1;
   const T f = RT(a, RT_SGSQRT, i), rm = RT(a, RT_RMED, i), r0 = RT(a, RT_RMED, 0);
@@ -214,7 +287,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
     b0[fpad(j)] = mk2(var, var * rm / r0);
   }
   __syncthreads();
-  V *Z = fft_run(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, G, StoreFree<V>());
+  V *Z = fft_any<NSEC, G>(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, StoreFree<V>());
   V *out_r = (V *)a.sg.spec_r, *out_t = (V *)a.sg.spec_t;
   for (int m = tid; m < a.sg.M; m += G) {
     V xr, xt;
@@ -230,14 +303,15 @@ __global__ void __launch_bounds__(256) k_sg_rows_fwd(KArgs<T> a) {
 // src/Kernels.cu:871-890), conjugated so that the forward routine runs the
 // inverse; the inverse's last stage stores rows < nrad ring-major (the
 // scattered side of the transpose is a store here, a contiguous load after).
-template <class T>
+template <class T, int N0>
 __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   pdl_enter();
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  const int m = blockIdx.x, n0 = 2 * a.P.nrad, nrad = a.P.nrad;
-  const int G = blockDim.x >> 1, g = threadIdx.x >= G ? 1 : 0, lt = threadIdx.x - g * G;
+  constexpr int GC = N0 > 0 ? sg_col_group(N0) : 0;
+  const int m = blockIdx.x, n0 = N0 > 0 ? N0 : 2 * a.P.nrad, nrad = n0 >> 1;
+  const int G = N0 > 0 ? GC : (int)(blockDim.x >> 1), g = threadIdx.x >= G ? 1 : 0, lt = threadIdx.x - g * G;
   V *tw = (V *)sg_raw;
   V *b0 = tw + n0 + g * 3 * fpadn(n0), *b1 = b0 + fpadn(n0), *K = b1 + fpadn(n0);
   const V *twg = (const V *)a.sg.tw0;
@@ -252,27 +326,34 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
     b0[fpad(k)] = (k < nrad) ? col[k] : mk2((T)0, (T)0);
   }
   __syncthreads();
-  V *X = fft_run(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V S, V *dst) {
+  auto conv = [&](int k, V S, V *dst) {
     const V Kk = K[fpad(k)];
     const T gx = (T)-1.0 * (Kk.x * S.x - Kk.y * S.y);
     const T gy = (T)-1.0 * (Kk.x * S.y + Kk.y * S.x);
     dst[fpad(k)] = mk2(gx, -gy);
-  });
-  V *Y = (X == b0) ? b1 : b0;
-  fft_run(X, Y, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, [&](int k, V z, V *) {
+  };
+  auto store = [&](int k, V z, V *) {
     if (k < nrad) row[(size_t)k * a.sg.M] = cconj(z);
-  });
+  };
+  if constexpr (N0 > 0) {
+    V *X = fft_run_c<N0, 0, GC>(b0, b1, tw, lt, conv);
+    fft_run_c<N0, 0, GC>(X, (X == b0) ? b1 : b0, tw, lt, store);
+  } else {
+    V *X = fft_run(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, conv);
+    fft_run(X, (X == b0) ? b1 : b0, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, store);
+  }
 }
 
 // Inverse azimuthal transform of each ring; its last stage applies
 // ComputeSgAccKernel (src/Kernels.cu:893-912).
-template <class T>
+template <class T, int NSEC>
 __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   pdl_enter();
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   using V = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char sg_raw[];
-  const int i = blockIdx.x, nsec = a.P.nsec, nrad = a.P.nrad, M = a.sg.M, tid = threadIdx.x, G = blockDim.x;
+  constexpr int G = 256;
+  const int i = blockIdx.x, nsec = NSEC > 0 ? NSEC : a.P.nsec, M = NSEC > 0 ? NSEC / 2 + 1 : a.sg.M, tid = threadIdx.x;
   V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
   const V *twg = (const V *)a.sg.tw1;
   // this ring's row of the ring-major spectra that k_sg_cols left
@@ -295,7 +376,7 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   const T normr = RT(a, RT_SGNORMR, i), normt = RT(a, RT_SGNORMT, i);
   const T selfc = (T)a.P.sgp_rstep, tstep = (T)a.P.sgp_tstep, eps = (T)a.P.sgp_eps, sgself = KC(T, a, KC_SGSELF);
   const size_t row = (size_t)i * nsec;
-  fft_run(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, G, [&](int j, V v, V *) {
+  fft_any<NSEC, G>(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, [&](int j, V v, V *) {
     const V z = cconj(v);
     const size_t q = row + j;
     a.d.sg_acct[q] = z.y * normt;
@@ -306,12 +387,48 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   });
 }
 
+// Kernel instance for a length: the compile-time plan when the length has one.
+template <class T>
+using SgKernel = void (*)(KArgs<T>);
+template <class T>
+SgKernel<T> sg_rows_fwd_fn(int nsec) {
+  switch (nsec) {
+    case 384: return k_sg_rows_fwd<T, 384>;
+    case 512: return k_sg_rows_fwd<T, 512>;
+    case 768: return k_sg_rows_fwd<T, 768>;
+    case 1024: return k_sg_rows_fwd<T, 1024>;
+    case 1536: return k_sg_rows_fwd<T, 1536>;
+    default: return k_sg_rows_fwd<T, 0>;
+  }
+}
+template <class T>
+SgKernel<T> sg_rows_inv_fn(int nsec) {
+  switch (nsec) {
+    case 384: return k_sg_rows_inv<T, 384>;
+    case 512: return k_sg_rows_inv<T, 512>;
+    case 768: return k_sg_rows_inv<T, 768>;
+    case 1024: return k_sg_rows_inv<T, 1024>;
+    case 1536: return k_sg_rows_inv<T, 1536>;
+    default: return k_sg_rows_inv<T, 0>;
+  }
+}
+template <class T>
+SgKernel<T> sg_cols_fn(int n0) {
+  switch (n0) {
+    case 256: return k_sg_cols<T, 256>;
+    case 512: return k_sg_cols<T, 512>;
+    case 1024: return k_sg_cols<T, 1024>;
+    case 2048: return k_sg_cols<T, 2048>;
+    default: return k_sg_cols<T, 0>;
+  }
+}
+
 // The azimuthal forward transforms of the rings (they read only the density).
 template <class T>
 void launch_sg_rows_fwd(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, nrad = a.P.nrad;
   const size_t vs = 2 * sizeof(T);
-  launch_k(a.pdl, k_sg_rows_fwd<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
+  launch_k(a.pdl, sg_rows_fwd_fn<T>(a.sg_generic ? 0 : nsec), dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_fwd");
 }
 
@@ -320,10 +437,9 @@ template <class T>
 void launch_sg_cols_inv(const KArgs<T> &a, cudaStream_t s) {
   const int nsec = a.P.nsec, nrad = a.P.nrad, n0 = 2 * nrad;
   const size_t vs = 2 * sizeof(T);
-  const int gc = sg_group(n0) < 128 ? sg_group(n0) : 128;
-  launch_k(a.pdl, k_sg_cols<T>, dim3(a.sg.M), dim3(2 * gc), (n0 + 6 * fpadn(n0)) * vs, s, a);
+  launch_k(a.pdl, sg_cols_fn<T>(a.sg_generic ? 0 : n0), dim3(a.sg.M), dim3(2 * sg_col_group(n0)), (n0 + 6 * fpadn(n0)) * vs, s, a);
   probe_mark(s, "k_sg_cols");
-  launch_k(a.pdl, k_sg_rows_inv<T>, dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
+  launch_k(a.pdl, sg_rows_inv_fn<T>(a.sg_generic ? 0 : nsec), dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
   probe_mark(s, "k_sg_rows_inv");
 }
 
@@ -396,12 +512,17 @@ cudaError_t prepare_sg_kernels(int nsec, int n0) {
   const int vs = 2 * sizeof(T);
   const int rows = (nsec + 2 * fpadn(nsec)) * vs, cols = (n0 + 6 * fpadn(n0)) * vs;
   const int rows64 = 2 * fpadn(nsec) * (int)sizeof(double2), cols64 = 2 * fpadn(n0) * (int)sizeof(double2);
-  for (const void *f : {(const void *)k_sg_rows_fwd<T>, (const void *)k_sg_cols<T>, (const void *)k_sg_rows_inv<T>})
-    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
-      return e;
-  if ((e = cudaFuncSetAttribute(k_sg_rows_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_sg_rows_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_sg_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols)) != cudaSuccess) return e;
+  // the instances for these lengths and the run-time-plan ones
+  for (int gen = 0; gen < 2; gen++) {
+    const void *fr = (const void *)sg_rows_fwd_fn<T>(gen ? 0 : nsec), *fi = (const void *)sg_rows_inv_fn<T>(gen ? 0 : nsec),
+               *fc = (const void *)sg_cols_fn<T>(gen ? 0 : n0);
+    for (const void *f : {fr, fc, fi})
+      if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(fr, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(fi, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(fc, cudaFuncAttributeMaxDynamicSharedMemorySize, cols)) != cudaSuccess) return e;
+  }
   if ((e = cudaFuncSetAttribute(k_sg_setup_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, rows64)) != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_sg_setup_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, cols64);
 }

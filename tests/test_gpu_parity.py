@@ -64,6 +64,8 @@ CASES = {
     # the three workloads (the isothermal one at full size)
     "c1_isothermal_128x384": lambda: (fg.load_config("c1"), 3, ()),
     "c2_selfgravity_alpha_rk5": lambda: (small("c2"), 3, ()),
+    # self-gravity at lengths with compile-time FFT plans (rings 384, columns 256)
+    "c2_selfgravity_128x384": lambda: (small("c2", nrad=128, nsec=384), 2, ()),
     "c3_adiabatic_cooling": lambda: (small("c3"), 3, ("energy",)),
     "c3_adiabatic_no_cooling": lambda: (small("c3", cooling=0), 2, ("energy",)),
     # boundaries
@@ -168,5 +170,20 @@ def test_register_azimuthal_kernel_matches_barrier_kernel(cfg):
     names = ("dens", "vrad", "vtheta") + (("energy",) if params.adiabatic else ())
     for name in names:
         assert rel_linf(a.field(name), b.field(name)) < 1e-11, name
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(fg.FARGO_FP64, 1e-12), (fg.FARGO_FP32_BULK, 1e-5)])
+def test_compile_time_fft_plans_match_runtime_plans(prec, tol):
+    # rings of 768 and columns of 512 (the 256x768 disk's lengths) with the
+    # compile-time Stockham plans vs the run-time plans: the same butterflies and
+    # twiddles, so the fields agree to rounding
+    params, planets = small("c2", nrad=256, nsec=768)
+    a = fg.Disk(params, planets, prec)
+    b = _disk_with_env(params, planets, prec, {"FARGO_SG_GENERIC": "1"})
+    assert a.step_DT() == b.step_DT()
+    for name in ("dens", "vrad", "vtheta"):
+        assert rel_linf(a.field(name), b.field(name)) < tol, name
     a.close()
     b.close()
