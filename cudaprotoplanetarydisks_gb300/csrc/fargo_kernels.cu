@@ -940,6 +940,18 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
   const bool col = j < nsec;
   const int jp = col ? jp1(j, nsec) : 0;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT), Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
+  // ring-table rows of rings i0-1 .. i0+TR+1 (zero outside 0 .. nrad), staged with
+  // the tile so that no phase after a barrier loads from global memory
+  __shared__ T sRT[5][TR + 3];  // INVDIFFRMED, RMED, RINF, RSUP, INVSURF
+  if (y == 0 && x < TR + 3) {
+    const int k = i0 - 1 + x;
+    const bool ok = k >= 0 && k <= nrad;
+    sRT[0][x] = ok ? RT(a, RT_INVDIFFRMED, k) : (T)0;
+    sRT[1][x] = ok ? RT(a, RT_RMED, k) : (T)0;
+    sRT[2][x] = ok ? RT(a, RT_RINF, k) : (T)0;
+    sRT[3][x] = ok ? RT(a, RT_RSUP, k) : (T)0;
+    sRT[4][x] = ok ? RT(a, RT_INVSURF, k) : (T)0;
+  }
   // LRMomenta and DivisePolarGrid over the tile and its halo (zero outside the grid)
   for (int rr = y; rr < TR + 4; rr += ny) {
     const int k = i0 - 2 + rr;
@@ -974,7 +986,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
   for (int dd = y; dd < TR + 2; dd += ny) {
     const int k = i0 - 1 + dd;
     const bool in = k > 0 && k < nrad - 1;
-    const T idm0 = in ? RT(a, RT_INVDIFFRMED, k) : (T)0.0, idm1 = in ? RT(a, RT_INVDIFFRMED, k + 1) : (T)0.0;
+    const T idm0 = in ? sRT[0][dd] : (T)0.0, idm1 = in ? sRT[0][dd + 1] : (T)0.0;
 #pragma unroll
     for (int f = 0; f < NS; f++) {
       T v = (T)0.0;
@@ -995,8 +1007,8 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
     const T v = sV[ss][x];
     T lo = (T)0.0, hi = (T)0.0;
     if (in) {
-      lo = RT(a, RT_RMED, m) - RT(a, RT_RMED, m - 1) - v * dt;
-      hi = RT(a, RT_RMED, m + 1) - RT(a, RT_RMED, m) + v * dt;
+      lo = sRT[1][ss + 1] - sRT[1][ss] - v * dt;
+      hi = sRT[1][ss + 2] - sRT[1][ss + 1] + v * dt;
     }
 #pragma unroll
     for (int f = 0; f < NS; f++) {
@@ -1018,7 +1030,7 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
     const int i = i0 + t;
     if (i >= nrad) break;
     const size_t q = (size_t)i * nsec + j;
-    const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
+    const T rinf = sRT[2][t + 1], rsup = sRT[3][t + 1], isurf = sRT[4][t + 1];
     const T v0 = sV[t][x], v1 = sV[t + 1][x];
     const T ds0 = sS[6][t][x], ds1 = sS[6][t + 1][x];
     T *out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
@@ -1195,6 +1207,18 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   T *QB = QA + 6 * nsec;       // the same after the first sweep
   const size_t row = (size_t)i * nsec;
   const T *src[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
+  // the ring's table values and the control scalars, loaded with the ring (no
+  // load after a barrier)
+  const T tdt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
+  const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
+  const T dxrad = RT(a, RT_DRAD, i) * tdt, isurf = RT(a, RT_INVSURF, i);
+  double azshift = 0.0, cdt = 0.0;
+  T invdt = (T)0;
+  if (tid == 0) {
+    azshift = RT64(a, RT_AZSHIFT, i);
+    cdt = a.d.ctl->dt;
+    invdt = sizeof(T) == 4 ? (T)a.d.ctl->f32[CTL_F_INVDT] : (T)(1.0 / cdt);
+  }
   // ring to shared memory; ComputeAverageThetaVelocitiesKernel
   SumAcc<T> vs;
   vs.zero();
@@ -1224,19 +1248,15 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
     // is an FP64 integer decision; the constant residual velocity is a field
     // value, formed in T from the per-ring factor rm 2pi/nsec and 1/dt
     const double vmed = v.value() * a.inv_nsec;
-    const double Ntilde = vmed * RT64(a, RT_AZSHIFT, i) * a.d.ctl->dt;
+    const double Ntilde = vmed * azshift * cdt;
     const double Nround = floor(Ntilde + 0.5);
     s_shift = (int)(long)Nround;
-    const T invdt = sizeof(T) == 4 ? (T)a.d.ctl->f32[CTL_F_INVDT] : (T)(1.0 / a.d.ctl->dt);
-    s_vct = (T)(Ntilde - Nround) * RT(a, RT_DXTHETA, i) * invdt;
+    s_vct = (T)(Ntilde - Nround) * dxtheta * invdt;
     s_vm.set(vmed);
   }
   __syncthreads();
   const T vct = s_vct;
   const bool split = P.fast_transport;  // NoSplitAdvection == NO
-  const T tdt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
-  const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
-  const T dxrad = RT(a, RT_DRAD, i) * tdt, isurf = RT(a, RT_INVSURF, i);
   int sh = s_shift % nsec;
   if (sh < 0) sh += nsec;
   // VthetaRes at cells j0 .. j0+4

@@ -355,12 +355,16 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
   constexpr int G = 256;
   const int i = blockIdx.x, nsec = NSEC > 0 ? NSEC : a.P.nsec, M = NSEC > 0 ? NSEC / 2 + 1 : a.sg.M, tid = threadIdx.x;
   V *tw = (V *)sg_raw, *b0 = tw + nsec, *b1 = b0 + fpadn(nsec);
+  T *dn = (T *)(b1 + fpadn(nsec));  // the ring's density, for the epilogue
   const V *twg = (const V *)a.sg.tw1;
+  const size_t row = (size_t)i * nsec;
+  const T normr = RT(a, RT_SGNORMR, i), normt = RT(a, RT_SGNORMT, i);
   // this ring's row of the ring-major spectra that k_sg_cols left
   const V *spr = (const V *)a.sg.spec2_r + (size_t)i * M, *spt = (const V *)a.sg.spec2_t + (size_t)i * M;
 #pragma unroll 4
   for (int m = tid; m < nsec; m += G) {
     tw[m] = twg[m];
+    dn[m] = a.d.dens[row + m];
     V hr, ht;
     if (m < M) {
       hr = spr[m];
@@ -373,18 +377,22 @@ __global__ void __launch_bounds__(256) k_sg_rows_inv(KArgs<T> a) {
     b0[fpad(m)] = mk2(hr.x - ht.y, -(hr.y + ht.x));
   }
   __syncthreads();
-  const T normr = RT(a, RT_SGNORMR, i), normt = RT(a, RT_SGNORMT, i);
   const T selfc = (T)a.P.sgp_rstep, tstep = (T)a.P.sgp_tstep, eps = (T)a.P.sgp_eps, sgself = KC(T, a, KC_SGSELF);
-  const size_t row = (size_t)i * nsec;
   fft_any<NSEC, G>(b0, b1, nsec, a.sg.rad1, a.sg.nst1, tw, tid, [&](int j, V v, V *) {
     const V z = cconj(v);
     const size_t q = row + j;
     a.d.sg_acct[q] = z.y * normt;
     T accr = z.x * normr;
     // FP64: the reference's expression; FP32: its constant factor folded once
-    accr += sizeof(T) == 8 ? (T)1.0 * a.d.dens[q] * selfc * tstep / eps : a.d.dens[q] * sgself;
+    accr += sizeof(T) == 8 ? (T)1.0 * dn[j] * selfc * tstep / eps : dn[j] * sgself;
     a.d.sg_accr[q] = accr;
   });
+}
+
+// dynamic shared memory of k_sg_rows_inv: twiddles, two FFT buffers, the density
+template <class T>
+static size_t sg_rows_inv_smem(int nsec) {
+  return (nsec + 2 * fpadn(nsec)) * 2 * sizeof(T) + nsec * sizeof(T);
 }
 
 // Kernel instance for a length: the compile-time plan when the length has one.
@@ -439,7 +447,7 @@ void launch_sg_cols_inv(const KArgs<T> &a, cudaStream_t s) {
   const size_t vs = 2 * sizeof(T);
   launch_k(a.pdl, sg_cols_fn<T>(a.sg_generic ? 0 : n0), dim3(a.sg.M), dim3(2 * sg_col_group(n0)), (n0 + 6 * fpadn(n0)) * vs, s, a);
   probe_mark(s, "k_sg_cols");
-  launch_k(a.pdl, sg_rows_inv_fn<T>(a.sg_generic ? 0 : nsec), dim3(nrad), dim3(256), (nsec + 2 * fpadn(nsec)) * vs, s, a);
+  launch_k(a.pdl, sg_rows_inv_fn<T>(a.sg_generic ? 0 : nsec), dim3(nrad), dim3(256), sg_rows_inv_smem<T>(nsec), s, a);
   probe_mark(s, "k_sg_rows_inv");
 }
 
@@ -520,7 +528,8 @@ cudaError_t prepare_sg_kernels(int nsec, int n0) {
       if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(fr, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
-    if ((e = cudaFuncSetAttribute(fi, cudaFuncAttributeMaxDynamicSharedMemorySize, rows)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute(fi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sg_rows_inv_smem<T>(nsec))) != cudaSuccess)
+      return e;
     if ((e = cudaFuncSetAttribute(fc, cudaFuncAttributeMaxDynamicSharedMemorySize, cols)) != cudaSuccess) return e;
   }
   if ((e = cudaFuncSetAttribute(k_sg_setup_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, rows64)) != cudaSuccess) return e;
