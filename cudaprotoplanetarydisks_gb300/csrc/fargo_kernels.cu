@@ -270,6 +270,10 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   if (cfl_ring) r.vm = s_vm;
   T *pot = a.d.potential + (size_t)i * nsec;
   T mx = (T)0.0;
+  // the planets' potential of the register-resident cells, stored after the
+  // last-block ticket (no later kernel of this launch reads it, so the fence
+  // before the ticket need not wait for it)
+  T ph[NC];
   const int nchunk = do_forces ? (nbody + 1) >> 1 : 1;
   for (int ch = 0; ch < nchunk; ch++) {
     const bool first = (ch == 0);
@@ -291,7 +295,7 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     fy0.zero();
     fx1.zero();
     fy1.zero();
-    auto cell = [&](int j, const CflCell<T> &e) {
+    auto cell = [&](int j, const CflCell<T> &e, T &phk) {
       if (first && cfl_ring) {
         const T S = cfl_cell_S(a, e, r);
         mx = (S > mx) ? S : mx;
@@ -313,19 +317,20 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
             if (P.indirect_term) pt += mp * s_pot[k][4] * (x * xp + y * yp);
             phi += pt;
           }
-          pot[j] = phi;
+          if (CPT > 0) phk = phi;
+          else pot[j] = phi;
         }
       }
     };
     if (CPT > 0) {
 #pragma unroll
       for (int k = 0; k < NC; k++)
-        if (tid + k * 256 < nsec) cell(tid + k * 256, q[k]);
+        if (tid + k * 256 < nsec) cell(tid + k * 256, q[k], ph[k]);
     } else {
       for (int j = tid; j < nsec; j += 256) {
         CflCell<T> e;
         cfl_cell_load(a, i, j, cfl_ring, do_forces, e);
-        cell(j, e);
+        cell(j, e, ph[0]);
       }
     }
     if (do_forces) {
@@ -374,6 +379,11 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   __threadfence();
   __syncthreads();
   if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
+  if (CPT > 0 && do_forces && P.nb > 0) {
+#pragma unroll
+    for (int k = 0; k < NC; k++)
+      if (tid + k * 256 < nsec) pot[tid + k * 256] = ph[k];
+  }
   __syncthreads();
   if (!s_last) return;
   __threadfence();
@@ -1268,13 +1278,18 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
     if (!split) vr = vr + vct;
     vel[c] = vr;
   }
-  // one sweep (QuantitiesAdvection) from ring Q; out == nullptr: store to global
+  // one sweep (QuantitiesAdvection) from ring Q; out == nullptr: store to global.
+  // Per interface c (between cells j0-1+c and j0+c) the upwind side, the
+  // coefficient of the upwind slope and the flux factor dxrad ds v are the same
+  // for every quantity: formed once, then each quantity adds its slopes, its
+  // upwind values and its update.
   auto sweep = [&](const T *Q, T *out, bool const_vel) {
     T v[5];
 #pragma unroll
     for (int c = 0; c < 5; c++) v[c] = const_vel ? vct : vel[c];
     // StarThetaKernel / StarThetaKernel2 on the density
-    T d[8], id[8], dq[6], ds[5];
+    T d[8], id[8], dq[6], coef[5], F[5];
+    bool upw[5];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
@@ -1288,8 +1303,13 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
     for (int c = 0; c < 5; c++) {
       const T ksi = v[c] * tdt;
-      ds[c] = (ksi > (T)0.0) ? d[c + 1] + (dxtheta - ksi) * dq[c] : d[c + 2] - (dxtheta + ksi) * dq[c + 1];
+      upw[c] = ksi > (T)0.0;
+      // x + (dxtheta - ksi) q' upwind from the left, x - (dxtheta + ksi) q' from the right
+      coef[c] = upw[c] ? dxtheta - ksi : -(dxtheta + ksi);
+      const T ds = (upw[c] ? d[c + 1] : d[c + 2]) + coef[c] * (upw[c] ? dq[c] : dq[c + 1]);
+      F[c] = dxrad * ds * v[c];
     }
+#pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
       const T *q = Q + f * nsec;
@@ -1311,14 +1331,10 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
         dw[k] = (dqp * dqm > (T)0.0) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
       }
 #pragma unroll
-      for (int c = 0; c < 5; c++) {
-        const T ksi = v[c] * tdt;
-        sw[c] = (ksi > (T)0.0) ? wv[c + 1] + (dxtheta - ksi) * dw[c] : wv[c + 2] - (dxtheta + ksi) * dw[c + 1];
-      }
+      for (int c = 0; c < 5; c++) sw[c] = (upw[c] ? wv[c + 1] : wv[c + 2]) + coef[c] * (upw[c] ? dw[c] : dw[c + 1]);
 #pragma unroll
       for (int c = 0; c < 4; c++) {
-        T varq = dxrad * sw[c] * ds[c] * v[c];
-        varq -= dxrad * sw[c + 1] * ds[c + 1] * v[c + 1];
+        const T varq = sw[c] * F[c] - sw[c + 1] * F[c + 1];
         const T nq = q[j0 + c] + varq * isurf;
         if (out) {
           out[f * nsec + j0 + c] = nq;
