@@ -930,11 +930,12 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
 // interfaces and the cell updates are each formed once, one barrier between
 // the phases.
 #define RAD_TR 16
+#define RAD_NY 10  // thread rows: at most two rows per phase for every warp
 #define RAD_NS 7   // streams: rmp, rmm, tmp, tmm, energy, density (as q/rho), raw density
 #define RAD_SMEM(T) \
   (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 2) + RAD_NS * (RAD_TR + 1)))
 template <class T>
-__global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
   pdl_enter();
   constexpr int TW = 32, TR = RAD_TR, NS = RAD_NS;
   extern __shared__ __align__(16) unsigned char rad_smem[];
@@ -945,7 +946,8 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
   T(*sS)[TR + 1][TW] = reinterpret_cast<T(*)[TR + 1][TW]>(sD + NS);      // interface values at i0 .. i0+TR
   const DevParams &P = a.P;
   const int nrad = P.nrad, nsec = P.nsec;
-  const int x = threadIdx.x, y = threadIdx.y, ny = blockDim.y;
+  constexpr int ny = RAD_NY;
+  const int x = threadIdx.x, y = threadIdx.y;
   const int j = blockIdx.x * TW + x, i0 = blockIdx.y * TR;
   const bool col = j < nsec;
   const int jp = col ? jp1(j, nsec) : 0;
@@ -1015,22 +1017,18 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
     const int m = i0 + ss;
     const bool in = m > 0 && m < nrad;
     const T v = sV[ss][x];
-    T lo = (T)0.0, hi = (T)0.0;
+    // the upwind side and the coefficient of its slope, the same for every stream:
+    // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise
+    const bool up = v > (T)0.0;
+    T coef = (T)0.0;
     if (in) {
-      lo = sRT[1][ss + 1] - sRT[1][ss] - v * dt;
-      hi = sRT[1][ss + 2] - sRT[1][ss + 1] + v * dt;
+      const T lo = sRT[1][ss + 1] - sRT[1][ss] - v * dt;
+      const T hi = sRT[1][ss + 2] - sRT[1][ss + 1] + v * dt;
+      coef = up ? lo * (T)0.5 : -(hi * (T)0.5);
     }
+    const int rw = up ? ss + 1 : ss + 2, rd = up ? ss : ss + 1;
 #pragma unroll
-    for (int f = 0; f < NS; f++) {
-      T st = (T)0.0;
-      if (in) {
-        if (v > (T)0.0)
-          st = sW[f][ss + 1][x] + lo * (T)0.5 * sD[f][ss][x];
-        else
-          st = sW[f][ss + 2][x] - hi * (T)0.5 * sD[f][ss + 1][x];
-      }
-      sS[f][ss][x] = st;
-    }
+    for (int f = 0; f < NS; f++) sS[f][ss][x] = in ? sW[f][rw][x] + coef * sD[f][rd][x] : (T)0.0;
   }
   __syncthreads();
   if (!col) return;
@@ -1043,12 +1041,13 @@ __global__ void __launch_bounds__(256) k_transport_radial(KArgs<T> a) {
     const T rinf = sRT[2][t + 1], rsup = sRT[3][t + 1], isurf = sRT[4][t + 1];
     const T v0 = sV[t][x], v1 = sV[t + 1][x];
     const T ds0 = sS[6][t][x], ds1 = sS[6][t + 1][x];
+    // the mass fluxes through the two interfaces, the same for every stream
+    const T F0 = dt * dtheta * rinf * ds0 * v0, F1 = dt * dtheta * rsup * ds1 * v1;
     T *out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
 #pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
-      T varq = dt * dtheta * rinf * sS[f][t][x] * ds0 * v0;
-      varq -= dt * dtheta * rsup * sS[f][t + 1][x] * ds1 * v1;
+      const T varq = sS[f][t][x] * F0 - sS[f][t + 1][x] * F1;
       out[f][q] = sQ[f][t][x] + varq * isurf;
       if (f == 5 && i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq;
     }
@@ -1507,7 +1506,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
-    launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, 8), RAD_SMEM(T), s, a);
+    launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, RAD_NY), RAD_SMEM(T), s, a);
     MARK("k_transport_radial");
     if (a.az_regs) {
       launch_k(a.pdl, k_transport_azimuthal4<T>, dim3(P.nrad), dim3((P.nsec / 4 + 31) / 32 * 32), az_smem_bytes, s, a);
