@@ -166,6 +166,37 @@ enum { KC_GM1 = 0, KC_GGM1, KC_INVDPHI, KC_SGSELF, KC_DTHETA, KC_COUNT };
 // A no-op for a kernel launched without the attribute.
 __device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Four consecutive field values (16-byte aligned) in one or two vector accesses.
+template <class T>
+__device__ __forceinline__ void load4(const T *__restrict__ p, T *out);
+template <>
+__device__ __forceinline__ void load4<float>(const float *__restrict__ p, float *out) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  out[0] = v.x;
+  out[1] = v.y;
+  out[2] = v.z;
+  out[3] = v.w;
+}
+template <>
+__device__ __forceinline__ void load4<double>(const double *__restrict__ p, double *out) {
+  const double2 v0 = *reinterpret_cast<const double2 *>(p), v1 = *reinterpret_cast<const double2 *>(p + 2);
+  out[0] = v0.x;
+  out[1] = v0.y;
+  out[2] = v1.x;
+  out[3] = v1.y;
+}
+template <class T>
+__device__ __forceinline__ void store4(T *p, const T *v);
+template <>
+__device__ __forceinline__ void store4<float>(float *p, const float *v) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store4<double>(double *p, const double *v) {
+  reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+  reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+}
+
 // Division in the transport sweeps: the fast reciprocal-based divide for float
 // fields (within 2 ulp; the FP32-bulk mode), IEEE division for double fields.
 __device__ __forceinline__ float bulk_div(float a, float b) { return __fdividef(a, b); }

@@ -142,11 +142,11 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
   fy.add(cellmass * dy * InvDist3);
 }
 
-// CPT > 0: nsec <= 256 * CPT, and every thread holds the inputs of its CPT cells
-// in registers, loaded in one batch ahead of the ring mean (one memory latency
-// instead of one per pass and per cell).  CPT = 0: any nsec, cells streamed.
-// Each thread visits its cells in the same order either way (j = tid, tid + 256,
-// ...), so both give the same sums.
+// V4 = 1 (nsec % 4 == 0, 260 <= nsec <= 1024): thread t holds the inputs of cells
+// 4t..4t+3 in registers, each stream read with one 16-byte load, in one batch
+// ahead of the ring mean (one memory latency, a few load instructions).  V4 = 0:
+// any nsec, 256 threads, cells j = tid, tid + 256, ... streamed.  Every sum runs
+// in a fixed order, so each instance is deterministic.
 // Per ring the CTA also forms the two time-step limits and folds them into the
 // control block's minima (64-bit integer atomicMin on the bit patterns of
 // non-negative doubles: order-free, so deterministic): C/sqrt(max S) of its cells
@@ -155,16 +155,16 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
 // ring i+1's own CTA sums it.  The minimum over rings of these correctly rounded,
 // monotone maps equals the map of the extreme S or difference, so the result is
 // that of one sqrt and one divide of the maxima, and the last CTA reads two words.
-template <class T, int CPT>
-__global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
+template <class T, int V4>
+__global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
   pdl_enter();
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
-  constexpr int NW = 8;                       // warps of the 256-thread CTA
+  constexpr int NW = 8;                       // most warps of a CTA (96 to 256 threads)
   constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
-  constexpr int NC = CPT > 0 ? CPT : 1;
+  constexpr int NC = V4 ? 4 : 1;
   const DevParams &P = a.P;
   const int i = blockIdx.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
-  const int lane = tid & 31, w = tid >> 5;
+  const int lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
   Ctl *c = a.d.ctl;
   __shared__ SumAcc<T> s_part[NW][NV];
   __shared__ SumAcc<T> s_vpart[2][NW];
@@ -221,28 +221,68 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   const T *vth1 = vth + nsec;
   CflCell<T> q[NC];
   T vn[NC];
-  if (CPT > 0) {
+  const int j0 = 4 * tid;
+  const bool own = V4 && j0 < nsec;
+  if (own) {
+    const size_t o = (size_t)i * nsec + j0;
+    T x[4];
+    load4(vth + j0, x);
 #pragma unroll
-    for (int k = 0; k < NC; k++) {
-      const int j = tid + k * 256;
-      if (j < nsec) {
-        cfl_cell_load(a, i, j, cfl_ring, do_forces, q[k]);
-        vn[k] = shear_ring ? vth1[j] : (T)0;
+    for (int c = 0; c < 4; c++) {
+      q[c].vt = x[c];
+      q[c].vtn = q[c].vr0 = q[c].vr1 = q[c].cs = q[c].dn = q[c].cf = q[c].sf = q[c].cp = q[c].sp = (T)0;
+      vn[c] = (T)0;
+    }
+    if (cfl_ring) {
+      load4(a.d.vrad + o, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) q[c].vr0 = x[c];
+      load4(a.d.vrad + o + nsec, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) q[c].vr1 = x[c];
+      if (a.d.cs) {
+        load4(a.d.cs + o, x);
+#pragma unroll
+        for (int c = 0; c < 4; c++) q[c].cs = x[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; c++) q[c].vtn = q[c + 1].vt;
+      q[3].vtn = vth[jp1(j0 + 3, nsec)];
+    }
+    if (do_forces) {
+      load4(a.d.dens + o, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) q[c].dn = x[c];
+      load4(a.d.cosFt + j0, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) q[c].cf = x[c];
+      load4(a.d.sinFt + j0, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) q[c].sf = x[c];
+      if (P.nb > 0) {
+        load4(a.d.cosP + j0, x);
+#pragma unroll
+        for (int c = 0; c < 4; c++) q[c].cp = x[c];
+        load4(a.d.sinP + j0, x);
+#pragma unroll
+        for (int c = 0; c < 4; c++) q[c].sp = x[c];
       }
     }
+    if (shear_ring) load4(vth1 + j0, vn);
   }
   if (do_cfl) {
     // ConditionCFLKernel1D: ring means of Vtheta (ring i, and ring i+1 for the shear)
     SumAcc<T> v, v1;
     v.zero();
     v1.zero();
-    if (CPT > 0) {
+    if (V4) {
+      if (own) {
 #pragma unroll
-      for (int k = 0; k < NC; k++)
-        if (tid + k * 256 < nsec) {
-          v.add(q[k].vt);
-          v1.add(vn[k]);
+        for (int c = 0; c < NC; c++) {
+          v.add(q[c].vt);
+          v1.add(vn[c]);
         }
+      }
     } else {
       for (int j = tid; j < nsec; j += 256) v.add(vth[j]);
       if (shear_ring)
@@ -259,7 +299,7 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   if (do_cfl && (tid == 0 || (tid == 32 && shear_ring))) {
     const int h = tid >> 5;
     SumAcc<T> v = s_vpart[h][0];
-    for (int k = 1; k < NW; k++) v.merge(s_vpart[h][k]);
+    for (int k = 1; k < nw; k++) v.merge(s_vpart[h][k]);
     const double vmoy = sizeof(T) == 8 ? v.value() / (double)nsec : v.value() * a.inv_nsec;
     if (h == 0) s_vm.set(vmoy);
     // ring angular velocity of the shear limit (ConditionCFLKernel2D2)
@@ -312,20 +352,22 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
           for (int k = 0; k < P.nb; k++) {
             const T xp = s_pot[k][0], yp = s_pot[k][1], mp = s_pot[k][2];
             const T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
-            const T distancesmooth = sqrt(distance + s_pot[k][3]);
-            T pt = -mp / distancesmooth;
+            // FP64: -mp / sqrt(d^2 + eps^2) as the reference; FP32: one reciprocal
+            // square root (within 2 ulp) instead of the IEEE sqrt and divide
+            T pt = sizeof(T) == 4 ? -mp * rsqrt(distance + s_pot[k][3]) : -mp / sqrt(distance + s_pot[k][3]);
             if (P.indirect_term) pt += mp * s_pot[k][4] * (x * xp + y * yp);
             phi += pt;
           }
-          if (CPT > 0) phk = phi;
+          if (V4) phk = phi;
           else pot[j] = phi;
         }
       }
     };
-    if (CPT > 0) {
+    if (V4) {
+      if (own) {
 #pragma unroll
-      for (int k = 0; k < NC; k++)
-        if (tid + k * 256 < nsec) cell(tid + k * 256, q[k], ph[k]);
+        for (int c = 0; c < NC; c++) cell(j0 + c, q[c], ph[c]);
+      }
     } else {
       for (int j = tid; j < nsec; j += 256) {
         CflCell<T> e;
@@ -361,12 +403,12 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   if (tid < 2 * nbody) {
     // ring partial sums stay SumAcc<T> (8 bytes either way) until the totals
     SumAcc<T> f = s_part[0][tid];
-    for (int k = 1; k < NW; k++) f.merge(s_part[k][tid]);
+    for (int k = 1; k < nw; k++) f.merge(s_part[k][tid]);
     reinterpret_cast<SumAcc<T> *>(a.d.ring_force)[(size_t)i * NV + tid] = f;
   }
   if (cfl_ring && tid == 32) {
     T m = s_mx[0];
-    for (int k = 1; k < NW; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
+    for (int k = 1; k < nw; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
     const double S = (double)m;
     if (S > 0.0) atomicMin(&c->ring_min[0], __double_as_longlong(div_once(CFLSECURITY, sqrt_once(S))));
   }
@@ -379,11 +421,7 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   __threadfence();
   __syncthreads();
   if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
-  if (CPT > 0 && do_forces && P.nb > 0) {
-#pragma unroll
-    for (int k = 0; k < NC; k++)
-      if (tid + k * 256 < nsec) pot[tid + k * 256] = ph[k];
-  }
+  if (own && do_forces && P.nb > 0) store4(pot + j0, ph);
   __syncthreads();
   if (!s_last) return;
   __threadfence();
@@ -395,10 +433,10 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
     const double tot = ring_total<T>(a.d.ring_force, nrad, NV, w, lane);  // valid in lane 0
     if (lane == 0) s_acc[w] = tot;
   }
-  if (do_cfl && (tid == 128 || tid == 160)) {
+  if (do_cfl && (tid == 64 || tid == 65)) {
     // smallest per-ring step (CFL over the rings i >= 1, shear over i < nrad - 1),
     // reset for the next launch
-    const int k = (tid - 128) >> 5;
+    const int k = tid - 64;
     const long long m = __ldcg(&c->ring_min[k]);
     c->ring_min[k] = FARGO_RING_NO_LIMIT;
     s_dtc[k] = (m == FARGO_RING_NO_LIMIT) ? 1e30 : __longlong_as_double(m);
@@ -455,16 +493,17 @@ __global__ void __launch_bounds__(256, 2) k_cfl_forces(KArgs<T> a) {
   }
 }
 
-// The CFL/force kernel for a ring of nsec cells: register-resident cells up to
-// 1024 per ring
+// The CFL/force kernel for a ring of nsec cells: four contiguous cells per
+// thread when nsec % 4 == 0 and 260 <= nsec <= 1024 (96 to 256 threads: every
+// single-thread role has tid < 96), else the streamed 256-thread form
 template <class T>
 void launch_cfl_forces(const KArgs<T> &a, cudaStream_t s) {
-  const int n = (a.P.nsec + 255) / 256;
-  const dim3 g(a.P.nrad), b(256);
-  if (n <= 2) launch_k(a.pdl, k_cfl_forces<T, 2>, g, b, 0, s, a);
-  else if (n == 3) launch_k(a.pdl, k_cfl_forces<T, 3>, g, b, 0, s, a);
-  else if (n == 4) launch_k(a.pdl, k_cfl_forces<T, 4>, g, b, 0, s, a);
-  else launch_k(a.pdl, k_cfl_forces<T, 0>, g, b, 0, s, a);
+  const int nsec = a.P.nsec;
+  const dim3 g(a.P.nrad);
+  if (nsec % 4 == 0 && nsec >= 260 && nsec <= 1024)
+    launch_k(a.pdl, k_cfl_forces<T, 1>, g, dim3((nsec / 4 + 31) / 32 * 32), 0, s, a);
+  else
+    launch_k(a.pdl, k_cfl_forces<T, 0>, g, dim3(256), 0, s, a);
 }
 
 // The planetary part of a substep (AdvanceSystemFromDisk, AdvanceSystemRK5,
@@ -1176,24 +1215,6 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
 // ring, the second sweep (or the only one) stores to global memory at the
 // shifted index.  Same per-cell arithmetic as k_transport_azimuthal.
 namespace {
-template <class T>
-__device__ __forceinline__ void az_load4(const T *__restrict__ p, T *out);
-template <>
-__device__ __forceinline__ void az_load4<float>(const float *__restrict__ p, float *out) {
-  const float4 v = *reinterpret_cast<const float4 *>(p);
-  out[0] = v.x;
-  out[1] = v.y;
-  out[2] = v.z;
-  out[3] = v.w;
-}
-template <>
-__device__ __forceinline__ void az_load4<double>(const double *__restrict__ p, double *out) {
-  const double2 v0 = *reinterpret_cast<const double2 *>(p), v1 = *reinterpret_cast<const double2 *>(p + 2);
-  out[0] = v0.x;
-  out[1] = v0.y;
-  out[2] = v1.x;
-  out[3] = v1.y;
-}
 __device__ __forceinline__ int az_wrap(int j, int n) { return j < 0 ? j + n : (j >= n ? j - n : j); }
 }  // namespace
 
@@ -1233,7 +1254,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   vs.zero();
   if (own) {
     T x[4];
-    az_load4(a.d.vtheta + row + j0, x);
+    load4(a.d.vtheta + row + j0, x);
 #pragma unroll
     for (int c = 0; c < 4; c++) {
       VT[j0 + c] = x[c];
@@ -1242,7 +1263,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
-      az_load4(src[f] + row + j0, x);
+      load4(src[f] + row + j0, x);
 #pragma unroll
       for (int c = 0; c < 4; c++) QA[f * nsec + j0 + c] = x[c];
     }
@@ -1645,8 +1666,7 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
   // shared split only when idle, so kernels that run side by side (the CFL/force
   // kernel, the self-gravity transforms, the planet update) and successive
   // kernels under programmatic launch can share SMs only with the same split.
-  const void *all[] = {(const void *)k_cfl_forces<T, 0>, (const void *)k_cfl_forces<T, 2>,
-                       (const void *)k_cfl_forces<T, 3>, (const void *)k_cfl_forces<T, 4>, (const void *)k_planets, (const void *)k_soundspeed<T>,
+  const void *all[] = {(const void *)k_cfl_forces<T, 0>, (const void *)k_cfl_forces<T, 1>, (const void *)k_planets, (const void *)k_soundspeed<T>,
                        (const void *)k_correct_vtheta<T>, (const void *)k_bc_open<T>,
                        (const void *)k_bc_nonreflecting<T>, (const void *)k_bc_evanescent<T>,
                        (const void *)k_source<T>, (const void *)k_visc_tau<T>, (const void *)k_visc_update<T>,

@@ -194,8 +194,45 @@ __host__ __device__ constexpr int plan_ns(int n, int s) {
   return ns;
 }
 
-template <int N, int RAD, int NS, int G, class V, class Out>
-__device__ __forceinline__ void fft_stage_c(const V *src, const V *tw, int lt, Out out) {
+// Twiddles of a stage: read from the shared table ...
+template <class V>
+struct TwShared {
+  const V *tw;
+  template <int S, int TWS>
+  __device__ __forceinline__ V get(int r, int jj) const {
+    return tw[r * jj * TWS];
+  }
+};
+// ... or held in registers, when every stage has at most one butterfly per
+// thread (N / radix <= G): a thread needs radix - 1 twiddles per stage, loaded
+// once from the global table and used by every transform of the kernel.
+template <int N>
+__host__ __device__ constexpr bool plan_fits(int g) {
+  for (int s = 0; s < plan_nst(N); s++)
+    if (N / plan_rad(N, s) > g) return false;
+  return true;
+}
+template <int N, class V>
+struct TwRegs {
+  V w[plan_nst(N)][7];
+  template <int S, int TWS>
+  __device__ __forceinline__ V get(int r, int) const {
+    return w[S][r - 1];
+  }
+};
+template <int N, int S, class V>
+__device__ __forceinline__ void tw_regs_load(TwRegs<N, V> &t, const V *twg, int lt) {
+  constexpr int R = plan_rad(N, S), NS = plan_ns(N, S), NR = N / R, TWS = N / (NS * R);
+  if constexpr (NS > 1) {
+    const int jj = (lt < NR ? lt : 0) % NS;
+#pragma unroll
+    for (int r = 1; r < R; r++) t.w[S][r - 1] = twg[r * jj * TWS];
+  }
+  if constexpr (S + 1 < plan_nst(N)) tw_regs_load<N, S + 1>(t, twg, lt);
+}
+
+template <int N, int S, int RAD, int NS, int G, class V, class Tw, class Out>
+__device__ __forceinline__ void fft_stage_c(const V *src, const Tw &tw, int lt, Out out) {
   constexpr int NR = N / RAD, TWS = N / (NS * RAD);
 #pragma unroll
   for (int k = 0; k < (NR + G - 1) / G; k++) {
@@ -206,7 +243,7 @@ __device__ __forceinline__ void fft_stage_c(const V *src, const V *tw, int lt, O
 #pragma unroll
       for (int r = 0; r < RAD; r++) {
         v[r] = src[fpad(j + r * NR)];
-        if (r > 0 && NS > 1) v[r] = cmul(v[r], tw[r * jj * TWS]);
+        if (r > 0 && NS > 1) v[r] = cmul(v[r], tw.template get<S, TWS>(r, jj));
       }
       butterfly<RAD>(v);
       const int idxD = jb * NS * RAD + jj;
@@ -216,15 +253,15 @@ __device__ __forceinline__ void fft_stage_c(const V *src, const V *tw, int lt, O
   }
 }
 
-template <int N, int S, int G, class V, class Last>
-__device__ __forceinline__ V *fft_run_c(V *d0, V *d1, const V *tw, int lt, Last last) {
+template <int N, int S, int G, class V, class Tw, class Last>
+__device__ __forceinline__ V *fft_run_c(V *d0, V *d1, const Tw &tw, int lt, Last last) {
   constexpr int R = plan_rad(N, S), NS = plan_ns(N, S), NST = plan_nst(N);
   if constexpr (S == NST - 1) {
-    fft_stage_c<N, R, NS, G>(d0, tw, lt, [&](int k, V v) { last(k, v, d1); });
+    fft_stage_c<N, S, R, NS, G>(d0, tw, lt, [&](int k, V v) { last(k, v, d1); });
     __syncthreads();
     return d1;
   } else {
-    fft_stage_c<N, R, NS, G>(d0, tw, lt, [&](int k, V v) { d1[fpad(k)] = v; });
+    fft_stage_c<N, S, R, NS, G>(d0, tw, lt, [&](int k, V v) { d1[fpad(k)] = v; });
     __syncthreads();
     return fft_run_c<N, S + 1, G>(d1, d0, tw, lt, last);
   }
@@ -233,7 +270,7 @@ __device__ __forceinline__ V *fft_run_c(V *d0, V *d1, const V *tw, int lt, Last 
 // The compile-time plan for N > 0, the run-time one (rad, nst) for N = 0.
 template <int N, int G, class V, class Last>
 __device__ __forceinline__ V *fft_any(V *d0, V *d1, int n, const int *rad, int nst, const V *tw, int lt, Last last) {
-  if constexpr (N > 0) return fft_run_c<N, 0, G>(d0, d1, tw, lt, last);
+  if constexpr (N > 0) return fft_run_c<N, 0, G>(d0, d1, TwShared<V>{tw}, lt, last);
   else return fft_run(d0, d1, n, rad, nst, tw, lt, G, last);
 }
 
@@ -318,8 +355,15 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   const V *kh = (const V *)(g == 0 ? a.sg.khat_r : a.sg.khat_t) + (size_t)m * n0;
   V *col = (V *)(g == 0 ? a.sg.spec_r : a.sg.spec_t) + (size_t)m * nrad;
   V *row = (V *)(g == 0 ? a.sg.spec2_r : a.sg.spec2_t) + m;  // ring-major output, stride M
+  // twiddles in registers when the plan allows it, else in shared memory
+  constexpr bool REG = N0 > 0 && plan_fits<(N0 > 0 ? N0 : 2)>(GC);
+  TwRegs<(N0 > 0 ? N0 : 2), V> tr;
+  if constexpr (REG) {
+    tw_regs_load<N0, 0>(tr, twg, lt);
+  } else {
 #pragma unroll 4
-  for (int k = threadIdx.x; k < n0; k += blockDim.x) tw[k] = twg[k];
+    for (int k = threadIdx.x; k < n0; k += blockDim.x) tw[k] = twg[k];
+  }
 #pragma unroll 4
   for (int k = lt; k < n0; k += G) {
     K[fpad(k)] = kh[k];
@@ -335,9 +379,12 @@ __global__ void __launch_bounds__(256) k_sg_cols(KArgs<T> a) {
   auto store = [&](int k, V z, V *) {
     if (k < nrad) row[(size_t)k * a.sg.M] = cconj(z);
   };
-  if constexpr (N0 > 0) {
-    V *X = fft_run_c<N0, 0, GC>(b0, b1, tw, lt, conv);
-    fft_run_c<N0, 0, GC>(X, (X == b0) ? b1 : b0, tw, lt, store);
+  if constexpr (REG) {
+    V *X = fft_run_c<N0, 0, GC>(b0, b1, tr, lt, conv);
+    fft_run_c<N0, 0, GC>(X, (X == b0) ? b1 : b0, tr, lt, store);
+  } else if constexpr (N0 > 0) {
+    V *X = fft_run_c<N0, 0, GC>(b0, b1, TwShared<V>{tw}, lt, conv);
+    fft_run_c<N0, 0, GC>(X, (X == b0) ? b1 : b0, TwShared<V>{tw}, lt, store);
   } else {
     V *X = fft_run(b0, b1, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, conv);
     fft_run(X, (X == b0) ? b1 : b0, n0, a.sg.rad0, a.sg.nst0, tw, lt, G, store);
