@@ -73,7 +73,7 @@ class FargoPlanet(ctypes.Structure):
 class FargoScalars(ctypes.Structure):
     _fields_ = [("physical_time", _D), ("omega_frame", _D), ("lost_mass", _D),
                 ("last_dt", _D), ("substeps", ctypes.c_longlong), ("last_cfl", _I), ("nb", _I),
-                ("launches_per_substep", _I), ("launches_per_dt", _I)]
+                ("launches_per_substep", _I), ("launches_per_dt", _I), ("padded_substeps", ctypes.c_longlong)]
 
 
 _DP = ctypes.POINTER(_D)

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
   __shared__ double s_om[2];
   __shared__ RingMean<T> s_vm;
   __shared__ int s_nbody, s_last;
-  __shared__ double s_ctl[5];  // DT, dtemp, sloppy_dt, PhysicalTime, err (read before any write)
+  __shared__ double s_ctl[6];  // DT, dtemp, sloppy_dt, PhysicalTime, err, done (read before any write)
   const bool do_cfl = (a.mode == 0 || a.mode == 1);
   const bool do_forces = (a.mode != 1);
   const bool do_step = (a.mode == 0 || a.mode == 2);
@@ -182,9 +182,10 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
   const bool shear_ring = do_cfl && i < nrad - 1;
   // the control scalars the last block's decision reads, fetched up front by
   // every block so that the last one has them at hand
-  if (tid >= 64 && tid < 69) {
+  if (tid >= 64 && tid < 70) {
     const int k = tid - 64;
-    s_ctl[k] = k == 0 ? c->DT : k == 1 ? c->dtemp : k == 2 ? c->sloppy_dt : k == 3 ? c->PhysicalTime : (double)c->err;
+    s_ctl[k] = k == 0 ? c->DT : k == 1 ? c->dtemp : k == 2 ? c->sloppy_dt : k == 3 ? c->PhysicalTime
+             : k == 4 ? (double)c->err : (double)c->done;
   }
   // planet parameters of this substep, computed after the previous planet update
   // (fargo_planet_params): bodies feeling the disk and the planets' potential terms
@@ -446,7 +447,13 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
     c->ticket = 0u;
     double dt;
     bool cfl_err = false;
-    if (do_cfl) {
+    // a substep entered with the DT already done pads a loop body of several
+    // substeps: it runs with dt = 0, which leaves the disk and the planets as they
+    // are, and takes no CFL decision
+    const bool pad = do_step && s_ctl[5] != 0.0;
+    if (pad) {
+      dt = 0.0;
+    } else if (do_cfl) {
       const double DeltaT = (a.mode == 1) ? s_ctl[0] : s_ctl[0] - s_ctl[1];
       double newdt = fmin(s_dtc[0], s_dtc[1]);
       if (DeltaT < newdt) newdt = DeltaT;
@@ -479,9 +486,13 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
       if (s_ctl[4] != 0.0 || cfl_err) dt = 0.0;
       c->dt = dt;
       c->f32[CTL_F_DT] = (float)dt;
-      c->f32[CTL_F_INVDT] = 1.0f / (float)dt;
-      c->dtemp = s_ctl[1] + dt;
-      c->nsub_dt += 1;
+      c->f32[CTL_F_INVDT] = dt != 0.0 ? 1.0f / (float)dt : 0.0f;
+      if (!pad) {
+        c->dtemp = s_ctl[1] + dt;
+        c->nsub_dt += 1;
+        c->dt_sub = dt;
+      }
+      c->padding = pad ? 1 : 0;
       c->t_sub = s_ctl[3];
     }
   }
@@ -863,7 +874,9 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
                        (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])) /
                       ((T)0.5 * (D[q] + D[q - nsec]));
   }
-  if (!a.P.evanescent && (i == 0 || i == nrad - 1)) a.d.vthetaint[q] = subkeplerian_edge(a, i);
+  // (not in a padded substep, dt = 0: the edge rings keep the velocities the last
+  // transport gave them)
+  if (!a.P.evanescent && (i == 0 || i == nrad - 1) && dt != (T)0.0) a.d.vthetaint[q] = subkeplerian_edge(a, i);
 }
 
 // Substep2Kernel (src/Kernels.cu:409-434) + kernel (src/Kernels.cu:438-479) +
@@ -955,6 +968,7 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
     T num = em * dt * D[q] / sm + ct * ei + dt * ct * (qp - qm * D[q] / sm);
     T den = dt + ct + KC(T, a, KC_GM1) * dt * ct * dv;
     enew = num / den;
+    if (dt == (T)0.0) enew = ei;  // a padded substep: (ct ei) / ct is not exactly ei
   }
   a.d.energy[q] = enew;
 }
@@ -1123,7 +1137,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   const double vmed = block_sum_d(s, s_red) / (double)nsec;
   if (tid == 0) {
     // ComputeConstantResidualKernel (FP64 split; Nshift is an integer decision)
-    const double invdt = 1.0 / dt;
+    const double invdt = dt != 0.0 ? 1.0 / dt : 0.0;
     const double dpinvns = 2.0 * PI / (double)nsec;
     const double Ntilde = vmed * RT64(a, RT_INVRMED, i) * dt * (double)nsec / 2.0 / PI;
     const double Nround = floor(Ntilde + 0.5);
@@ -1247,7 +1261,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   if (tid == 0) {
     azshift = RT64(a, RT_AZSHIFT, i);
     cdt = a.d.ctl->dt;
-    invdt = sizeof(T) == 4 ? (T)a.d.ctl->f32[CTL_F_INVDT] : (T)(1.0 / cdt);
+    invdt = sizeof(T) == 4 ? (T)a.d.ctl->f32[CTL_F_INVDT] : (cdt != 0.0 ? (T)(1.0 / cdt) : (T)0);
   }
   // ring to shared memory; ComputeAverageThetaVelocitiesKernel
   SumAcc<T> vs;
@@ -1384,14 +1398,19 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
   const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
-  const T Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
+  const T Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA), dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
   const int jm = jm1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens;
-  if (i == 0) a.d.vrad[q] = (T)0.0;
-  else a.d.vrad[q] = (a.d.radmomp[q - nsec] + a.d.radmomm[q]) / (D[q] + D[q - nsec] + (T)1e-20);
+  const T vr = (i == 0) ? (T)0.0 : (a.d.radmomp[q - nsec] + a.d.radmomm[q]) / (D[q] + D[q - nsec] + (T)1e-20);
   const T rm = RT(a, RT_RMED, i);
-  a.d.vtheta[q] = (a.d.thetamomp[qm] + a.d.thetamomm[q]) / (D[q] + D[qm] + (T)1e-15) / rm - rm * Om;
+  const T vt = (a.d.thetamomp[qm] + a.d.thetamomm[q]) / (D[q] + D[qm] + (T)1e-15) / rm - rm * Om;
+  // a substep with dt = 0 (a padded one) keeps the velocities: re-deriving them
+  // from the momenta is not exact
+  if (dt != (T)0.0) {
+    a.d.vrad[q] = vr;
+    a.d.vtheta[q] = vt;
+  }
   if (with_temperature) {
     if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / D[q];
     else a.d.temperature[q] = KC(T, a, KC_GM1) * a.d.energy[q] / D[q];
@@ -1423,7 +1442,12 @@ __global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
     s = block_sum_d(s, s_red);
     if (threadIdx.x == 0) c->LostMass += s;
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && c->padding) {
+    // a padded substep (dt = 0): nothing to count, the loop stays done
+    c->padded += 1;
+    c->padding = 0;
+    if (a.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_handle, 0u);
+  } else if (threadIdx.x == 0) {
     c->PhysicalTime += c->dt;
     c->substeps += 1;
     int done = !(c->dtemp < 0.999999999 * c->DT);
@@ -1445,6 +1469,7 @@ __global__ void k_dt_begin(Ctl *c) {
   c->done = 0;
   c->err = 0;
   c->ticket = 0u;
+  c->padding = 0;
   c->ring_min[0] = c->ring_min[1] = FARGO_RING_NO_LIMIT;
 }
 

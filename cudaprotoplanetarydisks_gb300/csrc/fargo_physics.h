@@ -58,10 +58,14 @@ struct Ctl {
   int cfl, done, err, nsub_dt;
   long long substeps;
   unsigned int ticket;        // last-block-done counter of the CFL/force kernel
-  unsigned int pad0;
+  int padding;                // 1: the running substep pads the loop body (dt = 0)
   // smallest per-ring CFL and shear time steps of the CFL/force kernel, as the
   // integers of their (non-negative) bit patterns; FARGO_RING_NO_LIMIT between launches
   long long ring_min[2];
+  // dt of the last substep that advanced the disk (a padded substep runs with
+  // dt = 0), and the number of padded substeps run
+  double dt_sub;
+  long long padded;
   // planetary system (Types.cuh:2-12)
   int nb;
   int pad1;
@@ -93,7 +97,7 @@ FARGO_HD void fargo_ctl_mirror(Ctl &c) {
   c.f32[CTL_F_INDX] = (float)c.ind_x;
   c.f32[CTL_F_INDY] = (float)c.ind_y;
   c.f32[CTL_F_DOMEGA] = (float)c.domega;
-  c.f32[CTL_F_INVDT] = 1.0f / (float)c.dt;
+  c.f32[CTL_F_INVDT] = c.dt != 0.0 ? 1.0f / (float)c.dt : 0.0f;
   c.ring_min[0] = c.ring_min[1] = FARGO_RING_NO_LIMIT;
 }
 
@@ -426,6 +430,14 @@ FARGO_HD double fargo_vkep(const DevParams &P, double r, double t, double t0, do
 // and RotatePsys; then the parameters of the next substep.  The disk
 // accelerations and the indirect term are those of this substep.
 FARGO_HD void fargo_planets_substep(Ctl &c, const DevParams &P, double dt, double t) {
+  // dt = 0 (a substep padding the DT loop, or one after a device error): nothing
+  // moves and the frame keeps its rate (the forced-circular and release-date
+  // updates re-derive positions from angles and would not reproduce them exactly)
+  if (dt == 0.0) {
+    c.domega = 0.0;
+    c.f32[CTL_F_DOMEGA] = 0.0f;
+    return;
+  }
   if (P.corotating) fargo_psys_info(c, P, 1);
   int b = 1;
   for (int k = 0; k < c.nb; k++) {

@@ -136,6 +136,7 @@ typedef struct fargo_scalars {
   int    nb;                    /* number of planets                      */
   int    launches_per_substep;  /* kernels launched by one hydro substep  */
   int    launches_per_dt;       /* kernels launched once per DT (prefix)  */
+  long long padded_substeps;    /* substeps run with dt = 0 to fill a loop body of two */
 } fargo_scalars;
 
 typedef struct fargo_ctx fargo_ctx;

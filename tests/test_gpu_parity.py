@@ -136,13 +136,16 @@ def _disk_with_env(params, planets, prec, env):
                 os.environ[k] = v
 
 
-@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_NO_SG_AHEAD", "FARGO_AZ_GLOBAL"])
+@pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_NO_SG_AHEAD", "FARGO_NO_PAD",
+                                 "FARGO_AZ_GLOBAL"])
 def test_code_paths_are_bitwise_identical(env):
     # the conditional-graph DT loop vs the host loop; programmatic dependent
     # launch vs plain launches; the rotated DT loop (each substep launches the
     # next one's CFL/force kernel and self-gravity transforms) vs the plain
     # one; the next substep's ring transforms launched after the azimuthal
-    # transport vs at the substep start; the shared-memory vs the global-memory ring
+    # transport vs at the substep start; two substeps per loop iteration (the
+    # second one run with dt = 0 once the DT is done) vs one; the shared-memory
+    # vs the global-memory ring
     # buffers of the barrier-per-phase azimuthal kernel
     params, planets = small("c2")
     base = {"FARGO_AZ_GENERIC": "1"} if env == "FARGO_AZ_GLOBAL" else {}
@@ -185,5 +188,29 @@ def test_compile_time_fft_plans_match_runtime_plans(prec, tol):
     assert a.step_DT() == b.step_DT()
     for name in ("dens", "vrad", "vtheta"):
         assert rel_linf(a.field(name), b.field(name)) < tol, name
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("cfg,kw", [("c1", {}), ("c3", {}), ("c3", {"cooling": 0}), ("c2", {"corotating": 1}),
+                                    ("c2", {"corotating": 1, "guiding_center": 1}), ("c1", {"sloppy_cfl": 1})])
+def test_padded_substeps_leave_the_disk_unchanged(cfg, kw):
+    # a loop body of two substeps runs the second one with dt = 0 when the DT
+    # ended after the first: every field, the planets and the clocks must be
+    # bitwise those of the one-substep loop, and the padded substeps must have run
+    params, planets = small(cfg, **kw)
+    a = fg.Disk(params, planets, fg.FARGO_FP64)
+    b = _disk_with_env(params, planets, fg.FARGO_FP64, {"FARGO_NO_PAD": "1"})
+    for _ in range(4):
+        assert a.step_DT() == b.step_DT()
+    names = ("dens", "vrad", "vtheta") + (("energy",) if params.adiabatic else ())
+    for name in names:
+        assert np.array_equal(a.field(name), b.field(name)), name
+    for pa, pb in zip(a.planets(), b.planets()):
+        assert (pa.x, pa.y, pa.vx, pa.vy) == (pb.x, pb.y, pb.vx, pb.vy)
+    sa, sb = a.scalars(), b.scalars()
+    assert (sa.physical_time, sa.omega_frame, sa.substeps, sa.last_dt) == \
+           (sb.physical_time, sb.omega_frame, sb.substeps, sb.last_dt)
+    assert sa.padded_substeps > 0 and sb.padded_substeps == 0
     a.close()
     b.close()
