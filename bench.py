@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
                     help="profiling target: warm-up DTs, then --steps substeps launched kernel by kernel "
                          "(kernels inside the DT graph's while loop are invisible to ncu)")
@@ -258,6 +259,57 @@ def time_e2e(disk, stream, steps, params):
     return wall, nsub, len(names) * nbytes, len(names) * nbytes
 
 
+def batch_ensemble(ndt=2, n=64):
+    """The batched ensemble (64 seeded disks, Nrad in {128..512}, Nsec = 3 Nrad):
+    FP32-bulk disks advanced side by side (fargo_batch) against the same disks in
+    plain FP64 one after another, after one warm-up DT each; the FP32 density
+    error against FP64 after the same DTs.  The ensemble's state (~1.4 GB FP32)
+    is larger than L2; the plain runs flush L2 before each disk."""
+    import numpy as np
+    import torch
+    import cudaprotoplanetarydisks_gb300 as fg
+    disks = fg.c4_disks(n)
+    cells = [p.nrad * p.nsec for p, _ in disks]
+    b = fg.Batch(disks, fg.FARGO_FP32_BULK)
+    b.run_async(1)
+    b.sync()
+    s0 = [d.scalars().substeps for d in b.disks]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run_async(ndt)
+    b.sync()
+    t32 = time.perf_counter() - t0
+    cu32 = sum((d.scalars().substeps - s0[k]) * cells[k] for k, d in enumerate(b.disks))
+    dens32 = [d.field("dens")[:-1] for d in b.disks]
+    launches32 = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
+                     for k, d in enumerate(b.disks))
+    b.close()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    t64, cu64, err = 0.0, 0, []
+    for k, (p, pl) in enumerate(disks):
+        d = fg.Disk(p, pl, fg.FARGO_FP64)
+        d.run(1)
+        s = d.scalars().substeps
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.run(ndt)
+        t64 += time.perf_counter() - t0
+        cu64 += (d.scalars().substeps - s) * cells[k]
+        ref = d.field("dens")[:-1]
+        err.append(float(np.linalg.norm(dens32[k] - ref) / np.linalg.norm(ref)))
+        d.close()
+    v32, v64 = cu32 / t32, cu64 / t64
+    return {"workload": f"{n} seeded disks, Nrad in {{128,192,256,384,512}}, Nsec = 3 Nrad, isothermal, "
+                        "alpha, one planet each (configs c4_disks)",
+            "cells": sum(cells), "dts_per_disk": ndt,
+            "fp32_batched": {"value": v32, "unit": METRIC, "seconds": t32, "gpu_launches_approx": launches32},
+            "fp64_plain_sequential": {"value": v64, "unit": METRIC, "seconds": t64},
+            "ratio_fp32_batched_to_fp64_plain": v32 / v64,
+            "fp32_dens_rel_l2_vs_fp64_max": max(err), "fp32_dens_rel_l2_vs_fp64_median": float(np.median(err)),
+            "timing": "host wall clock around run + sync (many streams: one per disk)"}
+
+
 def oracle_sample(params, planets, ndt, threads):
     from oracle.oracle import OracleDisk
     OracleDisk.set_threads(threads)
@@ -402,6 +454,8 @@ def run_own(args, world, rank, local):
         line["fp32_error_vs_fp64_oracle"] = {"after": f"{ndt} DTs", "fields": err}
         disk.close()
         o.close()
+    if not args.no_batch and world == 1:
+        line["batch_c4"] = batch_ensemble()
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

@@ -13,7 +13,7 @@ from . import _capi
 from ._capi import (FARGO_FP32_BULK, FARGO_FP64, FIELDS, SUB_BOUNDARY, SUB_ENERGY,  # noqa: F401
                     SUB_POTENTIAL, SUB_SOUNDSPEED, SUB_SOURCE, SUB_TEMPERATURE, SUB_TRANSPORT,
                     FargoParams, FargoPlanet, FargoScalars)
-from .config import default_params, load_config, read_par, read_planets  # noqa: F401
+from .config import c4_disks, default_params, load_config, read_par, read_planets  # noqa: F401
 
 _DP = ctypes.POINTER(ctypes.c_double)
 
@@ -29,11 +29,15 @@ def _ptr(a):
 class Disk:
     """One disk on one GPU.  precision: FARGO_FP64 (parity mode) or FARGO_FP32_BULK."""
 
-    def __init__(self, params, planets, precision=FARGO_FP64, stream=None):
+    def __init__(self, params, planets, precision=FARGO_FP64, stream=None, _handle=None):
         self.lib = _capi.load()
         self.params = params
         self.nrad, self.nsec = params.nrad, params.nsec
         self.precision = precision
+        self.owned = _handle is None
+        if _handle is not None:  # a disk of a Batch (owned by the batch)
+            self.h = _handle
+            return
         arr = (FargoPlanet * max(1, len(planets)))(*planets)
         h = ctypes.c_void_p()
         rc = self.lib.fargo_ctx_create(ctypes.byref(params), arr, len(planets), precision,
@@ -48,7 +52,8 @@ class Disk:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.fargo_ctx_destroy(self.h)
+            if self.owned:
+                self.lib.fargo_ctx_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -127,3 +132,74 @@ class Disk:
 
     def write_dims(self):
         self._check(self.lib.fargo_write_dims(self.h), "write_dims")
+
+
+class Batch:
+    """An ensemble of independent disks (fargo_batch_*): each disk keeps its own
+    fields, CFL step and DT graph; the batch runs the disks' graphs side by side.
+    disks: a list of (params, planets)."""
+
+    def __init__(self, disks, precision=FARGO_FP32_BULK):
+        self.lib = _capi.load()
+        n = len(disks)
+        params = (FargoParams * n)(*[p for p, _ in disks])
+        flat = [pl for _, pls in disks for pl in pls]
+        planets = (FargoPlanet * max(1, len(flat)))(*flat)
+        counts = (ctypes.c_int * n)(*[len(pls) for _, pls in disks])
+        h = ctypes.c_void_p()
+        rc = self.lib.fargo_batch_create(n, params, planets, counts, precision, ctypes.byref(h))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_create failed with status {rc}")
+        self.h = h
+        self.disks = [Disk(p, [], precision, _handle=ctypes.c_void_p(self.lib.fargo_batch_disk(h, k)))
+                      for k, (p, _) in enumerate(disks)]
+        self.cells = sum(p.nrad * p.nsec for p, _ in disks)
+
+    def __len__(self):
+        return len(self.disks)
+
+    def disk(self, k):
+        return self.disks[k]
+
+    def run_async(self, ndt):
+        rc = self.lib.fargo_batch_run_async(self.h, int(ndt))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_run_async: status {rc}")
+
+    def sync(self):
+        rc = self.lib.fargo_batch_sync(self.h)
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_sync: status {rc}")
+
+    def advance(self, t_end):
+        """Every disk to physical time t_end (whole DTs of its own); returns the
+        substeps of all disks."""
+        n = ctypes.c_longlong(0)
+        failed = ctypes.c_int(-1)
+        rc = self.lib.fargo_batch_advance(self.h, float(t_end), ctypes.byref(n), ctypes.byref(failed))
+        if rc != _capi.FARGO_OK:
+            msg = self.lib.fargo_last_error(self.disks[failed.value].h).decode() if failed.value >= 0 else ""
+            raise FargoError(f"fargo_batch_advance: status {rc} (disk {failed.value}): {msg}")
+        return n.value
+
+    def substeps(self):
+        return sum(d.scalars().substeps for d in self.disks)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for d in self.disks:
+                d.h = None
+            self.lib.fargo_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -108,6 +108,14 @@ SIGNATURES = [
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),
+    ("fargo_batch_create", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),
+                                _I, ctypes.POINTER(_P)]),
+    ("fargo_batch_destroy", None, [_P]),
+    ("fargo_batch_size", _I, [_P]),
+    ("fargo_batch_disk", _P, [_P, _I]),
+    ("fargo_batch_run_async", _I, [_P, _I]),
+    ("fargo_batch_sync", _I, [_P]),
+    ("fargo_batch_advance", _I, [_P, _D, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)]),
 ]
 
 _lib = None

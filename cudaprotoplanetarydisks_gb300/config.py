@@ -77,3 +77,31 @@ def load_config(name_or_path, **overrides):
             v = v.encode()
         setattr(params, k, v)
     return params, planets
+
+
+# the batched-ensemble workload: sizes and the seeded per-disk parameter draws
+C4_NRAD = (128, 192, 256, 384, 512)
+
+
+def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD):
+    """(params, planets) of n seeded disks: the isothermal c1 setup (log grid on
+    [0.4, 2.5], one planet on a fixed circular orbit at r = 1, FARGO transport)
+    with per-disk draws: Nrad uniform in nrad_choices, Nsec = 3 Nrad; planet mass
+    ratio q log-uniform in [1e-5, 3e-3]; alpha viscosity log-uniform in
+    [1e-4, 1e-2]; aspect ratio h uniform in [0.03, 0.08]; Sigma slope uniform in
+    [0, 1.5]; Sigma0 = 6.3662e-4; 1e-4 density noise seeded per disk."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n):
+        nrad = int(rng.choice(nrad_choices))
+        q = float(10 ** rng.uniform(np.log10(1e-5), np.log10(3e-3)))
+        alpha = float(10 ** rng.uniform(-4.0, -2.0))
+        h = float(rng.uniform(0.03, 0.08))
+        slope = float(rng.uniform(0.0, 1.5))
+        params, planets = load_config("c1", nrad=nrad, nsec=3 * nrad, viscosity=0.0, alphaviscosity=alpha,
+                                      aspectratio=h, sigmaslope=slope, sigma0=6.3662e-4,
+                                      noise_seed=seed * 1000 + k + 1)
+        planets[0].mass = q
+        out.append((params, planets))
+    return out

@@ -1,0 +1,129 @@
+// fargo_batch.cu -- an ensemble of independent disks advanced together.
+//
+// Every disk is a context of its own (fargo_ctx: fields, one DT graph with the
+// CFL loop on the device, its own streams), so every disk keeps its own CFL step
+// and substep count.  The batch enqueues the disks' DT graphs round-robin on their
+// streams and synchronises once: the GPU runs the graphs of many disks at the same
+// time, which fills the SMs that one small disk leaves idle (a 128x384 disk's
+// kernels are one partial wave each).  Nothing is shared between disks but the
+// device, so a disk's results are bitwise those of the same disk run alone.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fargo_gb300.h"
+
+struct fargo_batch {
+  std::vector<fargo_ctx *> disks;
+  std::vector<double> dt;  // DT of each disk (its parameter file's DT)
+};
+
+extern "C" {
+
+int fargo_batch_create(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
+                       int precision, fargo_batch **out) {
+  if (!out || n <= 0 || !params || !nplanets) return FARGO_ERR_INVALID;
+  *out = nullptr;
+  fargo_batch *b = new fargo_batch();
+  int off = 0;
+  for (int k = 0; k < n; k++) {
+    if (nplanets[k] < 0 || (nplanets[k] > 0 && !planets)) {
+      fargo_batch_destroy(b);
+      return FARGO_ERR_INVALID;
+    }
+    fargo_ctx *c = nullptr;
+    const int rc = fargo_ctx_create(&params[k], nplanets[k] ? planets + off : nullptr, nplanets[k], precision,
+                                    nullptr, &c);
+    if (rc != FARGO_OK) {
+      fargo_batch_destroy(b);
+      return rc;
+    }
+    b->disks.push_back(c);
+    b->dt.push_back(params[k].dt);
+    off += nplanets[k];
+  }
+  *out = b;
+  return FARGO_OK;
+}
+
+void fargo_batch_destroy(fargo_batch *b) {
+  if (!b) return;
+  for (fargo_ctx *c : b->disks) fargo_ctx_destroy(c);
+  delete b;
+}
+
+int fargo_batch_size(const fargo_batch *b) { return b ? (int)b->disks.size() : 0; }
+
+fargo_ctx *fargo_batch_disk(fargo_batch *b, int k) {
+  if (!b || k < 0 || k >= (int)b->disks.size()) return nullptr;
+  return b->disks[k];
+}
+
+// ndt[k] DTs on disk k (ndt == NULL: ndt_all on every disk), enqueued round-robin
+// (DT 1 of every disk, then DT 2, ...) so that every stream has work at once.
+static int enqueue(fargo_batch *b, const int *ndt, int ndt_all) {
+  int most = 0;
+  for (size_t k = 0; k < b->disks.size(); k++) most = std::max(most, ndt ? ndt[k] : ndt_all);
+  for (int d = 0; d < most; d++)
+    for (size_t k = 0; k < b->disks.size(); k++)
+      if (d < (ndt ? ndt[k] : ndt_all)) {
+        const int rc = fargo_run_async(b->disks[k], 1);
+        if (rc != FARGO_OK) return rc;
+      }
+  return FARGO_OK;
+}
+
+int fargo_batch_run_async(fargo_batch *b, int ndt) {
+  if (!b || ndt < 0) return FARGO_ERR_STATE;
+  return enqueue(b, nullptr, ndt);
+}
+
+int fargo_batch_sync(fargo_batch *b) {
+  if (!b) return FARGO_ERR_STATE;
+  for (fargo_ctx *c : b->disks) {
+    const int rc = fargo_sync(c);
+    if (rc != FARGO_OK) return rc;
+  }
+  return FARGO_OK;
+}
+
+// Every disk advances whole DTs (its own DT) until its physical time reaches t_end
+// (within 1e-9 of a DT); substeps of all disks are summed into *nsub.  A disk
+// whose device flags an error makes the call return that disk's status (its
+// message: fargo_last_error of fargo_batch_disk(b, k)); *failed = that k or -1.
+int fargo_batch_advance(fargo_batch *b, double t_end, long long *nsub, int *failed) {
+  if (failed) *failed = -1;
+  if (!b) return FARGO_ERR_STATE;
+  const size_t n = b->disks.size();
+  std::vector<int> ndt(n, 0);
+  std::vector<long long> s0(n, 0);
+  for (size_t k = 0; k < n; k++) {
+    fargo_scalars s;
+    int rc = fargo_get_scalars(b->disks[k], &s);
+    if (rc != FARGO_OK) return rc;
+    s0[k] = s.substeps;
+    const double left = (t_end - s.physical_time) / b->dt[k];
+    ndt[k] = left > 1e-9 ? (int)std::ceil(left - 1e-9) : 0;
+  }
+  int rc = enqueue(b, ndt.data(), 0);
+  if (rc != FARGO_OK) return rc;
+  long long tot = 0;
+  for (size_t k = 0; k < n; k++) {
+    // fargo_run with no DT reads the control block and reports a device error
+    long long sub = 0;
+    rc = fargo_run(b->disks[k], 0, &sub);
+    if (rc != FARGO_OK) {
+      if (failed) *failed = (int)k;
+      return rc;
+    }
+    fargo_scalars s;
+    if ((rc = fargo_get_scalars(b->disks[k], &s)) != FARGO_OK) return rc;
+    tot += s.substeps - s0[k];
+  }
+  if (nsub) *nsub = tot;
+  return FARGO_OK;
+}
+
+}  // extern "C"

@@ -238,6 +238,27 @@ int  fargo_condition_cfl_noalloc(const double *vrad, const double *vtheta, const
                                  int nrad, int nsec, int fast_transport, double deltaT,
                                  void *stream, int *cfl_out);
 
+/* ---- ensembles (no counterpart in the reference) -------------------------- */
+/* n independent disks (the batched-ensemble workload): disk k has params[k] and
+   the nplanets[k] bodies that follow those of disks 0..k-1 in planets.  Each disk
+   is a context of its own (own fields, DT graph, CFL step and streams); the batch
+   enqueues the disks' DT graphs round-robin so that the GPU runs many disks at
+   once.  A disk's results are bitwise those of the same disk run alone. */
+typedef struct fargo_batch fargo_batch;
+int  fargo_batch_create(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
+                        int precision, fargo_batch **out);
+void fargo_batch_destroy(fargo_batch *b);
+int  fargo_batch_size(const fargo_batch *b);
+/* Context of disk k (owned by the batch), for fields, planets and scalars. */
+fargo_ctx *fargo_batch_disk(fargo_batch *b, int k);
+/* ndt DTs on every disk, enqueued without a host synchronisation. */
+int  fargo_batch_run_async(fargo_batch *b, int ndt);
+int  fargo_batch_sync(fargo_batch *b);
+/* Every disk advances whole DTs of its own until its physical time reaches t_end;
+   *nsub (may be NULL) = substeps of all disks.  On a device error the status is
+   that disk's and *failed (may be NULL) = its index, else -1. */
+int  fargo_batch_advance(fargo_batch *b, double t_end, long long *nsub, int *failed);
+
 #ifdef __cplusplus
 }
 #endif
