@@ -68,6 +68,8 @@ struct fargo_ctx {
 };
 
 namespace {
+// ring buffers of the barrier-per-phase azimuthal kernel (AZ_NARR in fargo_kernels.cu)
+constexpr int AZ_NARR_HOST = 12;
 
 int set_err(fargo_ctx *c, int code, const std::string &msg) {
   if (c) c->err = msg;
@@ -361,14 +363,14 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     int dev = 0, maxsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    size_t need = (size_t)11 * p.nsec * E, need4 = (size_t)13 * p.nsec * E;
+    size_t need = (size_t)AZ_NARR_HOST * p.nsec * E, need4 = (size_t)13 * p.nsec * E;
     const char *fg = std::getenv("FARGO_AZ_GLOBAL");  // force the global-memory ring buffers
     const bool force_global = fg && fg[0] == '1';
     const char *fs = std::getenv("FARGO_AZ_GENERIC");  // force the barrier-per-phase kernel
     const bool force_generic = force_global || (fs && fs[0] == '1');
-    // FP32 fields only: in FP64 the halo recomputation doubles the divisions on
-    // the (narrow) FP64 pipe, and the barrier-per-phase kernel is faster
-    if (!force_generic && E == 4 && p.nsec % 4 == 0 && p.nsec / 4 <= 768 && need4 + 1024 <= (size_t)maxsm) {
+    // register-blocked kernel when its ring fits in shared memory (threads: nsec / 4,
+    // at most 768 for FP32 and 512 for FP64 fields)
+    if (!force_generic && p.nsec % 4 == 0 && p.nsec / 4 <= (E == 4 ? 768 : 512) && need4 + 1024 <= (size_t)maxsm) {
       c->az_smem = need4;
       c->az_regs = 1;
       CK(prepare_kernels<T>(need4, 1));
@@ -378,7 +380,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     } else {
       c->az_smem = 0;
       CK(prepare_kernels<T>(0, 0));
-      if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * 11 * p.nsec * E))) return rc;
+      if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * AZ_NARR_HOST * p.nsec * E))) return rc;
     }
   }
   CK(cudaStreamSynchronize(c->stream));

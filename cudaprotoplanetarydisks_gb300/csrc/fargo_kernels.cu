@@ -1114,7 +1114,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
 // and AdvectSHIFT (src/Kernels.cu:1049-1190).  The ring lives in shared memory
 // (or in global scratch when it does not fit); the FARGO shift is applied as an
 // index rotation when the ring is stored.
-#define AZ_NARR 11
+#define AZ_NARR 12
 template <class T>
 __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   pdl_enter();
@@ -1127,7 +1127,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   T *base = a.az_smem ? (T *)az_smem : a.d.az_scratch + (size_t)i * AZ_NARR * nsec;
   T *V = base, *Dn = base + nsec, *En = base + 2 * nsec, *M0 = base + 3 * nsec, *M1 = base + 4 * nsec,
     *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *S = base + 9 * nsec,
-    *DS = base + 10 * nsec;
+    *DS = base + 10 * nsec, *ID = base + 11 * nsec;
   const Ctl *c = a.d.ctl;
   const double dt = c->dt;
   const size_t row = (size_t)i * nsec;
@@ -1181,6 +1181,9 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   // QuantitiesAdvection with velocity vel[] (or the constant vconst)
   auto advect = [&](const T *vel, T vconst) {
     slope(Dn, B);
+    // DivisePolarGrid with the density's reciprocal, formed once per cell for every
+    // quantity (one divide per cell instead of one per quantity, within an ulp)
+    for (int j = tid; j < nsec; j += nt) ID[j] = (T)1.0 / (Dn[j] + (T)1e-20);
     __syncthreads();
     star(Dn, B, DS, vel, vconst);
     __syncthreads();
@@ -1188,7 +1191,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
       T *Q = qs[f];
-      for (int j = tid; j < nsec; j += nt) W[j] = Q[j] / (Dn[j] + (T)1e-20);
+      for (int j = tid; j < nsec; j += nt) W[j] = Q[j] * ID[j];
       __syncthreads();
       slope(W, B);
       __syncthreads();
@@ -1327,7 +1330,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
     for (int c = 0; c < 8; c++) {
       d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
-      id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell (FP32)
+      id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) {
@@ -1356,8 +1359,10 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
       T wv[8], dw[6], sw[5];
 #pragma unroll
       for (int c = 0; c < 8; c++) {
-        const T qc = q[az_wrap(j0 - 2 + c, nsec)];
-        wv[c] = sizeof(T) == 4 ? qc * id[c] : qc / (d[c] + (T)1e-20);
+        // DivisePolarGrid with the density's reciprocal, formed once per cell for
+        // every quantity (FP64: one divide per cell instead of one per quantity,
+        // within an ulp of q / rho)
+        wv[c] = q[az_wrap(j0 - 2 + c, nsec)] * id[c];
       }
 #pragma unroll
       for (int k = 0; k < 6; k++) {
