@@ -116,6 +116,14 @@ SIGNATURES = [
     ("fargo_batch_run_async", _I, [_P, _I]),
     ("fargo_batch_sync", _I, [_P]),
     ("fargo_batch_advance", _I, [_P, _D, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)]),
+    ("fargo_mlp_create", _I, [_I, ctypes.POINTER(_P)]),
+    ("fargo_mlp_destroy", None, [_P]),
+    ("fargo_mlp_set_params", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    ("fargo_mlp_get_params", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    ("fargo_mlp_get_grad", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
+    ("fargo_mlp_forward", _I, [_P, _P, _I, _P, _I, _P]),
+    ("fargo_mlp_backward", _I, [_P, _P, _I, _P, _P]),
+    ("fargo_mlp_adam", _I, [_P, ctypes.c_float, _P]),
 ]
 
 _lib = None

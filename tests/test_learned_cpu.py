@@ -1,0 +1,41 @@
+"""The MLP oracle (oracle/mlp_ref.py) pinned on the CPU: its backward pass against
+central finite differences of the exact FP64 network, and its BF16 rounding
+against torch's."""
+import numpy as np
+import torch
+
+from cudaprotoplanetarydisks_gb300.learned import NPARAM, init_params
+from oracle import mlp_ref
+
+
+def test_bf16_rounding_matches_torch():
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.normal(0, 1, 4000), rng.normal(0, 1e-3, 1000), [0.0, 1.0, -2.5, 65504.0, 1e-30]])
+    ours = mlp_ref.bf16(x)
+    ref = torch.tensor(x, dtype=torch.float32).to(torch.bfloat16).to(torch.float64).numpy()
+    assert np.array_equal(ours, ref)
+
+
+def test_oracle_gradient_matches_finite_differences():
+    assert mlp_ref.NPARAM == NPARAM
+    rng = np.random.default_rng(5)
+    P = init_params(1).astype(np.float64)
+    P[mlp_ref.OFF_B1:mlp_ref.OFF_W2] = rng.normal(0, 0.1, mlp_ref.NH)
+    X = rng.normal(0, 1, (24, mlp_ref.NIN))
+    dy = rng.normal(0, 1, (24, mlp_ref.NOUT))
+    y, cache = mlp_ref.forward(P, X, exact=True)
+    g = mlp_ref.backward(P, cache, dy, exact=True)
+
+    def f(Q):
+        return float((mlp_ref.forward(Q, X, exact=True)[0] * dy).sum())
+
+    idx = list(rng.choice(np.arange(mlp_ref.OFF_W1, mlp_ref.OFF_B1), 12, replace=False)) + \
+        list(rng.choice(np.arange(mlp_ref.OFF_W2, mlp_ref.OFF_B2), 8, replace=False)) + \
+        [mlp_ref.OFF_B1 + 3, mlp_ref.OFF_B2 + 7, mlp_ref.OFF_W3 + 5 * mlp_ref.NOUTP + 1, mlp_ref.OFF_B3]
+    h = 1e-6
+    for p in idx:
+        Qp, Qm = P.copy(), P.copy()
+        Qp[p] += h
+        Qm[p] -= h
+        fd = (f(Qp) - f(Qm)) / (2 * h)
+        assert abs(fd - g[p]) <= 1e-6 * max(1.0, abs(fd)), (p, fd, g[p])
