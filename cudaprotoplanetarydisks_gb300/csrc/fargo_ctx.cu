@@ -829,6 +829,23 @@ int fargo_step_DT(fargo_ctx *c, int *nsub) {
   return device_error(c);
 }
 
+int fargo_learned_view(fargo_ctx *c, LearnedView *v) {
+  if (!c || !v) return FARGO_ERR_STATE;
+  int rc = read_ctl(c);
+  if (rc) return rc;
+  v->dens = c->dens;
+  v->vrad = c->vrad;
+  v->vtheta = c->vtheta;
+  v->esize = (int)c->esize;
+  v->nrad = c->P.nrad;
+  v->nsec = c->P.nsec;
+  v->stream = (void *)c->stream;
+  v->rmed = c->h.Rmed.data();
+  v->surf = c->h.Surf.data();
+  v->planet_phi = c->nb > 0 ? std::atan2(c->pin_ctl->y[0], c->pin_ctl->x[0]) : 0.0;
+  return FARGO_OK;
+}
+
 int fargo_run_async(fargo_ctx *c, int ndt) {
   if (!c || ndt < 0) return FARGO_ERR_STATE;
   for (int k = 0; k < ndt; k++) {

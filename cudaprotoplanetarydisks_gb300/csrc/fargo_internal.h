@@ -58,6 +58,17 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
 DevParams host_dev_params(const fargo_params &p, int nb);
 long fargo_nearest_pow2(long n);
 
+// Device view of a context for the learned correction (fargo_learned.cu); the
+// call reads the control block (synchronises the context's stream)
+struct LearnedView {
+  void *dens, *vrad, *vtheta;   // fields, (nrad + 1) * nsec elements of esize bytes
+  int esize, nrad, nsec;
+  void *stream;                 // the context's cudaStream_t
+  const double *rmed, *surf;    // host mesh, nrad + 1 each
+  double planet_phi;            // azimuth of the first planet (0 without one)
+};
+extern "C" int fargo_learned_view(fargo_ctx *c, LearnedView *v);
+
 // output.cpp
 int host_write_field(const std::string &outdir, const char *name, int index, const double *data, size_t n);
 int host_write_planet_row(const std::string &outdir, int k, int index, const fargo_planet &b, double lost_mass,

@@ -283,6 +283,34 @@ int  fargo_mlp_backward(fargo_mlp *m, const void *x_bf16, int n, const float *dy
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr. */
 int  fargo_mlp_adam(fargo_mlp *m, float lr, void *stream);
 
+/* Coupling of the MLP to a coarse disk (device buffers; fields of esize bytes,
+   (nrad+1)*nsec elements; rmed and surf: FP64 device arrays of nrad+1).
+   features: x (BF16 [nrad*nsec][128]) from density and velocities; norm: 5 means
+   then 5 deviations of the input channels.  divergence: the density correction
+   ds (FP32 [nrad*nsec]) of the network outputs y (FP32 [nrad*nsec][2]) scaled by
+   scale (mass conserved by construction).  loss: ds, e = dL/dds, dy = dL/dy and
+   *loss (device double) = sum (ds - target)^2, for L = that sum * inv_var / n
+   (part: (n + 255) / 256 doubles of scratch). */
+int  fargo_learned_features(int esize, const void *dens, const void *vrad, const void *vtheta, const double *rmed,
+                            int nrad, int nsec, double phi_planet, const float *norm, void *x_bf16, void *stream);
+int  fargo_learned_divergence(const float *y, const double *surf, int nrad, int nsec, float scale, float *ds,
+                              void *stream);
+int  fargo_learned_loss(const float *y, const float *target, const double *surf, int nrad, int nsec, float scale,
+                        float inv_var, float *ds, float *e, float *dy, double *part, double *loss, void *stream);
+/* The coarse disk's density and velocities := the restriction of the fine disk's
+   (fine grid = factor x coarse in both directions; area-weighted density,
+   interface velocities averaged).  Synchronous. */
+int  fargo_learned_restrict(fargo_ctx *fine, fargo_ctx *coarse, int factor);
+/* Adds ds (device FP32 [nrad*nsec]) to the disk's density when every cell stays
+   positive and finite and |sum ds Surf| <= 1e-5 sum |ds Surf| (the plain step
+   judges the correction); *accepted = 1 then, else 0 and nothing changes.
+   *dmass (may be NULL) = sum ds Surf.  Synchronous. */
+int  fargo_learned_apply(fargo_ctx *ctx, const float *ds, int *accepted, double *dmass);
+/* fargo_learned_features on the disk's own state (the first planet's azimuth);
+   and the disk's density (rings 0..nrad-1) as FP32 into a device buffer.  Synchronous. */
+int  fargo_learned_features_ctx(fargo_ctx *ctx, const float *norm, void *x_bf16);
+int  fargo_learned_density(fargo_ctx *ctx, float *out);
+
 #ifdef __cplusplus
 }
 #endif

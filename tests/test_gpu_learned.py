@@ -57,3 +57,46 @@ def test_training_lowers_the_loss():
     torch.cuda.synchronize()
     assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
     m.close()
+
+
+# ---------------------------------------------------------------------------
+# the correction on coarse disks
+import cudaprotoplanetarydisks_gb300 as fg  # noqa: E402
+from cudaprotoplanetarydisks_gb300 import learned as L  # noqa: E402
+
+
+def small_disks(n, seed):
+    return fg.c4_disks(n, seed=seed, nrad_choices=(24,))
+
+
+def test_correction_conserves_mass_and_keeps_density_positive():
+    (params, planets), = small_disks(1, 3)
+    disk = fg.Disk(params, planets, fg.FARGO_FP32_BULK)
+    surf = disk.mesh()[3][:-1]
+    m0 = float((disk.field("dens")[:-1] * surf[:, None]).sum())
+    corr = L.Correction(L.MLP(params.nrad * params.nsec, seed=9), L.IDENTITY_NORM, 1e-7)
+    work = L.workspace(disk)
+    for _ in range(2):
+        _, accepted = corr.step_DT(disk, work)
+        assert accepted
+    d = disk.field("dens")[:-1]
+    m1 = float((d * surf[:, None]).sum())
+    assert d.min() > 0
+    # the plain step conserves mass to FP32 roundoff (walls), the correction exactly
+    assert abs(m1 - m0) <= 1e-5 * m0
+    disk.close()
+
+
+def test_learned_correction_gains_on_held_out_disks():
+    train_disks, held_out = small_disks(4, 11), small_disks(2, 12)
+    norm = L.feature_norm(L.generate(train_disks[:1], factor=4, spinup=2, ndt=2))
+    tr = L.generate(train_disks, factor=4, spinup=2, ndt=6, norm=norm)
+    ho = L.generate(held_out, factor=4, spinup=2, ndt=4, norm=norm)
+    scale, var = L.target_stats(tr)
+    mlp = L.MLP(24 * 72, seed=1)
+    losses = L.train(mlp, tr, scale, var, epochs=40, lr=3e-3)
+    assert losses[-1] < losses[0]
+    with_net, without = L.evaluate_loss(mlp, ho, scale, var)
+    print(f"held-out loss with the network {with_net:.3f}, without {without:.3f}")
+    assert with_net < without
+    mlp.close()
