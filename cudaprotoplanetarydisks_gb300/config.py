@@ -83,13 +83,14 @@ def load_config(name_or_path, **overrides):
 C4_NRAD = (128, 192, 256, 384, 512)
 
 
-def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD):
+def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD, sigma_noise=1e-4):
     """(params, planets) of n seeded disks: the isothermal c1 setup (log grid on
     [0.4, 2.5], one planet on a fixed circular orbit at r = 1, FARGO transport)
     with per-disk draws: Nrad uniform in nrad_choices, Nsec = 3 Nrad; planet mass
     ratio q log-uniform in [1e-5, 3e-3]; alpha viscosity log-uniform in
     [1e-4, 1e-2]; aspect ratio h uniform in [0.03, 0.08]; Sigma slope uniform in
-    [0, 1.5]; Sigma0 = 6.3662e-4; 1e-4 density noise seeded per disk."""
+    [0, 1.5]; Sigma0 = 6.3662e-4; density noise of relative amplitude sigma_noise
+    seeded per disk."""
     import numpy as np
     rng = np.random.Generator(np.random.PCG64(seed))
     out = []
@@ -101,7 +102,7 @@ def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD):
         slope = float(rng.uniform(0.0, 1.5))
         params, planets = load_config("c1", nrad=nrad, nsec=3 * nrad, viscosity=0.0, alphaviscosity=alpha,
                                       aspectratio=h, sigmaslope=slope, sigma0=6.3662e-4,
-                                      noise_seed=seed * 1000 + k + 1)
+                                      noise_seed=seed * 1000 + k + 1, sigma_noise=sigma_noise)
         planets[0].mass = q
         out.append((params, planets))
     return out

@@ -53,6 +53,8 @@ struct fargo_ctx {
   size_t az_smem = 0;
   int az_regs = 0;
   double *staging = nullptr;   // FP64 staging buffer of host <-> device transfers
+  double *lx_rmed = nullptr, *lx_surf = nullptr, *lx_ring = nullptr;  // learned correction (first use)
+  void *lx_cand = nullptr;
   int launches_per_substep = 0, launches_per_dt = 0;
   std::vector<std::string> kernel_names;
   // graph of one DT
@@ -843,6 +845,19 @@ int fargo_learned_view(fargo_ctx *c, LearnedView *v) {
   v->rmed = c->h.Rmed.data();
   v->surf = c->h.Surf.data();
   v->planet_phi = c->nb > 0 ? std::atan2(c->pin_ctl->y[0], c->pin_ctl->x[0]) : 0.0;
+  if (!c->lx_rmed) {
+    const size_t n1 = (size_t)c->P.nrad + 1;
+    if ((rc = dev_alloc(c, (void **)&c->lx_rmed, n1 * 8))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->lx_surf, n1 * 8))) return rc;
+    if ((rc = dev_alloc(c, (void **)&c->lx_ring, 3 * n1 * 8))) return rc;
+    if ((rc = dev_alloc(c, &c->lx_cand, (size_t)c->P.nrad * c->P.nsec * c->esize))) return rc;
+    CK(cudaMemcpy(c->lx_rmed, c->h.Rmed.data(), n1 * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->lx_surf, c->h.Surf.data(), n1 * 8, cudaMemcpyHostToDevice));
+  }
+  v->rmed_dev = c->lx_rmed;
+  v->surf_dev = c->lx_surf;
+  v->ring = c->lx_ring;
+  v->cand = c->lx_cand;
   return FARGO_OK;
 }
 

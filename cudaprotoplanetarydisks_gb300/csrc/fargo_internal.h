@@ -66,6 +66,11 @@ struct LearnedView {
   void *stream;                 // the context's cudaStream_t
   const double *rmed, *surf;    // host mesh, nrad + 1 each
   double planet_phi;            // azimuth of the first planet (0 without one)
+  // device copies of rmed and surf, and scratch (a candidate density, 3 doubles
+  // per ring), allocated with the context on first use
+  const double *rmed_dev, *surf_dev;
+  double *ring;
+  void *cand;
 };
 extern "C" int fargo_learned_view(fargo_ctx *c, LearnedView *v);
 

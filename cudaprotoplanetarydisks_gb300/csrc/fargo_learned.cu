@@ -1,10 +1,13 @@
 // fargo_learned.cu -- the learned coarse-grid correction around the stencil MLP.
 //
 // Inputs of the network, per coarse cell (i, j): the 5x5 neighbourhood (rings
-// clamped at the edges, sectors periodic) of 5 channels -- log Sigma, the
-// cell-centred v_r, the cell-centred v_theta minus the Keplerian speed r^-1/2,
-// log r, and the azimuth from the planet over pi -- normalised by per-channel
-// means and deviations of the training data, 125 values padded to 128 (BF16).
+// clamped at the edges, sectors periodic) of 5 channels, relative to the centre
+// cell so that small perturbations survive BF16: Sigma / Sigma(i, j) - 1 (the
+// centre slot: log Sigma(i, j)), the cell-centred v_r, the cell-centred v_theta
+// minus the centre's (the centre slot: v_theta minus the Keplerian speed
+// r^-1/2), log r minus the centre's (the centre slot: log r), and the azimuth
+// from the planet over pi; each of the 125 values normalised by its mean and
+// deviation over the training data, padded to 128 (BF16).
 //
 // Outputs: y_r(i, j), y_phi(i, j), mass-flux corrections through the cell's inner
 // radial and left azimuthal interfaces, in units of s * Surf_i (s: the target
@@ -31,7 +34,7 @@ typedef __nv_bfloat16 bf16;
 __device__ __forceinline__ int wrapj(int j, int n) { return j < 0 ? j + n : (j >= n ? j - n : j); }
 
 struct FeatNorm {
-  float mean[5], inv_std[5];
+  float mean[125], inv_std[125];
 };
 
 template <class T>
@@ -43,21 +46,28 @@ __global__ void k_features(const T *__restrict__ dens, const T *__restrict__ vra
   const int i = q / nsec, j = q % nsec;
   bf16 *row = x + (size_t)q * 128;
   const float dphi = 6.28318530717958648f / (float)nsec;
+  const size_t c0 = (size_t)i * nsec + j;
+  const double d0 = (double)dens[c0];
+  const float vt0 = 0.5f * ((float)vtheta[c0] + (float)vtheta[(size_t)i * nsec + wrapj(j + 1, nsec)]);
+  const float lr0 = logf((float)rmed[i]);
   for (int di = -2; di <= 2; di++) {
     const int ii = min(max(i + di, 0), nrad - 1);
     const float r = (float)rmed[ii];
-    const float vk = rsqrtf(r), lr = logf(r);
     for (int dj = -2; dj <= 2; dj++) {
       const int jj = wrapj(j + dj, nsec), jp = wrapj(jj + 1, nsec);
       const size_t c = (size_t)ii * nsec + jj;
+      const bool centre = di == 0 && dj == 0;
       float ang = (jj + 0.5f) * dphi - phi_planet;  // cell centre azimuth relative to the planet
       ang -= 6.28318530717958648f * floorf(ang * 0.15915494309189535f + 0.5f);
-      const float v[5] = {logf((float)dens[c]), 0.5f * ((float)vrad[c] + (float)vrad[c + nsec]),
-                          0.5f * ((float)vtheta[c] + (float)vtheta[(size_t)ii * nsec + jp]) - vk, lr,
+      const float vt = 0.5f * ((float)vtheta[c] + (float)vtheta[(size_t)ii * nsec + jp]);
+      const float v[5] = {centre ? logf((float)d0) : (float)((double)dens[c] / d0 - 1.0),
+                          0.5f * ((float)vrad[c] + (float)vrad[c + nsec]),
+                          centre ? vt0 - rsqrtf(r) : vt - vt0, centre ? lr0 : logf(r) - lr0,
                           ang * 0.31830988618379067f};
       const int base = ((di + 2) * 5 + (dj + 2)) * 5;
 #pragma unroll
-      for (int ch = 0; ch < 5; ch++) row[base + ch] = __float2bfloat16_rn((v[ch] - nm.mean[ch]) * nm.inv_std[ch]);
+      for (int ch = 0; ch < 5; ch++)
+        row[base + ch] = __float2bfloat16_rn((v[ch] - nm.mean[base + ch]) * nm.inv_std[base + ch]);
     }
   }
   row[125] = row[126] = row[127] = __float2bfloat16_rn(0.0f);
@@ -194,13 +204,6 @@ __global__ void k_density_out(const T *__restrict__ d, int n, float *__restrict_
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) out[q] = (float)d[q];
 }
-
-int upload(const double *host, size_t n, double **dev) {
-  if (cudaMalloc(dev, n * 8) != cudaSuccess) return FARGO_ERR_CUDA;
-  if (cudaMemcpy(*dev, host, n * 8, cudaMemcpyHostToDevice) != cudaSuccess) return FARGO_ERR_CUDA;
-  return FARGO_OK;
-}
-
 }  // namespace
 
 extern "C" {
@@ -210,9 +213,9 @@ int fargo_learned_features(int esize, const void *dens, const void *vrad, const 
   if ((esize != 4 && esize != 8) || !dens || !vrad || !vtheta || !rmed || !norm || !x || nrad < 1 || nsec < 1)
     return FARGO_ERR_INVALID;
   FeatNorm nm;
-  for (int c = 0; c < 5; c++) {
+  for (int c = 0; c < 125; c++) {
     nm.mean[c] = norm[c];
-    nm.inv_std[c] = norm[5 + c] > 0.0f ? 1.0f / norm[5 + c] : 1.0f;
+    nm.inv_std[c] = norm[125 + c] > 0.0f ? 1.0f / norm[125 + c] : 1.0f;
   }
   const int n = nrad * nsec;
   const cudaStream_t s = (cudaStream_t)stream;
@@ -256,12 +259,9 @@ int fargo_learned_restrict(fargo_ctx *fine, fargo_ctx *coarse, int factor) {
   if (factor < 1 || f.nrad != factor * c.nrad || f.nsec != factor * c.nsec || f.esize != c.esize)
     return FARGO_ERR_INVALID;
   const size_t nc = (size_t)(c.nrad + 1) * c.nsec;
-  double *fsurf = nullptr, *buf = nullptr;
-  if ((rc = upload(f.surf, f.nrad + 1, &fsurf))) return rc;
-  if (cudaMalloc(&buf, 3 * nc * 8) != cudaSuccess) {
-    cudaFree(fsurf);
-    return FARGO_ERR_CUDA;
-  }
+  const double *fsurf = f.surf_dev;
+  double *buf = nullptr;
+  if (cudaMalloc(&buf, 3 * nc * 8) != cudaSuccess) return FARGO_ERR_CUDA;
   const int nb = (int)((nc + 255) / 256);
   const cudaStream_t s = (cudaStream_t)f.stream;
   if (f.esize == 4)
@@ -274,7 +274,6 @@ int fargo_learned_restrict(fargo_ctx *fine, fargo_ctx *coarse, int factor) {
   cudaError_t e = cudaMemcpyAsync(h.data(), buf, 3 * nc * 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFree(buf);
-  cudaFree(fsurf);
   if (e != cudaSuccess) return FARGO_ERR_CUDA;
   return fargo_set_fields(coarse, h.data(), h.data() + nc, h.data() + 2 * nc, nullptr);
 }
@@ -284,11 +283,9 @@ int fargo_learned_features_ctx(fargo_ctx *ctx, const float *norm, void *x) {
   int rc;
   if (!norm || !x) return FARGO_ERR_INVALID;
   if ((rc = fargo_learned_view(ctx, &v))) return rc;
-  double *rmed = nullptr;
-  if ((rc = upload(v.rmed, v.nrad + 1, &rmed))) return rc;
-  rc = fargo_learned_features(v.esize, v.dens, v.vrad, v.vtheta, rmed, v.nrad, v.nsec, v.planet_phi, norm, x, v.stream);
+  rc = fargo_learned_features(v.esize, v.dens, v.vrad, v.vtheta, v.rmed_dev, v.nrad, v.nsec, v.planet_phi, norm, x,
+                              v.stream);
   const cudaError_t e = cudaStreamSynchronize((cudaStream_t)v.stream);
-  cudaFree(rmed);
   return rc ? rc : (e == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA);
 }
 
@@ -314,11 +311,10 @@ int fargo_learned_apply(fargo_ctx *ctx, const float *ds, int *accepted, double *
   *accepted = 0;
   if ((rc = fargo_learned_view(ctx, &v))) return rc;
   const size_t n = (size_t)v.nrad * v.nsec;
-  double *surf = nullptr, *ring = nullptr;
-  void *cand = nullptr;
-  if ((rc = upload(v.surf, v.nrad + 1, &surf))) return rc;
-  cudaError_t e = cudaMalloc(&ring, (size_t)3 * v.nrad * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&cand, n * v.esize);
+  const double *surf = v.surf_dev;
+  double *ring = v.ring;
+  void *cand = v.cand;
+  cudaError_t e = cudaSuccess;
   const cudaStream_t s = (cudaStream_t)v.stream;
   std::vector<double> h(3 * (size_t)v.nrad);
   if (e == cudaSuccess) {
@@ -344,9 +340,6 @@ int fargo_learned_apply(fargo_ctx *ctx, const float *ds, int *accepted, double *
       if (e == cudaSuccess) *accepted = 1;
     }
   }
-  if (cand) cudaFree(cand);
-  if (ring) cudaFree(ring);
-  cudaFree(surf);
   return e == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
 }
 

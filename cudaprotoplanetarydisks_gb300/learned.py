@@ -108,7 +108,7 @@ def _fp(arr):
 
 
 class Correction:
-    """One trained network with its input normalisation (5 channel means, then 5
+    """One trained network with its input normalisation (125 means, then 125
     deviations) and output scale.  step_DT advances a coarse disk one DT: the
     plain step, then the network's conservative density correction, applied only
     when the density stays positive and the mass change at roundoff."""
@@ -137,10 +137,13 @@ class Correction:
         torch.cuda.synchronize()
 
     def step_DT(self, disk, work):
-        """work: buffers from workspace(disk).  Returns (substeps, accepted)."""
+        """work: buffers from workspace(disk).  Returns (substeps, accepted).  The
+        network reads the plain step's result: over one DT the orbital advection
+        carries the gas tens of cells in azimuth, so the correction is a function
+        of the state it corrects, not of the state a DT earlier."""
         x, y, ds, surf = work
-        self.features(disk, x)
         n = disk.step_DT()
+        self.features(disk, x)
         self.correction(x, y, ds, surf, disk.nrad, disk.nsec)
         acc = ctypes.c_int(0)
         dm = ctypes.c_double(0.0)
@@ -185,15 +188,19 @@ def restrict(fine, coarse, factor):
         raise RuntimeError(f"fargo_learned_restrict: status {rc}")
 
 
-IDENTITY_NORM = np.array([0, 0, 0, 0, 0, 1, 1, 1, 1, 1], dtype=np.float32)
+IDENTITY_NORM = np.concatenate([np.zeros(125), np.ones(125)]).astype(np.float32)
 
 
-def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None):
+def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None, reset_every=1):
     """Training pairs from the plain solver: for every (params, planets) of a
-    coarse disk, its fine teacher runs `spinup` DTs, then for `ndt` DTs the
-    coarse disk starts from the restricted fine state, takes one plain DT, and the
-    target is the restricted fine density after the same DT minus the coarse one.
-    Returns samples [(x, target, surf, nrad, nsec)] on the GPU."""
+    coarse disk, its fine teacher runs `spinup` DTs, then the coarse disk starts
+    from the restricted fine state and both take `ndt` DTs; after each, the inputs
+    are the coarse result and the target is the restricted fine density minus the
+    coarse one.  The coarse disk restarts from the restricted fine state every
+    `reset_every` DTs: with 1 every pair starts on the teacher's trajectory, with
+    more the later pairs start from states the coarse solver drifted to, and their
+    targets pull back to the teacher.  Returns samples
+    [(x, target, surf, nrad, nsec)] on the GPU."""
     import torch
     from . import Disk, FARGO_FP32_BULK
     prec = FARGO_FP32_BULK if precision is None else precision
@@ -201,7 +208,7 @@ def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None):
     samples = []
     for params, planets in disks:
         fine = Disk(fine_params(params, factor), planets, prec)
-        coarse = Disk(params, planets, prec)
+        coarse, ref = Disk(params, planets, prec), Disk(params, planets, prec)
         fine.run(spinup)
         n = params.nrad * params.nsec
         surf = torch.tensor(coarse.mesh()[3], dtype=torch.float64, device="cuda")
@@ -209,26 +216,28 @@ def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None):
         target_state = torch.empty(n, dtype=torch.float32, device="cuda")
         restrict(fine, coarse, factor)
         corr = Correction(None, norm, 1.0)
-        for _ in range(ndt):
+        for k in range(ndt):
             x = torch.empty((n, NIN), dtype=torch.bfloat16, device="cuda")
-            corr.features(coarse, x)
             coarse.step_DT()
             fine.step_DT()
+            corr.features(coarse, x)
             density(coarse, after)
-            restrict(fine, coarse, factor)
-            density(coarse, target_state)
+            restrict(fine, ref, factor)
+            density(ref, target_state)
             samples.append((x, (target_state - after).contiguous(), surf, params.nrad, params.nsec))
-        fine.close()
-        coarse.close()
+            if (k + 1) % reset_every == 0:
+                restrict(fine, coarse, factor)
+        for d in (fine, coarse, ref):
+            d.close()
     return samples
 
 
-def feature_norm(samples, nsample=4):
-    """Channel means and deviations of identity-normalised features."""
+def feature_norm(samples, nsample=8):
+    """Means and deviations of each of the 125 identity-normalised inputs."""
     import torch
-    xs = torch.cat([s[0][:, :125].float().reshape(-1, 25, 5) for s in samples[:nsample]], dim=0)
-    mean = xs.mean(dim=(0, 1))
-    std = xs.std(dim=(0, 1)).clamp_min(1e-12)
+    xs = torch.cat([s[0][:, :125].float() for s in samples[:nsample]], dim=0)
+    mean = xs.mean(dim=0)
+    std = xs.std(dim=0).clamp_min(1e-12)
     return np.concatenate([mean.cpu().numpy(), std.cpu().numpy()]).astype(np.float32)
 
 
@@ -257,45 +266,133 @@ def _buffers(n):
             torch.empty(1, dtype=torch.float64, device="cuda"))
 
 
-def train(mlp, samples, scale, var, epochs=10, lr=2e-3, seed=0):
-    """Adam on the normalised loss mean((ds - target)^2) / var over the samples,
-    one sample (every cell of one coarse disk at one DT) per step.  Returns the
-    loss of every step."""
+def _sample_var(target):
+    return max(float((target.double() ** 2).mean().item()), 1e-300)
+
+
+def train(mlp, samples, scale, var=None, epochs=10, lr=2e-3, seed=0):
+    """Adam on the loss mean((ds - target)^2) / mean(target^2) of one sample (every
+    cell of one coarse disk at one DT) per step: each sample weighs the same
+    whatever the size of its disk's correction (var: unused, kept for the
+    signature).  Returns the mean loss of every epoch."""
     import torch
     lib = _capi.load()
     rng = np.random.default_rng(seed)
     n_max = max(s[3] * s[4] for s in samples)
     y = torch.empty((n_max, NOUT), dtype=torch.float32, device="cuda")
     buf = _buffers(n_max)
-    losses = []
+    norms = [_sample_var(s[1]) for s in samples]
+    epoch_losses = []
     for ep in range(epochs):
         lr_ep = lr * 0.5 * (1.0 + math.cos(math.pi * ep / max(1, epochs)))
+        acc = []
         for k in rng.permutation(len(samples)):
             x, target, surf, nrad, nsec = samples[k]
             n = nrad * nsec
             mlp.forward(x, y[:n], train=True)
-            _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / var, [b[:n] if b.dim() and b.shape[0] >= n
-                                                                                   else b for b in buf])
+            _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / norms[k],
+                       [b[:n] if b.dim() and b.shape[0] >= n else b for b in buf])
             mlp.backward(x, buf[2][:n])
             mlp.adam(lr_ep)
-            losses.append(float(buf[4].item()) / (n * var))
+            acc.append(float(buf[4].item()) / (n * norms[k]))
+        epoch_losses.append(float(np.mean(acc)))
     torch.cuda.synchronize()
-    return losses
+    return epoch_losses
 
 
-def evaluate_loss(mlp, samples, scale, var):
-    """Mean normalised loss of the network on samples, and of no correction."""
+def evaluate_loss(mlp, samples, scale, var=None):
+    """Mean over samples of mean((ds - target)^2) / mean(target^2) with the
+    network's correction ds; without a correction that ratio is 1."""
     import torch
     lib = _capi.load()
     n_max = max(s[3] * s[4] for s in samples)
     y = torch.empty((n_max, NOUT), dtype=torch.float32, device="cuda")
     buf = _buffers(n_max)
-    with_net, without = [], []
+    with_net = []
     for x, target, surf, nrad, nsec in samples:
         n = nrad * nsec
+        v = _sample_var(target)
         mlp.forward(x, y[:n])
-        _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / var, [b[:n] if b.dim() and b.shape[0] >= n
-                                                                             else b for b in buf])
-        with_net.append(float(buf[4].item()) / (n * var))
-        without.append(float((target.double() ** 2).sum().item()) / (n * var))
-    return float(np.mean(with_net)), float(np.mean(without))
+        _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / v,
+                   [b[:n] if b.dim() and b.shape[0] >= n else b for b in buf])
+        with_net.append(float(buf[4].item()) / (n * v))
+    return float(np.mean(with_net)), 1.0
+
+
+def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, ndt_eval=10, epochs=40, lr=1e-3,
+               seed=2025, sigma_noise=1e-4, reset_every=4):
+    """Coarse disks of nrad x 3 nrad drawn from the ensemble distribution, a
+    factor-x finer plain run of each as teacher: train on n_train disks, then on
+    n_test held-out disks report the one-DT loss with and without the network and
+    a rollout of ndt_eval DTs from the restricted teacher state: after every DT
+    the relative L2 error of the plain and the learned coarse density against the
+    restricted teacher, at the end the same for the azimuthally averaged profile,
+    then the wall time per DT of each run."""
+    import time
+    import torch
+    from . import Disk, FARGO_FP32_BULK, c4_disks
+    tr_disks = c4_disks(n_train, seed=seed, nrad_choices=(nrad,), sigma_noise=sigma_noise)
+    te_disks = c4_disks(n_test, seed=seed + 1, nrad_choices=(nrad,), sigma_noise=sigma_noise)
+    t0 = time.perf_counter()
+    norm = feature_norm(generate(tr_disks[:2], factor, spinup, 2))
+    tr = generate(tr_disks, factor, spinup, ndt_train, norm, reset_every=reset_every)
+    ho = generate(te_disks, factor, spinup, 4, norm)
+    t_gen = time.perf_counter() - t0
+    scale, var = target_stats(tr)
+    mlp = MLP(nrad * 3 * nrad, seed=seed)
+    t0 = time.perf_counter()
+    losses = train(mlp, tr, scale, var, epochs=epochs, lr=lr)
+    t_train = time.perf_counter() - t0
+    with_net, without = evaluate_loss(mlp, ho, scale, var)
+    del tr, ho
+    torch.cuda.empty_cache()
+    corr = Correction(mlp, norm, scale)
+    roll = []
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    for params, planets in te_disks:
+        fine = Disk(fine_params(params, factor), planets, FARGO_FP32_BULK)
+        fine.run(spinup)
+        plain, learn, ref = (Disk(params, planets, FARGO_FP32_BULK) for _ in range(3))
+        for d in (plain, learn, ref):
+            restrict(fine, d, factor)
+        work = workspace(learn)
+        err = {"plain": [], "learned": []}
+        for _ in range(ndt_eval):
+            fine.step_DT()
+            plain.step_DT()
+            corr.step_DT(learn, work)
+            restrict(fine, ref, factor)
+            r = ref.field("dens")[:-1]
+            err["plain"].append(rel(plain.field("dens")[:-1], r))
+            err["learned"].append(rel(learn.field("dens")[:-1], r))
+        prof = {k: d.field("dens")[:-1].mean(axis=1) for k, d in (("ref", ref), ("plain", plain), ("learned", learn))}
+        t = {}
+        for name, run in (("fine", lambda: fine.run(ndt_eval)), ("plain", lambda: plain.run(ndt_eval)),
+                          ("learned", lambda: [corr.step_DT(learn, work) for _ in range(ndt_eval)])):
+            t0 = time.perf_counter()
+            run()
+            t[name] = (time.perf_counter() - t0) / ndt_eval
+        roll.append({"field_err": err, "profile_err": {k: rel(prof[k], prof["ref"]) for k in ("plain", "learned")},
+                     "s_per_dt": t})
+        for d in (fine, plain, learn, ref):
+            d.close()
+    avg = lambda get: float(np.mean([get(r) for r in roll]))  # noqa: E731
+    return {
+        "workload": f"{n_train} training and {n_test} held-out disks of the ensemble distribution at "
+                    f"{nrad}x{3 * nrad}, teacher {factor * nrad}x{3 * factor * nrad} (plain method, FP32-bulk)",
+        "train": {"samples": n_train * ndt_train, "epochs": epochs, "first_epoch_loss": losses[0],
+                  "last_epoch_loss": losses[-1],
+                  "seconds_data": t_gen, "seconds_training": t_train},
+        "held_out_one_dt_loss": {"with_network": with_net, "without": without},
+        "rollout_dts": ndt_eval,
+        "field_err_rel_per_dt": {k: [avg(lambda r, i=i, k=k: r["field_err"][k][i]) for i in range(ndt_eval)]
+                                 for k in ("plain", "learned")},
+        "profile_err_rel": {k: avg(lambda r, k=k: r["profile_err"][k]) for k in ("plain", "learned")},
+        "s_per_dt": {k: avg(lambda r, k=k: r["s_per_dt"][k]) for k in ("fine", "plain", "learned")},
+        "corrections": {"accepted": corr.accepted, "rejected": corr.rejected},
+    }
+
+
+if __name__ == "__main__":
+    import json
+    print(json.dumps(experiment()))

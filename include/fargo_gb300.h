@@ -285,8 +285,8 @@ int  fargo_mlp_adam(fargo_mlp *m, float lr, void *stream);
 
 /* Coupling of the MLP to a coarse disk (device buffers; fields of esize bytes,
    (nrad+1)*nsec elements; rmed and surf: FP64 device arrays of nrad+1).
-   features: x (BF16 [nrad*nsec][128]) from density and velocities; norm: 5 means
-   then 5 deviations of the input channels.  divergence: the density correction
+   features: x (BF16 [nrad*nsec][128]) from density and velocities; norm: 125 means
+   then 125 deviations of the inputs.  divergence: the density correction
    ds (FP32 [nrad*nsec]) of the network outputs y (FP32 [nrad*nsec][2]) scaled by
    scale (mass conserved by construction).  loss: ds, e = dL/dds, dy = dL/dy and
    *loss (device double) = sum (ds - target)^2, for L = that sum * inv_var / n

@@ -98,5 +98,5 @@ def test_learned_correction_gains_on_held_out_disks():
     assert losses[-1] < losses[0]
     with_net, without = L.evaluate_loss(mlp, ho, scale, var)
     print(f"held-out loss with the network {with_net:.3f}, without {without:.3f}")
-    assert with_net < without
+    assert with_net < 0.5 * without
     mlp.close()
