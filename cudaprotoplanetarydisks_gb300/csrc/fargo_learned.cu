@@ -37,40 +37,68 @@ struct FeatNorm {
   float mean[125], inv_std[125];
 };
 
+// One warp per 32 consecutive cells: each lane forms its cell's 125 inputs in a
+// shared row (stride FEAT_LDW words: the lanes' stores of one input fall in
+// distinct banks), then the warp writes the 32 rows of 256 bytes out as
+// contiguous 128-byte segments.  FP32 arithmetic; the density contrast is
+// (Sigma - Sigma_c) / Sigma_c with the difference taken in the field's type.
+#define FEAT_LDW 65
 template <class T>
-__global__ void k_features(const T *__restrict__ dens, const T *__restrict__ vrad, const T *__restrict__ vtheta,
-                           const double *__restrict__ rmed, int nrad, int nsec, float phi_planet, FeatNorm nm,
-                           bf16 *__restrict__ x) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nrad * nsec) return;
-  const int i = q / nsec, j = q % nsec;
-  bf16 *row = x + (size_t)q * 128;
-  const float dphi = 6.28318530717958648f / (float)nsec;
-  const size_t c0 = (size_t)i * nsec + j;
-  const double d0 = (double)dens[c0];
-  const float vt0 = 0.5f * ((float)vtheta[c0] + (float)vtheta[(size_t)i * nsec + wrapj(j + 1, nsec)]);
-  const float lr0 = logf((float)rmed[i]);
-  for (int di = -2; di <= 2; di++) {
-    const int ii = min(max(i + di, 0), nrad - 1);
-    const float r = (float)rmed[ii];
-    for (int dj = -2; dj <= 2; dj++) {
-      const int jj = wrapj(j + dj, nsec), jp = wrapj(jj + 1, nsec);
-      const size_t c = (size_t)ii * nsec + jj;
-      const bool centre = di == 0 && dj == 0;
-      float ang = (jj + 0.5f) * dphi - phi_planet;  // cell centre azimuth relative to the planet
-      ang -= 6.28318530717958648f * floorf(ang * 0.15915494309189535f + 0.5f);
-      const float vt = 0.5f * ((float)vtheta[c] + (float)vtheta[(size_t)ii * nsec + jp]);
-      const float v[5] = {centre ? logf((float)d0) : (float)((double)dens[c] / d0 - 1.0),
-                          0.5f * ((float)vrad[c] + (float)vrad[c + nsec]),
-                          centre ? vt0 - rsqrtf(r) : vt - vt0, centre ? lr0 : logf(r) - lr0,
-                          ang * 0.31830988618379067f};
-      const int base = ((di + 2) * 5 + (dj + 2)) * 5;
+__global__ void __launch_bounds__(128) k_features(const T *__restrict__ dens, const T *__restrict__ vrad,
+                                                  const T *__restrict__ vtheta, const double *__restrict__ rmed,
+                                                  int nrad, int nsec, float phi_planet, FeatNorm nm,
+                                                  bf16 *__restrict__ x) {
+  __shared__ unsigned srow[4][32 * FEAT_LDW];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = nrad * nsec, q0 = (blockIdx.x * 4 + w) * 32;
+  if (q0 >= n) return;  // whole warps
+  const int q = q0 + lane;
+  bf16 *row = reinterpret_cast<bf16 *>(&srow[w][lane * FEAT_LDW]);
+  if (q < n) {
+    const int i = q / nsec, j = q - (q / nsec) * nsec;
+    const float dphi = 6.28318530717958648f / (float)nsec;
+    const size_t c0 = (size_t)i * nsec + j;
+    const T d0 = dens[c0];
+    const float inv_d0 = 1.0f / (float)d0;
+    const float vt0 = 0.5f * ((float)vtheta[c0] + (float)vtheta[(size_t)i * nsec + wrapj(j + 1, nsec)]);
+    const float lr0 = logf((float)rmed[i]);
 #pragma unroll
-      for (int ch = 0; ch < 5; ch++)
-        row[base + ch] = __float2bfloat16_rn((v[ch] - nm.mean[base + ch]) * nm.inv_std[base + ch]);
+    for (int di = -2; di <= 2; di++) {
+      const int ii = min(max(i + di, 0), nrad - 1);
+      const float r = (float)rmed[ii];
+      const float lr = di == 0 ? lr0 : logf(r) - lr0;
+#pragma unroll
+      for (int dj = -2; dj <= 2; dj++) {
+        const int jj = wrapj(j + dj, nsec), jp = wrapj(jj + 1, nsec);
+        const size_t c = (size_t)ii * nsec + jj;
+        float ang = (jj + 0.5f) * dphi - phi_planet;  // cell centre azimuth relative to the planet
+        ang -= 6.28318530717958648f * floorf(ang * 0.15915494309189535f + 0.5f);
+        float v[5];
+        if (di == 0 && dj == 0) {
+          v[0] = logf((float)d0);
+          v[2] = vt0 - rsqrtf(r);
+          v[3] = lr0;
+        } else {
+          v[0] = (float)(dens[c] - d0) * inv_d0;
+          v[2] = 0.5f * ((float)vtheta[c] + (float)vtheta[(size_t)ii * nsec + jp]) - vt0;
+          v[3] = di == 0 ? 0.0f : lr;
+        }
+        v[1] = 0.5f * ((float)vrad[c] + (float)vrad[c + nsec]);
+        v[4] = ang * 0.31830988618379067f;
+        const int base = ((di + 2) * 5 + (dj + 2)) * 5;
+#pragma unroll
+        for (int ch = 0; ch < 5; ch++)
+          row[base + ch] = __float2bfloat16_rn((v[ch] - nm.mean[base + ch]) * nm.inv_std[base + ch]);
+      }
     }
+    row[125] = row[126] = row[127] = __float2bfloat16_rn(0.0f);
   }
-  row[125] = row[126] = row[127] = __float2bfloat16_rn(0.0f);
+  __syncwarp();
+  for (int r = 0; r < 32 && q0 + r < n; r++) {
+    unsigned *dst = reinterpret_cast<unsigned *>(x + (size_t)(q0 + r) * 128);
+    dst[lane] = srow[w][r * FEAT_LDW + lane];
+    dst[lane + 32] = srow[w][r * FEAT_LDW + lane + 32];
+  }
 }
 
 // dSigma of the flux corrections (see the file comment)
@@ -219,13 +247,13 @@ int fargo_learned_features(int esize, const void *dens, const void *vrad, const 
   }
   const int n = nrad * nsec;
   const cudaStream_t s = (cudaStream_t)stream;
+  const int nb = (n + 127) / 128;  // 4 warps of 32 cells
   if (esize == 4)
-    k_features<float><<<(n + 255) / 256, 256, 0, s>>>((const float *)dens, (const float *)vrad, (const float *)vtheta,
-                                                       rmed, nrad, nsec, (float)phi_planet, nm, (bf16 *)x);
+    k_features<float><<<nb, 128, 0, s>>>((const float *)dens, (const float *)vrad, (const float *)vtheta, rmed, nrad,
+                                         nsec, (float)phi_planet, nm, (bf16 *)x);
   else
-    k_features<double><<<(n + 255) / 256, 256, 0, s>>>((const double *)dens, (const double *)vrad,
-                                                        (const double *)vtheta, rmed, nrad, nsec, (float)phi_planet,
-                                                        nm, (bf16 *)x);
+    k_features<double><<<nb, 128, 0, s>>>((const double *)dens, (const double *)vrad, (const double *)vtheta, rmed,
+                                          nrad, nsec, (float)phi_planet, nm, (bf16 *)x);
   return cudaGetLastError() == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
 }
 

@@ -2,8 +2,8 @@
 its C-ABI, on device buffers held by torch tensors.
 
 The network maps a coarse cell's 5x5 neighbourhood of 5 channels (padded to 128
-inputs) through two GELU layers of width 64 to 2 outputs, the radial and azimuthal
-mass-flux corrections of the cell.  Weights and activations are BF16 on the tensor
+inputs) through two GELU layers (tanh form) of width 64 to 2 outputs, the radial
+and azimuthal mass-flux corrections of the cell.  Weights and activations are BF16 on the tensor
 cores with FP32 accumulation; the master weights and the optimiser (Adam) are
 FP32.  Everything here launches the library's kernels; nothing is computed on the
 host but the learning-rate schedule.
@@ -39,7 +39,8 @@ def init_params(seed=0):
 
 class MLP:
     """fargo_mlp_*: forward/backward/Adam on at most max_rows rows per call.
-    x: torch.bfloat16 [n, 128] on the GPU; y, dy: torch.float32 [n, 2]."""
+    x: torch.bfloat16 [n, 128] on the GPU; y, dy: torch.float32 [n, 2].  The
+    backward pass recomputes the forward pass of its rows (train is ignored)."""
 
     def __init__(self, max_rows, params=None, seed=0):
         self.lib = _capi.load()

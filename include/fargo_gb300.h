@@ -263,11 +263,13 @@ int  fargo_batch_advance(fargo_batch *b, double t_end, long long *nsub, int *fai
 /* The stencil MLP: 128 inputs -> 64 (GELU) -> 64 (GELU) -> 2 outputs, BF16 on
    the tensor cores with FP32 accumulation.  Parameters: FP32 blob of
    FARGO_MLP_NPARAM floats, W1 [128][64], b1 [64], W2 [64][64], b2 [64], W3 [64][8]
-   (columns 2..7 zero), b3 [8] (entries 2..7 zero); W[in][out].  Inputs: BF16
-   [n][128] device rows; outputs: FP32 [n][2] device rows. */
+   (columns 2..7 zero), b3 [8] (entries 2..7 zero); W[in][out].  GELU in its tanh
+   form.  Inputs: BF16 [n][128] device rows, 16-byte aligned; outputs and their
+   gradients: FP32 [n][2] device rows, 8-byte aligned. */
 #define FARGO_MLP_NPARAM (128 * 64 + 64 + 64 * 64 + 64 + 64 * 8 + 8)
 typedef struct fargo_mlp fargo_mlp;
-/* Workspace for at most max_rows rows (pre-activations, per-CTA gradients). */
+/* Calls of at most max_rows rows; the workspace is the per-CTA gradient partials
+   of one persistent grid (the device's resident CTAs). */
 int  fargo_mlp_create(int max_rows, fargo_mlp **out);
 void fargo_mlp_destroy(fargo_mlp *m);
 /* Host FP32 blobs; setting the parameters resets the Adam moments. */
@@ -275,10 +277,11 @@ int  fargo_mlp_set_params(fargo_mlp *m, const float *host);
 int  fargo_mlp_get_params(fargo_mlp *m, float *host);
 /* Gradient of the last fargo_mlp_backward (host FP32 blob). */
 int  fargo_mlp_get_grad(fargo_mlp *m, float *host);
-/* y = f(x) on n rows; train != 0 keeps the pre-activations for the backward pass. */
+/* y = f(x) on n rows.  train is accepted for compatibility and ignored: the
+   backward pass recomputes the forward pass of its rows. */
 int  fargo_mlp_forward(fargo_mlp *m, const void *x_bf16, int n, float *y, int train, void *stream);
-/* dL/dparameters from dL/dy (FP32 [n][2]) after a training forward pass of the
-   same rows; summed over the rows in a fixed order (deterministic). */
+/* dL/dparameters from dL/dy (FP32 [n][2]) of the rows x; summed over the rows in
+   a fixed order (deterministic on a given device). */
 int  fargo_mlp_backward(fargo_mlp *m, const void *x_bf16, int n, const float *dy, void *stream);
 /* One Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr. */
 int  fargo_mlp_adam(fargo_mlp *m, float lr, void *stream);

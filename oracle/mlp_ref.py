@@ -8,7 +8,8 @@ no learned part); this file restates the design the kernels implement:
     z1 = bf16(x W1 + b1), h1 = bf16(gelu(z1)), z2 = bf16(h1 W2 + b2),
     h2 = bf16(gelu(z2)), y = h2 W3[:, :2] + b3[:2]
 
-with BF16 weights and inputs, sums in FP64 (the kernels accumulate in FP32), and
+with GELU in its tanh form z (1 + tanh u) / 2, u = sqrt(2/pi) (z + 0.044715 z^3)
+(Hendrycks & Gimpel 2016), BF16 weights and inputs, sums in FP64 (the kernels accumulate in FP32), and
 the backward pass with the kernels' rounding points (dy, dz2, dz1 rounded to
 BF16).  `exact=True` drops every rounding: the plain FP64 network, whose
 gradient the tests check against finite differences.
@@ -35,15 +36,20 @@ def bf16(x):
     return rounded.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-_erf = np.vectorize(math.erf)
+def _sig(z):
+    """sigma(2u), u = sqrt(2/pi) (z + 0.044715 z^3): GELU in its tanh form
+    (Hendrycks & Gimpel 2016), z (1 + tanh u) / 2 = z sigma(2u)."""
+    u2 = 2.0 * math.sqrt(2.0 / math.pi) * (z + 0.044715 * z ** 3)
+    return 0.5 * (1.0 + np.tanh(0.5 * u2))
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    return z * _sig(z)
 
 
 def gelu_d(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    s = _sig(z)
+    return s + z * s * (1.0 - s) * 2.0 * math.sqrt(2.0 / math.pi) * (1.0 + 3.0 * 0.044715 * z * z)
 
 
 def unpack(P, exact=False):

@@ -15,14 +15,15 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("n", [16, 200, 1000])
+@pytest.mark.parametrize("n", [16, 200, 1000, 100003])
 def test_forward_and_gradients_match_oracle(n):
+    # 100003 rows: many tiles per persistent CTA and a ragged last tile
     rng = np.random.default_rng(n)
     P = init_params(2)
     P[mlp_ref.OFF_B1:mlp_ref.OFF_W2] = rng.normal(0, 0.1, mlp_ref.NH)
     X = mlp_ref.bf16(rng.normal(0, 1, (n, NIN)))
     dy = rng.normal(0, 1, (n, NOUT)).astype(np.float32)
-    m = MLP(1024, P)
+    m = MLP(max(n, 1024), P)
     xd = torch.tensor(X, dtype=torch.float32).to(torch.bfloat16).cuda()
     yd = torch.zeros((n, NOUT), dtype=torch.float32, device="cuda")
     m.forward(xd, yd, train=True)
@@ -30,11 +31,42 @@ def test_forward_and_gradients_match_oracle(n):
     torch.cuda.synchronize()
     y_ref, cache = mlp_ref.forward(P, X)
     g_ref = mlp_ref.backward(P, cache, dy)
-    assert rel(yd.cpu().numpy(), y_ref) < 1e-2
+    ey = rel(yd.cpu().numpy(), y_ref)
     g = m.grad()
-    for lo, hi in ((mlp_ref.OFF_W1, mlp_ref.OFF_B1), (mlp_ref.OFF_B1, mlp_ref.OFF_W2), (mlp_ref.OFF_W2, mlp_ref.OFF_B2),
-                   (mlp_ref.OFF_B2, mlp_ref.OFF_W3), (mlp_ref.OFF_W3, mlp_ref.OFF_B3), (mlp_ref.OFF_B3, mlp_ref.NPARAM)):
-        assert rel(g[lo:hi], g_ref[lo:hi]) < 3e-2, (lo, hi)
+    eg = [rel(g[lo:hi], g_ref[lo:hi]) for lo, hi in (
+        (mlp_ref.OFF_W1, mlp_ref.OFF_B1), (mlp_ref.OFF_B1, mlp_ref.OFF_W2), (mlp_ref.OFF_W2, mlp_ref.OFF_B2),
+        (mlp_ref.OFF_B2, mlp_ref.OFF_W3), (mlp_ref.OFF_W3, mlp_ref.OFF_B3), (mlp_ref.OFF_B3, mlp_ref.NPARAM))]
+    print(f"n={n}: y rel {ey:.2e}, gradient rel per block " + " ".join(f"{e:.2e}" for e in eg))
+    # BF16 rounding points shared with the oracle; FP32 against FP64 sums and the
+    # SFU exponential flip a few roundings (observed at most 8e-5 / 1.2e-4)
+    assert ey < 1e-3
+    assert max(eg) < 2e-3
+    # the padded columns of the last layer get no gradient
+    w3 = g[mlp_ref.OFF_W3:mlp_ref.OFF_B3].reshape(mlp_ref.NH, mlp_ref.NOUTP)
+    assert not w3[:, NOUT:].any() and not g[mlp_ref.OFF_B3 + NOUT:].any()
+    m.close()
+
+
+def test_backward_is_deterministic():
+    rng = np.random.default_rng(8)
+    n = 50000
+    xd = torch.tensor(rng.normal(0, 1, (n, NIN)), dtype=torch.float32).to(torch.bfloat16).cuda()
+    dy = torch.tensor(rng.normal(0, 1, (n, NOUT)), dtype=torch.float32).cuda()
+    m = MLP(n, seed=3)
+    m.backward(xd, dy)
+    g1 = m.grad()
+    m.backward(xd, dy)
+    assert np.array_equal(g1, m.grad())
+    m.close()
+
+
+def test_misaligned_rows_are_rejected():
+    m = MLP(64, seed=0)
+    x = torch.zeros((65, NIN), dtype=torch.bfloat16, device="cuda")
+    y = torch.zeros((64, NOUT), dtype=torch.float32, device="cuda")
+    xv = x.view(-1)[4:4 + 64 * NIN].view(64, NIN)  # 8-byte offset: not 16-byte aligned
+    with pytest.raises(RuntimeError):
+        m.forward(xv, y)
     m.close()
 
 
