@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-correction measurement")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
                     help="profiling target: warm-up DTs, then --steps substeps launched kernel by kernel "
                          "(kernels inside the DT graph's while loop are invisible to ncu)")
@@ -310,6 +311,32 @@ def batch_ensemble(ndt=2, n=64):
             "timing": "host wall clock around run + sync (many streams: one per disk)"}
 
 
+def learned_c5():
+    """The learned coarse-grid correction: 256 x 768 disks of the ensemble
+    distribution with a 4x finer plain run as teacher.  Training pairs come from
+    the plain solver; on held-out disks: the one-DT loss with and without the
+    network, a 10-DT rollout from the restricted teacher state (density relative
+    L2 against the restricted teacher after 1 and 10 DTs, plain and learned), the
+    wall time per DT of teacher, plain and learned runs; and the MLP kernels'
+    throughput on one 256 x 768 disk's rows (CUDA events, 50 launches)."""
+    from cudaprotoplanetarydisks_gb300 import learned as L
+    r = L.experiment()
+    kernels = L.kernel_timing()
+    fe = r["field_err_rel_per_dt"]
+    return {
+        "workload": r["workload"],
+        "train": r["train"],
+        "held_out_one_dt_loss": r["held_out_one_dt_loss"],
+        "rollout_dens_rel_l2": {"after_1_dt": {"plain": fe["plain"][0], "learned": fe["learned"][0]},
+                                f"after_{r['rollout_dts']}_dts": {"plain": fe["plain"][-1],
+                                                                  "learned": fe["learned"][-1]}},
+        "profile_rel_l2_after_rollout": r["profile_err_rel"],
+        "s_per_dt": r["s_per_dt"],
+        "corrections": r["corrections"],
+        "mlp_kernels": kernels,
+    }
+
+
 def oracle_sample(params, planets, ndt, threads):
     from oracle.oracle import OracleDisk
     OracleDisk.set_threads(threads)
@@ -456,6 +483,8 @@ def run_own(args, world, rank, local):
         o.close()
     if not args.no_batch and world == 1:
         line["batch_c4"] = batch_ensemble()
+    if not args.no_learned and world == 1:
+        line["learned_c5"] = learned_c5()
     print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

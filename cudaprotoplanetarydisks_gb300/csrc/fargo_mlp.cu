@@ -138,7 +138,7 @@ struct MlpFwdW {
 };
 struct MlpBwdW {
   bf16 w2[MLP_H][MLP_LDH];
-  bf16 w3[MLP_H][16];  // W3 [64][8] with k (= out) padded to 16
+  bf16 w3[MLP_H][24];  // W3 [64][8], k (= out) zero-padded to 16; rows of 48 bytes
 };
 
 __device__ void load_fwd_weights(MlpFwdW &s, const float *__restrict__ P, int tid, int nt) {
@@ -166,8 +166,8 @@ __device__ void load_bwd_weights(MlpBwdW &s, const float *__restrict__ P, int ti
     const int k = e / MLP_H, n = e % MLP_H;
     s.w2[k][n] = __float2bfloat16_rn(P[MLP_OFF_W2 + e]);
   }
-  for (int e = tid; e < MLP_H * 16; e += nt) {
-    const int k = e / 16, n = e % 16;
+  for (int e = tid; e < MLP_H * 24; e += nt) {
+    const int k = e / 24, n = e % 24;
     s.w3[k][n] = __float2bfloat16_rn(n < MLP_OUT ? P[MLP_OFF_W3 + k * MLP_OUTP + n] : 0.0f);
   }
 }
@@ -187,11 +187,15 @@ __device__ __forceinline__ void stage_rows16(bf16 *buf, const bf16 *__restrict__
 // (16 rows, stride MLP_LDX).  Out: z1p/z2p, the BF16 pre-activations in C layout
 // (rows g, g+8 of column pair 2t of tile nt), and h2 (GELU(z2)) as the A
 // fragments of the next k blocks; GELU(z1) and GELU(z2) also stored row-major to
-// h1s/h2s (stride MLP_LDH) when those are given.
+// h1s/h2s (stride MLP_LDH) when those are given.  LDSM_B: B fragments by ldmatrix
+// (fewer instructions) or by 32-bit loads (fewer live registers: the backward pass).
+template <bool LDSM_B>
 __device__ __forceinline__ void layers12(const MlpFwdW &s, const bf16 *xs, int lane, unsigned (&z1p)[8][2],
                                          unsigned (&z2p)[8][2], unsigned (&h2)[4][4], bf16 *h1s, bf16 *h2s) {
   const int g = lane >> 2, t = lane & 3, q = lane >> 3, rr = lane & 7;
   const bf16 *arow = xs + (rr + 8 * (q & 1)) * MLP_LDX + 8 * (q >> 1);
+  // B from WT[n][k]: blocks (n0, k0), (n0, k0+8), (n0+8, k0), (n0+8, k0+8)
+  const int brow = rr + 8 * (q >> 1), bcol = 8 * (q & 1);
   float c[8][4];
 #pragma unroll
   for (int nt = 0; nt < 8; nt++) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
@@ -199,10 +203,20 @@ __device__ __forceinline__ void layers12(const MlpFwdW &s, const bf16 *xs, int l
   for (int kb = 0; kb < MLP_IN / 16; kb++) {
     unsigned a[4];
     ldsm_x4(a, arow + kb * 16);
+    if (LDSM_B) {
 #pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-      const unsigned b[2] = {ld_u32(&s.w1t[nt * 8 + g][kb * 16 + 2 * t]), ld_u32(&s.w1t[nt * 8 + g][kb * 16 + 2 * t + 8])};
-      mma16816(c[nt], a, b);
+      for (int np = 0; np < 4; np++) {  // B fragments of n-tiles 2np, 2np+1
+        unsigned b[4];
+        ldsm_x4(b, &s.w1t[np * 16 + brow][kb * 16 + bcol]);
+        mma16816(c[2 * np], a, &b[0]);
+        mma16816(c[2 * np + 1], a, &b[2]);
+      }
+    } else {
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        const unsigned b[2] = {ld_u32(&s.w1t[nt * 8 + g][kb * 16 + 2 * t]), ld_u32(&s.w1t[nt * 8 + g][kb * 16 + 2 * t + 8])};
+        mma16816(c[nt], a, b);
+      }
     }
   }
   // bias, keep z, GELU (of the BF16-rounded z, as the backward pass sees it)
@@ -226,10 +240,20 @@ __device__ __forceinline__ void layers12(const MlpFwdW &s, const bf16 *xs, int l
   for (int nt = 0; nt < 8; nt++) c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
 #pragma unroll
   for (int kb = 0; kb < 4; kb++) {
+    if (LDSM_B) {
 #pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-      const unsigned b[2] = {ld_u32(&s.w2t[nt * 8 + g][kb * 16 + 2 * t]), ld_u32(&s.w2t[nt * 8 + g][kb * 16 + 2 * t + 8])};
-      mma16816(c[nt], h1[kb], b);
+      for (int np = 0; np < 4; np++) {
+        unsigned b[4];
+        ldsm_x4(b, &s.w2t[np * 16 + brow][kb * 16 + bcol]);
+        mma16816(c[2 * np], h1[kb], &b[0]);
+        mma16816(c[2 * np + 1], h1[kb], &b[2]);
+      }
+    } else {
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        const unsigned b[2] = {ld_u32(&s.w2t[nt * 8 + g][kb * 16 + 2 * t]), ld_u32(&s.w2t[nt * 8 + g][kb * 16 + 2 * t + 8])};
+        mma16816(c[nt], h1[kb], b);
+      }
     }
   }
 #pragma unroll
@@ -270,13 +294,15 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float *__restrict__ P
     cp_async_wait<1>();
     __syncwarp();
     unsigned z1p[8][2], z2p[8][2], h2[4][4];
-    layers12(s.w, &s.xb[w][buf][0][0], lane, z1p, z2p, h2, nullptr, nullptr);
+    layers12<true>(s.w, &s.xb[w][buf][0][0], lane, z1p, z2p, h2, nullptr, nullptr);
     // layer 3: 16 x 64 . 64 x 8
     float c3[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int kb = 0; kb < 4; kb++) {
-      const unsigned b[2] = {ld_u32(&s.w.w3t[g][kb * 16 + 2 * t]), ld_u32(&s.w.w3t[g][kb * 16 + 2 * t + 8])};
-      mma16816(c3, h2[kb], b);
+    for (int kp = 0; kp < 2; kp++) {  // B fragments of k blocks 2kp, 2kp+1
+      unsigned b[4];
+      ldsm_x4(b, &s.w.w3t[lane & 7][kp * 32 + 8 * (lane >> 3)]);
+      mma16816(c3, h2[2 * kp], &b[0]);
+      mma16816(c3, h2[2 * kp + 1], &b[2]);
     }
     const int r0 = tile * 16;
     if (t == 0) {  // columns 0, 1
@@ -340,15 +366,18 @@ __global__ void __launch_bounds__(128, 2) k_mlp_backward(const float *__restrict
     // ---- data gradients of the warp's 16 rows
     {
       unsigned z1p[8][2], z2p[8][2], h2[4][4];
-      layers12(s.f, &s.xs[rw][0], lane, z1p, z2p, h2, &s.h1s[rw][0], &s.h2s[rw][0]);
+      layers12<false>(s.f, &s.xs[rw][0], lane, z1p, z2p, h2, &s.h1s[rw][0], &s.h2s[rw][0]);
       // dh2 = dy W3^T: A = dy (16 x 16, columns >= 8 zero)
       const unsigned a[4] = {ld_u32(&s.dys[rw + g][2 * t]), ld_u32(&s.dys[rw + g + 8][2 * t]), 0u, 0u};
       float c[8][4];
 #pragma unroll
-      for (int nt = 0; nt < 8; nt++) {
-        c[nt][0] = c[nt][1] = c[nt][2] = c[nt][3] = 0.0f;
-        const unsigned b[2] = {ld_u32(&s.b.w3[nt * 8 + g][2 * t]), ld_u32(&s.b.w3[nt * 8 + g][2 * t + 8])};
-        mma16816(c[nt], a, b);
+      for (int np = 0; np < 4; np++) {
+        unsigned b[4];
+        ldsm_x4(b, &s.b.w3[np * 16 + rr + 8 * (q >> 1)][8 * (q & 1)]);
+        c[2 * np][0] = c[2 * np][1] = c[2 * np][2] = c[2 * np][3] = 0.0f;
+        c[2 * np + 1][0] = c[2 * np + 1][1] = c[2 * np + 1][2] = c[2 * np + 1][3] = 0.0f;
+        mma16816(c[2 * np], a, &b[0]);
+        mma16816(c[2 * np + 1], a, &b[2]);
       }
       // dz2 = dh2 GELU'(z2), BF16, as A fragments and row-major in dz2s
       unsigned d2[4][4];
@@ -369,10 +398,11 @@ __global__ void __launch_bounds__(128, 2) k_mlp_backward(const float *__restrict
 #pragma unroll
       for (int kb = 0; kb < 4; kb++)
 #pragma unroll
-        for (int nt = 0; nt < 8; nt++) {
-          const unsigned b[2] = {ld_u32(&s.b.w2[nt * 8 + g][kb * 16 + 2 * t]),
-                                 ld_u32(&s.b.w2[nt * 8 + g][kb * 16 + 2 * t + 8])};
-          mma16816(c[nt], d2[kb], b);
+        for (int np = 0; np < 4; np++) {
+          unsigned b[4];
+          ldsm_x4(b, &s.b.w2[np * 16 + rr + 8 * (q >> 1)][kb * 16 + 8 * (q & 1)]);
+          mma16816(c[2 * np], d2[kb], &b[0]);
+          mma16816(c[2 * np + 1], d2[kb], &b[2]);
         }
 #pragma unroll
       for (int nt = 0; nt < 8; nt++) {

@@ -394,6 +394,55 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
     }
 
 
+def kernel_timing(nrad=256, reps=50, seed=5):
+    """The correction's kernels on one nrad x 3 nrad disk: MLP forward and backward
+    (with its gradient reduction) on the disk's rows of random inputs, timed with
+    CUDA events over reps launches, and the features of the disk's state (a
+    synchronous call: wall time).  Algorithmic flops per row: forward
+    2 (128 64 + 64 64 + 64 2); backward the forward's layers 1-2 (recomputed), the
+    data gradients dh2, dh1 and the weight gradients dW1, dW2, dW3."""
+    import time
+    import torch
+    from . import Disk, FARGO_FP32_BULK, c4_disks
+    (params, planets), = c4_disks(1, seed=seed, nrad_choices=(nrad,))
+    disk = Disk(params, planets, FARGO_FP32_BULK)
+    n = disk.nrad * disk.nsec
+    mlp = MLP(n, seed=1)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    x = torch.randn((n, NIN), device="cuda", generator=g).to(torch.bfloat16)
+    y = torch.empty((n, NOUT), device="cuda")
+    dy = torch.randn((n, NOUT), device="cuda", generator=g)
+
+    def ev(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps * 1e3
+
+    fwd_us, bwd_us = ev(lambda: mlp.forward(x, y)), ev(lambda: mlp.backward(x, dy))
+    corr = Correction(mlp, IDENTITY_NORM, 1.0)
+    corr.features(disk, x)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        corr.features(disk, x)
+    feat_us = (time.perf_counter() - t0) / reps * 1e6
+    mlp.close()
+    disk.close()
+    f_fwd = 2 * (128 * 64 + 64 * 64 + 64 * 2)
+    f_bwd = 2 * (128 * 64 + 64 * 64) + 2 * (2 * 64 + 64 * 64) + 2 * (128 * 64 + 64 * 64 + 64 * 2)
+    return {"rows": n, "tensor_path": "mma.sync m16n8k16 BF16, FP32 accumulate",
+            "forward_us": fwd_us, "forward_tflops": f_fwd * n / fwd_us * 1e-6,
+            "backward_us": bwd_us, "backward_tflops": f_bwd * n / bwd_us * 1e-6,
+            "backward_includes": "forward recompute and the per-CTA gradient reduction",
+            "features_wall_us": feat_us}
+
+
 if __name__ == "__main__":
     import json
-    print(json.dumps(experiment()))
+    import sys
+    print(json.dumps(kernel_timing() if "--kernels" in sys.argv[1:] else experiment()))
