@@ -133,6 +133,11 @@ class Disk:
     def write_dims(self):
         self._check(self.lib.fargo_write_dims(self.h), "write_dims")
 
+    def restart(self, index):
+        """Fields, planets and time of output `index` in the disk's OUTPUTDIR
+        (fargo_restart)."""
+        self._check(self.lib.fargo_restart(self.h, int(index)), "restart")
+
 
 class Batch:
     """An ensemble of independent disks (fargo_batch_*): each disk keeps its own

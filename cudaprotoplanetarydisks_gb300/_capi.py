@@ -105,6 +105,7 @@ SIGNATURES = [
     ("fargo_condition_cfl", _I, [_P, _D, ctypes.POINTER(_I)]),
     ("fargo_write_outputs", _I, [_P, _I]),
     ("fargo_write_dims", _I, [_P]),
+    ("fargo_restart", _I, [_P, _I]),
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),

@@ -1,14 +1,17 @@
 // driver.cpp -- fargo_gb300, the command-line driver (the reference's main(),
 // src/Main.cu:89-363) on top of the C-ABI.
 //
-//   echo 0 | fargo_gb300 [-switches] [--fp32] parameters.par
+//   echo 0 | fargo_gb300 [-switches] [-s index] [--fp32] parameters.par
 //
 // Reads the device ordinal from standard input like the reference
 // (src/Main.cu:92-97; 0 when nothing is given), parses the .par file and the
 // planet .cfg (ReadVariables, InitPlanetarySystem), writes dims.dat /
 // used_rad.dat / planet<k>.dat, then runs NTOT+1 DT steps, writing the field
 // dumps before each step whose index is a multiple of NINTERM
-// (src/Main.cu:309-333), and prints the elapsed seconds of the loop.
+// (src/Main.cu:309-333), and prints the elapsed seconds of the loop.  -s index
+// restarts from output `index` of an earlier run in the same OUTPUTDIR (FARGO's
+// restart, which the reference parses but never performs): the loop resumes at
+// DT step index * NINTERM.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -20,7 +23,7 @@
 #include "fargo_gb300.h"
 
 static void usage(const char *exe) {
-  std::printf("Usage : %s [-abcdeimnptvz] [--fp32] parameters file\n", exe);
+  std::printf("Usage : %s [-abcdeimnptvz] [-s index] [--fp32] parameters file\n", exe);
   std::exit(1);
 }
 
@@ -39,13 +42,22 @@ int main(int argc, char **argv) {
   std::string parfile, switches;
   int precision = FARGO_FP64;
   bool disable = false;
+  int restart = -1;
   for (int i = 1; i < argc; i++) {
     if (std::strcmp(argv[i], "--fp32") == 0) {
       precision = FARGO_FP32_BULK;
     } else if (argv[i][0] == '-') {
       switches += argv[i] + 1;
       if (std::strchr(argv[i], 'n')) disable = true;
-      if (std::strchr(argv[i], 's') || std::strchr(argv[i], 'o') || std::strchr(argv[i], 'f')) i++;  // option value
+      const bool has_s = std::strchr(argv[i], 's') != nullptr;
+      if (has_s || std::strchr(argv[i], 'o') || std::strchr(argv[i], 'f')) i++;  // option value
+      if (has_s) {
+        restart = i < argc ? std::atoi(argv[i]) : -1;
+        if (restart < 0) {
+          std::printf("Incorrect restart number\n");
+          usage(argv[0]);
+        }
+      }
     } else {
       parfile = argv[i];
     }
@@ -76,13 +88,16 @@ int main(int argc, char **argv) {
     std::fprintf(stderr, "initialisation failed (status %d)\n", rc);
     return 1;
   }
-  if ((rc = fargo_write_dims(ctx)) != FARGO_OK) {
+  // a restart keeps dims.dat and the planet files of the earlier run
+  rc = restart >= 0 ? fargo_restart(ctx, restart) : fargo_write_dims(ctx);
+  if (rc != FARGO_OK) {
     std::fprintf(stderr, "%s\n", fargo_last_error(ctx));
     fargo_ctx_destroy(ctx);
     return 1;
   }
+  if (restart >= 0) std::printf("restarting from output %d\n", restart);
   auto t0 = std::chrono::steady_clock::now();
-  for (int i = 0; i <= p.ntot; i++) {
+  for (int i = restart >= 0 ? restart * p.ninterm : 0; i <= p.ntot; i++) {
     if (p.ninterm > 0 && (i / p.ninterm) * p.ninterm == i) {
       std::printf("\n*** OUTPUT %d ***\n", i / p.ninterm);
       if ((rc = fargo_write_outputs(ctx, i / p.ninterm)) != FARGO_OK) break;

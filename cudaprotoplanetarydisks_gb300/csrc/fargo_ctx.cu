@@ -960,4 +960,46 @@ int fargo_write_dims(fargo_ctx *c) {
   return FARGO_OK;
 }
 
+int fargo_restart(fargo_ctx *c, int index) {
+  if (!c) return FARGO_ERR_STATE;
+  if (index < 0) return set_err(c, FARGO_ERR_INVALID, "negative restart index");
+  const fargo_params &p = c->P;
+  const std::string dir = p.outputdir;
+  const size_t n = c->h.size_grid, nout = (size_t)p.nrad * p.nsec;
+  const char *names[4] = {"dens", "vrad", "vtheta", "energy"};
+  const int which[4] = {FARGO_FIELD_DENS, FARGO_FIELD_VRAD, FARGO_FIELD_VTHETA, FARGO_FIELD_ENERGY};
+  std::vector<double> f[4];
+  int rc;
+  for (int q = 0; q < 4; q++) {
+    if (q == 3 && !p.adiabatic) continue;
+    f[q].resize(n);
+    if ((rc = fargo_get_field(c, which[q], f[q].data()))) return rc;  // ring nrad: the created context's
+    if ((rc = host_read_field(dir, names[q], index, f[q].data(), nout)))
+      return set_err(c, rc, std::string("cannot read ") + names[q] + std::to_string(index) + ".dat");
+  }
+  if ((rc = fargo_set_fields(c, f[0].data(), f[1].data(), f[2].data(), p.adiabatic ? f[3].data() : nullptr)))
+    return rc;
+  if ((rc = read_ctl(c))) return rc;
+  Ctl &k = *c->pin_ctl;
+  double lost = 0.0, t = (double)index * p.ninterm * p.dt, omega = k.OmegaFrame;
+  for (int b = 0; b < k.nb; b++) {
+    fargo_planet pl{};
+    if ((rc = host_read_planet_row(dir, b, index, pl, &lost, &t, &omega)))
+      return set_err(c, rc, "cannot read row " + std::to_string(index) + " of planet" + std::to_string(b) + ".dat");
+    k.x[b] = pl.x;
+    k.y[b] = pl.y;
+    k.vx[b] = pl.vx;
+    k.vy[b] = pl.vy;
+    k.mass[b] = pl.mass;
+  }
+  k.PhysicalTime = t;
+  k.OmegaFrame = omega;
+  k.LostMass = lost;
+  fargo_planet_params(k, c->dp, k.PhysicalTime);
+  if ((rc = write_ctl(c))) return rc;
+  for (int b = 0; b < k.nb; b++)
+    if ((rc = host_truncate_planet_file(dir, b, index))) return set_err(c, rc, "cannot rewrite planet file");
+  return FARGO_OK;
+}
+
 }  // extern "C"

@@ -80,3 +80,7 @@ int host_write_planet_row(const std::string &outdir, int k, int index, const far
                           double physical_time, double omega_frame);
 int host_write_dims(const fargo_params &p, int nb);
 int host_write_used_rad(const fargo_params &p, const HostState &h);
+int host_read_field(const std::string &outdir, const char *name, int index, double *data, size_t n);
+int host_read_planet_row(const std::string &outdir, int k, int index, fargo_planet &b, double *lost_mass,
+                         double *physical_time, double *omega_frame);
+int host_truncate_planet_file(const std::string &outdir, int k, int index);

@@ -8,7 +8,9 @@
 #include <sys/types.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <string>
+#include <vector>
 
 #include "fargo_internal.h"
 
@@ -62,6 +64,67 @@ int host_write_used_rad(const fargo_params &p, const HostState &h) {
   FILE *f = std::fopen(fn.c_str(), "w");
   if (!f) return FARGO_ERR_IO;
   for (int i = 0; i <= p.nrad; i++) std::fprintf(f, "%.18g\n", h.Radii[i]);
+  std::fclose(f);
+  return FARGO_OK;
+}
+
+// ---- restart (FARGO's -s index; the reference parses the switch but never
+// restores anything, src/Main.cu:152-160)
+
+int host_read_field(const std::string &outdir, const char *name, int index, double *data, size_t n) {
+  char fname[1024];
+  std::snprintf(fname, sizeof(fname), "%s%s/%s%d.dat", outdir.c_str(), name, name, index);
+  FILE *f = std::fopen(fname, "r");
+  if (!f) return FARGO_ERR_IO;
+  const size_t r = std::fread(data, sizeof(double), n, f);
+  std::fclose(f);
+  return r == n ? FARGO_OK : FARGO_ERR_IO;
+}
+
+// Row `index` of planet<k>.dat (the layout host_write_planet_row writes)
+int host_read_planet_row(const std::string &outdir, int k, int index, fargo_planet &b, double *lost_mass,
+                         double *physical_time, double *omega_frame) {
+  char fname[1024];
+  std::snprintf(fname, sizeof(fname), "%splanet%d.dat", outdir.c_str(), k);
+  FILE *f = std::fopen(fname, "r");
+  if (!f) return FARGO_ERR_IO;
+  char line[2048];
+  int rc = FARGO_ERR_IO;
+  while (std::fgets(line, sizeof(line), f)) {
+    int idx = -1;
+    double v[8];
+    if (std::sscanf(line, "%d %lf %lf %lf %lf %lf %lf %lf %lf", &idx, &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6],
+                    &v[7]) == 9 &&
+        idx == index) {
+      b.x = v[0];
+      b.y = v[1];
+      b.vx = v[2];
+      b.vy = v[3];
+      b.mass = v[4];
+      *lost_mass = v[5];
+      *physical_time = v[6];
+      *omega_frame = v[7];
+      rc = FARGO_OK;
+    }
+  }
+  std::fclose(f);
+  return rc;
+}
+
+// Keeps the rows of planet<k>.dat whose index is below `index`
+int host_truncate_planet_file(const std::string &outdir, int k, int index) {
+  char fname[1024];
+  std::snprintf(fname, sizeof(fname), "%splanet%d.dat", outdir.c_str(), k);
+  FILE *f = std::fopen(fname, "r");
+  if (!f) return FARGO_ERR_IO;
+  std::vector<std::string> keep;
+  char line[2048];
+  while (std::fgets(line, sizeof(line), f))
+    if (std::atoi(line) < index) keep.push_back(line);
+  std::fclose(f);
+  f = std::fopen(fname, "w");
+  if (!f) return FARGO_ERR_IO;
+  for (const std::string &l : keep) std::fputs(l.c_str(), f);
   std::fclose(f);
   return FARGO_OK;
 }

@@ -214,6 +214,17 @@ int  fargo_condition_cfl(fargo_ctx *ctx, double deltaT, int *cfl);
 int  fargo_write_outputs(fargo_ctx *ctx, int index);
 /* WriteDim (src/Output.cu:19-35) + EmptyPlanetSystemFile (37-58). */
 int  fargo_write_dims(fargo_ctx *ctx);
+/* Restart from output `index` of an earlier run with the same parameters and
+   OUTPUTDIR: FARGO's "-s index", which the reference parses but never acts on
+   (src/Main.cu:152-160).  Density, velocities (and energy when adiabatic) from
+   the field dumps (ring nrad keeps the created context's values: the dumps hold
+   nrad rings); positions, velocities and masses of the planets, PhysicalTime,
+   OmegaFrame and LostMass from row `index` of planet<k>.dat; the planet files
+   are cut to the rows before `index`, so that writing output `index` again
+   continues them.  The run's start time stays that of the created context.
+   FARGO_ERR_IO when a file or row is missing; without planets the time is
+   index * NINTERM * DT. */
+int  fargo_restart(fargo_ctx *ctx, int index);
 
 /* ---- measurement (no counterpart in the reference) ----------------------- */
 /* Runs reps hydro substeps launch by launch with a CUDA event after every kernel

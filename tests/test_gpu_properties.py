@@ -111,3 +111,47 @@ RadialSpacing LOGARITHM\nNtot 2\nNinterm 1\nDT 0.314159265359\nOutputDir {tmp_pa
     d2 = np.fromfile(tmp_path / "dens" / "dens2.dat", dtype=np.float64)
     assert np.array_equal(d2, disk.field("dens")[:-1].ravel())
     disk.close()
+
+
+@pytest.mark.parametrize("fp32", [False, True])
+def test_driver_restart_continues_the_run(tmp_path, fp32):
+    """-s 1 from a copy of a run's outputs gives output 2 and the planet rows of
+    the uninterrupted run, bitwise."""
+    import shutil
+    exe = os.path.join(ROOT, "cudaprotoplanetarydisks_gb300", "fargo_gb300")
+    cfg = os.path.join(ROOT, "cudaprotoplanetarydisks_gb300", "configs", "c1_planet.cfg")
+
+    def par(outdir):
+        p = outdir / "run.par"
+        p.write_text(f"""AspectRatio 0.05\nSigma0 6.3662e-4\nViscosity 1e-5\nSigmaSlope 0.5
+PlanetConfig {cfg}\nForcedCircular NO\nThicknessSmoothing 0.6\nNrad 64\nNsec 192\nRmin 0.4\nRmax 2.5
+RadialSpacing LOGARITHM\nNtot 4\nNinterm 2\nDT 0.314159265359\nOutputDir {outdir}/\nSigmaNoise 1e-4\n""")
+        return str(p)
+
+    extra = ["--fp32"] if fp32 else []
+    a = tmp_path / "a"
+    a.mkdir()
+    r = subprocess.run([exe] + extra + [par(a)], input="0\n", capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    b = tmp_path / "b"
+    shutil.copytree(a, b)
+    for name in ("dens", "vrad", "vtheta"):
+        (b / name / f"{name}2.dat").unlink()
+    r = subprocess.run([exe, "-s", "1"] + extra + [par(b)], input="0\n", capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "restarting from output 1" in r.stdout
+    for name in ("dens", "vrad", "vtheta"):
+        x = np.fromfile(a / name / f"{name}2.dat", dtype=np.float64)
+        y = np.fromfile(b / name / f"{name}2.dat", dtype=np.float64)
+        assert np.array_equal(x, y), (name, float(np.abs(x - y).max()))
+    assert (a / "planet0.dat").read_text() == (b / "planet0.dat").read_text()
+
+
+def test_restart_with_missing_output_fails(tmp_path):
+    params = fg.read_par(os.path.join(ROOT, "cudaprotoplanetarydisks_gb300", "configs", "c1_isothermal.par"))
+    params.nrad, params.nsec = 32, 96
+    params.outputdir = (str(tmp_path) + "/").encode()
+    disk = fg.Disk(params, [], fg.FARGO_FP64)
+    with pytest.raises(RuntimeError):
+        disk.restart(3)
+    disk.close()
