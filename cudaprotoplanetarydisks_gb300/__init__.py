@@ -10,7 +10,7 @@ import ctypes
 import numpy as np
 
 from . import _capi
-from ._capi import (FARGO_FP32_BULK, FARGO_FP64, FIELDS, SUB_BOUNDARY, SUB_ENERGY,  # noqa: F401
+from ._capi import (FARGO_FP32_BULK, FARGO_FP64, FIELDS, FORCE_LEVELS, SUB_BOUNDARY, SUB_ENERGY,  # noqa: F401
                     SUB_POTENTIAL, SUB_SOUNDSPEED, SUB_SOURCE, SUB_TEMPERATURE, SUB_TRANSPORT,
                     FargoParams, FargoPlanet, FargoScalars)
 from .config import c4_disks, default_params, load_config, read_par, read_planets  # noqa: F401
@@ -137,6 +137,18 @@ class Disk:
         """Fields, planets and time of output `index` in the disk's OUTPUTDIR
         (fargo_restart)."""
         self._check(self.lib.fargo_restart(self.h, int(index)), "restart")
+
+    def compute_force(self, x, y, smoothing, mass, a, rh):
+        """The disk's force on (x, y) by inner/outer cells and Hill-cut level
+        (fargo_compute_force): array [4, FORCE_LEVELS] = fx inner, fx outer,
+        fy inner, fy outer."""
+        out = (ctypes.c_double * (4 * FORCE_LEVELS))()
+        self._check(self.lib.fargo_compute_force(self.h, x, y, smoothing, mass, a, rh, out), "compute_force")
+        return np.array(out).reshape(4, FORCE_LEVELS)
+
+    def update_log(self, timestep):
+        """Appends the torque-log rows of every planet (fargo_update_log)."""
+        self._check(self.lib.fargo_update_log(self.h, int(timestep)), "update_log")
 
 
 class Batch:

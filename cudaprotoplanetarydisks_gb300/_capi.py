@@ -14,6 +14,7 @@ FARGO_ERR_STATE = 5
 
 FARGO_FP64 = 0
 FARGO_FP32_BULK = 1
+FORCE_LEVELS = 11  # FARGO_FORCE_LEVELS: the reference's dimfxy
 
 SUB_BOUNDARY = 1
 SUB_SOURCE = 2
@@ -106,6 +107,8 @@ SIGNATURES = [
     ("fargo_write_outputs", _I, [_P, _I]),
     ("fargo_write_dims", _I, [_P]),
     ("fargo_restart", _I, [_P, _I]),
+    ("fargo_compute_force", _I, [_P, _D, _D, _D, _D, _D, _D, ctypes.POINTER(_D)]),
+    ("fargo_update_log", _I, [_P, _I]),
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),

@@ -27,7 +27,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 CUFLAGS = ARCH + COMMON + ["--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 LIB_SOURCES = ["params.cpp", "setup.cpp", "fargo_kernels.cu", "fargo_sg.cu", "fargo_ctx.cu", "output.cpp",
-               "fargo_noalloc.cu", "fargo_batch.cu", "fargo_mlp.cu", "fargo_learned.cu"]
+               "fargo_noalloc.cu", "fargo_batch.cu", "fargo_mlp.cu", "fargo_learned.cu",
+               "fargo_force_diag.cu"]
 EXE_SOURCES = ["driver.cpp"]
 HEADERS = ["fargo_internal.h", "fargo_device.cuh"]
 

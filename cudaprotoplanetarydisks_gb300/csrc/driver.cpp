@@ -1,7 +1,7 @@
 // driver.cpp -- fargo_gb300, the command-line driver (the reference's main(),
 // src/Main.cu:89-363) on top of the C-ABI.
 //
-//   echo 0 | fargo_gb300 [-switches] [-s index] [--fp32] parameters.par
+//   echo 0 | fargo_gb300 [-switches] [-s index] [--fp32] [--torques] parameters.par
 //
 // Reads the device ordinal from standard input like the reference
 // (src/Main.cu:92-97; 0 when nothing is given), parses the .par file and the
@@ -11,7 +11,9 @@
 // (src/Main.cu:309-333), and prints the elapsed seconds of the loop.  -s index
 // restarts from output `index` of an earlier run in the same OUTPUTDIR (FARGO's
 // restart, which the reference parses but never performs): the loop resumes at
-// DT step index * NINTERM.
+// DT step index * NINTERM.  --torques writes the torque logs every DT (UpdateLog,
+// whose call the reference keeps commented out at src/Main.cu:315), with the
+// reference's TimeStep: the index of the last output written.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -23,7 +25,7 @@
 #include "fargo_gb300.h"
 
 static void usage(const char *exe) {
-  std::printf("Usage : %s [-abcdeimnptvz] [-s index] [--fp32] parameters file\n", exe);
+  std::printf("Usage : %s [-abcdeimnptvz] [-s index] [--fp32] [--torques] parameters file\n", exe);
   std::exit(1);
 }
 
@@ -43,9 +45,12 @@ int main(int argc, char **argv) {
   int precision = FARGO_FP64;
   bool disable = false;
   int restart = -1;
+  bool torques = false;
   for (int i = 1; i < argc; i++) {
     if (std::strcmp(argv[i], "--fp32") == 0) {
       precision = FARGO_FP32_BULK;
+    } else if (std::strcmp(argv[i], "--torques") == 0) {
+      torques = true;
     } else if (argv[i][0] == '-') {
       switches += argv[i] + 1;
       if (std::strchr(argv[i], 'n')) disable = true;
@@ -97,8 +102,11 @@ int main(int argc, char **argv) {
   }
   if (restart >= 0) std::printf("restarting from output %d\n", restart);
   auto t0 = std::chrono::steady_clock::now();
+  int timestep = restart >= 0 ? restart : 0;
   for (int i = restart >= 0 ? restart * p.ninterm : 0; i <= p.ntot; i++) {
+    if (torques && (rc = fargo_update_log(ctx, timestep)) != FARGO_OK) break;
     if (p.ninterm > 0 && (i / p.ninterm) * p.ninterm == i) {
+      timestep = i / p.ninterm;
       std::printf("\n*** OUTPUT %d ***\n", i / p.ninterm);
       if ((rc = fargo_write_outputs(ctx, i / p.ninterm)) != FARGO_OK) break;
     }

@@ -831,7 +831,7 @@ int fargo_step_DT(fargo_ctx *c, int *nsub) {
   return device_error(c);
 }
 
-int fargo_learned_view(fargo_ctx *c, LearnedView *v) {
+int fargo_disk_view(fargo_ctx *c, DiskView *v) {
   if (!c || !v) return FARGO_ERR_STATE;
   int rc = read_ctl(c);
   if (rc) return rc;
@@ -957,6 +957,42 @@ int fargo_write_dims(fargo_ctx *c) {
   int rc;
   if ((rc = host_write_used_rad(c->P, c->h))) return set_err(c, rc, "cannot write used_rad.dat");
   if ((rc = host_write_dims(c->P, c->nb))) return set_err(c, rc, "cannot write dims.dat");
+  return FARGO_OK;
+}
+
+// UpdateLog src/Force.cu:19-84: smoothing and Hill radius of each planet as
+// there (RocheSmoothing or Compute_smoothing), ComputeForce, the rows.
+int fargo_update_log(fargo_ctx *c, int timestep) {
+  if (!c) return FARGO_ERR_STATE;
+  int rc;
+  if ((rc = read_ctl(c))) return rc;
+  const Ctl k = *c->pin_ctl;
+  const DevParams &P = c->dp;
+  const std::string dir = c->P.outputdir;
+  const int L = FARGO_FORCE_LEVELS;
+  for (int b = 0; b < k.nb; b++) {
+    const double x = k.x[b], y = k.y[b], vx = k.vx[b], vy = k.vy[b], m = k.mass[b];
+    const double r = sqrt(x * x + y * y), a = sqrt(x * x + y * y);
+    const double rh = pow(m / 3., 1. / 3.) * a + 1e-15;
+    const double sm = P.roche_smoothing ? r * pow(m / 3., 1. / 3.) * P.rochesmoothing
+                                        : fargo_smoothing(P, r, k.PhysicalTime, k.PhysicalTimeInitial);
+    double gf[4 * FARGO_FORCE_LEVELS];
+    if ((rc = fargo_compute_force(c, x, y, sm, m, a, rh, gf))) return rc;
+    const double fxi = gf[0], fxei = gf[L - 1], fxo = gf[L], fxeo = gf[2 * L - 1];
+    const double fyi = gf[2 * L], fyei = gf[3 * L - 1], fyo = gf[3 * L], fyeo = gf[4 * L - 1];
+    const double row[9] = {x * fyi - y * fxi,   x * fyo - y * fxo,   x * fyei - y * fxei,   x * fyeo - y * fxeo,
+                           vx * fxi + vy * fyi, vx * fxo + vy * fyo, vx * fxei + vy * fyei, vx * fxeo + vy * fyeo,
+                           k.PhysicalTime};
+    if ((rc = host_append_row(dir, "tqwk" + std::to_string(b) + ".dat", timestep, row, 9)))
+      return set_err(c, rc, "cannot write tqwk file");
+    if (c->P.self_gravity) continue;
+    for (int l = 0; l < L; l++) {
+      const double lr[5] = {x * gf[2 * L + l] - y * gf[l], x * gf[3 * L + l] - y * gf[L + l],
+                            vx * gf[l] + vy * gf[2 * L + l], vx * gf[L + l] + vy * gf[3 * L + l], k.PhysicalTime};
+      if ((rc = host_append_row(dir, "tqwk" + std::to_string(b) + "_" + std::to_string(l) + ".dat", timestep, lr, 5)))
+        return set_err(c, rc, "cannot write tqwk file");
+    }
+  }
   return FARGO_OK;
 }
 

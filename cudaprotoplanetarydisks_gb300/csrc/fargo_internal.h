@@ -58,9 +58,10 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
 DevParams host_dev_params(const fargo_params &p, int nb);
 long fargo_nearest_pow2(long n);
 
-// Device view of a context for the learned correction (fargo_learned.cu); the
-// call reads the control block (synchronises the context's stream)
-struct LearnedView {
+// Device view of a context for the kernels outside the step (the learned
+// correction, fargo_learned.cu; the disk-force diagnostic, fargo_force_diag.cu);
+// the call reads the control block (synchronises the context's stream)
+struct DiskView {
   void *dens, *vrad, *vtheta;   // fields, (nrad + 1) * nsec elements of esize bytes
   int esize, nrad, nsec;
   void *stream;                 // the context's cudaStream_t
@@ -72,7 +73,7 @@ struct LearnedView {
   double *ring;
   void *cand;
 };
-extern "C" int fargo_learned_view(fargo_ctx *c, LearnedView *v);
+extern "C" int fargo_disk_view(fargo_ctx *c, DiskView *v);
 
 // output.cpp
 int host_write_field(const std::string &outdir, const char *name, int index, const double *data, size_t n);
@@ -84,3 +85,4 @@ int host_read_field(const std::string &outdir, const char *name, int index, doub
 int host_read_planet_row(const std::string &outdir, int k, int index, fargo_planet &b, double *lost_mass,
                          double *physical_time, double *omega_frame);
 int host_truncate_planet_file(const std::string &outdir, int k, int index);
+int host_append_row(const std::string &outdir, const std::string &file, int index, const double *v, int nv);

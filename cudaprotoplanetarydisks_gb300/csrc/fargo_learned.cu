@@ -281,9 +281,9 @@ int fargo_learned_loss(const float *y, const float *target, const double *surf, 
 // Sets the coarse disk's density and velocities to the restriction of the fine
 // disk's (fine grid = factor x the coarse one in both directions, same extent).
 int fargo_learned_restrict(fargo_ctx *fine, fargo_ctx *coarse, int factor) {
-  LearnedView f, c;
+  DiskView f, c;
   int rc;
-  if ((rc = fargo_learned_view(fine, &f)) || (rc = fargo_learned_view(coarse, &c))) return rc;
+  if ((rc = fargo_disk_view(fine, &f)) || (rc = fargo_disk_view(coarse, &c))) return rc;
   if (factor < 1 || f.nrad != factor * c.nrad || f.nsec != factor * c.nsec || f.esize != c.esize)
     return FARGO_ERR_INVALID;
   const size_t nc = (size_t)(c.nrad + 1) * c.nsec;
@@ -307,10 +307,10 @@ int fargo_learned_restrict(fargo_ctx *fine, fargo_ctx *coarse, int factor) {
 }
 
 int fargo_learned_features_ctx(fargo_ctx *ctx, const float *norm, void *x) {
-  LearnedView v;
+  DiskView v;
   int rc;
   if (!norm || !x) return FARGO_ERR_INVALID;
-  if ((rc = fargo_learned_view(ctx, &v))) return rc;
+  if ((rc = fargo_disk_view(ctx, &v))) return rc;
   rc = fargo_learned_features(v.esize, v.dens, v.vrad, v.vtheta, v.rmed_dev, v.nrad, v.nsec, v.planet_phi, norm, x,
                               v.stream);
   const cudaError_t e = cudaStreamSynchronize((cudaStream_t)v.stream);
@@ -318,10 +318,10 @@ int fargo_learned_features_ctx(fargo_ctx *ctx, const float *norm, void *x) {
 }
 
 int fargo_learned_density(fargo_ctx *ctx, float *out) {
-  LearnedView v;
+  DiskView v;
   int rc;
   if (!out) return FARGO_ERR_INVALID;
-  if ((rc = fargo_learned_view(ctx, &v))) return rc;
+  if ((rc = fargo_disk_view(ctx, &v))) return rc;
   const int n = v.nrad * v.nsec;
   const cudaStream_t s = (cudaStream_t)v.stream;
   if (v.esize == 4) k_density_out<float><<<(n + 255) / 256, 256, 0, s>>>((const float *)v.dens, n, out);
@@ -333,11 +333,11 @@ int fargo_learned_density(fargo_ctx *ctx, float *out) {
 // every cell stays positive and |sum ds Surf| <= 1e-5 sum |ds| Surf (+1e-300);
 // *accepted = 1 then, else 0 and the density is unchanged.  *dmass: sum ds Surf.
 int fargo_learned_apply(fargo_ctx *ctx, const float *ds, int *accepted, double *dmass) {
-  LearnedView v;
+  DiskView v;
   int rc;
   if (!ds || !accepted) return FARGO_ERR_INVALID;
   *accepted = 0;
-  if ((rc = fargo_learned_view(ctx, &v))) return rc;
+  if ((rc = fargo_disk_view(ctx, &v))) return rc;
   const size_t n = (size_t)v.nrad * v.nsec;
   const double *surf = v.surf_dev;
   double *ring = v.ring;

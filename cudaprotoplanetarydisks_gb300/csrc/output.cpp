@@ -128,3 +128,15 @@ int host_truncate_planet_file(const std::string &outdir, int k, int index) {
   std::fclose(f);
   return FARGO_OK;
 }
+
+// One row "index\tv0\tv1..." (%.18g) appended to OUTPUTDIR/<file>
+int host_append_row(const std::string &outdir, const std::string &file, int index, const double *v, int nv) {
+  const std::string fname = outdir + file;
+  FILE *f = std::fopen(fname.c_str(), "a");
+  if (!f) return FARGO_ERR_IO;
+  std::fprintf(f, "%d", index);
+  for (int q = 0; q < nv; q++) std::fprintf(f, "\t%.18g", v[q]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  return FARGO_OK;
+}

@@ -226,6 +226,25 @@ int  fargo_write_dims(fargo_ctx *ctx);
    index * NINTERM * DT. */
 int  fargo_restart(fargo_ctx *ctx, int index);
 
+/* ---- disk forces and the torque logs --------------------------------------- */
+#define FARGO_FORCE_LEVELS 11   /* dimfxy, src/Main.cu:74 */
+/* ComputeForce (src/Force.cu:102-131, ComputeForceKernel src/Kernels.cu:693-729):
+   the disk's force on the point (x, y) with the given smoothing, split into inner
+   (Rmed < a) and outer cells and over FARGO_FORCE_LEVELS Hill cuts (level k
+   weights a cell by 1 - exp(-d^2 / (rh k / (levels - 1))^2); level 0 is uncut).
+   global_force: 4 * FARGO_FORCE_LEVELS doubles, fx inner [k], fx outer
+   [levels + k], fy inner [2 levels + k], fy outer [3 levels + k] (the reference's
+   GlobalForce).  mass is unused, as in the reference.  Synchronous. */
+int  fargo_compute_force(fargo_ctx *ctx, double x, double y, double smoothing, double mass, double a, double rh,
+                         double *global_force);
+/* UpdateLog (src/Force.cu:19-84; the reference's call is commented out at
+   src/Main.cu:315): for every planet k, appends to OUTPUTDIR/tqwk<k>.dat the row
+   timestep, the torques of the inner, outer, Hill-cut inner and Hill-cut outer
+   disk, the same four powers, PhysicalTime; without self-gravity also, per
+   level l, to tqwk<k>_<l>.dat: timestep, inner and outer torque, inner and
+   outer power, PhysicalTime.  Synchronous. */
+int  fargo_update_log(fargo_ctx *ctx, int timestep);
+
 /* ---- measurement (no counterpart in the reference) ----------------------- */
 /* Runs reps hydro substeps launch by launch with a CUDA event after every kernel
    and returns the mean device time (ms) of each kernel of one substep, in launch
