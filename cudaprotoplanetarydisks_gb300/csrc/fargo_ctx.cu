@@ -296,7 +296,7 @@ int build_graph(fargo_ctx *c) {
   g_probe = nullptr;
   CK(cudaStreamEndCapture(c->stream, &body));
   c->launches_per_substep = probe.count / per_body;
-  CK(cudaGraphInstantiate(&c->exec, g, 0));
+  CK(cudaGraphInstantiate(&c->exec, g, cudaGraphInstantiateFlagUseNodePriority));
   c->graph = g;
   c->cond_handle = a.cond_handle;
   return FARGO_OK;
@@ -667,22 +667,30 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   if (npd && npd[0] == '1') c->use_pad = false;
   const char *sgg = std::getenv("FARGO_SG_GENERIC");
   if (sgg && sgg[0] == '1') c->sg_generic = true;
+  // stream priorities (FARGO_PRIO): 0 all equal; 1 the hydro chain and the
+  // planets above the self-gravity transforms; 2 the transforms above the rest.
+  // The caller's stream keeps its own priority.
+  int prio_lo = 0, prio_hi = 0, prio_mode = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  const char *pr = std::getenv("FARGO_PRIO");
+  if (pr) prio_mode = std::atoi(pr);
+  const int p_main = prio_mode == 1 ? prio_hi : prio_lo, p_sg = prio_mode == 2 ? prio_hi : prio_lo;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {
     c->stream = (cudaStream_t)stream;
   } else {
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, p_main);
     if (e != cudaSuccess) {
       delete c;
       return FARGO_ERR_CUDA;
     }
     c->own_stream = true;
   }
-  e = cudaStreamCreateWithFlags(&c->side.s, cudaStreamNonBlocking);
+  e = cudaStreamCreateWithPriority(&c->side.s, cudaStreamNonBlocking, p_main);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side.s2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->side.s2, cudaStreamNonBlocking, p_sg);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.fork2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->side.join2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost((void **)&c->pin_ctl, sizeof(Ctl));

@@ -147,14 +147,15 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
 // ahead of the ring mean (one memory latency, a few load instructions).  V4 = 0:
 // any nsec, 256 threads, cells j = tid, tid + 256, ... streamed.  Every sum runs
 // in a fixed order, so each instance is deterministic.
-// Per ring the CTA also forms the two time-step limits and folds them into the
-// control block's minima (64-bit integer atomicMin on the bit patterns of
-// non-negative doubles: order-free, so deterministic): C/sqrt(max S) of its cells
-// (rings >= 1) and the shear limit 2 pi C / nsec / |Omega_i - Omega_i+1| (rings <
-// nrad - 1), with Omega_i+1 from the mean of ring i+1 summed in the same order as
-// ring i+1's own CTA sums it.  The minimum over rings of these correctly rounded,
-// monotone maps equals the map of the extreme S or difference, so the result is
-// that of one sqrt and one divide of the maxima, and the last CTA reads two words.
+// Per ring the CTA also folds the arguments of the two time-step limits into the
+// control block's maxima (64-bit integer atomicMax on the bit patterns of
+// positive doubles: order-free, so deterministic): the largest S of its cells
+// (rings >= 1; limit C/sqrt(S)) and |Omega_i - Omega_i+1| (rings < nrad - 1; limit
+// 2 pi C / nsec / |...|), with Omega_i+1 from the mean of ring i+1 summed in the
+// same order as ring i+1's own CTA sums it.  Both limits are correctly rounded,
+// monotone non-increasing maps, so the smallest limit over the rings is the map
+// of the largest argument: the last CTA takes one sqrt and two divides of the two
+// words it reads, and no other CTA waits on an FP64 divide.
 template <class T, int V4>
 __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
   pdl_enter();
@@ -411,12 +412,12 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
     T m = s_mx[0];
     for (int k = 1; k < nw; k++) m = (s_mx[k] > m) ? s_mx[k] : m;
     const double S = (double)m;
-    if (S > 0.0) atomicMin(&c->ring_min[0], __double_as_longlong(div_once(CFLSECURITY, sqrt_once(S))));
+    if (S > 0.0) atomicMax(&c->ring_max[0], __double_as_longlong(S));
   }
   if (shear_ring && tid == 64) {
     // NaN differences are skipped (d > 0 is false), as fmin skips them
     const double d = fabs(s_om[0] - s_om[1]);
-    if (d > 0.0) atomicMin(&c->ring_min[1], __double_as_longlong(div_once(a.shear_k, d)));
+    if (d > 0.0) atomicMax(&c->ring_max[1], __double_as_longlong(d));
   }
   // last block: CFL decision, force totals
   __threadfence();
@@ -435,12 +436,13 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
     if (lane == 0) s_acc[w] = tot;
   }
   if (do_cfl && (tid == 64 || tid == 65)) {
-    // smallest per-ring step (CFL over the rings i >= 1, shear over i < nrad - 1),
-    // reset for the next launch
+    // smallest per-ring step (CFL over the rings i >= 1, shear over i < nrad - 1)
+    // from the largest argument; the maxima reset for the next launch
     const int k = tid - 64;
-    const long long m = __ldcg(&c->ring_min[k]);
-    c->ring_min[k] = FARGO_RING_NO_LIMIT;
-    s_dtc[k] = (m == FARGO_RING_NO_LIMIT) ? 1e30 : __longlong_as_double(m);
+    const long long m = __ldcg(&c->ring_max[k]);
+    c->ring_max[k] = FARGO_RING_NO_LIMIT;
+    const double x = __longlong_as_double(m);
+    s_dtc[k] = (m == FARGO_RING_NO_LIMIT) ? 1e30 : k == 0 ? div_once(CFLSECURITY, sqrt_once(x)) : div_once(a.shear_k, x);
   }
   __syncthreads();
   if (tid == 0) {
@@ -1475,7 +1477,7 @@ __global__ void k_dt_begin(Ctl *c) {
   c->err = 0;
   c->ticket = 0u;
   c->padding = 0;
-  c->ring_min[0] = c->ring_min[1] = FARGO_RING_NO_LIMIT;
+  c->ring_max[0] = c->ring_max[1] = FARGO_RING_NO_LIMIT;
 }
 
 // ---------------------------------------------------------------------------

@@ -39,8 +39,10 @@ inline void probe_mark(cudaStream_t s, const char *name) {
   g_probe->count++;
 }
 
-// Kernel launch, with the programmatic-stream-serialization attribute when pdl
-// is set (the kernel begins with pdl_enter()).
+// Kernel launch with the stream's priority as the launch's own (so that a graph
+// captured from the stream keeps it per node), and the
+// programmatic-stream-serialization attribute when pdl is set (the kernel begins
+// with pdl_enter()).
 template <typename... Exp, typename... Act>
 inline void launch_k(int pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                      Act &&...args) {
@@ -49,11 +51,15 @@ inline void launch_k(int pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute at[2];
+  int prio = 0;
+  cudaStreamGetPriority(s, &prio);
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = prio;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = pdl ? 1 : 0;
+  cfg.numAttrs = pdl ? 2 : 1;
   cudaLaunchKernelEx(&cfg, kern, static_cast<Exp>(args)...);
 }
 

@@ -46,7 +46,7 @@ struct DevParams {
 
 // "No limit" of a per-ring time step: a NaN bit pattern, above every non-negative
 // double (+inf included) when compared as a signed 64-bit integer.
-#define FARGO_RING_NO_LIMIT 0x7ff8000000000000LL
+#define FARGO_RING_NO_LIMIT 0LL  // the bit pattern of +0.0: no ring has a limit
 
 struct Ctl {
   // time state (reference globals PhysicalTime, OmegaFrame, LostMass; AlgoGas locals)
@@ -59,9 +59,10 @@ struct Ctl {
   long long substeps;
   unsigned int ticket;        // last-block-done counter of the CFL/force kernel
   int padding;                // 1: the running substep pads the loop body (dt = 0)
-  // smallest per-ring CFL and shear time steps of the CFL/force kernel, as the
-  // integers of their (non-negative) bit patterns; FARGO_RING_NO_LIMIT between launches
-  long long ring_min[2];
+  // largest per-ring S (sum of squared inverse time steps) and angular-velocity
+  // difference of the CFL/force kernel, as the integers of their (positive) bit
+  // patterns; FARGO_RING_NO_LIMIT between launches
+  long long ring_max[2];
   // dt of the last substep that advanced the disk (a padded substep runs with
   // dt = 0), and the number of padded substeps run
   double dt_sub;
@@ -98,7 +99,7 @@ FARGO_HD void fargo_ctl_mirror(Ctl &c) {
   c.f32[CTL_F_INDY] = (float)c.ind_y;
   c.f32[CTL_F_DOMEGA] = (float)c.domega;
   c.f32[CTL_F_INVDT] = c.dt != 0.0 ? 1.0f / (float)c.dt : 0.0f;
-  c.ring_min[0] = c.ring_min[1] = FARGO_RING_NO_LIMIT;
+  c.ring_max[0] = c.ring_max[1] = FARGO_RING_NO_LIMIT;
 }
 
 // AspectRatioHost / AspectRatioDevice  src/Viscosity.cu:93-107, src/Kernels.cu:1377-1392

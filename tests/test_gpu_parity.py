@@ -137,7 +137,7 @@ def _disk_with_env(params, planets, prec, env):
 
 
 @pytest.mark.parametrize("env", ["FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_ROTATE", "FARGO_NO_SG_AHEAD", "FARGO_NO_PAD",
-                                 "FARGO_AZ_GLOBAL"])
+                                 "FARGO_AZ_GLOBAL", "FARGO_PRIO"])
 def test_code_paths_are_bitwise_identical(env):
     # the conditional-graph DT loop vs the host loop; programmatic dependent
     # launch vs plain launches; the rotated DT loop (each substep launches the
@@ -146,7 +146,8 @@ def test_code_paths_are_bitwise_identical(env):
     # transport vs at the substep start; two substeps per loop iteration (the
     # second one run with dt = 0 once the DT is done) vs one; the shared-memory
     # vs the global-memory ring
-    # buffers of the barrier-per-phase azimuthal kernel
+    # buffers of the barrier-per-phase azimuthal kernel; stream priorities (the
+    # hydro chain above the self-gravity transforms) vs equal ones
     params, planets = small("c2")
     base = {"FARGO_AZ_GENERIC": "1"} if env == "FARGO_AZ_GLOBAL" else {}
     a = _disk_with_env(params, planets, fg.FARGO_FP64, base)
