@@ -271,20 +271,31 @@ def batch_ensemble(ndt=2, n=64):
     import cudaprotoplanetarydisks_gb300 as fg
     disks = fg.c4_disks(n)
     cells = [p.nrad * p.nsec for p, _ in disks]
-    b = fg.Batch(disks, fg.FARGO_FP32_BULK)
-    b.run_async(1)
-    b.sync()
-    s0 = [d.scalars().substeps for d in b.disks]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    b.run_async(ndt)
-    b.sync()
-    t32 = time.perf_counter() - t0
-    cu32 = sum((d.scalars().substeps - s0[k]) * cells[k] for k, d in enumerate(b.disks))
-    dens32 = [d.field("dens")[:-1] for d in b.disks]
-    launches32 = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
-                     for k, d in enumerate(b.disks))
-    b.close()
+
+    def batched(variant):
+        b = fg.Batch(disks, fg.FARGO_FP32_BULK, variant=variant)
+        b.run_async(1)
+        b.sync()
+        s0 = [d.scalars().substeps for d in b.disks]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run_async(ndt)
+        b.sync()
+        t = time.perf_counter() - t0
+        cu = sum((d.scalars().substeps - s0[k]) * cells[k] for k, d in enumerate(b.disks))
+        dens = [d.field("dens")[:-1] for d in b.disks]
+        launches = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
+                       for k, d in enumerate(b.disks))
+        b.close()
+        return t, cu, dens, launches
+
+    t32, cu32, dens32, launches32 = batched(None)
+    # the schedule autotuner (fargo_batch_autotune), then the tuned variant timed as above
+    t_tune = time.perf_counter()
+    variant, r_best, r_default = fg.autotune(disks, fg.FARGO_FP32_BULK, ndt=1)
+    t_tune = time.perf_counter() - t_tune
+    tt, cut, dens_t, _ = batched(variant)
+    assert all(np.array_equal(x, y) for x, y in zip(dens32, dens_t))  # variants change speed only
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     t64, cu64, err = 0.0, 0, []
     for k, (p, pl) in enumerate(disks):
@@ -305,6 +316,8 @@ def batch_ensemble(ndt=2, n=64):
                         "alpha, one planet each (configs c4_disks)",
             "cells": sum(cells), "dts_per_disk": ndt,
             "fp32_batched": {"value": v32, "unit": METRIC, "seconds": t32, "gpu_launches_approx": launches32},
+            "fp32_batched_autotuned": {"value": cut / tt, "unit": METRIC, "seconds": tt, "variant": variant.as_dict(),
+                                       "search": {"seconds": t_tune, "rate_default": r_default, "rate_kept": r_best}},
             "fp64_plain_sequential": {"value": v64, "unit": METRIC, "seconds": t64},
             "ratio_fp32_batched_to_fp64_plain": v32 / v64,
             "fp32_dens_rel_l2_vs_fp64_max": max(err), "fp32_dens_rel_l2_vs_fp64_median": float(np.median(err)),

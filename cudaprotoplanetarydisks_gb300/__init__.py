@@ -12,7 +12,7 @@ import numpy as np
 from . import _capi
 from ._capi import (FARGO_FP32_BULK, FARGO_FP64, FIELDS, FORCE_LEVELS, SUB_BOUNDARY, SUB_ENERGY,  # noqa: F401
                     SUB_POTENTIAL, SUB_SOUNDSPEED, SUB_SOURCE, SUB_TEMPERATURE, SUB_TRANSPORT,
-                    FargoParams, FargoPlanet, FargoScalars)
+                    FargoParams, FargoPlanet, FargoScalars, FargoVariant)
 from .config import c4_disks, default_params, load_config, read_par, read_planets  # noqa: F401
 
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -151,20 +151,49 @@ class Disk:
         self._check(self.lib.fargo_update_log(self.h, int(timestep)), "update_log")
 
 
+def _batch_arrays(disks):
+    n = len(disks)
+    params = (FargoParams * n)(*[p for p, _ in disks])
+    flat = [pl for _, pls in disks for pl in pls]
+    planets = (FargoPlanet * max(1, len(flat)))(*flat)
+    counts = (ctypes.c_int * n)(*[len(pls) for _, pls in disks])
+    return params, planets, counts
+
+
+def default_variant():
+    """The default execution variant (with the FARGO_* switches applied)."""
+    v = FargoVariant()
+    _capi.load().fargo_variant_default(ctypes.byref(v))
+    return v
+
+
+def autotune(disks, precision=FARGO_FP32_BULK, ndt=2):
+    """fargo_batch_autotune: the fastest execution variant of this ensemble, with
+    its rate and the default's (cell-updates/s)."""
+    params, planets, counts = _batch_arrays(disks)
+    v = FargoVariant()
+    best, dflt = ctypes.c_double(), ctypes.c_double()
+    rc = _capi.load().fargo_batch_autotune(len(disks), params, planets, counts, precision, int(ndt), ctypes.byref(v),
+                                          ctypes.byref(best), ctypes.byref(dflt))
+    if rc != _capi.FARGO_OK:
+        raise FargoError(f"fargo_batch_autotune: status {rc}")
+    return v, best.value, dflt.value
+
+
 class Batch:
     """An ensemble of independent disks (fargo_batch_*): each disk keeps its own
     fields, CFL step and DT graph; the batch runs the disks' graphs side by side.
-    disks: a list of (params, planets)."""
+    disks: a list of (params, planets); variant: a FargoVariant for every disk
+    (None: the default), e.g. the one autotune() returns."""
 
-    def __init__(self, disks, precision=FARGO_FP32_BULK):
+    def __init__(self, disks, precision=FARGO_FP32_BULK, variant=None):
         self.lib = _capi.load()
         n = len(disks)
-        params = (FargoParams * n)(*[p for p, _ in disks])
-        flat = [pl for _, pls in disks for pl in pls]
-        planets = (FargoPlanet * max(1, len(flat)))(*flat)
-        counts = (ctypes.c_int * n)(*[len(pls) for _, pls in disks])
+        params, planets, counts = _batch_arrays(disks)
         h = ctypes.c_void_p()
-        rc = self.lib.fargo_batch_create(n, params, planets, counts, precision, ctypes.byref(h))
+        rc = self.lib.fargo_batch_create_variant(n, params, planets, counts, precision,
+                                                 ctypes.byref(variant) if variant is not None else None,
+                                                 ctypes.byref(h))
         if rc != _capi.FARGO_OK:
             raise FargoError(f"fargo_batch_create failed with status {rc}")
         self.h = h

@@ -71,6 +71,15 @@ class FargoPlanet(ctypes.Structure):
                 ("feel_disk", _I), ("feel_others", _I)]
 
 
+class FargoVariant(ctypes.Structure):
+    """fargo_variant: the execution variant of a context (bitwise-equal results)."""
+    _fields_ = [("graph", ctypes.c_int), ("pdl", ctypes.c_int), ("pad", ctypes.c_int), ("sg_ahead", ctypes.c_int),
+                ("rotate", ctypes.c_int), ("az_generic", ctypes.c_int), ("priority", ctypes.c_int)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class FargoScalars(ctypes.Structure):
     _fields_ = [("physical_time", _D), ("omega_frame", _D), ("lost_mass", _D),
                 ("last_dt", _D), ("substeps", ctypes.c_longlong), ("last_cfl", _I), ("nb", _I),
@@ -114,6 +123,13 @@ SIGNATURES = [
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),
     ("fargo_batch_create", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),
                                 _I, ctypes.POINTER(_P)]),
+    ("fargo_batch_create_variant", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet),
+                                        ctypes.POINTER(_I), _I, ctypes.POINTER(FargoVariant), ctypes.POINTER(_P)]),
+    ("fargo_batch_autotune", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),
+                                  _I, _I, ctypes.POINTER(FargoVariant), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    ("fargo_variant_default", None, [ctypes.POINTER(FargoVariant)]),
+    ("fargo_ctx_create_variant", _I, [ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), _I, _I, _P,
+                                      ctypes.POINTER(FargoVariant), ctypes.POINTER(_P)]),
     ("fargo_batch_destroy", None, [_P]),
     ("fargo_batch_size", _I, [_P]),
     ("fargo_batch_disk", _P, [_P, _I]),

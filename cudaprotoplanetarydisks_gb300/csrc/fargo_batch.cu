@@ -8,6 +8,7 @@
 // kernels are one partial wave each).  Nothing is shared between disks but the
 // device, so a disk's results are bitwise those of the same disk run alone.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -24,6 +25,11 @@ extern "C" {
 
 int fargo_batch_create(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
                        int precision, fargo_batch **out) {
+  return fargo_batch_create_variant(n, params, planets, nplanets, precision, nullptr, out);
+}
+
+int fargo_batch_create_variant(int n, const fargo_params *params, const fargo_planet *planets,
+                               const int *nplanets, int precision, const fargo_variant *v, fargo_batch **out) {
   if (!out || n <= 0 || !params || !nplanets) return FARGO_ERR_INVALID;
   *out = nullptr;
   fargo_batch *b = new fargo_batch();
@@ -34,8 +40,8 @@ int fargo_batch_create(int n, const fargo_params *params, const fargo_planet *pl
       return FARGO_ERR_INVALID;
     }
     fargo_ctx *c = nullptr;
-    const int rc = fargo_ctx_create(&params[k], nplanets[k] ? planets + off : nullptr, nplanets[k], precision,
-                                    nullptr, &c);
+    const int rc = fargo_ctx_create_variant(&params[k], nplanets[k] ? planets + off : nullptr, nplanets[k],
+                                            precision, nullptr, v, &c);
     if (rc != FARGO_OK) {
       fargo_batch_destroy(b);
       return rc;
@@ -123,6 +129,74 @@ int fargo_batch_advance(fargo_batch *b, double t_end, long long *nsub, int *fail
     tot += s.substeps - s0[k];
   }
   if (nsub) *nsub = tot;
+  return FARGO_OK;
+}
+
+// Cell updates per second of the disks in variant v: a fresh batch, one warm-up
+// DT, then ndt DTs on every disk
+static int batch_rate(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
+                      int precision, const fargo_variant &v, int ndt, double *rate) {
+  fargo_batch *b = nullptr;
+  int rc = fargo_batch_create_variant(n, params, planets, nplanets, precision, &v, &b);
+  if (rc != FARGO_OK) return rc;
+  std::vector<long long> s0(n);
+  if ((rc = fargo_batch_run_async(b, 1)) == FARGO_OK) rc = fargo_batch_sync(b);
+  for (int k = 0; k < n && rc == FARGO_OK; k++) {
+    fargo_scalars s;
+    rc = fargo_get_scalars(b->disks[k], &s);
+    s0[k] = s.substeps;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  if (rc == FARGO_OK && (rc = fargo_batch_run_async(b, ndt)) == FARGO_OK) rc = fargo_batch_sync(b);
+  const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  double cells = 0.0;
+  for (int k = 0; k < n && rc == FARGO_OK; k++) {
+    fargo_scalars s;
+    rc = fargo_get_scalars(b->disks[k], &s);
+    cells += (double)(s.substeps - s0[k]) * params[k].nrad * params[k].nsec;
+  }
+  fargo_batch_destroy(b);
+  if (rc == FARGO_OK) *rate = t > 0.0 ? cells / t : 0.0;
+  return rc;
+}
+
+int fargo_batch_autotune(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
+                         int precision, int ndt, fargo_variant *best, double *rate_best, double *rate_default) {
+  if (!best || n <= 0 || !params || !nplanets || ndt < 1) return FARGO_ERR_INVALID;
+  fargo_variant v;
+  fargo_variant_default(&v);
+  double r = 0.0;
+  int rc = batch_rate(n, params, planets, nplanets, precision, v, ndt, &r);
+  if (rc != FARGO_OK) return rc;
+  if (rate_default) *rate_default = r;
+  bool sg = false;
+  for (int k = 0; k < n; k++) sg = sg || params[k].self_gravity;
+  // one knob at a time: every other value of the knob on the best variant so far
+  struct Knob {
+    int fargo_variant::*field;
+    int nvals;  // values 0 .. nvals - 1
+    bool on;
+  } knobs[] = {{&fargo_variant::pad, 2, true},
+               {&fargo_variant::priority, 3, true},
+               {&fargo_variant::sg_ahead, 2, sg},
+               {&fargo_variant::pdl, 2, true}};
+  for (const Knob &kn : knobs) {
+    if (!kn.on) continue;
+    const fargo_variant base = v;
+    for (int val = 0; val < kn.nvals; val++) {
+      if (val == base.*kn.field) continue;
+      fargo_variant cand = base;
+      cand.*kn.field = val;
+      double cr = 0.0;
+      if ((rc = batch_rate(n, params, planets, nplanets, precision, cand, ndt, &cr)) != FARGO_OK) return rc;
+      if (cr > r * 1.005) {
+        r = cr;
+        v = cand;
+      }
+    }
+  }
+  *best = v;
+  if (rate_best) *rate_best = r;
   return FARGO_OK;
 }
 

@@ -67,6 +67,7 @@ struct fargo_ctx {
   bool use_sg_ahead = true;   // ring transforms of the next substep beside the end of this one
   bool use_pad = true;        // two substeps per loop body, the second padded (dt = 0) after the DT's last
   bool sg_generic = false;    // run-time FFT plans only (the compile-time ones compared in the tests)
+  bool az_generic = false;    // barrier-per-phase azimuthal kernel instead of the register-blocked one
 };
 
 namespace {
@@ -368,8 +369,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     size_t need = (size_t)AZ_NARR_HOST * p.nsec * E, need4 = (size_t)13 * p.nsec * E;
     const char *fg = std::getenv("FARGO_AZ_GLOBAL");  // force the global-memory ring buffers
     const bool force_global = fg && fg[0] == '1';
-    const char *fs = std::getenv("FARGO_AZ_GENERIC");  // force the barrier-per-phase kernel
-    const bool force_generic = force_global || (fs && fs[0] == '1');
+    const bool force_generic = force_global || c->az_generic;  // the barrier-per-phase kernel
     // register-blocked kernel when its ring fits in shared memory (threads: nsec / 4,
     // at most 768 for FP32 and 512 for FP64 fields)
     if (!force_generic && p.nsec % 4 == 0 && p.nsec / 4 <= (E == 4 ? 768 : 512) && need4 + 1024 <= (size_t)maxsm) {
@@ -644,9 +644,35 @@ void *field_ptr(fargo_ctx *c, int which) {
 
 extern "C" {
 
+static bool env_on(const char *name) {
+  const char *v = std::getenv(name);
+  return v && v[0] == '1';
+}
+
+void fargo_variant_default(fargo_variant *v) {
+  if (!v) return;
+  v->graph = env_on("FARGO_NO_GRAPH") ? 0 : 1;
+  v->pdl = env_on("FARGO_NO_PDL") ? 0 : 1;
+  v->pad = env_on("FARGO_NO_PAD") ? 0 : 1;
+  v->sg_ahead = env_on("FARGO_NO_SG_AHEAD") ? 0 : 1;
+  v->rotate = env_on("FARGO_ROTATE") ? 1 : 0;
+  v->az_generic = env_on("FARGO_AZ_GENERIC") ? 1 : 0;
+  const char *pr = std::getenv("FARGO_PRIO");
+  v->priority = pr ? std::atoi(pr) : 0;
+}
+
 int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb, int precision, void *stream,
                      fargo_ctx **out) {
+  return fargo_ctx_create_variant(p, planets, nb, precision, stream, nullptr, out);
+}
+
+int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets, int nb, int precision, void *stream,
+                             const fargo_variant *variant, fargo_ctx **out) {
   if (!p || !out || nb < 0 || nb > FARGO_MAXPL || (nb > 0 && !planets)) return FARGO_ERR_INVALID;
+  fargo_variant v;
+  if (variant) v = *variant;
+  else fargo_variant_default(&v);
+  if (v.priority < 0 || v.priority > 2) return FARGO_ERR_INVALID;
   if (precision != FARGO_FP64 && precision != FARGO_FP32_BULK) return FARGO_ERR_INVALID;
   if (p->nrad < 8 || p->nsec < 8 || !p->is_disk || !(p->dt > 0.0)) return FARGO_ERR_INVALID;
   fargo_ctx *c = new fargo_ctx();
@@ -655,26 +681,19 @@ int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
   c->precision = precision;
   c->esize = precision == FARGO_FP64 ? 8 : 4;
   c->dp = host_dev_params(*p, nb);
-  const char *ng = std::getenv("FARGO_NO_GRAPH");
-  if (ng && ng[0] == '1') c->use_graph = false;
-  const char *np = std::getenv("FARGO_NO_PDL");
-  if (np && np[0] == '1') c->use_pdl = false;
-  const char *nr = std::getenv("FARGO_ROTATE");
-  if (nr && nr[0] == '1') c->use_rotation = true;
-  const char *na = std::getenv("FARGO_NO_SG_AHEAD");
-  if (na && na[0] == '1') c->use_sg_ahead = false;
-  const char *npd = std::getenv("FARGO_NO_PAD");
-  if (npd && npd[0] == '1') c->use_pad = false;
-  const char *sgg = std::getenv("FARGO_SG_GENERIC");
-  if (sgg && sgg[0] == '1') c->sg_generic = true;
-  // stream priorities (FARGO_PRIO): 0 all equal; 1 the hydro chain and the
-  // planets above the self-gravity transforms; 2 the transforms above the rest.
-  // The caller's stream keeps its own priority.
-  int prio_lo = 0, prio_hi = 0, prio_mode = 0;
+  c->use_graph = v.graph != 0;
+  c->use_pdl = v.pdl != 0;
+  c->use_rotation = v.rotate != 0;
+  c->use_sg_ahead = v.sg_ahead != 0;
+  c->use_pad = v.pad != 0;
+  c->az_generic = v.az_generic != 0;
+  c->sg_generic = env_on("FARGO_SG_GENERIC");  // a parity-test switch, not a variant
+  // stream priorities: 0 all equal; 1 the hydro chain and the planets above the
+  // self-gravity transforms; 2 the transforms above the rest.  The caller's
+  // stream keeps its own priority.
+  int prio_lo = 0, prio_hi = 0;
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-  const char *pr = std::getenv("FARGO_PRIO");
-  if (pr) prio_mode = std::atoi(pr);
-  const int p_main = prio_mode == 1 ? prio_hi : prio_lo, p_sg = prio_mode == 2 ? prio_hi : prio_lo;
+  const int p_main = v.priority == 1 ? prio_hi : prio_lo, p_sg = v.priority == 2 ? prio_hi : prio_lo;
   int rc = FARGO_OK;
   cudaError_t e;
   if (stream) {

@@ -165,6 +165,24 @@ int  fargo_planets_read(const char *cfgfile, const fargo_params *p,
    stream: a cudaStream_t to launch on, or NULL for a context-owned stream. */
 int  fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
                       int precision, void *stream, fargo_ctx **out);
+/* Execution variants of a context: every combination gives bitwise the same
+   results (the step's schedule changes, not its arithmetic). */
+typedef struct {
+  int graph;       /* 1: one CUDA graph per DT, CFL loop on the device; 0: host loop */
+  int pdl;         /* programmatic dependent launch between the step kernels */
+  int pad;         /* two substeps per loop iteration, the second with dt = 0 after the DT's last */
+  int sg_ahead;    /* the next substep's self-gravity ring transforms beside the end of this one */
+  int rotate;      /* rotated DT loop (self-gravity of each substep launched by the previous one) */
+  int az_generic;  /* barrier-per-phase azimuthal transport instead of the register-blocked one */
+  int priority;    /* 0 equal stream priorities; 1 hydro chain above self-gravity; 2 the reverse */
+} fargo_variant;
+/* The default variant, with the FARGO_NO_GRAPH, FARGO_NO_PDL, FARGO_NO_PAD,
+   FARGO_NO_SG_AHEAD, FARGO_ROTATE, FARGO_AZ_GENERIC and FARGO_PRIO switches
+   applied (fargo_ctx_create uses it). */
+void fargo_variant_default(fargo_variant *v);
+/* fargo_ctx_create with an explicit variant (NULL: the default). */
+int  fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets, int nb, int precision,
+                              void *stream, const fargo_variant *v, fargo_ctx **out);
 void fargo_ctx_destroy(fargo_ctx *ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char *fargo_last_error(const fargo_ctx *ctx);
@@ -277,6 +295,19 @@ int  fargo_condition_cfl_noalloc(const double *vrad, const double *vtheta, const
 typedef struct fargo_batch fargo_batch;
 int  fargo_batch_create(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
                         int precision, fargo_batch **out);
+/* The same with every disk in variant v (NULL: the default). */
+int  fargo_batch_create_variant(int n, const fargo_params *params, const fargo_planet *planets,
+                                const int *nplanets, int precision, const fargo_variant *v, fargo_batch **out);
+/* Autotuner of the ensemble's schedule: starting from the default variant, tries
+   the alternatives of one knob at a time (padding, stream priorities, the
+   self-gravity schedule when a disk has self-gravity, programmatic launch), each
+   on a fresh batch of these disks (one warm-up DT, then ndt DTs on every disk,
+   host clock around enqueue and synchronisation), and keeps an alternative that
+   raises the batch's cell-updates/s by more than 0.5%.  *best: the variant kept;
+   *rate_best, *rate_default (may be NULL): its rate and the default's.  The
+   variants give identical results, so the choice changes speed only. */
+int  fargo_batch_autotune(int n, const fargo_params *params, const fargo_planet *planets, const int *nplanets,
+                          int precision, int ndt, fargo_variant *best, double *rate_best, double *rate_default);
 void fargo_batch_destroy(fargo_batch *b);
 int  fargo_batch_size(const fargo_batch *b);
 /* Context of disk k (owned by the batch), for fields, planets and scalars. */

@@ -62,3 +62,36 @@ def test_invalid_create_is_rejected_without_gpu_work():
     assert lib.fargo_ctx_create(ctypes.byref(p), None, 0, 7, None, ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
     assert lib.fargo_ctx_create(ctypes.byref(p), None, -1, 0, None, ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
     assert lib.fargo_last_error(None) == b"no context"
+
+
+def test_variant_layout_and_default_switches(monkeypatch):
+    prog = ["#include <stdio.h>", '#include "fargo_gb300.h"',
+            'int main(void){printf("%zu\\n", sizeof(fargo_variant)); return 0;}']
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "v.c")
+        open(c, "w").write("\n".join(prog))
+        exe = os.path.join(d, "v")
+        subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        size = int(subprocess.run([exe], capture_output=True, text=True, check=True).stdout)
+    assert size == ctypes.sizeof(_capi.FargoVariant)
+    lib = _capi.load()
+    for name in ("FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_NO_PAD", "FARGO_NO_SG_AHEAD", "FARGO_ROTATE",
+                 "FARGO_AZ_GENERIC", "FARGO_PRIO"):
+        monkeypatch.delenv(name, raising=False)
+    v = _capi.FargoVariant()
+    lib.fargo_variant_default(ctypes.byref(v))
+    assert v.as_dict() == {"graph": 1, "pdl": 1, "pad": 1, "sg_ahead": 1, "rotate": 0, "az_generic": 0,
+                           "priority": 0}
+    monkeypatch.setenv("FARGO_NO_PAD", "1")
+    monkeypatch.setenv("FARGO_ROTATE", "1")
+    monkeypatch.setenv("FARGO_PRIO", "2")
+    lib.fargo_variant_default(ctypes.byref(v))
+    assert (v.pad, v.rotate, v.priority, v.graph) == (0, 1, 2, 1)
+    # an unknown priority mode is rejected before any device call
+    p = _capi.FargoParams()
+    lib.fargo_params_default(ctypes.byref(p))
+    p.nrad = 64
+    v.priority = 5
+    h = ctypes.c_void_p()
+    assert lib.fargo_ctx_create_variant(ctypes.byref(p), None, 0, 0, None, ctypes.byref(v),
+                                        ctypes.byref(h)) == _capi.FARGO_ERR_INVALID

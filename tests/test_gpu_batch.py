@@ -47,3 +47,27 @@ def test_advance_reaches_t_end_on_every_disk():
     # a second call with the same t_end does nothing
     assert batch.advance(t_end) == 0
     batch.close()
+
+
+def test_batch_variant_is_bitwise_the_default():
+    disks = small_ensemble(3)
+    v = fg.default_variant()
+    v.pad, v.priority, v.pdl = 0, 1, 0
+    a = fg.Batch(disks, fg.FARGO_FP32_BULK)
+    b = fg.Batch(disks, fg.FARGO_FP32_BULK, variant=v)
+    for x in (a, b):
+        x.run_async(2)
+        x.sync()
+    for k in range(len(disks)):
+        for name in ("dens", "vrad", "vtheta"):
+            assert np.array_equal(a.disk(k).field(name), b.disk(k).field(name)), (k, name)
+    a.close()
+    b.close()
+
+
+def test_autotune_keeps_a_variant_at_least_as_fast():
+    disks = small_ensemble(4)
+    v, best, default = fg.autotune(disks, fg.FARGO_FP32_BULK, ndt=1)
+    assert best >= default > 0
+    assert set(v.as_dict()) == {"graph", "pdl", "pad", "sg_ahead", "rotate", "az_generic", "priority"}
+    assert v.priority in (0, 1, 2) and v.pad in (0, 1) and v.pdl in (0, 1)
