@@ -52,7 +52,7 @@ struct fargo_ctx {
   int rad1[16], nst1 = 0, rad0[16], nst0 = 0;
   size_t az_smem = 0;
   int az_regs = 0;
-  double *staging = nullptr;   // FP64 staging buffer of host <-> device transfers
+  double *staging = nullptr;   // FP64 staging slots of host <-> device transfers (FP32 fields)
   double *lx_rmed = nullptr, *lx_surf = nullptr, *lx_ring = nullptr;  // learned correction (first use)
   void *lx_cand = nullptr;
   int launches_per_substep = 0, launches_per_dt = 0;
@@ -190,33 +190,53 @@ int dev_alloc(fargo_ctx *c, void **p, size_t bytes) {
 
 // host FP64 -> device T (FP32 fields are converted on the device from an FP64
 // staging buffer, so the host side always moves FP64 arrays)
-int upload(fargo_ctx *c, void *dst, const double *src, size_t n) {
-  if (c->esize == 8 || !c->staging || n > c->h.size_grid) {
-    if (c->esize == 8) {
-      CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
-    } else {
-      std::vector<float> tmp(n);
-      for (size_t k = 0; k < n; k++) tmp[k] = (float)src[k];
-      CK(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
-      CK(cudaStreamSynchronize(c->stream));
-    }
+// Enqueues one host -> device transfer on the context's stream; FP32 fields go
+// through staging slot `slot` (one field each, so that the transfers of one call
+// need no synchronisation between them).  The caller synchronises the stream
+// before the host array may change.
+static int upload_async(fargo_ctx *c, void *dst, const double *src, size_t n, int slot) {
+  if (c->esize == 8) {
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+  } else if (!c->staging || n > c->h.size_grid || slot >= FARGO_STAGING_SLOTS) {
+    std::vector<float> tmp(n);
+    for (size_t k = 0; k < n; k++) tmp[k] = (float)src[k];
+    CK(cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
   } else {
-    CK(cudaMemcpyAsync(c->staging, src, n * 8, cudaMemcpyHostToDevice, c->stream));
-    launch_convert_from_f64(c->staging, dst, n, (int)c->esize, c->stream);
+    double *st = c->staging + (size_t)slot * c->h.size_grid;
+    CK(cudaMemcpyAsync(st, src, n * 8, cudaMemcpyHostToDevice, c->stream));
+    launch_convert_from_f64(st, dst, n, (int)c->esize, c->stream);
     CK(cudaGetLastError());
   }
+  return FARGO_OK;
+}
+
+static int download_async(fargo_ctx *c, double *dst, const void *src, size_t n, int slot) {
+  if (c->esize == 8) {
+    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    if (slot >= FARGO_STAGING_SLOTS) {  // reuse slot 0 after the transfers before it
+      CK(cudaStreamSynchronize(c->stream));
+      slot = 0;
+    }
+    double *st = c->staging + (size_t)slot * c->h.size_grid;
+    launch_convert_to_f64(src, st, n, (int)c->esize, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst, st, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  return FARGO_OK;
+}
+
+int upload(fargo_ctx *c, void *dst, const double *src, size_t n) {
+  int rc = upload_async(c, dst, src, n, 0);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 
 int download(fargo_ctx *c, double *dst, const void *src, size_t n) {
-  if (c->esize == 8) {
-    CK(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToHost, c->stream));
-  } else {
-    launch_convert_to_f64(src, c->staging, n, (int)c->esize, c->stream);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(dst, c->staging, n * 8, cudaMemcpyDeviceToHost, c->stream));
-  }
+  int rc = download_async(c, dst, src, n, 0);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
@@ -360,7 +380,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   if ((rc = dev_alloc(c, &c->sinFt, (size_t)p.nsec * E))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->ring_force, n1 * (FARGO_MAXPL + 1) * 2 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->lostbydisk, (size_t)p.nsec * 8))) return rc;
-  if (c->esize == 4 && (rc = dev_alloc(c, (void **)&c->staging, sg * 8))) return rc;
+  if (c->esize == 4 && (rc = dev_alloc(c, (void **)&c->staging, FARGO_STAGING_SLOTS * sg * 8))) return rc;
   // azimuthal transport ring buffers: shared memory when they fit
   {
     int dev = 0, maxsm = 0;
@@ -752,26 +772,28 @@ void fargo_ctx_destroy(fargo_ctx *c) {
 
 const char *fargo_last_error(const fargo_ctx *c) { return c ? c->err.c_str() : "no context"; }
 
+// All requested fields enqueued back to back, one synchronisation per call
 int fargo_get_fields(fargo_ctx *c, double *dens, double *vrad, double *vtheta, double *energy, double *temperature) {
   if (!c) return FARGO_ERR_STATE;
   const size_t n = c->h.size_grid;
-  int rc;
-  if (dens && (rc = download(c, dens, c->dens, n))) return rc;
-  if (vrad && (rc = download(c, vrad, c->vrad, n))) return rc;
-  if (vtheta && (rc = download(c, vtheta, c->vtheta, n))) return rc;
-  if (energy && (rc = download(c, energy, c->energy, n))) return rc;
-  if (temperature && (rc = download(c, temperature, c->temperature, n))) return rc;
+  double *dst[5] = {dens, vrad, vtheta, energy, temperature};
+  const void *src[5] = {c->dens, c->vrad, c->vtheta, c->energy, c->temperature};
+  int rc, slot = 0;
+  for (int k = 0; k < 5; k++)
+    if (dst[k] && (rc = download_async(c, dst[k], src[k], n, slot++))) return rc;
+  CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 
 int fargo_set_fields(fargo_ctx *c, const double *dens, const double *vrad, const double *vtheta, const double *energy) {
   if (!c) return FARGO_ERR_STATE;
   const size_t n = c->h.size_grid;
-  int rc;
-  if (dens && (rc = upload(c, c->dens, dens, n))) return rc;
-  if (vrad && (rc = upload(c, c->vrad, vrad, n))) return rc;
-  if (vtheta && (rc = upload(c, c->vtheta, vtheta, n))) return rc;
-  if (energy && (rc = upload(c, c->energy, energy, n))) return rc;
+  const double *src[4] = {dens, vrad, vtheta, energy};
+  void *dst[4] = {c->dens, c->vrad, c->vtheta, c->energy};
+  int rc, slot = 0;
+  for (int k = 0; k < 4; k++)
+    if (src[k] && (rc = upload_async(c, dst[k], src[k], n, slot++))) return rc;
+  CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 

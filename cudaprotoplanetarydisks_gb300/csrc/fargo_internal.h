@@ -36,6 +36,9 @@ enum RingTab {
   RT_COUNT
 };
 
+// FP64 staging slots (one field each) of a context's FP32 host <-> device transfers
+#define FARGO_STAGING_SLOTS 4
+
 struct HostState {
   int nrad = 0, nsec = 0;
   size_t size_grid = 0;
