@@ -114,6 +114,27 @@ __global__ void k_divergence(const float *__restrict__ y, const double *__restri
   ds[q] = scale * ((yr0 - yr1 * s1) + (yp0 - yp1));
 }
 
+// Ring-neutral projection of the radial outputs: y_r(i, .) minus its mean over
+// the ring (FP64 sum in a fixed order), in place.  Applied to y before the
+// divergence, every ring's mass change sum_j dSigma Surf_i vanishes, so the
+// azimuthally averaged density is the plain step's; the projection is symmetric,
+// so applied to dL/dy_r it is also its own adjoint.
+__global__ void k_ring_center(float *__restrict__ y2, int nsec) {
+  __shared__ double red[256];
+  const int i = blockIdx.x, tid = threadIdx.x;
+  float *row = y2 + (size_t)i * nsec * 2;
+  double sum = 0.0;
+  for (int j = tid; j < nsec; j += blockDim.x) sum += (double)row[(size_t)j * 2];
+  red[tid] = sum;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (tid < w) red[tid] += red[tid + w];
+    __syncthreads();
+  }
+  const float mean = (float)(red[0] / (double)nsec);
+  for (int j = tid; j < nsec; j += blockDim.x) row[(size_t)j * 2] -= mean;
+}
+
 // e = 2 (dSigma - target) / (n var); per-block sums of (dSigma - target)^2
 __global__ void k_residual(const float *__restrict__ ds, const float *__restrict__ target, int n, float e_scale,
                            float *__restrict__ e, double *__restrict__ part) {
@@ -254,6 +275,12 @@ int fargo_learned_features(int esize, const void *dens, const void *vrad, const 
   else
     k_features<double><<<nb, 128, 0, s>>>((const double *)dens, (const double *)vrad, (const double *)vtheta, rmed,
                                           nrad, nsec, (float)phi_planet, nm, (bf16 *)x);
+  return cudaGetLastError() == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
+}
+
+int fargo_learned_ring_center(float *y, int nrad, int nsec, void *stream) {
+  if (!y || nrad < 1 || nsec < 1) return FARGO_ERR_INVALID;
+  k_ring_center<<<nrad, 256, 0, (cudaStream_t)stream>>>(y, nsec);
   return cudaGetLastError() == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
 }
 

@@ -112,12 +112,15 @@ class Correction:
     """One trained network with its input normalisation (125 means, then 125
     deviations) and output scale.  step_DT advances a coarse disk one DT: the
     plain step, then the network's conservative density correction, applied only
-    when the density stays positive and the mass change at roundoff."""
+    when the density stays positive and the mass change at roundoff.
+    ring_neutral: the radial outputs lose their ring means (fargo_learned_ring_center),
+    so that the correction keeps every ring's mass (the averaged profile)."""
 
-    def __init__(self, mlp, norm, scale):
+    def __init__(self, mlp, norm, scale, ring_neutral=False):
         self.mlp = mlp
         self.norm = np.ascontiguousarray(norm, dtype=np.float32)
         self.scale = float(scale)
+        self.ring_neutral = bool(ring_neutral)
         self.lib = _capi.load()
         self.accepted = 0
         self.rejected = 0
@@ -131,6 +134,8 @@ class Correction:
         """ds = divergence of the network's flux corrections for features x."""
         import torch
         self.mlp.forward(x, y)
+        if self.ring_neutral:
+            ring_center(y, nrad, nsec)
         rc = self.lib.fargo_learned_divergence(ctypes.c_void_p(y.data_ptr()), ctypes.c_void_p(surf.data_ptr()), nrad,
                                                nsec, ctypes.c_float(self.scale), ctypes.c_void_p(ds.data_ptr()), None)
         if rc != _capi.FARGO_OK:
@@ -259,6 +264,13 @@ def _loss_call(lib, y, target, surf, nrad, nsec, scale, inv_var, buf):
         raise RuntimeError(f"fargo_learned_loss: status {rc}")
 
 
+def ring_center(y, nrad, nsec):
+    """fargo_learned_ring_center on the first nrad * nsec rows of y (in place)."""
+    rc = _capi.load().fargo_learned_ring_center(ctypes.c_void_p(y.data_ptr()), nrad, nsec, None)
+    if rc != _capi.FARGO_OK:
+        raise RuntimeError(f"fargo_learned_ring_center: status {rc}")
+
+
 def _buffers(n):
     import torch
     return (torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(n, dtype=torch.float32, device="cuda"),
@@ -271,11 +283,12 @@ def _sample_var(target):
     return max(float((target.double() ** 2).mean().item()), 1e-300)
 
 
-def train(mlp, samples, scale, var=None, epochs=10, lr=2e-3, seed=0):
+def train(mlp, samples, scale, var=None, epochs=10, lr=2e-3, seed=0, ring_neutral=False):
     """Adam on the loss mean((ds - target)^2) / mean(target^2) of one sample (every
     cell of one coarse disk at one DT) per step: each sample weighs the same
     whatever the size of its disk's correction (var: unused, kept for the
-    signature).  Returns the mean loss of every epoch."""
+    signature).  ring_neutral: through the ring-mean projection of the radial
+    outputs (its adjoint is itself).  Returns the mean loss of every epoch."""
     import torch
     lib = _capi.load()
     rng = np.random.default_rng(seed)
@@ -291,8 +304,12 @@ def train(mlp, samples, scale, var=None, epochs=10, lr=2e-3, seed=0):
             x, target, surf, nrad, nsec = samples[k]
             n = nrad * nsec
             mlp.forward(x, y[:n], train=True)
+            if ring_neutral:
+                ring_center(y, nrad, nsec)
             _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / norms[k],
                        [b[:n] if b.dim() and b.shape[0] >= n else b for b in buf])
+            if ring_neutral:
+                ring_center(buf[2], nrad, nsec)
             mlp.backward(x, buf[2][:n])
             mlp.adam(lr_ep)
             acc.append(float(buf[4].item()) / (n * norms[k]))
@@ -301,7 +318,7 @@ def train(mlp, samples, scale, var=None, epochs=10, lr=2e-3, seed=0):
     return epoch_losses
 
 
-def evaluate_loss(mlp, samples, scale, var=None):
+def evaluate_loss(mlp, samples, scale, var=None, ring_neutral=False):
     """Mean over samples of mean((ds - target)^2) / mean(target^2) with the
     network's correction ds; without a correction that ratio is 1."""
     import torch
@@ -314,6 +331,8 @@ def evaluate_loss(mlp, samples, scale, var=None):
         n = nrad * nsec
         v = _sample_var(target)
         mlp.forward(x, y[:n])
+        if ring_neutral:
+            ring_center(y, nrad, nsec)
         _loss_call(lib, y[:n], target, surf, nrad, nsec, scale, 1.0 / v,
                    [b[:n] if b.dim() and b.shape[0] >= n else b for b in buf])
         with_net.append(float(buf[4].item()) / (n * v))
@@ -321,7 +340,7 @@ def evaluate_loss(mlp, samples, scale, var=None):
 
 
 def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, ndt_eval=10, epochs=40, lr=1e-3,
-               seed=2025, sigma_noise=1e-4, reset_every=4):
+               seed=2025, sigma_noise=1e-4, reset_every=4, ring_neutral=True):
     """Coarse disks of nrad x 3 nrad drawn from the ensemble distribution, a
     factor-x finer plain run of each as teacher: train on n_train disks, then on
     n_test held-out disks report the one-DT loss with and without the network and
@@ -342,12 +361,12 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
     scale, var = target_stats(tr)
     mlp = MLP(nrad * 3 * nrad, seed=seed)
     t0 = time.perf_counter()
-    losses = train(mlp, tr, scale, var, epochs=epochs, lr=lr)
+    losses = train(mlp, tr, scale, var, epochs=epochs, lr=lr, ring_neutral=ring_neutral)
     t_train = time.perf_counter() - t0
-    with_net, without = evaluate_loss(mlp, ho, scale, var)
+    with_net, without = evaluate_loss(mlp, ho, scale, var, ring_neutral=ring_neutral)
     del tr, ho
     torch.cuda.empty_cache()
-    corr = Correction(mlp, norm, scale)
+    corr = Correction(mlp, norm, scale, ring_neutral=ring_neutral)
     roll = []
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
     for params, planets in te_disks:
@@ -381,6 +400,7 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
     return {
         "workload": f"{n_train} training and {n_test} held-out disks of the ensemble distribution at "
                     f"{nrad}x{3 * nrad}, teacher {factor * nrad}x{3 * factor * nrad} (plain method, FP32-bulk)",
+        "ring_neutral": bool(ring_neutral),
         "train": {"samples": n_train * ndt_train, "epochs": epochs, "first_epoch_loss": losses[0],
                   "last_epoch_loss": losses[-1],
                   "seconds_data": t_gen, "seconds_training": t_train},

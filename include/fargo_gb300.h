@@ -359,6 +359,12 @@ int  fargo_learned_features(int esize, const void *dens, const void *vrad, const
                             int nrad, int nsec, double phi_planet, const float *norm, void *x_bf16, void *stream);
 int  fargo_learned_divergence(const float *y, const double *surf, int nrad, int nsec, float scale, float *ds,
                               void *stream);
+/* Ring-neutral outputs: subtracts from the radial outputs y[.][0] of every ring
+   their mean over the ring, in place.  Applied to y before fargo_learned_divergence,
+   the correction leaves every ring's mass (the azimuthally averaged density)
+   unchanged; applied to dL/dy after fargo_learned_loss, it gives the gradient
+   through the projection (the projection is its own adjoint). */
+int  fargo_learned_ring_center(float *y, int nrad, int nsec, void *stream);
 int  fargo_learned_loss(const float *y, const float *target, const double *surf, int nrad, int nsec, float scale,
                         float inv_var, float *ds, float *e, float *dy, double *part, double *loss, void *stream);
 /* The coarse disk's density and velocities := the restriction of the fine disk's

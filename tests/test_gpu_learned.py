@@ -1,6 +1,8 @@
 """The stencil MLP's tensor-core kernels against the CPU oracle: forward outputs
 and parameter gradients with the kernels' BF16 rounding points, and a training
 run that lowers the loss."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -132,3 +134,26 @@ def test_learned_correction_gains_on_held_out_disks():
     print(f"held-out loss with the network {with_net:.3f}, without {without:.3f}")
     assert with_net < 0.5 * without
     mlp.close()
+
+
+def test_ring_neutral_correction_keeps_every_ring_mass():
+    rng = np.random.default_rng(21)
+    nrad, nsec = 12, 40
+    n = nrad * nsec
+    y = torch.tensor(rng.normal(0, 1, (n, NOUT)), dtype=torch.float32, device="cuda")
+    y_ref = y.cpu().numpy().astype(np.float64)
+    L.ring_center(y, nrad, nsec)
+    yr = y_ref[:, 0].reshape(nrad, nsec)
+    expect = (yr - yr.mean(axis=1, keepdims=True)).ravel()
+    assert np.allclose(y.cpu().numpy()[:, 0], expect, atol=1e-6)
+    assert np.array_equal(y.cpu().numpy()[:, 1], y_ref[:, 1].astype(np.float32))
+    # the divergence of ring-neutral outputs moves no mass between rings
+    surf = torch.tensor(np.linspace(1e-3, 4e-3, nrad + 1), dtype=torch.float64, device="cuda")
+    ds = torch.empty(n, dtype=torch.float32, device="cuda")
+    rc = L._capi.load().fargo_learned_divergence(ctypes.c_void_p(y.data_ptr()), ctypes.c_void_p(surf.data_ptr()),
+                                                 nrad, nsec, ctypes.c_float(1.0), ctypes.c_void_p(ds.data_ptr()),
+                                                 None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    ring_dm = (ds.cpu().numpy().astype(np.float64).reshape(nrad, nsec)).sum(axis=1)
+    assert np.abs(ring_dm).max() < 1e-4, np.abs(ring_dm).max()
