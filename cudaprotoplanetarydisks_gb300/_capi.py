@@ -147,6 +147,7 @@ SIGNATURES = [
     ("fargo_learned_features", _I, [_I, _P, _P, _P, _P, _I, _I, _D, ctypes.POINTER(ctypes.c_float), _P, _P]),
     ("fargo_learned_divergence", _I, [_P, _P, _I, _I, ctypes.c_float, _P, _P]),
     ("fargo_learned_ring_center", _I, [_P, _I, _I, _P]),
+    ("fargo_learned_divergence_limited", _I, [_P, _P, ctypes.c_float, ctypes.c_float, _P]),
     ("fargo_learned_loss", _I, [_P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P, _P, _P]),
     ("fargo_learned_restrict", _I, [_P, _P, _I]),
     ("fargo_learned_apply", _I, [_P, _P, ctypes.POINTER(_I), ctypes.POINTER(_D)]),

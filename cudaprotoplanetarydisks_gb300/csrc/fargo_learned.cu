@@ -114,6 +114,56 @@ __global__ void k_divergence(const float *__restrict__ y, const double *__restri
   ds[q] = scale * ((yr0 - yr1 * s1) + (yp0 - yp1));
 }
 
+// Positivity limiter of the correction (donor-cell limiting in the manner of
+// flux-corrected transport, Zalesak 1979).  In mass units the correction moves
+// s y_r(i, j) Surf_i through the inner face of (i, j) (into the cell when
+// positive) and s y_phi(i, j) Surf_i through its left face.  R(i, j) = the
+// fraction of its outflows a cell can afford: min(1, beta Sigma Surf_i / outflow).
+// Every face flux is then scaled by the R of its donor cell, so no cell loses more
+// than beta of its mass and each face keeps one flux for both cells (the total
+// mass is conserved as before).
+template <class T>
+__global__ void k_limit_ratio(const float *__restrict__ y, const T *__restrict__ dens,
+                              const double *__restrict__ surf, int nrad, int nsec, float scale, float beta,
+                              float *__restrict__ R) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrad * nsec) return;
+  const int i = q / nsec, j = q % nsec;
+  const double s = scale, Si = surf[i];
+  double out = 0.0;
+  if (i > 0) out += fmax(0.0, -s * y[(size_t)q * 2] * Si);
+  if (i + 1 < nrad) out += fmax(0.0, s * y[((size_t)q + nsec) * 2] * surf[i + 1]);
+  out += fmax(0.0, -s * y[(size_t)q * 2 + 1] * Si);
+  out += fmax(0.0, s * y[((size_t)i * nsec + wrapj(j + 1, nsec)) * 2 + 1] * Si);
+  const double avail = (double)beta * (double)dens[q] * Si;
+  R[q] = out > avail ? (float)(avail / out) : 1.0f;
+}
+
+// dSigma of the limited face fluxes
+__global__ void k_divergence_limited(const float *__restrict__ y, const double *__restrict__ surf,
+                                     const float *__restrict__ R, int nrad, int nsec, float scale,
+                                     float *__restrict__ ds) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nrad * nsec) return;
+  const int i = q / nsec, j = q % nsec;
+  const int jl = wrapj(j - 1, nsec), jr = wrapj(j + 1, nsec);
+  const double s = scale, Si = surf[i];
+  double fin = 0.0, fout = 0.0;
+  if (i > 0) {  // into (i, j) through its inner face; donor (i - 1, j) when positive
+    const double F = s * y[(size_t)q * 2] * Si;
+    fin = F * (F < 0.0 ? R[q] : R[q - nsec]);
+  }
+  if (i + 1 < nrad) {  // out of (i, j) through its outer face; donor (i, j) when positive
+    const double F = s * y[((size_t)q + nsec) * 2] * surf[i + 1];
+    fout = F * (F > 0.0 ? R[q] : R[q + nsec]);
+  }
+  const double G = s * y[(size_t)q * 2 + 1] * Si;  // into (i, j) from (i, j - 1)
+  const double gin = G * (G < 0.0 ? R[q] : R[(size_t)i * nsec + jl]);
+  const double H = s * y[((size_t)i * nsec + jr) * 2 + 1] * Si;  // out of (i, j) into (i, j + 1)
+  const double gout = H * (H > 0.0 ? R[q] : R[(size_t)i * nsec + jr]);
+  ds[q] = (float)((fin - fout + gin - gout) / Si);
+}
+
 // Ring-neutral projection of the radial outputs: y_r(i, .) minus its mean over
 // the ring (FP64 sum in a fixed order), in place.  Applied to y before the
 // divergence, every ring's mass change sum_j dSigma Surf_i vanishes, so the
@@ -276,6 +326,23 @@ int fargo_learned_features(int esize, const void *dens, const void *vrad, const 
     k_features<double><<<nb, 128, 0, s>>>((const double *)dens, (const double *)vrad, (const double *)vtheta, rmed,
                                           nrad, nsec, (float)phi_planet, nm, (bf16 *)x);
   return cudaGetLastError() == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
+}
+
+int fargo_learned_divergence_limited(fargo_ctx *ctx, const float *y, float scale, float beta, float *ds) {
+  if (!y || !ds || !(beta > 0.0f && beta < 1.0f)) return FARGO_ERR_INVALID;
+  DiskView v;
+  int rc;
+  if ((rc = fargo_disk_view(ctx, &v))) return rc;
+  const int n = v.nrad * v.nsec, nb = (n + 255) / 256;
+  const cudaStream_t s = (cudaStream_t)v.stream;
+  float *R = (float *)v.cand;  // scratch: the candidate density of fargo_learned_apply comes later
+  if (v.esize == 4)
+    k_limit_ratio<float><<<nb, 256, 0, s>>>(y, (const float *)v.dens, v.surf_dev, v.nrad, v.nsec, scale, beta, R);
+  else
+    k_limit_ratio<double><<<nb, 256, 0, s>>>(y, (const double *)v.dens, v.surf_dev, v.nrad, v.nsec, scale, beta, R);
+  k_divergence_limited<<<nb, 256, 0, s>>>(y, v.surf_dev, R, v.nrad, v.nsec, scale, ds);
+  if (cudaGetLastError() != cudaSuccess) return FARGO_ERR_CUDA;
+  return cudaStreamSynchronize(s) == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
 }
 
 int fargo_learned_ring_center(float *y, int nrad, int nsec, void *stream) {

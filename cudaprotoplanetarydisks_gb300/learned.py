@@ -114,28 +114,44 @@ class Correction:
     plain step, then the network's conservative density correction, applied only
     when the density stays positive and the mass change at roundoff.
     ring_neutral: the radial outputs lose their ring means (fargo_learned_ring_center),
-    so that the correction keeps every ring's mass (the averaged profile)."""
+    so that the correction keeps every ring's mass (the averaged profile).
+    limiter: beta of fargo_learned_divergence_limited (no cell gives more than that
+    fraction of its mass), or None for the plain divergence."""
 
-    def __init__(self, mlp, norm, scale, ring_neutral=False):
+    def __init__(self, mlp, norm, scale, ring_neutral=False, limiter=None):
         self.mlp = mlp
         self.norm = np.ascontiguousarray(norm, dtype=np.float32)
         self.scale = float(scale)
         self.ring_neutral = bool(ring_neutral)
+        self.limiter = limiter
         self.lib = _capi.load()
         self.accepted = 0
         self.rejected = 0
+        self.rejected_mass = 0
+        self.rejected_positivity = 0
 
     def features(self, disk, x):
         rc = self.lib.fargo_learned_features_ctx(disk.h, _fp(self.norm), ctypes.c_void_p(x.data_ptr()))
         if rc != _capi.FARGO_OK:
             raise RuntimeError(f"fargo_learned_features_ctx: status {rc}")
 
-    def correction(self, x, y, ds, surf, nrad, nsec):
-        """ds = divergence of the network's flux corrections for features x."""
+    def correction(self, x, y, ds, surf, nrad, nsec, disk=None):
+        """ds = divergence of the network's flux corrections for features x (with
+        the limiter on the grid and density of disk, when set)."""
         import torch
         self.mlp.forward(x, y)
         if self.ring_neutral:
             ring_center(y, nrad, nsec)
+        if self.limiter is not None and disk is not None:
+            # the limiter runs on the disk's own stream, which does not wait for
+            # the default stream the network ran on
+            torch.cuda.synchronize()
+            rc = self.lib.fargo_learned_divergence_limited(disk.h, ctypes.c_void_p(y.data_ptr()),
+                                                           ctypes.c_float(self.scale), ctypes.c_float(self.limiter),
+                                                           ctypes.c_void_p(ds.data_ptr()))
+            if rc != _capi.FARGO_OK:
+                raise RuntimeError(f"fargo_learned_divergence_limited: status {rc}")
+            return
         rc = self.lib.fargo_learned_divergence(ctypes.c_void_p(y.data_ptr()), ctypes.c_void_p(surf.data_ptr()), nrad,
                                                nsec, ctypes.c_float(self.scale), ctypes.c_void_p(ds.data_ptr()), None)
         if rc != _capi.FARGO_OK:
@@ -150,7 +166,7 @@ class Correction:
         x, y, ds, surf = work
         n = disk.step_DT()
         self.features(disk, x)
-        self.correction(x, y, ds, surf, disk.nrad, disk.nsec)
+        self.correction(x, y, ds, surf, disk.nrad, disk.nsec, disk)
         acc = ctypes.c_int(0)
         dm = ctypes.c_double(0.0)
         rc = self.lib.fargo_learned_apply(disk.h, ctypes.c_void_p(ds.data_ptr()), ctypes.byref(acc), ctypes.byref(dm))
@@ -160,6 +176,14 @@ class Correction:
             self.accepted += 1
         else:
             self.rejected += 1
+            # which judgement failed: the mass change against the correction's size
+            # (the same test as the library's), else positivity or finiteness
+            size = float((ds[:disk.nrad * disk.nsec].double().view(disk.nrad, disk.nsec).abs()
+                          * surf[:disk.nrad].view(-1, 1)).sum())
+            if abs(dm.value) > 1e-5 * size + 1e-300:
+                self.rejected_mass += 1
+            else:
+                self.rejected_positivity += 1
         return n, bool(acc.value)
 
 
@@ -340,7 +364,7 @@ def evaluate_loss(mlp, samples, scale, var=None, ring_neutral=False):
 
 
 def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, ndt_eval=10, epochs=40, lr=1e-3,
-               seed=2025, sigma_noise=1e-4, reset_every=4, ring_neutral=True):
+               seed=2025, sigma_noise=1e-4, reset_every=4, ring_neutral=True, limiter=0.5):
     """Coarse disks of nrad x 3 nrad drawn from the ensemble distribution, a
     factor-x finer plain run of each as teacher: train on n_train disks, then on
     n_test held-out disks report the one-DT loss with and without the network and
@@ -366,7 +390,7 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
     with_net, without = evaluate_loss(mlp, ho, scale, var, ring_neutral=ring_neutral)
     del tr, ho
     torch.cuda.empty_cache()
-    corr = Correction(mlp, norm, scale, ring_neutral=ring_neutral)
+    corr = Correction(mlp, norm, scale, ring_neutral=ring_neutral, limiter=limiter)
     roll = []
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
     for params, planets in te_disks:
@@ -401,6 +425,7 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
         "workload": f"{n_train} training and {n_test} held-out disks of the ensemble distribution at "
                     f"{nrad}x{3 * nrad}, teacher {factor * nrad}x{3 * factor * nrad} (plain method, FP32-bulk)",
         "ring_neutral": bool(ring_neutral),
+        "limiter": limiter,
         "train": {"samples": n_train * ndt_train, "epochs": epochs, "first_epoch_loss": losses[0],
                   "last_epoch_loss": losses[-1],
                   "seconds_data": t_gen, "seconds_training": t_train},
@@ -410,7 +435,8 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
                                  for k in ("plain", "learned")},
         "profile_err_rel": {k: avg(lambda r, k=k: r["profile_err"][k]) for k in ("plain", "learned")},
         "s_per_dt": {k: avg(lambda r, k=k: r["s_per_dt"][k]) for k in ("fine", "plain", "learned")},
-        "corrections": {"accepted": corr.accepted, "rejected": corr.rejected},
+        "corrections": {"accepted": corr.accepted, "rejected": corr.rejected,
+                        "rejected_mass": corr.rejected_mass, "rejected_positivity": corr.rejected_positivity},
     }
 
 

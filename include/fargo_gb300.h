@@ -365,6 +365,15 @@ int  fargo_learned_divergence(const float *y, const double *surf, int nrad, int 
    unchanged; applied to dL/dy after fargo_learned_loss, it gives the gradient
    through the projection (the projection is its own adjoint). */
 int  fargo_learned_ring_center(float *y, int nrad, int nsec, void *stream);
+/* fargo_learned_divergence on the disk's grid with a positivity limiter
+   (donor-cell, as in flux-corrected transport): every face flux of the
+   correction is scaled by the fraction of its outflows its donor cell can
+   afford, so that no cell loses more than beta (0 < beta < 1) of its current
+   mass; each face keeps one flux, so the total mass is conserved as without the
+   limiter.  Where the corrections are small against the density nothing
+   changes.  Runs on the context's stream: y must be complete when it is
+   called.  Synchronous. */
+int  fargo_learned_divergence_limited(fargo_ctx *ctx, const float *y, float scale, float beta, float *ds);
 int  fargo_learned_loss(const float *y, const float *target, const double *surf, int nrad, int nsec, float scale,
                         float inv_var, float *ds, float *e, float *dy, double *part, double *loss, void *stream);
 /* The coarse disk's density and velocities := the restriction of the fine disk's

@@ -157,3 +157,36 @@ def test_ring_neutral_correction_keeps_every_ring_mass():
     torch.cuda.synchronize()
     ring_dm = (ds.cpu().numpy().astype(np.float64).reshape(nrad, nsec)).sum(axis=1)
     assert np.abs(ring_dm).max() < 1e-4, np.abs(ring_dm).max()
+
+
+def test_limited_correction_keeps_density_positive_and_mass():
+    (params, planets), = small_disks(1, 5)
+    disk = fg.Disk(params, planets, fg.FARGO_FP32_BULK)
+    disk.step_DT()
+    nrad, nsec = params.nrad, params.nsec
+    n = nrad * nsec
+    surf = disk.mesh()[3]
+    surf_d = torch.tensor(surf, dtype=torch.float64, device="cuda")
+    dens = disk.field("dens")[:-1].astype(np.float64)
+    rng = np.random.default_rng(2)
+    y = torch.tensor(rng.normal(0, 1, (n, NOUT)), dtype=torch.float32, device="cuda")
+    lib = L._capi.load()
+    plain = torch.empty(n, dtype=torch.float32, device="cuda")
+    lim = torch.empty(n, dtype=torch.float32, device="cuda")
+    beta = 0.5
+    for scale, big in ((float(dens.mean()), True), (1e-7 * float(dens.mean()), False)):
+        assert lib.fargo_learned_divergence(ctypes.c_void_p(y.data_ptr()), ctypes.c_void_p(surf_d.data_ptr()), nrad,
+                                            nsec, ctypes.c_float(scale), ctypes.c_void_p(plain.data_ptr()), None) == 0
+        assert lib.fargo_learned_divergence_limited(disk.h, ctypes.c_void_p(y.data_ptr()), ctypes.c_float(scale),
+                                                    ctypes.c_float(beta), ctypes.c_void_p(lim.data_ptr())) == 0
+        torch.cuda.synchronize()
+        dp = plain.cpu().numpy().astype(np.float64).reshape(nrad, nsec)
+        dl = lim.cpu().numpy().astype(np.float64).reshape(nrad, nsec)
+        mass_l = (dl * surf[:nrad, None]).sum()
+        assert abs(mass_l) <= 1e-5 * (np.abs(dl) * surf[:nrad, None]).sum()
+        assert (dens + dl >= (1.0 - beta) * dens * (1.0 - 1e-5)).all()
+        if big:
+            assert (dens + dp < 0).any()  # the unlimited correction would empty cells
+        else:
+            assert np.allclose(dl, dp, rtol=1e-5, atol=1e-12 * float(dens.mean()))
+    disk.close()

@@ -53,6 +53,23 @@ def run_pair(params, planets, ndt, fields=("dens", "vrad", "vtheta")):
         ref.close()
 
 
+def test_c1_full_length_matches_oracle():
+    """The isothermal workload at full size over its stated length (200 hydro
+    substeps): the same CFL decisions DT after DT and every field within the bar."""
+    params, planets = fg.load_config("c1")
+    disk = fg.Disk(params, planets, fg.FARGO_FP64)
+    ref = OracleDisk(params, planets)
+    try:
+        while ref.scalars().substeps < 200:
+            assert disk.step_DT() == ref.step_DT()
+            compare(disk, ref, ("dens", "vrad", "vtheta"))
+        compare_planets(disk, ref)
+        assert disk.scalars().substeps == ref.scalars().substeps >= 200
+    finally:
+        disk.close()
+        ref.close()
+
+
 def with_planets(planets, **kw):
     for p in planets:
         for k, v in kw.items():
