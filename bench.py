@@ -66,6 +66,27 @@ def dist_env():
     return world, rank, local
 
 
+def reduce_over_ranks(ms, nsub):
+    """Replicas only: the job's time is the slowest rank's and its work every
+    rank's.  (max of ms, sum of nsub) over the ranks of the default process group
+    (nccl: CUDA tensors; gloo: CPU tensors); the inputs alone without one."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms), float(nsub)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    n = torch.tensor([float(nsub)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(n.item())
+
+
+def job_value(nsub_all, cells, ms_max):
+    """Whole-job cell-updates/s: every rank's cell updates over the slowest time."""
+    return nsub_all * cells / (ms_max * 1e-3)
+
+
 def workload(cfg):
     import cudaprotoplanetarydisks_gb300 as fg
     params, planets = fg.load_config(cfg)
@@ -395,16 +416,8 @@ def run_own(args, world, rank, local):
         ms, nsub, npad = time_device(disk, stream, args.steps, flush)
         barrier()
         clocks = sampler.stop() if sampler else None
-        t = torch.tensor([ms, float(nsub)], dtype=torch.float64, device="cuda")
-        if world > 1:
-            import torch.distributed as dist
-            tmax = t.clone()
-            dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
-            dist.all_reduce(t[1:2], op=dist.ReduceOp.SUM)
-            ms_max, nsub_all = float(tmax[0]), float(t[1])
-        else:
-            ms_max, nsub_all = ms, float(nsub)
-        r = {"ms_total": ms_max, "substeps": nsub_all, "value": nsub_all * cells / (ms_max * 1e-3),
+        ms_max, nsub_all = reduce_over_ranks(ms, nsub)
+        r = {"ms_total": ms_max, "substeps": nsub_all, "value": job_value(nsub_all, cells, ms_max),
              "ms_per_step": ms_max / args.steps, "substeps_per_step": nsub / args.steps}
         sc = disk.scalars()
         # padded substeps (dt = 0, filling a loop body of two) launch their kernels too
