@@ -390,9 +390,9 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     const char *fg = std::getenv("FARGO_AZ_GLOBAL");  // force the global-memory ring buffers
     const bool force_global = fg && fg[0] == '1';
     const bool force_generic = force_global || c->az_generic;  // the barrier-per-phase kernel
-    // register-blocked kernel when its ring fits in shared memory (threads: nsec / 4,
-    // at most 768 for FP32 and 512 for FP64 fields)
-    if (!force_generic && p.nsec % 4 == 0 && p.nsec / 4 <= (E == 4 ? 768 : 512) && need4 + 1024 <= (size_t)maxsm) {
+    // register-blocked kernel when its ring fits in shared memory (chunks of four
+    // cells over at most 768 FP32 / 512 FP64 threads)
+    if (!force_generic && p.nsec % 4 == 0 && need4 + 1024 <= (size_t)maxsm) {
       c->az_smem = need4;
       c->az_regs = 1;
       CK(prepare_kernels<T>(need4, 1));

@@ -1226,11 +1226,13 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   }
 }
 
-// The same transport in registers, for nsec % 4 == 0: thread t owns cells
-// 4t..4t+3 of the ring and reads halos of two cells on either side from shared
-// memory, so each sweep (slopes, upwind interface values and the update of all
-// transported quantities, which depend only on themselves and on the old density)
-// is one pass without barriers.  The first sweep writes a second copy of the
+// The same transport in registers, for nsec % 4 == 0: a thread owns chunks of
+// four cells (chunk k = cells 4k..4k+3; thread t takes chunks t, t + blockDim,
+// ..., one chunk each up to 768 FP32 / 512 FP64 threads, several on wider rings)
+// and reads halos of two cells on either side from shared memory, so each sweep
+// (slopes, upwind interface values and the update of all transported quantities,
+// which depend only on themselves and on the old density) is one pass without
+// barriers.  The first sweep writes a second copy of the
 // ring, the second sweep (or the only one) stores to global memory at the
 // shifted index.  Same per-cell arithmetic as k_transport_azimuthal.
 namespace {
@@ -1238,7 +1240,15 @@ __device__ __forceinline__ int az_wrap(int j, int n) { return j < 0 ? j + n : (j
 }  // namespace
 
 #define AZ4_NARR 13
+// threads of the register kernel: one per chunk of four cells, at most 768 (FP32)
+// or 512 (FP64) (the register budget of one CTA per SM), whole warps
 template <class T>
+inline int az4_threads(int nsec) {
+  const int most = sizeof(T) == 8 ? 512 : 768;
+  const int n = nsec / 4 < most ? nsec / 4 : most;
+  return (n + 31) / 32 * 32;
+}
+template <class T, bool MC>  // MC: several chunks per thread (rings wider than the CTA)
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
   pdl_enter();
   extern __shared__ __align__(16) unsigned char az_smem[];
@@ -1249,8 +1259,15 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   const DevParams &P = a.P;
   const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x;
   const int lane = tid & 31, w = tid >> 5, nw = (blockDim.x + 31) >> 5;
-  const bool own = tid < (nsec >> 2);
-  const int j0 = 4 * tid;
+  const int nchunk = nsec >> 2;
+  // body(j0) for the thread's chunks: one chunk in straight-line code when !MC
+  auto each_chunk = [&](auto &&body) {
+    if (MC) {
+      for (int ch = tid; ch < nchunk; ch += (int)blockDim.x) body(4 * ch);
+    } else if (tid < nchunk) {
+      body(4 * tid);
+    }
+  };
   T *VT = (T *)az_smem;
   T *QA = VT + nsec;           // M0 M1 M2 M3 En Dn, nsec each
   T *QB = QA + 6 * nsec;       // the same after the first sweep
@@ -1271,7 +1288,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   // ring to shared memory; ComputeAverageThetaVelocitiesKernel
   SumAcc<T> vs;
   vs.zero();
-  if (own) {
+  each_chunk([&](int j0) {
     T x[4];
     load4(a.d.vtheta + row + j0, x);
 #pragma unroll
@@ -1286,7 +1303,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
       for (int c = 0; c < 4; c++) QA[f * nsec + j0 + c] = x[c];
     }
-  }
+  });
   warp_sum(vs);
   if (lane == 0) s_part[w] = vs;
   __syncthreads();
@@ -1308,24 +1325,26 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   const bool split = P.fast_transport;  // NoSplitAdvection == NO
   int sh = s_shift % nsec;
   if (sh < 0) sh += nsec;
-  // VthetaRes at cells j0 .. j0+4
-  T vel[5];
-#pragma unroll
-  for (int c = 0; c < 5; c++) {
-    const T vt = own ? VT[az_wrap(j0 + c, nsec)] : (T)0;
-    T vr = s_vm.sub_from(vt);
-    if (!split) vr = vr + vct;
-    vel[c] = vr;
-  }
-  // one sweep (QuantitiesAdvection) from ring Q; out == nullptr: store to global.
+  const RingMean<T> vm = s_vm;
+  // one sweep (QuantitiesAdvection) of the chunk at j0 from ring Q; out == nullptr:
+  // store to global.
   // Per interface c (between cells j0-1+c and j0+c) the upwind side, the
   // coefficient of the upwind slope and the flux factor dxrad ds v are the same
   // for every quantity: formed once, then each quantity adds its slopes, its
   // upwind values and its update.
-  auto sweep = [&](const T *Q, T *out, bool const_vel) {
+  auto sweep = [&](const T *Q, T *out, bool const_vel, int j0) {
+    // VthetaRes at cells j0 .. j0+4
     T v[5];
 #pragma unroll
-    for (int c = 0; c < 5; c++) v[c] = const_vel ? vct : vel[c];
+    for (int c = 0; c < 5; c++) {
+      if (const_vel) {
+        v[c] = vct;
+      } else {
+        T vr = vm.sub_from(VT[az_wrap(j0 + c, nsec)]);
+        if (!split) vr = vr + vct;
+        v[c] = vr;
+      }
+    }
     // StarThetaKernel / StarThetaKernel2 on the density
     T d[8], id[8], dq[6], coef[5], F[5];
     bool upw[5];
@@ -1389,11 +1408,11 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
     }
   };
   if (split) {
-    if (own) sweep(QA, QB, false);
+    each_chunk([&](int j0) { sweep(QA, QB, false, j0); });
     __syncthreads();
-    if (own) sweep(QB, nullptr, true);
+    each_chunk([&](int j0) { sweep(QB, nullptr, true, j0); });
   } else {
-    if (own) sweep(QA, nullptr, false);
+    each_chunk([&](int j0) { sweep(QA, nullptr, false, j0); });
   }
 }
 
@@ -1562,7 +1581,11 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
     launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, RAD_NY), RAD_SMEM(T), s, a);
     MARK("k_transport_radial");
     if (a.az_regs) {
-      launch_k(a.pdl, k_transport_azimuthal4<T>, dim3(P.nrad), dim3((P.nsec / 4 + 31) / 32 * 32), az_smem_bytes, s, a);
+      const int nt4 = az4_threads<T>(P.nsec);
+      if (P.nsec / 4 > nt4)
+        launch_k(a.pdl, k_transport_azimuthal4<T, true>, dim3(P.nrad), dim3(nt4), az_smem_bytes, s, a);
+      else
+        launch_k(a.pdl, k_transport_azimuthal4<T, false>, dim3(P.nrad), dim3(nt4), az_smem_bytes, s, a);
     } else {
       int nt = P.nsec >= 1024 ? 512 : 256;
       a.az_smem = az_smem_bytes > 0;
@@ -1703,7 +1726,8 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
                        (const void *)k_bc_nonreflecting<T>, (const void *)k_bc_evanescent<T>,
                        (const void *)k_source<T>, (const void *)k_visc_tau<T>, (const void *)k_visc_update<T>,
                        (const void *)k_artvisc<T>, (const void *)k_energy<T>, (const void *)k_transport_radial<T>,
-                       (const void *)k_transport_azimuthal<T>, (const void *)k_transport_azimuthal4<T>,
+                       (const void *)k_transport_azimuthal<T>, (const void *)k_transport_azimuthal4<T, false>,
+                       (const void *)k_transport_azimuthal4<T, true>,
                        (const void *)k_velocities<T>, (const void *)k_temperature<T>, (const void *)k_end<T>,
                        (const void *)k_dt_begin};
   cudaError_t e;
@@ -1713,8 +1737,13 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
   e = cudaFuncSetAttribute(k_transport_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM(T));
   if (e != cudaSuccess) return e;
   if (az_smem_bytes == 0) return cudaSuccess;
-  if (az_regs)
-    return cudaFuncSetAttribute(k_transport_azimuthal4<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
+  if (az_regs) {
+    e = cudaFuncSetAttribute(k_transport_azimuthal4<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)az_smem_bytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_transport_azimuthal4<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)az_smem_bytes);
+  }
   return cudaFuncSetAttribute(k_transport_azimuthal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)az_smem_bytes);
 }
 

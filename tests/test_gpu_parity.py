@@ -85,6 +85,9 @@ CASES = {
     "c2_selfgravity_128x384": lambda: (small("c2", nrad=128, nsec=384), 2, ()),
     "c3_adiabatic_cooling": lambda: (small("c3"), 3, ("energy",)),
     "c3_adiabatic_no_cooling": lambda: (small("c3", cooling=0), 2, ("energy",)),
+    # a ring wider than the register azimuthal kernel's CTA (2176 > 4 x 512 FP64
+    # cells): several chunks of four cells per thread
+    "wide_ring_register_chunks": lambda: (small("c1", nrad=24, nsec=2176), 2, ()),
     # boundaries
     "open_inner": lambda: (small("c1", open_inner=1), 2, ()),
     "evanescent": lambda: (small("c1", evanescent=1), 2, ()),
