@@ -134,6 +134,8 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.dtheta = 2.0 * FARGO_PI / (double)c->P.nsec;
   a.inv_nsec = 1.0 / (double)c->P.nsec;
   a.shear_k = 2.0 * FARGO_PI * FARGO_CFLSECURITY / (double)c->P.nsec;
+  a.nr_k1 = pow(c->h.Rinf[1], -1.5) - 1.0;
+  a.nr_k2 = c->P.nrad >= 2 ? pow(c->h.Rinf[c->P.nrad - 2], -1.5) - 1.0 : 0.0;
   {
     const double g = c->P.adiabaticindex;
     a.k64[KC_GM1] = g - 1.0;

@@ -60,6 +60,7 @@ struct KArgs {
   double k64[8];
   float k32[8];
   double lr01, lr12;   // log(Rmed[0]/Rmed[1]), log(Rmed[1]/Rmed[2]) for the Qplus extrapolation
+  double nr_k1, nr_k2; // Rinf[1]^-1.5 - 1 and Rinf[nrad-2]^-1.5 - 1 of the non-reflecting boundary
   int mode;            // CFL/force kernel mode
   int az_smem;         // azimuthal kernel keeps its ring in shared memory
   int az_regs;         // register-blocked azimuthal kernel (nsec % 4 == 0)

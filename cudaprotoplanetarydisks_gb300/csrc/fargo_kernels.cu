@@ -602,88 +602,110 @@ __global__ void k_bc_open(KArgs<T> a) {
 }
 
 // NonReflectingBoundary src/SideEuler.cu:45-76 with kernels src/Kernels.cu:498-607,
-// in one CTA.  NonReflectingBoundaryKernel2 runs nsec2pot threads without a
-// j < nsec guard; its extra threads write Vrad ring 2 (from ring 3) and ring
-// nrad (from ring nrad-1 after its update), as a launch whose threads run in
-// increasing j would.  The sound-speed ring nrad read there is zero.
+// as four launches so that its FP64 work spreads over many SMs (one CTA would
+// run it on one SM's FP64 pipe):
+//   k_bc_nr_means(0): the ring means of the sound speed (rings 0, 1, nrad-1, nrad-2)
+//   k_bc_nr_cells:    the shift of rings 0 and nrad-1 (NonReflectingBoundaryKernel)
+//                     and the Vrad update (NonReflectingBoundaryKernel2)
+//   k_bc_nr_means(1): the ring means of density and energy on rings 0 and nrad-1
+//   k_bc_nr_adjust:   ReduceMean + MinusMeanKernel
+// NonReflectingBoundaryKernel2 runs nsec2pot threads without a j < nsec guard; its
+// extra threads write Vrad ring 2 (from ring 3) and ring nrad (from ring nrad-1
+// after its update), as a launch whose threads run in increasing j would: the
+// thread of cell j does both, reading old values before it writes them.  The
+// sound-speed ring nrad read there is zero.
 template <class T>
-__global__ void __launch_bounds__(1024) k_bc_nonreflecting(KArgs<T> a) {
+__device__ __forceinline__ double nr_cs(const KArgs<T> &a, int i, int j) {
+  const int nsec = a.P.nsec;
+  return a.d.cs ? (double)a.d.cs[(size_t)i * nsec + j] : (i < a.P.nrad ? (double)RT(a, RT_CS, i) : 0.0);
+}
+
+// the two shifts (in sectors) of the boundary rings from the sound-speed means
+template <class T>
+__device__ __forceinline__ void nr_angles(const KArgs<T> &a, const double *m, int &ia, int &ia2) {
+  const int nsec = a.P.nsec, nrad = a.P.nrad;
+  double dangle = a.nr_k1 / (.5 * (m[0] + m[1]));
+  dangle *= (RT64(a, RT_RMED, 1) - RT64(a, RT_RMED, 0));
+  ia = (int)(dangle / 2.0 / PI * (double)nsec + .5);
+  double dangle2 = a.nr_k2 / (.5 * (m[2] + m[3]));
+  dangle2 *= (RT64(a, RT_RMED, nrad - 1) - RT64(a, RT_RMED, nrad - 2));
+  ia2 = (int)(dangle2 / 2.0 / PI * (double)nsec + .5);
+}
+
+// CTA r of 4: the FP64 mean of ring r's quantity into bc_mean[4 which + r]
+template <class T>
+__global__ void __launch_bounds__(256) k_bc_nr_means(KArgs<T> a, int which) {
   pdl_enter();
   __shared__ double s_red[32];
-  __shared__ int s_angle[2];
-  const int nsec = a.P.nsec, nrad = a.P.nrad, tid = threadIdx.x;
+  const int nsec = a.P.nsec, nrad = a.P.nrad, r = blockIdx.x;
+  double s = 0.0;
+  if (which == 0) {
+    const int ring = r == 0 ? 0 : r == 1 ? 1 : r == 2 ? nrad - 1 : nrad - 2;
+    for (int j = threadIdx.x; j < nsec; j += blockDim.x) s += nr_cs(a, ring, j);
+  } else {
+    const T *src = (r & 2 ? a.d.energy : a.d.dens) + (size_t)(r & 1 ? nrad - 1 : 0) * nsec;
+    for (int j = threadIdx.x; j < nsec; j += blockDim.x) s += (double)src[j];
+  }
+  const double tot = block_sum_d(s, s_red);
+  // order of bc_mean[4..7]: density ring 0, density ring nrad-1, energy ring 0, energy ring nrad-1
+  if (threadIdx.x == 0) a.d.ctl->bc_mean[4 * which + r] = tot / nsec;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_bc_nr_cells(KArgs<T> a) {
+  pdl_enter();
+  const int nsec = a.P.nsec, nrad = a.P.nrad;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nsec) return;
   T *D = a.d.dens, *E = a.d.energy, *V = a.d.vrad;
-  const T *CS = a.d.cs;
-  auto cs_at = [&](int i, int j) -> double {
-    return CS ? (double)CS[(size_t)i * nsec + j] : (i < nrad ? (double)RT(a, RT_CS, i) : 0.0);
-  };
   double m[4];
-  const int rings[4] = {0, 1, nrad - 1, nrad - 2};
-  for (int r = 0; r < 4; r++) {
-    double s = 0.0;
-    for (int j = tid; j < nsec; j += blockDim.x) s += cs_at(rings[r], j);
-    m[r] = block_sum_d(s, s_red) / nsec;
-  }
-  if (tid == 0) {
-    auto Rinf = [&](int k) { return RT64(a, RT_RINF, k); };
-    auto Rmed = [&](int k) { return RT64(a, RT_RMED, k); };
-    double dangle = (pow(Rinf(1), -1.5) - 1.0) / (.5 * (m[0] + m[1]));
-    dangle *= (Rmed(1) - Rmed(0));
-    s_angle[0] = (int)(dangle / 2.0 / PI * (double)nsec + .5);
-    double dangle2 = (pow(Rinf(nrad - 2), -1.5) - 1.0) / (.5 * (m[2] + m[3]));
-    dangle2 *= (Rmed(nrad - 1) - Rmed(nrad - 2));
-    s_angle[1] = (int)(dangle2 / 2.0 / PI * (double)nsec + .5);
-  }
-  __syncthreads();
-  const int ia = s_angle[0], ia2 = s_angle[1];
-  // NonReflectingBoundaryKernel: ring 0 from ring 1 (shifted), ring nrad-1 from ring nrad-2
-  for (int j = tid; j < nsec; j += blockDim.x) {
-    // the reference wraps a shift once (|shift| < nsec in practice); a full
-    // modulo keeps every index inside the ring for any shift
-    int t = ((j + ia) % nsec + nsec) % nsec;
-    D[t] = D[nsec + j];
-    E[t] = E[nsec + j];
-    const long ii = nrad - 1;
-    const long src = (ii - 1) * nsec + (((j - ia2) % nsec + nsec) % nsec);
-    D[ii * nsec + j] = D[src];
-    E[ii * nsec + j] = E[src];
-  }
-  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 4; r++) m[r] = a.d.ctl->bc_mean[r];
+  int ia, ia2;
+  nr_angles(a, m, ia, ia2);
+  // NonReflectingBoundaryKernel: ring 0 from ring 1 (shifted), ring nrad-1 from
+  // ring nrad-2; the reference wraps a shift once (|shift| < nsec in practice), a
+  // full modulo keeps every index inside the ring for any shift
+  const int t = ((j + ia) % nsec + nsec) % nsec;
+  D[t] = D[nsec + j];
+  E[t] = E[nsec + j];
+  const long ii = nrad - 1;
+  const long src = (ii - 1) * nsec + (((j - ia2) % nsec + nsec) % nsec);
+  D[ii * nsec + j] = D[src];
+  E[ii * nsec + j] = E[src];
+  // NonReflectingBoundaryKernel2 (ring 1 and ring nrad-1 read only rings 1, 2,
+  // nrad-2, which no thread writes before these reads)
   const double sm1 = RT64(a, RT_SIGMAMED, 1), sm2 = RT64(a, RT_SIGMAMED, nrad - 2);
-  // NonReflectingBoundaryKernel2, threads j < nsec
-  for (int j = tid; j < nsec; j += blockDim.x) {
-    double vm = -cs_at(1, j) * ((double)D[nsec + j] - sm1) / sm1;
-    V[nsec + j] = (T)(2.0 * vm - (double)V[2 * nsec + j]);
-    long ii = nrad - 1;
-    vm = cs_at(ii, j) * ((double)D[(ii - 1) * nsec + j] - sm2) / sm2;
-    V[ii * nsec + j] = (T)(2. * vm - (double)V[(ii - 1) * nsec + j]);
+  const T v2 = V[2 * nsec + j];
+  double vm = -nr_cs(a, 1, j) * ((double)D[nsec + j] - sm1) / sm1;
+  V[nsec + j] = (T)(2.0 * vm - (double)v2);
+  vm = nr_cs(a, (int)ii, j) * ((double)D[(ii - 1) * nsec + j] - sm2) / sm2;
+  const T vlast = (T)(2. * vm - (double)V[(ii - 1) * nsec + j]);
+  V[ii * nsec + j] = vlast;
+  // ... its threads nsec + j < nsec2pot: Vrad ring 2 (after ring 1 read it) and
+  // ring nrad (from ring nrad-1 as just updated, density after the shift)
+  if (j < a.P.nsec2pot - nsec) {
+    vm = -nr_cs(a, 2, j) * ((double)D[2 * nsec + j] - sm1) / sm1;
+    V[2 * nsec + j] = (T)(2.0 * vm - (double)V[3 * nsec + j]);
+    vm = nr_cs(a, nrad, j) * ((double)D[ii * nsec + j] - sm2) / sm2;
+    V[(size_t)nrad * nsec + j] = (T)(2. * vm - (double)vlast);
   }
-  __syncthreads();
-  // ... threads j in [nsec, nsec2pot): flat index past the ring
-  for (int jj = tid; jj < a.P.nsec2pot - nsec; jj += blockDim.x) {
-    double vm = -cs_at(2, jj) * ((double)D[2 * nsec + jj] - sm1) / sm1;
-    V[2 * nsec + jj] = (T)(2.0 * vm - (double)V[3 * nsec + jj]);
-    long ii = nrad;
-    vm = cs_at((int)ii, jj) * ((double)D[(ii - 1) * nsec + jj] - sm2) / sm2;
-    V[ii * nsec + jj] = (T)(2. * vm - (double)V[(ii - 1) * nsec + jj]);
-  }
-  __syncthreads();
-  // ReduceMean + MinusMeanKernel
-  double md[4];
-  const T *src4[4] = {D, D + (size_t)(nrad - 1) * nsec, E, E + (size_t)(nrad - 1) * nsec};
-  for (int r = 0; r < 4; r++) {
-    double s = 0.0;
-    for (int j = tid; j < nsec; j += blockDim.x) s += (double)src4[r][j];
-    md[r] = block_sum_d(s, s_red) / nsec;
-  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_bc_nr_adjust(KArgs<T> a) {
+  pdl_enter();
+  const int nsec = a.P.nsec, nrad = a.P.nrad;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nsec) return;
+  const double *md = a.d.ctl->bc_mean + 4;
+  T *D = a.d.dens, *E = a.d.energy;
   const double s0 = RT64(a, RT_SIGMAMED, 0), s1 = RT64(a, RT_SIGMAMED, nrad - 1);
   const double e0 = RT64(a, RT_ENERGYMED, 0), e1 = RT64(a, RT_ENERGYMED, nrad - 1);
-  for (int j = tid; j < nsec; j += blockDim.x) {
-    D[j] += (T)(s0 - md[0]);
-    E[j] += (T)(e0 - md[2]);
-    D[(size_t)(nrad - 1) * nsec + j] += (T)(s1 - md[1]);
-    E[(size_t)(nrad - 1) * nsec + j] += (T)(e1 - md[3]);
-  }
+  D[j] += (T)(s0 - md[0]);
+  E[j] += (T)(e0 - md[2]);
+  D[(size_t)(nrad - 1) * nsec + j] += (T)(s1 - md[1]);
+  E[(size_t)(nrad - 1) * nsec + j] += (T)(e1 - md[3]);
 }
 
 // EvanescentBoundary src/SideEuler.cu:104-123; kernel src/Kernels.cu:967-1015.
@@ -1680,8 +1702,15 @@ void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
       launch_k(a.pdl, k_soundspeed<T>, dim3(P.nrad), dim3(256), 0, s, a);
       MARK("k_soundspeed");
     }
-    launch_k(a.pdl, k_bc_nonreflecting<T>, dim3(1), dim3(1024), 0, s, a);
-    MARK("k_bc_nonreflecting");
+    const dim3 gj((P.nsec + 255) / 256);
+    launch_k(a.pdl, k_bc_nr_means<T>, dim3(4), dim3(256), 0, s, a, 0);
+    MARK("k_bc_nr_means");
+    launch_k(a.pdl, k_bc_nr_cells<T>, gj, dim3(256), 0, s, a);
+    MARK("k_bc_nr_cells");
+    launch_k(a.pdl, k_bc_nr_means<T>, dim3(4), dim3(256), 0, s, a, 1);
+    MARK("k_bc_nr_means");
+    launch_k(a.pdl, k_bc_nr_adjust<T>, gj, dim3(256), 0, s, a);
+    MARK("k_bc_nr_adjust");
   }
   if (P.evanescent) {
     const dim3 b2(64, 4);
@@ -1723,7 +1752,8 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
   // kernels under programmatic launch can share SMs only with the same split.
   const void *all[] = {(const void *)k_cfl_forces<T, 0>, (const void *)k_cfl_forces<T, 1>, (const void *)k_planets, (const void *)k_soundspeed<T>,
                        (const void *)k_correct_vtheta<T>, (const void *)k_bc_open<T>,
-                       (const void *)k_bc_nonreflecting<T>, (const void *)k_bc_evanescent<T>,
+                       (const void *)k_bc_nr_means<T>, (const void *)k_bc_nr_cells<T>,
+                       (const void *)k_bc_nr_adjust<T>, (const void *)k_bc_evanescent<T>,
                        (const void *)k_source<T>, (const void *)k_visc_tau<T>, (const void *)k_visc_update<T>,
                        (const void *)k_artvisc<T>, (const void *)k_energy<T>, (const void *)k_transport_radial<T>,
                        (const void *)k_transport_azimuthal<T>, (const void *)k_transport_azimuthal4<T, false>,

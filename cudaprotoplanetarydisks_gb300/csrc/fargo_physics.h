@@ -67,6 +67,9 @@ struct Ctl {
   // dt = 0), and the number of padded substeps run
   double dt_sub;
   long long padded;
+  // ring means of the non-reflecting boundary: sound speed of rings 0, 1, nrad-1,
+  // nrad-2, then density and energy of rings 0 and nrad-1 after the shift
+  double bc_mean[8];
   // planetary system (Types.cuh:2-12)
   int nb;
   int pad1;
