@@ -92,7 +92,9 @@ def workload(cfg):
     params, planets = fg.load_config(cfg)
     name = {"c1": "isothermal disk 128x384, 1 planet (fixed orbit)",
             "c2": "self-gravitating disk 256x768, alpha viscosity, migrating planet",
-            "c3": "adiabatic disk with cooling 1024x3072, 1 planet"}.get(cfg, cfg)
+            "c3": "adiabatic disk with cooling 1024x3072, 1 planet",
+            "wide": "adiabatic disk 2048x4096, non-reflecting inner boundary, guiding-center frame, "
+                    "Jupiter-mass planet"}.get(cfg, cfg)
     return params, planets, name
 
 

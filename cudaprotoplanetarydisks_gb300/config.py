@@ -15,6 +15,7 @@ NAMED = {
     "c1": "c1_isothermal.par",
     "c2": "c2_selfgravity.par",
     "c3": "c3_adiabatic.par",
+    "wide": "wide_template4.par",
 }
 
 
@@ -65,7 +66,7 @@ def read_planets(params, par_path=None, cap=64):
 
 
 def load_config(name_or_path, **overrides):
-    """(params, planets) of a named workload (c1, c2, c3) or of a .par path.
+    """(params, planets) of a named workload (c1, c2, c3, wide) or of a .par path.
     Keyword overrides set FargoParams members (e.g. nrad=64, nsec=192)."""
     path = name_or_path
     if name_or_path in NAMED:
