@@ -206,7 +206,7 @@ def ncu_traffic(kernel, cfg, mode="fp32"):
     scale = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
     for line in open(path):
         cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cells) > 4 and cells[0] == kernel:
+        if len(cells) >= 4 and cells[0] == kernel:
             try:
                 rd, ru = cells[2].split()
                 wr, wu = cells[3].split()
