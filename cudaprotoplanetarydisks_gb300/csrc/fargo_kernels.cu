@@ -1313,17 +1313,14 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   each_chunk([&](int j0) {
     T x[4];
     load4(a.d.vtheta + row + j0, x);
+    store4(VT + j0, x);
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-      VT[j0 + c] = x[c];
-      vs.add(x[c]);
-    }
+    for (int c = 0; c < 4; c++) vs.add(x[c]);
 #pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
       load4(src[f] + row + j0, x);
-#pragma unroll
-      for (int c = 0; c < 4; c++) QA[f * nsec + j0 + c] = x[c];
+      store4(QA + f * nsec + j0, x);
     }
   });
   warp_sum(vs);
@@ -1356,13 +1353,22 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
   // upwind values and its update.
   auto sweep = [&](const T *Q, T *out, bool const_vel, int j0) {
     // VthetaRes at cells j0 .. j0+4
+    // shared memory is read in whole chunks (16-byte accesses, no bank conflicts):
+    // the thread's chunk and its neighbours' (the ring wraps chunk by chunk)
+    const int jm = j0 == 0 ? nsec - 4 : j0 - 4, jp = j0 + 4 == nsec ? 0 : j0 + 4;
     T v[5];
+    if (const_vel) {
 #pragma unroll
-    for (int c = 0; c < 5; c++) {
-      if (const_vel) {
-        v[c] = vct;
-      } else {
-        T vr = vm.sub_from(VT[az_wrap(j0 + c, nsec)]);
+      for (int c = 0; c < 5; c++) v[c] = vct;
+    } else {
+      T x[4];
+      load4(VT + j0, x);
+#pragma unroll
+      for (int c = 0; c < 4; c++) v[c] = x[c];
+      v[4] = VT[jp];
+#pragma unroll
+      for (int c = 0; c < 5; c++) {
+        T vr = vm.sub_from(v[c]);
         if (!split) vr = vr + vct;
         v[c] = vr;
       }
@@ -1370,11 +1376,29 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
     // StarThetaKernel / StarThetaKernel2 on the density
     T d[8], id[8], dq[6], coef[5], F[5];
     bool upw[5];
+    // cells j0-2 .. j0+5 of ring quantity f: two of the previous chunk, the
+    // thread's chunk, two of the next
+    // (FP64: element by element, which needs fewer live registers)
+    auto halo8 = [&](const T *qf, T (&h)[8]) {
+      if (sizeof(T) == 4) {
+        T x[4];
+        load4(qf + jm, x);
+        h[0] = x[2];
+        h[1] = x[3];
+        load4(qf + j0, x);
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      d[c] = Q[5 * nsec + az_wrap(j0 - 2 + c, nsec)];
-      id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell
-    }
+        for (int c = 0; c < 4; c++) h[2 + c] = x[c];
+        load4(qf + jp, x);
+        h[6] = x[0];
+        h[7] = x[1];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 8; c++) h[c] = qf[az_wrap(j0 - 2 + c, nsec)];
+      }
+    };
+    halo8(Q + 5 * nsec, d);
+#pragma unroll
+    for (int c = 0; c < 8; c++) id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
@@ -1399,13 +1423,14 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
              : f == 3 ? a.d.thetamomm
              : f == 4 ? a.d.energy
                       : a.d.dens;
-      T wv[8], dw[6], sw[5];
+      T qv[8], wv[8], dw[6], sw[5];
+      halo8(q, qv);
 #pragma unroll
       for (int c = 0; c < 8; c++) {
         // DivisePolarGrid with the density's reciprocal, formed once per cell for
         // every quantity (FP64: one divide per cell instead of one per quantity,
         // within an ulp of q / rho)
-        wv[c] = q[az_wrap(j0 - 2 + c, nsec)] * id[c];
+        wv[c] = qv[c] * id[c];
       }
 #pragma unroll
       for (int k = 0; k < 6; k++) {
@@ -1414,17 +1439,21 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
       }
 #pragma unroll
       for (int c = 0; c < 5; c++) sw[c] = (upw[c] ? wv[c + 1] : wv[c + 2]) + coef[c] * (upw[c] ? dw[c] : dw[c + 1]);
+      T nq[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) {
         const T varq = sw[c] * F[c] - sw[c + 1] * F[c + 1];
-        const T nq = q[j0 + c] + varq * isurf;
-        if (out) {
-          out[f * nsec + j0 + c] = nq;
-        } else {
+        nq[c] = qv[2 + c] + varq * isurf;
+      }
+      if (out) {
+        store4(out + f * nsec + j0, nq);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
           // AdvectSHIFT: out[j] = q[(j - Nshift) mod nsec]
           int jo = j0 + c + sh;
           if (jo >= nsec) jo -= nsec;
-          dst[row + jo] = nq;
+          dst[row + jo] = nq[c];
         }
       }
     }
