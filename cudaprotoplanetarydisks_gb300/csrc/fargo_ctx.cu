@@ -774,15 +774,31 @@ void fargo_ctx_destroy(fargo_ctx *c) {
 
 const char *fargo_last_error(const fargo_ctx *c) { return c ? c->err.c_str() : "no context"; }
 
-// All requested fields enqueued back to back, one synchronisation per call
+// All requested fields enqueued back to back (FP32 fields: one conversion
+// launch through the staging slots), one synchronisation per call
 int fargo_get_fields(fargo_ctx *c, double *dens, double *vrad, double *vtheta, double *energy, double *temperature) {
   if (!c) return FARGO_ERR_STATE;
   const size_t n = c->h.size_grid;
   double *dst[5] = {dens, vrad, vtheta, energy, temperature};
   const void *src[5] = {c->dens, c->vrad, c->vtheta, c->energy, c->temperature};
-  int rc, slot = 0;
-  for (int k = 0; k < 5; k++)
-    if (dst[k] && (rc = download_async(c, dst[k], src[k], n, slot++))) return rc;
+  if (c->esize == 4 && c->staging) {
+    ConvFields p{};
+    double *host[5];
+    for (int k = 0; k < 5; k++)
+      if (dst[k]) {
+        p.src[p.nf] = src[k];
+        p.dst[p.nf] = c->staging + (size_t)p.nf * n;
+        host[p.nf++] = dst[k];
+      }
+    if (p.nf) launch_convert_to_f64_multi(p, n, 4, c->stream);
+    CK(cudaGetLastError());
+    for (int f = 0; f < p.nf; f++)
+      CK(cudaMemcpyAsync(host[f], p.dst[f], n * 8, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    int rc, slot = 0;
+    for (int k = 0; k < 5; k++)
+      if (dst[k] && (rc = download_async(c, dst[k], src[k], n, slot++))) return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
@@ -792,9 +808,22 @@ int fargo_set_fields(fargo_ctx *c, const double *dens, const double *vrad, const
   const size_t n = c->h.size_grid;
   const double *src[4] = {dens, vrad, vtheta, energy};
   void *dst[4] = {c->dens, c->vrad, c->vtheta, c->energy};
-  int rc, slot = 0;
-  for (int k = 0; k < 4; k++)
-    if (src[k] && (rc = upload_async(c, dst[k], src[k], n, slot++))) return rc;
+  if (c->esize == 4 && c->staging) {
+    ConvFields p{};
+    for (int k = 0; k < 4; k++)
+      if (src[k]) {
+        double *st = c->staging + (size_t)p.nf * n;
+        CK(cudaMemcpyAsync(st, src[k], n * 8, cudaMemcpyHostToDevice, c->stream));
+        p.src[p.nf] = st;
+        p.dst[p.nf++] = dst[k];
+      }
+    if (p.nf) launch_convert_from_f64_multi(p, n, 4, c->stream);
+    CK(cudaGetLastError());
+  } else {
+    int rc, slot = 0;
+    for (int k = 0; k < 4; k++)
+      if (src[k] && (rc = upload_async(c, dst[k], src[k], n, slot++))) return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }

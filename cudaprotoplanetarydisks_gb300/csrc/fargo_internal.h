@@ -37,7 +37,7 @@ enum RingTab {
 };
 
 // FP64 staging slots (one field each) of a context's FP32 host <-> device transfers
-#define FARGO_STAGING_SLOTS 4
+#define FARGO_STAGING_SLOTS 5
 
 struct HostState {
   int nrad = 0, nsec = 0;

@@ -1819,6 +1819,27 @@ __global__ void k_convert_to_f64(const T *__restrict__ in, double *__restrict__ 
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
     out[k] = (double)in[k];
 }
+// Several fields in one launch (the fields of one host transfer)
+template <class T>
+__global__ void k_convert_from_f64_multi(ConvFields p, size_t n) {
+  pdl_enter();
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    for (int f = 0; f < p.nf; f++) ((T *)p.dst[f])[k] = (T)((const double *)p.src[f])[k];
+}
+template <class T>
+__global__ void k_convert_to_f64_multi(ConvFields p, size_t n) {
+  pdl_enter();
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    for (int f = 0; f < p.nf; f++) ((double *)p.dst[f])[k] = (double)((const T *)p.src[f])[k];
+}
+void launch_convert_from_f64_multi(const ConvFields &p, size_t n, int esize, cudaStream_t s) {
+  if (esize == 4) k_convert_from_f64_multi<float><<<608, 256, 0, s>>>(p, n);
+  else k_convert_from_f64_multi<double><<<608, 256, 0, s>>>(p, n);
+}
+void launch_convert_to_f64_multi(const ConvFields &p, size_t n, int esize, cudaStream_t s) {
+  if (esize == 4) k_convert_to_f64_multi<float><<<608, 256, 0, s>>>(p, n);
+  else k_convert_to_f64_multi<double><<<608, 256, 0, s>>>(p, n);
+}
 void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s) {
   if (esize == 4) k_convert_from_f64<float><<<608, 256, 0, s>>>(in, (float *)out, n);
   else k_convert_from_f64<double><<<608, 256, 0, s>>>(in, (double *)out, n);

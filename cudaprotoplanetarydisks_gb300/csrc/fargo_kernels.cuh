@@ -65,6 +65,14 @@ inline void launch_k(int pdl, void (*kern)(Exp...), dim3 grid, dim3 block, size_
 
 void launch_convert_from_f64(const double *in, void *out, size_t n, int esize, cudaStream_t s);
 void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cudaStream_t s);
+// up to five fields converted in one launch: src[f] -> dst[f], n elements each
+struct ConvFields {
+  const void *src[5];
+  void *dst[5];
+  int nf;
+};
+void launch_convert_from_f64_multi(const ConvFields &p, size_t n, int esize, cudaStream_t s);
+void launch_convert_to_f64_multi(const ConvFields &p, size_t n, int esize, cudaStream_t s);
 
 // Second and third streams: the planet update of a substep runs beside the hydro
 // kernels (forked after k_cfl_forces, joined at the end of the substep); the
