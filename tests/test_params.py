@@ -117,7 +117,7 @@ Saturn    2.0  3e-4   0.5  YES yes
     assert pl[0].vy == vy and pl[0].vx == -1e-10 * vy
 
 
-@pytest.mark.parametrize("name", ["c1", "c2", "c3"])
+@pytest.mark.parametrize("name", ["c1", "c2", "c3", "wide"])
 def test_shipped_workloads_parse(name):
     p, pl = fg.load_config(name)
     assert p.log_grid == 1 and len(pl) == 1
@@ -126,3 +126,18 @@ def test_shipped_workloads_parse(name):
         assert abs(p.sigma0 * 2 * math.pi * 3.6 - 0.02) < 1e-12
     if name == "c3":
         assert p.adiabatic == 1 and p.cooling == 1 and (p.nrad, p.nsec) == (1024, 3072)
+    if name == "wide":
+        # the reference's in/template4.par setup
+        assert p.adiabatic == 1 and p.cooling == 0 and (p.nrad, p.nsec) == (2048, 4096)
+        assert p.non_reflecting == 1 and p.corotating == 1 and p.guiding_center == 1
+
+
+def test_ensemble_draws_are_seeded():
+    a = fg.c4_disks(8, seed=3)
+    b = fg.c4_disks(8, seed=3)
+    c = fg.c4_disks(8, seed=4)
+    key = lambda d: [(p.nrad, p.nsec, p.alphaviscosity, p.aspectratio, p.sigmaslope, pl[0].mass) for p, pl in d]  # noqa: E731
+    assert key(a) == key(b) != key(c)
+    for p, pl in a:
+        assert p.nsec == 3 * p.nrad and p.nrad in fg.config.C4_NRAD and len(pl) == 1
+        assert 1e-5 <= pl[0].mass <= 3e-3 and 0.03 <= p.aspectratio <= 0.08
