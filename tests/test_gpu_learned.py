@@ -190,3 +190,30 @@ def test_limited_correction_keeps_density_positive_and_mass():
         else:
             assert np.allclose(dl, dp, rtol=1e-5, atol=1e-12 * float(dens.mean()))
     disk.close()
+
+
+@pytest.mark.parametrize("prec", [fg.FARGO_FP32_BULK, fg.FARGO_FP64])
+def test_features_match_oracle(prec):
+    import math
+
+    from oracle import features_ref
+    (params, planets), = small_disks(1, 7)
+    disk = fg.Disk(params, planets, prec)
+    disk.step_DT()
+    n = params.nrad * params.nsec
+    x = torch.empty((n, NIN), dtype=torch.bfloat16, device="cuda")
+    L.Correction(None, L.IDENTITY_NORM, 1.0).features(disk, x)
+    got = x.float().cpu().numpy().astype(np.float64)
+    p = disk.planets()[0]
+    ref = features_ref.features(disk.field("dens"), disk.field("vrad"), disk.field("vtheta"), disk.mesh()[1],
+                                math.atan2(p.y, p.x))
+    disk.close()
+    assert not got[:, 125:].any()
+    diff = np.abs(got - ref)[:, :125].reshape(n, 25, 5)
+    # the azimuth channel wraps at +-1: a cell at the wrap point may land on either side
+    diff[:, :, 4] = np.minimum(diff[:, :, 4], np.abs(diff[:, :, 4] - 2.0))
+    r = np.abs(ref)[:, :125].reshape(n, 25, 5)
+    # BF16 output (relative half-ulp 2^-9; a rounding flip from the FP32 arithmetic
+    # gives one ulp, 2^-8), plus the FP32 arithmetic's absolute error per channel
+    atol = np.array([1e-9, 1e-9, 2e-6, 1e-6, 1e-6])
+    assert (diff <= 2.0 ** -7 * r + atol).all(), float((diff - 2.0 ** -7 * r).max())

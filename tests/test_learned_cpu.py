@@ -39,3 +39,28 @@ def test_oracle_gradient_matches_finite_differences():
         Qm[p] -= h
         fd = (f(Qp) - f(Qm)) / (2 * h)
         assert abs(fd - g[p]) <= 1e-6 * max(1.0, abs(fd)), (p, fd, g[p])
+
+
+def test_feature_oracle_layout():
+    """oracle/features_ref.py against the definition, cell by cell, on a tiny grid."""
+    from oracle import features_ref
+    nrad, nsec = 5, 8
+    rng = np.random.default_rng(0)
+    d = 1.0 + 0.01 * rng.random((nrad + 1, nsec))
+    vr, vt = rng.random((nrad + 1, nsec)), rng.random((nrad + 1, nsec))
+    rm = np.linspace(1.0, 2.0, nrad + 1)
+    f = features_ref.features(d, vr, vt, rm, 0.3)
+    assert f.shape == (nrad * nsec, 128) and not f[:, 125:].any()
+    i, j = 2, 3
+    row = f[i * nsec + j]
+    centre = (2 * 5 + 2) * 5
+    assert np.isclose(row[centre], np.log(d[i, j])) and np.isclose(row[centre + 3], np.log(rm[i]))
+    right = (2 * 5 + 3) * 5  # di = 0, dj = +1
+    assert np.isclose(row[right], d[i, j + 1] / d[i, j] - 1)
+    assert np.isclose(row[right + 1], 0.5 * (vr[i, j + 1] + vr[i + 1, j + 1]))
+    vtc = lambda a, b: 0.5 * (vt[a, b] + vt[a, (b + 1) % nsec])  # noqa: E731
+    assert np.isclose(row[right + 2], vtc(i, j + 1) - vtc(i, j)) and row[right + 3] == 0.0
+    outer = (0 * 5 + 2) * 5  # di = -2 at ring 0 is clamped to ring 0
+    row0 = f[0 * nsec + j]
+    assert np.isclose(row0[outer], 0.0) and row0[outer + 3] == 0.0
+    assert np.all(np.abs(f[:, 4::5][:, :25]) <= 1.0)
