@@ -217,3 +217,23 @@ def test_features_match_oracle(prec):
     # gives one ulp, 2^-8), plus the FP32 arithmetic's absolute error per channel
     atol = np.array([1e-9, 1e-9, 2e-6, 1e-6, 1e-6])
     assert (diff <= 2.0 ** -7 * r + atol).all(), float((diff - 2.0 ** -7 * r).max())
+
+
+def test_divergence_loss_and_adjoint_match_oracle():
+    from oracle import flux_ref
+    rng = np.random.default_rng(31)
+    nrad, nsec, scale, inv_var = 20, 60, 0.37, 2.5
+    n = nrad * nsec
+    surf = np.linspace(1e-3, 5e-3, nrad + 1)
+    y = rng.normal(0, 1, (n, NOUT)).astype(np.float32)
+    target = rng.normal(0, 1, n).astype(np.float32)
+    ds_ref, loss_ref, dy_ref = flux_ref.loss(y, target, surf, nrad, nsec, scale, inv_var)
+    buf = L._buffers(n)
+    L._loss_call(L._capi.load(), torch.tensor(y).cuda(), torch.tensor(target).cuda(),
+                 torch.tensor(surf, dtype=torch.float64).cuda(), nrad, nsec, scale, inv_var, buf)
+    torch.cuda.synchronize()
+    ds, dy, lo = buf[0].cpu().numpy(), buf[2].cpu().numpy(), float(buf[4].item())
+    # FP32 kernels against FP64: a few ulps per value
+    assert rel(ds, ds_ref) < 1e-6
+    assert abs(lo - loss_ref) < 1e-5 * loss_ref
+    assert rel(dy, dy_ref) < 1e-5

@@ -64,3 +64,29 @@ def test_feature_oracle_layout():
     row0 = f[0 * nsec + j]
     assert np.isclose(row0[outer], 0.0) and row0[outer + 3] == 0.0
     assert np.all(np.abs(f[:, 4::5][:, :25]) <= 1.0)
+
+
+def test_flux_oracle_adjoint_and_mass():
+    """oracle/flux_ref.py: the adjoint is the transpose (<D y, e> = <y, D^T e>), the
+    divergence conserves mass (sum dSigma Surf = 0) and the loss gradient matches
+    central finite differences."""
+    from oracle import flux_ref
+    rng = np.random.default_rng(9)
+    nrad, nsec, scale = 6, 10, 0.7
+    surf = np.linspace(1.0, 3.0, nrad + 1)
+    y = rng.normal(0, 1, (nrad * nsec, 2))
+    e = rng.normal(0, 1, nrad * nsec)
+    ds = flux_ref.divergence(y, surf, nrad, nsec, scale)
+    assert abs(np.dot(ds, e) - np.sum(y * flux_ref.adjoint(e, surf, nrad, nsec, scale))) < 1e-10
+    assert abs((ds.reshape(nrad, nsec) * surf[:nrad, None]).sum()) < 1e-12
+    target = rng.normal(0, 1, nrad * nsec)
+    _, _, g = flux_ref.loss(y, target, surf, nrad, nsec, scale, 1.3)
+
+    def f(yy):
+        return flux_ref.loss(yy, target, surf, nrad, nsec, scale, 1.3)[1] * 1.3 / (nrad * nsec)
+
+    for k in ((0, 0), (nsec + 3, 0), (17, 1), (nrad * nsec - 1, 1)):
+        yp, ym = y.copy(), y.copy()
+        yp[k] += 1e-6
+        ym[k] -= 1e-6
+        assert abs((f(yp) - f(ym)) / 2e-6 - g[k]) < 1e-7, k
