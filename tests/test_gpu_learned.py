@@ -237,3 +237,20 @@ def test_divergence_loss_and_adjoint_match_oracle():
     assert rel(ds, ds_ref) < 1e-6
     assert abs(lo - loss_ref) < 1e-5 * loss_ref
     assert rel(dy, dy_ref) < 1e-5
+
+
+@pytest.mark.parametrize("prec,tol", [(fg.FARGO_FP64, 1e-13), (fg.FARGO_FP32_BULK, 2e-7)])
+def test_restriction_matches_oracle(prec, tol):
+    from oracle import flux_ref
+    (params, planets), = fg.c4_disks(1, seed=13, nrad_choices=(12,))
+    fine = fg.Disk(L.fine_params(params, 4), planets, prec)
+    fine.step_DT()
+    coarse = fg.Disk(params, planets, prec)
+    L.restrict(fine, coarse, 4)
+    ref = flux_ref.restrict(fine.field("dens"), fine.field("vrad"), fine.field("vtheta"), fine.mesh()[3], 4)
+    for name, r in zip(("dens", "vrad", "vtheta"), ref):
+        got = coarse.field(name)
+        assert got.shape == r.shape
+        assert np.abs(got - r).max() <= tol * np.abs(r).max(), (name, float(np.abs(got - r).max()))
+    fine.close()
+    coarse.close()

@@ -90,3 +90,19 @@ def test_flux_oracle_adjoint_and_mass():
         yp[k] += 1e-6
         ym[k] -= 1e-6
         assert abs((f(yp) - f(ym)) / 2e-6 - g[k]) < 1e-7, k
+
+
+def test_restriction_oracle_keeps_constants_and_mass():
+    from oracle import flux_ref
+    F, nrad, nsec = 4, 3, 5
+    rng = np.random.default_rng(2)
+    surf = np.linspace(1.0, 2.0, F * nrad + 1)
+    const = np.full((F * nrad + 1, F * nsec), 2.0)
+    d, vr, vt = flux_ref.restrict(const, -0.5 * const, 0.25 * const, surf, F)
+    assert d.shape == vr.shape == vt.shape == (nrad + 1, nsec)
+    assert np.allclose(d, 2.0) and np.allclose(vr, -1.0) and np.allclose(vt, 0.5)
+    # the density restriction is area-weighted: it keeps the mass
+    fd = 1.0 + rng.random((F * nrad + 1, F * nsec))
+    d, _, _ = flux_ref.restrict(fd, fd, fd, surf, F)
+    coarse_surf = F * surf[:F * nrad].reshape(nrad, F).sum(axis=1)
+    assert np.isclose((d[:nrad] * coarse_surf[:, None]).sum(), (fd[:F * nrad] * surf[:F * nrad, None]).sum())
