@@ -468,8 +468,9 @@ def run_own(args, world, rank, local):
         "metric": METRIC, "value": f32["value"], "unit": "cell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 fields and self-gravity FFT; f64 CFL decision, planets, ring means, FARGO split; "
-                 "compensated f32 (float-float) force and ring sums",
+        "dtype": "f32",
+        "precision_detail": "f32 fields and self-gravity FFT; f64 CFL decision, planets, ring means, FARGO "
+                            "split; compensated f32 (float-float) force and ring sums",
         "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
         "config": config_obj(params, wname, args.config,
                              {"precision": "FP32_BULK", "parallelism": f"replicas x{world}",
