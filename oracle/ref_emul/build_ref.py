@@ -57,7 +57,7 @@ def build(force=False):
     if not os.path.isdir(os.path.join(REF, "src")):
         return None
     os.makedirs(os.path.join(OUT, "src"), exist_ok=True)
-    deps = [os.path.join(HERE, f) for f in ("emul.h", "emul.cpp", "noise_wrap.cpp", "build_ref.py")]
+    deps = [os.path.join(HERE, f) for f in ("emul.h", "emul.cpp", "noise_wrap.cpp", "sg_wrap.cpp", "build_ref.py")]
     if not force and os.path.exists(EXE) and all(os.path.getmtime(d) <= os.path.getmtime(EXE) for d in deps):
         return EXE
     inc = ["-include", os.path.join(HERE, "emul.h"), "-I" + os.path.join(HERE, "fake_include"),
@@ -72,15 +72,17 @@ def build(force=False):
         obj = cpp[:-4] + ".o"
         objs.append(obj)
         jobs.append(["g++"] + FLAGS + inc + ["-c", cpp, "-o", obj])
-    for f in ("emul.cpp", "noise_wrap.cpp"):
+    for f in ("emul.cpp", "noise_wrap.cpp", "sg_wrap.cpp"):
         obj = os.path.join(OUT, f[:-4] + ".o")
         objs.append(obj)
-        jobs.append(["g++"] + FLAGS + ["-I" + os.path.join(HERE, "fake_include"), "-c", os.path.join(HERE, f),
+        jobs.append(["g++"] + FLAGS + ["-I" + os.path.join(HERE, "fake_include"),
+                                       "-I" + os.path.join(REF, "include"), "-c", os.path.join(HERE, f),
                                        "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(_compile, jobs))
     link = ["g++", "-fopenmp"] + objs + ["-o", EXE, "-Wl,--wrap=_Z14InitGasDensityPd",
-                                         "-Wl,--wrap=_Z13InitGasEnergyPd"]
+                                         "-Wl,--wrap=_Z13InitGasEnergyPd",
+                                         "-Wl,--wrap=_Z24Init_planetarysys_withSGP16planetary_system"]
     _compile(link)
     return EXE
 

@@ -15,12 +15,18 @@ uint3 threadIdx, blockIdx;
 dim3 blockDim, gridDim;
 double sdata[1 << 16];  // `extern __shared__ double sdata[]` of DeviceReduceKernel
 
+// Every allocation is zero-filled (device memory is zero after allocation in
+// practice) and preceded by a zeroed guard: Update_sgvelocityKernel reads
+// SG_Acct[(j-1)%nsec] = SG_Acct[-1] at i = j = 0 (src/Kernels.cu:930), and here that
+// read sees 0.0, the value the oracle uses, instead of the allocator's bookkeeping.
+constexpr size_t kGuard = 256;
 cudaError_t cudaMalloc(void **p, size_t n) {
-  *p = std::calloc(n ? n : 1, 1);  // device memory is zero after allocation in practice
+  char *b = static_cast<char *>(std::calloc(kGuard + (n ? n : 1), 1));
+  *p = b ? b + kGuard : nullptr;
   return *p ? cudaSuccess : cudaErrorMemoryAllocation;
 }
 cudaError_t cudaFree(void *p) {
-  std::free(p);
+  if (p) std::free(static_cast<char *>(p) - kGuard);
   return cudaSuccess;
 }
 cudaError_t cudaMemset(void *p, int v, size_t n) {
