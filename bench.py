@@ -1,25 +1,32 @@
 #!/usr/bin/env python
 """Benchmark of the FARGO-ADSG hydro step on GB300.
 
-Workload (default): the self-gravitating disk, 256 x 768 log grid on
-[0.4, 4.0], Sigma ~ 1/r with disk mass 0.02, alpha = 1e-3, self-gravity through a
-2*Nrad zero-padded log-r FFT convolution (softening 0.3 h), one migrating
-planet q = 5e-4 from r = 1.5 with the indirect term, 1e-3 seeded noise
-(cudaprotoplanetarydisks_gb300/configs/c2_selfgravity.par).  A step is one DT
-(AlgoGas: CFL-subcycled hydro substeps); the metric counts cell updates,
-Nrad * Nsec per hydro substep.
+Workload (default, --config c3): the adiabatic disk with cooling, 1024 x 3072
+log grid on [0.3, 3.0], gamma = 1.4, cooling time 10 r^(2+2f), alpha = 1e-3,
+Sigma ~ r^-0.5, one planet q = 1e-3 on a fixed circular orbit at r = 1, seeded
+1e-4 noise on Sigma and energy (cudaprotoplanetarydisks_gb300/configs/
+c3_adiabatic.par), the largest single-disk configuration of the benchmark set.
+A step is one DT (AlgoGas: CFL-subcycled hydro substeps); the metric counts cell
+updates, Nrad * Nsec per hydro substep.
 
-Own arm: the state stays in HBM; each timed step is one graph launch of a DT
-(CFL loop on the device), timed with CUDA events on the launching stream, with an
-L2 flush (a 256 MiB write) before every timed step.  The headline is the
-FP32-bulk mode; the FP64 mode is measured in the same run, and the FP32 fields
-are compared with the FP64 oracle after the same steps.  e2e: the same metric
+Own arm, headline: the FP64 mode (the reference's arithmetic).  The state stays
+in HBM (about 0.5 GB, above the 129 MB L2); each timed step is one graph launch of
+a DT (CFL loop on the device), timed with CUDA events on the launching stream,
+with an L2 flush (a 256 MiB write) before every timed step.  e2e: the same metric
 through the C-ABI with host buffers (pinned FP64 arrays copied in and out every
-step).
+step).  Beside it: the FP32-bulk mode (own value, e2e and field errors against
+the FP64 mode after the same DTs), the self-gravitating 256 x 768 disk in both
+modes, the batched ensemble and the learned correction.  The roofline of the
+FP64 mode is its FP64 pipe (measured peak: fargo_fp64_pipe_peak).
 
---impl reference: the reference has no CPU implementation of this path (every
-substep is a CUDA kernel); its CPU restatement (the oracle, OpenMP over rings)
-is timed on all host cores.
+CPU baselines: the reference's own sources compiled for the CPU
+(oracle/_ref/fargo_ref_cpu, blocks of each launch on the host cores) on a bounded
+sample of the same disk -- the DT shortened to about one hydro substep, so that
+each AlgoGas call is a sample of the workload's substeps -- on all host cores and
+on one; and the oracle (the C++ restatement) on all host cores.
+
+--impl reference: the reference's own code on the host cores (the CPU build
+above), on the same workload and metric, never loading this package's library.
 
 --gpus N (torchrun, one rank per GPU): replicas only -- every rank advances its
 own disk; value = all ranks' cell updates / the slowest rank's time.
@@ -28,11 +35,11 @@ import argparse
 import ctypes
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -40,17 +47,30 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s"
 L2_FLUSH_BYTES = 256 << 20
-REF_BUDGET_S = 90.0  # time budget of the CPU reference arm's timed sample
+CONFIG_DIR = os.path.join(ROOT, "cudaprotoplanetarydisks_gb300", "configs")
+CONFIG_FILES = {"c1": "c1_isothermal.par", "c2": "c2_selfgravity.par", "c3": "c3_adiabatic.par",
+                "wide": "wide_template4.par"}
+WORKLOADS = {"c1": "isothermal disk 128x384, 1 planet (fixed orbit)",
+             "c2": "self-gravitating disk 256x768, alpha viscosity, migrating planet",
+             "c3": "adiabatic disk with cooling 1024x3072, alpha viscosity, 1 planet (fixed orbit)",
+             "wide": "adiabatic disk 2048x4096, non-reflecting inner boundary, guiding-center frame, "
+                     "Jupiter-mass planet"}
+# the CPU samples' DT is the workload's DT over this divisor: about one hydro
+# substep per AlgoGas call (twice the substeps per DT measured on the workload,
+# as the first substeps of a run take a smaller CFL step)
+SAMPLE_DT_DIVISOR = {"c1": 30, "c2": 54, "c3": 220, "wide": 200}
+REF_EXE = os.path.join(ROOT, "oracle", "_ref", "fargo_ref_cpu")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="c3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the 256x768 self-gravitating disk extra")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-correction measurement")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
@@ -90,17 +110,12 @@ def job_value(nsub_all, cells, ms_max):
 def workload(cfg):
     import cudaprotoplanetarydisks_gb300 as fg
     params, planets = fg.load_config(cfg)
-    name = {"c1": "isothermal disk 128x384, 1 planet (fixed orbit)",
-            "c2": "self-gravitating disk 256x768, alpha viscosity, migrating planet",
-            "c3": "adiabatic disk with cooling 1024x3072, 1 planet",
-            "wide": "adiabatic disk 2048x4096, non-reflecting inner boundary, guiding-center frame, "
-                    "Jupiter-mass planet"}.get(cfg, cfg)
-    return params, planets, name
+    return params, planets, WORKLOADS.get(cfg, cfg)
 
 
 def config_obj(params, name, cfg, extra=None):
-    c = {"workload": name, "config_file": f"configs/{cfg}", "nrad": params.nrad, "nsec": params.nsec,
-         "cells": params.nrad * params.nsec, "self_gravity": bool(params.self_gravity),
+    c = {"workload": name, "config_file": f"configs/{CONFIG_FILES.get(cfg, cfg)}", "nrad": params.nrad,
+         "nsec": params.nsec, "cells": params.nrad * params.nsec, "self_gravity": bool(params.self_gravity),
          "adiabatic": bool(params.adiabatic), "DT": params.dt, "step": "one DT (AlgoGas, CFL-subcycled)",
          "l2": "flushed (256 MiB write) before every timed step"}
     if extra:
@@ -197,23 +212,49 @@ def kernel_bytes(name, params, esize):
     return 0
 
 
+def _profile_rows(cfg, mode):
+    """Rows (cells split on '|') of the committed ncu summary
+    profiles/kernels_<cfg>_<mode>.md, keyed by kernel name without template
+    arguments."""
+    path = os.path.join(ROOT, "profiles", f"kernels_{cfg}_{mode}.md")
+    rows = {}
+    if not os.path.exists(path):
+        return rows
+    for line in open(path):
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) >= 4:
+            rows.setdefault(cells[0].split("<")[0], cells)
+    return rows
+
+
 def ncu_traffic(kernel, cfg, mode="fp32"):
     """DRAM bytes (read + write) of one launch of `kernel` from the committed ncu
     summary profiles/kernels_<cfg>_<mode>.md (one cold-cache capture), or None."""
-    path = os.path.join(ROOT, "profiles", f"kernels_{cfg}_{mode}.md")
-    if not os.path.exists(path):
+    cells = _profile_rows(cfg, mode).get(kernel)
+    if cells is None:
         return None
+    if mode == "fp64":  # columns: launches, avg us, read MB, write MB, ...
+        try:
+            return (float(cells[3]) + float(cells[4])) * 1e6
+        except (ValueError, IndexError):
+            return None
     scale = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
-    for line in open(path):
-        cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cells) >= 4 and cells[0] == kernel:
-            try:
-                rd, ru = cells[2].split()
-                wr, wu = cells[3].split()
-                return float(rd) * scale[ru] + float(wr) * scale[wu]
-            except (ValueError, KeyError):
-                return None
-    return None
+    try:
+        rd, ru = cells[2].split()
+        wr, wu = cells[3].split()
+        return float(rd) * scale[ru] + float(wr) * scale[wu]
+    except (ValueError, KeyError):
+        return None
+
+
+def ncu_fp64_instructions(kernel, cfg):
+    """FP64-pipe thread instructions of one launch of `kernel` (warp instructions
+    x 32) from the committed ncu summary profiles/kernels_<cfg>_fp64.md, or None."""
+    cells = _profile_rows(cfg, "fp64").get(kernel)
+    try:
+        return float(cells[6]) * 32.0
+    except (TypeError, ValueError, IndexError):
+        return None
 
 
 def measured_peaks():
@@ -253,8 +294,6 @@ def time_device(disk, stream, steps, flush):
 def time_e2e(disk, stream, steps, params):
     """Through the C-ABI with host buffers: pinned FP64 host arrays are copied in,
     one DT runs, the fields are copied out, every step."""
-    import ctypes
-
     import numpy as np
     import torch
     shape = (params.nrad + 1, params.nsec)
@@ -284,6 +323,333 @@ def time_e2e(disk, stream, steps, params):
     return wall, nsub, len(names) * nbytes, len(names) * nbytes
 
 
+def kernel_times(disk, reps=3):
+    """Per-kernel device time of one substep, launch by launch (CUDA events between
+    kernels), after the timed region: [(name, ms)]."""
+    ms_k = (ctypes.c_double * 96)()
+    nk = ctypes.c_int(0)
+    rc = disk.lib.fargo_time_substep_kernels(disk.h, reps, ms_k, 96, ctypes.byref(nk))
+    if rc != 0:
+        return []
+    return [(disk.lib.fargo_substep_kernel_name(disk.h, k).decode(), ms_k[k]) for k in range(nk.value)]
+
+
+def dominant(kern, params):
+    """The kernel with the largest device time per substep on the critical path
+    (k_planets runs on a second stream beside the hydro kernels outside a
+    corotating frame): (name, total ms per substep, launches per substep)."""
+    agg = {}
+    for nm, t in kern:
+        a = agg.setdefault(nm, [0.0, 0])
+        a[0] += t
+        a[1] += 1
+    crit = {k: v for k, v in agg.items() if not (k == "k_planets" and not params.corotating)}
+    if not crit:
+        return "none", 1.0, 1, agg
+    nm, (ms, n) = max(crit.items(), key=lambda kv: kv[1][0])
+    return nm, ms, n, agg
+
+
+def step_alg_bytes(params, esize):
+    """Algorithmic bytes per cell update of the whole step: every state field read
+    and written once per substep (+ the self-gravity FFT round trips)."""
+    nf = 3 + (1 if params.adiabatic else 0)
+    return 2 * nf * esize + (128 if params.self_gravity else 0)
+
+
+def measure_mode(fg, params, planets, prec, stream, flush, steps, warmup, clocks_gpu=None, e2e=True):
+    """One precision mode on one disk: device-resident value, e2e through the
+    C-ABI, launches in the timed region and per-kernel times."""
+    disk = fg.Disk(params, planets, prec, stream=stream.cuda_stream)
+    for _ in range(warmup):
+        disk.run(1)
+    sampler = ClockSampler(clocks_gpu) if clocks_gpu is not None else None
+    import torch
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+    ms, nsub, npad = time_device(disk, stream, steps, flush)
+    torch.cuda.synchronize()
+    r = {"ms": ms, "substeps": nsub, "padded_substeps": npad}
+    if sampler:
+        r["clocks"] = sampler.stop()
+    sc = disk.scalars()
+    # padded substeps (dt = 0, filling a loop body of two) launch their kernels too
+    r["launches"] = int(steps * sc.launches_per_dt + (nsub + npad) * sc.launches_per_substep)
+    if e2e:
+        wall, n_e2e, bi, bo = time_e2e(disk, stream, steps, params)
+        r["e2e"] = (wall, n_e2e, bi, bo)
+    r["kernels"] = kernel_times(disk)
+    disk.close()
+    return r
+
+
+def fp32_errors(fg, params, planets, stream, ndt=2):
+    """Per-field relative L2 / Linf error of the FP32-bulk mode against the FP64
+    mode of the same code after the same DTs from the same initial state (the FP64
+    mode matches the oracle within 1e-9: tests/test_gpu_parity.py)."""
+    import numpy as np
+    d32 = fg.Disk(params, planets, fg.FARGO_FP32_BULK, stream=stream.cuda_stream)
+    d64 = fg.Disk(params, planets, fg.FARGO_FP64, stream=stream.cuda_stream)
+    d32.run(ndt)
+    d64.run(ndt)
+    names = ["dens", "vrad", "vtheta"] + (["energy"] if params.adiabatic else [])
+    err = {}
+    for nm in names:
+        a, b = d32.field(nm)[:-1], d64.field(nm)[:-1]
+        err[nm] = {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                   "rel_linf": float(np.abs(a - b).max() / np.abs(b).max())}
+    d32.close()
+    d64.close()
+    return {"after": f"{ndt} DTs", "against": "FP64 mode of this code", "fields": err}
+
+
+# ---------------------------------------------------------------------------
+# the reference's own sources on the CPU (oracle/_ref/fargo_ref_cpu)
+def _par_values(text):
+    vals = {}
+    for line in text.splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and not parts[0].startswith("#"):
+            vals[parts[0].upper()] = parts[1]
+    return vals
+
+
+def reference_cpu_sample(cfg, ndt, threads, sample_divisor=None):
+    """Runs the reference's main() (CPU build) on the workload's .par with the DT
+    shortened to about one hydro substep, for ndt DTs, on `threads` host threads
+    (blocks of each launch in parallel).  Returns (substeps, AlgoGas seconds,
+    cells) over all DTs, from the binary's REFSTEP lines.  Reads no product code."""
+    if not os.path.exists(REF_EXE):
+        raise RuntimeError(f"{REF_EXE} is missing (build(): oracle/ref_emul/build_ref.py)")
+    src = os.path.join(CONFIG_DIR, CONFIG_FILES[cfg])
+    text = open(src).read()
+    vals = _par_values(text)
+    divisor = sample_divisor or SAMPLE_DT_DIVISOR.get(cfg, 100)
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        keep = []
+        for line in text.splitlines():
+            k = line.split()[0].upper() if line.split() else ""
+            if k in ("NTOT", "NINTERM", "DT", "OUTPUTDIR", "PLANETCONFIG"):
+                continue
+            keep.append(line)
+        keep += [f"Ntot {ndt - 1}", "Ninterm 1000000000",
+                 f"DT {float(vals.get('DT', '0.314159265359')) / divisor!r}", f"OutputDir {out}/"]
+        if "PLANETCONFIG" in vals:
+            keep.append(f"PlanetConfig {os.path.join(CONFIG_DIR, vals['PLANETCONFIG'])}")
+        par = os.path.join(d, "run.par")
+        open(par, "w").write("\n".join(keep) + "\n")
+        env = dict(os.environ)
+        env["FARGO_REF_THREADS"] = str(threads)
+        env["OMP_NUM_THREADS"] = str(threads)
+        for key, var in (("SIGMANOISE", "FARGO_REF_SIGMA_NOISE"), ("ENERGYNOISE", "FARGO_REF_ENERGY_NOISE"),
+                         ("NOISESEED", "FARGO_REF_NOISE_SEED")):
+            if key in vals:
+                env[var] = vals[key]
+        r = subprocess.run([REF_EXE, par], input="0\n", capture_output=True, text=True, env=env, cwd=d,
+                           timeout=3600)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference CPU build failed ({r.returncode}): {(r.stdout + r.stderr)[-600:]}")
+        steps = [m.groups() for m in re.finditer(r"REFSTEP (\d+) (\d+) ([0-9.eE+-]+)", r.stderr)]
+    cells = int(vals["NRAD"]) * int(vals["NSEC"])
+    return [(int(s), float(t)) for _, s, t in steps], cells, divisor
+
+
+def cpu_baselines(cfg, params, planets):
+    """cpu_baseline (the reference's own code, all host cores) plus the one-core
+    figure and the oracle (C++ restatement) on all host cores, each on a bounded
+    sample of the workload."""
+    cores = os.cpu_count() or 1
+    out = {}
+    steps, cells, div = reference_cpu_sample(cfg, 3, cores)
+    n, t = sum(s for s, _ in steps[1:]), sum(x for _, x in steps[1:])
+    out["cpu_baseline"] = {"value": n * cells / t, "unit": METRIC, "cores": cores, "kind": "reference",
+                           "sample": f"the reference's own sources compiled for the CPU (blocks of each launch "
+                                     f"on {cores} host threads), DT shortened to DT/{div}: {n} hydro substeps "
+                                     f"in 2 timed AlgoGas calls after 1 untimed"}
+    steps1, _, _ = reference_cpu_sample(cfg, 1, 1)
+    n1, t1 = sum(s for s, _ in steps1), sum(x for _, x in steps1)
+    out["cpu_baseline_1core"] = {"value": n1 * cells / t1, "unit": METRIC, "cores": 1, "kind": "reference",
+                                 "sample": f"the same build on one host thread: {n1} hydro substep(s) in one "
+                                           f"AlgoGas call (DT/{div})"}
+    from oracle.oracle import OracleDisk
+    OracleDisk.set_threads(cores)
+    p = type(params).from_buffer_copy(params)
+    p.dt = params.dt / div
+    o = OracleDisk(p, planets)
+    t0 = time.perf_counter()
+    no = o.step_DT() + o.step_DT()
+    to = time.perf_counter() - t0
+    o.close()
+    out["cpu_baseline_port"] = {"value": no * cells / to, "unit": METRIC, "cores": cores, "kind": "port",
+                                "sample": f"the oracle (C++ restatement, OpenMP over rings): {no} hydro substeps "
+                                          f"(2 DTs of DT/{div})"}
+    return out
+
+
+# ---------------------------------------------------------------------------
+def run_own(args, world, rank, local):
+    import torch
+
+    import cudaprotoplanetarydisks_gb300 as fg
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    params, planets, wname = workload(args.config)
+    cells = params.nrad * params.nsec
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # headline: FP64 (the reference's arithmetic), clocks sampled in its timed region
+    barrier()
+    r64 = measure_mode(fg, params, planets, fg.FARGO_FP64, stream, flush, args.steps, args.warmup,
+                       clocks_gpu=local)
+    barrier()
+    ms_max, nsub_all = reduce_over_ranks(r64["ms"], r64["substeps"])
+    r32 = measure_mode(fg, params, planets, fg.FARGO_FP32_BULK, stream, flush, args.steps, args.warmup)
+    ms32_max, nsub32_all = reduce_over_ranks(r32["ms"], r32["substeps"])
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    hbm_peak, peak_kind = measured_peaks()
+    value = job_value(nsub_all, cells, ms_max)
+    wall, n_e2e, bi, bo = r64["e2e"]
+    # roofline of the dominant FP64 kernel: HBM bytes, and its FP64 pipe (the bound)
+    dname, dms, dn, agg64 = dominant(r64["kernels"], params)
+    davg = dms / dn
+    alg = kernel_bytes(dname, params, 8)
+    achieved = alg / (davg * 1e-3) / 1e9
+    dfma = ctypes.c_double(0.0)
+    rc = fg._capi.load().fargo_fp64_pipe_peak(ctypes.byref(dfma))
+    fp64_instr = ncu_fp64_instructions(dname, args.config)
+    fp64_pipe = {"unit": "G FP64-pipe thread instructions/s", "peak": dfma.value / 1e9 if rc == 0 else None,
+                 "peak_source": "fargo_fp64_pipe_peak (independent DFMA chains on every SM, measured in this run)",
+                 "instructions_per_launch": fp64_instr,
+                 "instructions_source": f"profiles/kernels_{args.config}_fp64.md (ncu sm__inst_executed_pipe_fp64 x 32)"}
+    if fp64_instr and rc == 0:
+        fp64_pipe["achieved"] = fp64_instr / (davg * 1e-3) / 1e9
+        fp64_pipe["frac"] = fp64_pipe["achieved"] / fp64_pipe["peak"]
+    sb64 = step_alg_bytes(params, 8)
+    # FP32-bulk beside it
+    d32, d32ms, d32n, agg32 = dominant(r32["kernels"], params)
+    alg32 = kernel_bytes(d32, params, 4)
+    ach32 = alg32 / (d32ms / d32n * 1e-3) / 1e9
+    w32, n32e, bi32, bo32 = r32["e2e"]
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded uniform noise on Sigma and energy, reference .par/.cfg interface)",
+        "config": config_obj(params, wname, args.config,
+                             {"precision": "FP64", "parallelism": f"replicas x{world}",
+                              "substeps_per_step": r64["substeps"] / args.steps}),
+        "e2e": {"value": n_e2e * cells * world / wall, "unit": METRIC, "h2d_bytes_per_step": bi,
+                "d2h_bytes_per_step": bo, "ms_per_step": wall * 1e3 / args.steps,
+                "path": "fargo_set_fields + fargo_step_DT + fargo_get_fields (C-ABI, pinned FP64 host arrays)"},
+        "gpu_launches": r64["launches"],
+        "clocks": r64["clocks"],
+        "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": hbm_peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "alg_bytes_per_launch": alg, "avg_launch_ms": davg,
+                     "traffic": ncu_traffic(dname, args.config, "fp64"),
+                     "traffic_source": f"profiles/kernels_{args.config}_fp64.md (ncu, one cold-cache launch)",
+                     "fp64_pipe": fp64_pipe,
+                     "note": "the FP64 kernels are bound by the FP64 pipe (83-90% busy in ncu), not by HBM; "
+                             "fp64_pipe.frac is the roofline fraction that applies"},
+        "step_roofline": {"alg_bytes_per_cell_update": sb64, "achieved_GBs": value * sb64 / 1e9,
+                          "frac": value * sb64 / 1e9 / hbm_peak},
+        "kernels_ms": {nm: round(t / n, 5) for nm, (t, n) in agg64.items()},
+        "fp32_bulk": {
+            "value": job_value(nsub32_all, cells, ms32_max), "unit": METRIC, "ms_per_step": ms32_max / args.steps,
+            "dtype": "f32",
+            "precision_detail": "f32 fields and arithmetic; f64 CFL decision, planets, ring means, FARGO split; "
+                                "compensated f32 (float-float) force and ring sums",
+            "e2e": {"value": n32e * cells * world / w32, "unit": METRIC, "h2d_bytes_per_step": bi32,
+                    "d2h_bytes_per_step": bo32},
+            "gpu_launches": r32["launches"],
+            "roofline": {"bound": "hbm", "kernel": d32, "achieved": ach32, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": ach32 / hbm_peak, "alg_bytes_per_launch": alg32,
+                         "avg_launch_ms": d32ms / d32n, "traffic": ncu_traffic(d32, args.config, "fp32")},
+            "step_roofline": {"alg_bytes_per_cell_update": step_alg_bytes(params, 4),
+                              "frac": job_value(nsub32_all, cells, ms32_max) * step_alg_bytes(params, 4)
+                              / 1e9 / hbm_peak},
+            "kernels_ms": {nm: round(t / n, 5) for nm, (t, n) in dominant(r32["kernels"], params)[3].items()},
+            "error_vs_fp64": fp32_errors(fg, params, planets, stream),
+        },
+    }
+    if not args.no_cpu_baseline:
+        line.update(cpu_baselines(args.config, params, planets))
+    if not args.no_extra and world == 1 and args.config != "c2":
+        p2, pl2, n2 = workload("c2")
+        e = {"workload": n2, "config_file": "configs/c2_selfgravity.par"}
+        for prec, key in ((fg.FARGO_FP64, "fp64"), (fg.FARGO_FP32_BULK, "fp32_bulk")):
+            r = measure_mode(fg, p2, pl2, prec, stream, flush, 50, args.warmup, e2e=(key == "fp64"))
+            e[key] = {"value": r["substeps"] * p2.nrad * p2.nsec / (r["ms"] * 1e-3), "unit": METRIC,
+                      "ms_per_step": r["ms"] / 50, "steps": 50}
+            if "e2e" in r:
+                w, ne, _, _ = r["e2e"]
+                e[key]["e2e"] = ne * p2.nrad * p2.nsec / w
+        e["fp32_error_vs_fp64"] = fp32_errors(fg, p2, pl2, stream)
+        line["c2"] = e
+    if not args.no_batch and world == 1:
+        line["batch_c4"] = batch_ensemble()
+    if not args.no_learned and world == 1:
+        line["learned_c5"] = learned_c5()
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args, world, rank):
+    """The reference's own code on the host cores: its sources compiled for the CPU
+    (oracle/_ref/fargo_ref_cpu), the blocks of each launch on every host thread,
+    on the same workload and metric.  Each step is one AlgoGas call of a bounded
+    sample (DT shortened to about one hydro substep); warm-up calls are untimed.
+    Only rank 0 runs; this never loads the product library."""
+    if rank != 0:
+        return
+    cfg = args.config
+    cores = os.cpu_count() or 1
+    steps, cells, div = reference_cpu_sample(cfg, args.warmup + args.steps, cores)
+    timed = steps[args.warmup:]
+    n, t = sum(s for s, _ in timed), sum(x for _, x in timed)
+    value = n * cells / t
+    vals = _par_values(open(os.path.join(CONFIG_DIR, CONFIG_FILES[cfg])).read())
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t * 1e3 / max(1, len(timed)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "impl": "reference", "dtype": "f64",
+        "data": "synthetic (seeded uniform noise on Sigma and energy, reference .par/.cfg interface)",
+        "config": {"workload": WORKLOADS.get(cfg, cfg), "config_file": f"configs/{CONFIG_FILES.get(cfg, cfg)}",
+                   "nrad": int(vals["NRAD"]), "nsec": int(vals["NSEC"]), "cells": cells, "precision": "FP64",
+                   "step": f"one AlgoGas call with DT shortened to DT/{div} (about one hydro substep)",
+                   "parallelism": "host cores"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "reference",
+                         "sample": f"{len(timed)} AlgoGas calls ({n} hydro substeps) after {args.warmup} untimed, "
+                                   f"DT/{div}; the reference's sources compiled for the CPU, blocks of each "
+                                   f"launch on {cores} host threads"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference runs every substep as a CUDA kernel and has no CPU path of its own; this arm runs "
+                "its unmodified kernels and host code on the CPU through an emulation of the launch syntax "
+                "(oracle/ref_emul), bitwise equal to the golden fixtures",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
 def batch_ensemble(ndt=2, n=64):
     """The batched ensemble (64 seeded disks, Nrad in {128..512}, Nsec = 3 Nrad):
     FP32-bulk disks advanced side by side (fargo_batch) against the same disks in
@@ -372,190 +738,6 @@ def learned_c5():
         "corrections": r["corrections"],
         "mlp_kernels": kernels,
     }
-
-
-def oracle_sample(params, planets, ndt, threads):
-    from oracle.oracle import OracleDisk
-    OracleDisk.set_threads(threads)
-    o = OracleDisk(params, planets)
-    t0 = time.perf_counter()
-    n = 0
-    for _ in range(ndt):
-        n += o.step_DT()
-    dt = time.perf_counter() - t0
-    return o, n, dt
-
-
-def run_own(args, world, rank, local):
-    import numpy as np
-    import torch
-
-    import cudaprotoplanetarydisks_gb300 as fg
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    params, planets, wname = workload(args.config)
-    cells = params.nrad * params.nsec
-    stream = torch.cuda.Stream()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    results = {}
-    for prec, key in ((fg.FARGO_FP32_BULK, "fp32"), (fg.FARGO_FP64, "fp64")):
-        disk = fg.Disk(params, planets, prec, stream=stream.cuda_stream)
-        for _ in range(args.warmup):
-            disk.run(1)
-        sampler = ClockSampler(local) if key == "fp32" else None
-        barrier()
-        if sampler:
-            sampler.start()
-        ms, nsub, npad = time_device(disk, stream, args.steps, flush)
-        barrier()
-        clocks = sampler.stop() if sampler else None
-        ms_max, nsub_all = reduce_over_ranks(ms, nsub)
-        r = {"ms_total": ms_max, "substeps": nsub_all, "value": job_value(nsub_all, cells, ms_max),
-             "ms_per_step": ms_max / args.steps, "substeps_per_step": nsub / args.steps}
-        sc = disk.scalars()
-        # padded substeps (dt = 0, filling a loop body of two) launch their kernels too
-        r["launches"] = int(args.steps * sc.launches_per_dt + (nsub + npad) * sc.launches_per_substep)
-        r["padded_substeps"] = npad
-        if key == "fp32":
-            r["clocks"] = clocks
-            wall, n_e2e, bi, bo = time_e2e(disk, stream, args.steps, params)
-            r["e2e"] = {"value": n_e2e * cells * world / wall, "unit": METRIC,
-                        "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "ms_per_step": wall * 1e3 / args.steps}
-        # per-kernel device time (launch by launch, after the timed region)
-        ms_k = (ctypes.c_double * 96)()
-        nk = ctypes.c_int(0)
-        rc = disk.lib.fargo_time_substep_kernels(disk.h, 5, ms_k, 96, ctypes.byref(nk))
-        kern = []
-        if rc == 0:
-            for k in range(nk.value):
-                nm = disk.lib.fargo_substep_kernel_name(disk.h, k).decode()
-                kern.append((nm, ms_k[k]))
-        r["kernels"] = kern
-        disk.close()
-        results[key] = r
-    if rank != 0:
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
-        return
-    hbm_peak, peak_kind = measured_peaks()
-    f32 = results["fp32"]
-    # dominant kernel of the headline mode, with its algorithmic bytes
-    agg = {}
-    for nm, t in f32["kernels"]:
-        a = agg.setdefault(nm, [0.0, 0])
-        a[0] += t
-        a[1] += 1
-    # k_planets runs on a second stream beside the hydro kernels (outside a
-    # corotating frame), off the substep's critical path
-    crit = {k: v for k, v in agg.items() if not (k == "k_planets" and not params.corotating)}
-    dom = max(crit.items(), key=lambda kv: kv[1][0]) if crit else ("none", [1.0, 1])
-    dom_name, (dom_ms, dom_n) = dom
-    dom_avg_ms = dom_ms / dom_n
-    alg = kernel_bytes(dom_name, params, 4)
-    achieved = alg / (dom_avg_ms * 1e-3) / 1e9
-    step_alg = 24 + (128 if params.self_gravity else 0) + (8 if params.adiabatic else 0)
-    line = {
-        "metric": METRIC, "value": f32["value"], "unit": "cell-updates/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32",
-        "precision_detail": "f32 fields and self-gravity FFT; f64 CFL decision, planets, ring means, FARGO "
-                            "split; compensated f32 (float-float) force and ring sums",
-        "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
-        "config": config_obj(params, wname, args.config,
-                             {"precision": "FP32_BULK", "parallelism": f"replicas x{world}",
-                              "substeps_per_step": f32["substeps_per_step"]}),
-        "e2e": f32["e2e"],
-        "gpu_launches": f32["launches"],
-        "clocks": f32["clocks"],
-        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm_peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "alg_bytes_per_launch": alg, "avg_launch_ms": dom_avg_ms,
-                     "traffic": ncu_traffic(dom_name, args.config),
-                     "traffic_source": f"profiles/kernels_{args.config}_fp32.md (ncu, one cold-cache launch)"},
-        "step_roofline": {"alg_bytes_per_cell_update": step_alg,
-                          "achieved_GBs": f32["value"] * step_alg / 1e9,
-                          "frac": f32["value"] * step_alg / 1e9 / hbm_peak},
-        "kernels_ms": {nm: round(t / n, 5) for nm, (t, n) in agg.items()},
-        "fp64": {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms_per_step"],
-                 "gpu_launches": results["fp64"]["launches"],
-                 "kernels_ms": {nm: round(t, 5) for nm, t in results["fp64"]["kernels"]}},
-    }
-    # CPU baseline (oracle, all host cores) on a bounded sample, and the FP32 error
-    # against the FP64 oracle after the same DTs
-    if not args.no_cpu_baseline:
-        import numpy as np
-        ndt = 2
-        cores = os.cpu_count() or 1
-        o, n_cpu, t_cpu = oracle_sample(params, planets, ndt, cores)
-        line["cpu_baseline"] = {"value": n_cpu * cells / t_cpu, "unit": METRIC, "cores": cores, "kind": "port",
-                                "sample": f"{ndt} DTs ({n_cpu} substeps) of the same disk from its initial state"}
-        disk = fg.Disk(params, planets, fg.FARGO_FP32_BULK, stream=stream.cuda_stream)
-        for _ in range(ndt):
-            disk.step_DT()
-        err = {}
-        for nm in ("dens", "vrad", "vtheta"):
-            a, b = disk.field(nm)[:-1], o.field(nm)[:-1]
-            err[nm] = {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
-                       "rel_linf": float(np.abs(a - b).max() / np.abs(b).max())}
-        line["fp32_error_vs_fp64_oracle"] = {"after": f"{ndt} DTs", "fields": err}
-        disk.close()
-        o.close()
-    if not args.no_batch and world == 1:
-        line["batch_c4"] = batch_ensemble()
-    if not args.no_learned and world == 1:
-        line["learned_c5"] = learned_c5()
-    print(json.dumps(line), flush=True)
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
-
-
-def run_reference(args, world, rank):
-    if rank != 0:
-        return
-    params, planets, wname = workload(args.config)
-    cells = params.nrad * params.nsec
-    cores = os.cpu_count() or 1
-    from oracle.oracle import OracleDisk
-    OracleDisk.set_threads(cores)
-    o = OracleDisk(params, planets)
-    for _ in range(args.warmup):
-        o.step_DT()
-    # a bounded sample: the first timed DT sets how many fit in REF_BUDGET_S
-    t0 = time.perf_counter()
-    n = o.step_DT()
-    steps = 1
-    cap = max(1, min(args.steps, int(REF_BUDGET_S / max(time.perf_counter() - t0, 1e-9))))
-    while steps < cap:
-        n += o.step_DT()
-        steps += 1
-    dt = time.perf_counter() - t0
-    value = n * cells / dt
-    line = {
-        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt * 1e3 / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "impl": "reference", "dtype": "f64",
-        "data": "synthetic (seeded 1e-3 uniform noise on Sigma, reference .par/.cfg interface)",
-        "config": config_obj(params, wname, args.config, {"precision": "FP64", "parallelism": "host cores"}),
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
-                         "sample": f"{steps} of the {args.steps} requested DTs ({n} substeps, about "
-                                   f"{REF_BUDGET_S:.0f} s at most) after {args.warmup} warm-up DTs"},
-        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference runs every substep as a CUDA kernel and has no CPU path; "
-                "this arm times its CPU restatement (the oracle) with OpenMP over rings",
-    }
-    print(json.dumps(line), flush=True)
 
 
 def run_profile(args):

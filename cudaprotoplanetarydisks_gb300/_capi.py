@@ -120,6 +120,7 @@ SIGNATURES = [
     ("fargo_update_log", _I, [_P, _I]),
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
+    ("fargo_fp64_pipe_peak", _I, [ctypes.POINTER(_D)]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),
     ("fargo_batch_create", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),
                                 _I, ctypes.POINTER(_P)]),

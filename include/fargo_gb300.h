@@ -270,17 +270,27 @@ int  fargo_update_log(fargo_ctx *ctx, int timestep);
 int  fargo_time_substep_kernels(fargo_ctx *ctx, int reps, double *ms_per_kernel, int cap, int *nkernels);
 /* Name of kernel k of the last fargo_time_substep_kernels call (NULL if none). */
 const char *fargo_substep_kernel_name(const fargo_ctx *ctx, int k);
+/* Measured peak of the FP64 pipe of the current device: thread-level FP64 fused
+   multiply-adds per second (*dfma_per_s) of a kernel of independent DFMA chains
+   filling every SM, timed with CUDA events after a warm-up launch.  The roofline
+   of the FP64 mode, whose kernels are bound by this pipe.  Synchronous. */
+int  fargo_fp64_pipe_peak(double *dfma_per_s);
 
 /* ---- allocation-free CFL (no counterpart in the reference) --------------- */
-/* The CFL integer of fargo_condition_cfl for callers that cannot call cudaMalloc
+/* The CFL integer of ConditionCFL for callers that cannot call cudaMalloc
    (device memory owned by another allocator, or a loop that must not take
    cudaMalloc's implicit synchronisation).  Inputs are the caller's FP64 device
    arrays: vrad, vtheta, soundspeed ((nrad+1)*nsec each, ring-major) and rinf,
    rmed, rsup (nrad+1 each); *cfl_out is a device int written on `stream`
-   (-1 when the time step is not finite).  Allocates nothing: its scratch is a
-   fixed array inside the library, at most 16384 rings (larger nrad:
-   FARGO_ERR_INVALID).  The first call on a device sets up that device (make it
-   before any stream capture); calls that overlap on the GPU race on the array. */
+   (-1 when the time step is not finite).  Arithmetic: the reference's own
+   (ring means summed in sector order, every term divided as written, no fused
+   multiply-add), so on identical inputs the integer is the reference's;
+   fargo_condition_cfl (tree sums, per-ring reciprocals) can differ from it by one
+   at a rounding tie.  Allocates nothing: its scratch is a fixed array inside the
+   library, at most 16384 rings and 16384 sectors (larger: FARGO_ERR_INVALID).
+   The first call on a device sets up that device (make it before any stream
+   capture, and do not use the entry point across a device reset); calls that
+   overlap on the GPU race on the array. */
 int  fargo_condition_cfl_noalloc(const double *vrad, const double *vtheta, const double *soundspeed,
                                  const double *rinf, const double *rmed, const double *rsup,
                                  int nrad, int nsec, int fast_transport, double deltaT,

@@ -11,8 +11,8 @@
 #include "fake_include/cufft.h"
 #include "../fft_ref.h"
 
-uint3 threadIdx, blockIdx;
-dim3 blockDim, gridDim;
+thread_local uint3 threadIdx, blockIdx;
+thread_local dim3 blockDim, gridDim;
 double sdata[1 << 16];  // `extern __shared__ double sdata[]` of DeviceReduceKernel
 
 // Every allocation is zero-filled (device memory is zero after allocation in
@@ -80,23 +80,44 @@ void emu_syncthreads() {
   swapcontext(&g_cur->ctx, &g_sched);
 }
 
+// Host threads over the blocks of a launch (FARGO_REF_THREADS, default 1).  No
+// reference kernel but DeviceReduceKernel (run in order, below) uses shared
+// memory, barriers or atomics, and none reads in one launch what another block
+// of the same launch writes, so the blocks' order does not change the result
+// (checked bitwise against the one-thread fixtures by tests/test_ref_cpu.py).
+int emu_ref_threads() {
+  static int n = [] {
+    const char *s = std::getenv("FARGO_REF_THREADS");
+    const int v = s ? std::atoi(s) : 1;
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
 void emu_run(const EmuCfg &c, void (*fn)(void *), void *body) {
   gridDim = c.g;
   blockDim = c.b;
   const unsigned nthr = c.b.x * c.b.y * c.b.z;
+  if (!c.sync) {
+    const long nblk = (long)c.g.x * c.g.y * c.g.z;
+#pragma omp parallel for schedule(static) num_threads(emu_ref_threads()) if (emu_ref_threads() > 1 && nblk > 1)
+    for (long b = 0; b < nblk; b++) {
+      gridDim = c.g;
+      blockDim = c.b;
+      blockIdx = uint3{(unsigned)(b % c.g.x), (unsigned)((b / c.g.x) % c.g.y), (unsigned)(b / ((long)c.g.x * c.g.y))};
+      for (unsigned tz = 0; tz < c.b.z; tz++)
+        for (unsigned ty = 0; ty < c.b.y; ty++)
+          for (unsigned tx = 0; tx < c.b.x; tx++) {
+            threadIdx = uint3{tx, ty, tz};
+            fn(body);
+          }
+    }
+    return;
+  }
   for (unsigned bz = 0; bz < c.g.z; bz++)
     for (unsigned by = 0; by < c.g.y; by++)
       for (unsigned bx = 0; bx < c.g.x; bx++) {
         blockIdx = uint3{bx, by, bz};
-        if (!c.sync) {
-          for (unsigned tz = 0; tz < c.b.z; tz++)
-            for (unsigned ty = 0; ty < c.b.y; ty++)
-              for (unsigned tx = 0; tx < c.b.x; tx++) {
-                threadIdx = uint3{tx, ty, tz};
-                fn(body);
-              }
-          continue;
-        }
         // cooperative threads: run each until its next barrier, in thread order
         static std::vector<Fiber> pool;  // stacks are allocated once and reused
         if (pool.size() < nthr) pool.resize(nthr);

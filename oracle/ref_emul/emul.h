@@ -27,8 +27,8 @@ struct dim3 {
   unsigned int x, y, z;
   dim3(unsigned int a = 1, unsigned int b = 1, unsigned int c = 1) : x(a), y(b), z(c) {}
 };
-extern uint3 threadIdx, blockIdx;
-extern dim3 blockDim, gridDim;
+extern thread_local uint3 threadIdx, blockIdx;
+extern thread_local dim3 blockDim, gridDim;
 #define warpSize 32
 #define __global__
 #define __device__

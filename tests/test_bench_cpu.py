@@ -55,3 +55,42 @@ def test_single_gpu_environment(monkeypatch):
     for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)
     assert bench.dist_env() == (1, 0, 0)
+
+
+def test_fp64_profile_columns():
+    # profiles/kernels_c3_fp64.md: FP64-pipe warp instructions per launch, DRAM MB
+    n = bench.ncu_fp64_instructions("k_transport_azimuthal", "c3")
+    assert n is not None and n > 3145728 * 100  # hundreds of FP64 instructions per cell
+    assert bench.ncu_fp64_instructions("no_such_kernel", "c3") is None
+    t = bench.ncu_traffic("k_transport_radial", "c3", "fp64")
+    assert t is not None and 1e8 < t < 1e9
+
+
+def test_step_algorithmic_bytes():
+    p, _ = fg.load_config("c3")
+    assert bench.step_alg_bytes(p, 8) == 64 and bench.step_alg_bytes(p, 4) == 32
+    p2, _ = fg.load_config("c2")
+    assert bench.step_alg_bytes(p2, 8) == 48 + 128
+
+
+def test_reference_arm_never_loads_the_product(tmp_path):
+    # the reference arm runs the reference's own code (its CPU build) and must not
+    # map libfargo_gb300.so: run it in a fresh process on the small isothermal disk
+    import json
+    import subprocess
+    import sys
+    if not os.path.exists(bench.REF_EXE):
+        import pytest
+        pytest.skip("the CPU build of the reference is not built here")
+    code = ("import sys, json, bench; sys.argv = ['bench.py', '--impl', 'reference', '--config', 'c1', "
+            "'--steps', '2', '--warmup', '1']; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(json.dumps({'product_imported': 'cudaprotoplanetarydisks_gb300' in sys.modules, "
+            "'lib_mapped': 'libfargo_gb300' in maps}))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    line, probe = lines[0], lines[1]
+    assert line["impl"] == "reference" and line["cpu_baseline"]["kind"] == "reference"
+    assert line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert not probe["product_imported"] and not probe["lib_mapped"]

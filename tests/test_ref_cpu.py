@@ -1,0 +1,42 @@
+"""The CPU build of the reference (oracle/_ref/fargo_ref_cpu) against the golden
+fixtures it made.
+
+The fixtures of tests/golden/ were made with every block of every launch run in
+order on one host thread and DeviceReduceKernel's blocks run as cooperative fibers.
+The build now restates DeviceReduce's summation order without fibers
+(oracle/ref_emul/reduce_wrap.cpp) and may run the blocks of a launch on several
+host threads (FARGO_REF_THREADS).  Neither may change a bit: every dumped field
+and planet row of the seven cases must be reproduced exactly, on one thread and on
+four.  This build is bench.py's reference arm.
+"""
+import os
+import platform
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+EXE = os.path.join(ROOT, "oracle", "_ref", "fargo_ref_cpu")
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+pytestmark = pytest.mark.skipif(not os.path.exists(EXE), reason="the CPU build of the reference is not built here")
+
+
+@pytest.mark.parametrize("threads", ["1", "4"])
+@pytest.mark.parametrize("name", ["iso", "open", "evanescent", "nonreflecting", "adiabatic_cooling",
+                                  "corotating_rk5", "selfgravity"])
+def test_reference_cpu_build_reproduces_fixture(name, threads, monkeypatch):
+    import make_golden as mg
+    rec_file = dict(np.load(os.path.join(HERE, "golden", f"ref_{name}.npz")))
+    if str(rec_file["machine"]) != platform.machine():
+        pytest.skip("fixtures were made on another machine type")
+    monkeypatch.setenv("FARGO_REF_THREADS", threads)
+    rec = mg.run_case(EXE, name)
+    assert int(rec["returncode"]) == 0
+    keys = [k for k in rec_file if k.endswith("_sha256")]
+    assert keys
+    for k in keys:
+        assert str(rec[k]) == str(rec_file[k]), k
+    assert np.array_equal(rec["planet_rows"], rec_file["planet_rows"])
