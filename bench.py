@@ -438,7 +438,12 @@ def reference_cpu_sample(cfg, ndt, threads, sample_divisor=None):
         keep += [f"Ntot {ndt - 1}", "Ninterm 1000000000",
                  f"DT {float(vals.get('DT', '0.314159265359')) / divisor!r}", f"OutputDir {out}/"]
         if "PLANETCONFIG" in vals:
-            keep.append(f"PlanetConfig {os.path.join(CONFIG_DIR, vals['PLANETCONFIG'])}")
+            # the reference keeps the planet file's path in a fixed-size buffer
+            # (src/Main.cu:248-249): a short copy beside the run
+            cfg_path = os.path.join(d, "planet.cfg")
+            with open(os.path.join(CONFIG_DIR, vals["PLANETCONFIG"])) as f_in, open(cfg_path, "w") as f_out:
+                f_out.write(f_in.read())
+            keep.append(f"PlanetConfig {cfg_path}")
         par = os.path.join(d, "run.par")
         open(par, "w").write("\n".join(keep) + "\n")
         env = dict(os.environ)

@@ -198,10 +198,54 @@ __device__ __forceinline__ void store4<double>(double *p, const double *v) {
   reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
 }
 
+// FP64 division for the per-cell arithmetic of the FP64 mode, which is bound by
+// GB300's narrow FP64 pipe.  Markstein's method (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev.
+// 34(1), 1990): the hardware reciprocal estimate (rcp.approx.ftz.f64), one
+// Newton-Raphson step y' = y + y (1 - b y), the quotient q = a y', and one
+// correction q' = q + (a - b q) y' with the residual formed exactly by a fused
+// multiply-add.  Five FP64-pipe operations.  The corrected quotient is within about
+// 2^-80 of a / b before its final rounding, so it is the correctly rounded quotient
+// except where a / b lies that close to a rounding midpoint (then one ulp off).
+// Outside |a|, |b| in [2^-500, 2^501) -- zero, subnormal, infinite or NaN operands,
+// or a quotient that could leave the normal range -- it is IEEE a / b.
+__device__ __forceinline__ double fdiv64(double a, double b) {
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  const unsigned eb = ((unsigned)__double2hiint(b) >> 20) & 0x7ffu;
+  if (ea - 523u > 1000u || eb - 523u > 1000u) return a / b;
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(b));
+  y = fma(y, fma(-b, y, 1.0), y);
+  const double q = a * y;
+  return fma(fma(-b, q, a), y, q);
+}
+
+// Division in the bulk per-cell arithmetic: fdiv64 for double fields, IEEE
+// division for float fields (the FP32-bulk arithmetic as before).
+template <class T>
+__device__ __forceinline__ T qdiv(T a, T b) { return a / b; }
+template <>
+__device__ __forceinline__ double qdiv<double>(double a, double b) { return fdiv64(a, b); }
+
 // Division in the transport sweeps: the fast reciprocal-based divide for float
-// fields (within 2 ulp; the FP32-bulk mode), IEEE division for double fields.
+// fields (within 2 ulp; the FP32-bulk mode), fdiv64 for double fields.
 __device__ __forceinline__ float bulk_div(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double bulk_div(double a, double b) { return a / b; }
+__device__ __forceinline__ double bulk_div(double a, double b) { return fdiv64(a, b); }
+
+// Sign tests x > 0 and x < 0 of a non-NaN value.  For double, on the bit pattern
+// with the integer pipe (a positive double is a positive 64-bit integer; a
+// negative one other than -0 is an unsigned integer above 2^63), leaving the FP64
+// pipe to the arithmetic; for float, the plain comparison.
+template <class T>
+__device__ __forceinline__ bool gt0(T x) { return x > (T)0; }
+template <>
+__device__ __forceinline__ bool gt0<double>(double x) { return __double_as_longlong(x) > 0LL; }
+template <class T>
+__device__ __forceinline__ bool lt0(T x) { return x < (T)0; }
+template <>
+__device__ __forceinline__ bool lt0<double>(double x) {
+  return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ULL;
+}
 
 // preferred shared-memory carveout (percent) of every step kernel
 #define FARGO_SMEM_CARVEOUT 100

@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
             const T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
             // FP64: -mp / sqrt(d^2 + eps^2) as the reference; FP32: one reciprocal
             // square root (within 2 ulp) instead of the IEEE sqrt and divide
-            T pt = sizeof(T) == 4 ? -mp * rsqrt(distance + s_pot[k][3]) : -mp / sqrt(distance + s_pot[k][3]);
+            T pt = sizeof(T) == 4 ? -mp * rsqrt(distance + s_pot[k][3]) : qdiv(-mp, (T)sqrt(distance + s_pot[k][3]));
             if (P.indirect_term) pt += mp * s_pot[k][4] * (x * xp + y * yp);
             phi += pt;
           }
@@ -555,7 +555,7 @@ __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
   s.zero();
   for (int j = threadIdx.x; j < nsec; j += blockDim.x) {
     size_t q = (size_t)i * nsec + j;
-    T cs = sqrt(KC(T, a, KC_GGM1) * a.d.energy[q] / a.d.dens[q]);
+    T cs = sqrt(qdiv(KC(T, a, KC_GGM1) * a.d.energy[q], a.d.dens[q]));
     a.d.cs[q] = cs;
     s.add(cs);
   }
@@ -788,7 +788,7 @@ __device__ __forceinline__ SrcCell<T> source_cell(const KArgs<T> &a, int i, int 
     const T p1 = press(q - nsec, i - 1);
     const T f1 = phi(q - nsec, i - 1, j);
     const T idr = RT(a, RT_INVDIFFRMED, i);
-    T gradp = (p0 - p1) * (T)2.0 / (D[q] + D[q - nsec]) * idr;
+    T gradp = qdiv((p0 - p1) * (T)2.0, D[q] + D[q - nsec]) * idr;
     T gradphi = (f0 - f1) * idr;
     const T *V = a.d.vtheta;
     T vt2 = V[q] + V[(size_t)i * nsec + jp] + V[q - nsec] + V[(size_t)(i - 1) * nsec + jp];
@@ -805,7 +805,7 @@ __device__ __forceinline__ SrcCell<T> source_cell(const KArgs<T> &a, int i, int 
     o.vr = vr;
   }
   const T idx = RT(a, RT_INVDXTHETA, i);
-  T gradp = (p0 - pm) * (T)2.0 / (D[q] + D[qm]) * idx;
+  T gradp = qdiv((p0 - pm) * (T)2.0, D[q] + D[qm]) * idx;
   T gradphi = (f0 - fm) * idx;
   T vt = a.d.vtheta[q] - dt * (gradp + gradphi);
   vt += dt * RT(a, RT_SUPPTORQUE, i);
@@ -887,16 +887,18 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
   const T *D = a.d.dens, *TRR = a.d.taurr, *TRP = a.d.taurp, *TPP = a.d.taupp;
   const T invdphi = KC(T, a, KC_INVDPHI);
   if (i > 0 && i < nrad - 1) {
-    a.d.vthetaint[q] += dt * RT(a, RT_INVRMED, i) *
-                        ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) * RT(a, RT_INVDIFFRSUP, i) +
-                         (TPP[q] - TPP[qm]) * invdphi + (T)0.5 * (TRP[q] + TRP[q + nsec])) /
-                        ((T)0.5 * (D[q] + D[qm]));
+    a.d.vthetaint[q] += qdiv(dt * RT(a, RT_INVRMED, i) *
+                                 ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) *
+                                      RT(a, RT_INVDIFFRSUP, i) +
+                                  (TPP[q] - TPP[qm]) * invdphi + (T)0.5 * (TRP[q] + TRP[q + nsec])),
+                             (T)0.5 * (D[q] + D[qm]));
   }
   if (i > 0) {
-    a.d.vradint[q] += dt * RT(a, RT_INVRINF, i) *
-                      ((RT(a, RT_RMED, i) * TRR[q] - RT(a, RT_RMED, i - 1) * TRR[q - nsec]) * RT(a, RT_INVDIFFRMED, i) +
-                       (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])) /
-                      ((T)0.5 * (D[q] + D[q - nsec]));
+    a.d.vradint[q] += qdiv(dt * RT(a, RT_INVRINF, i) *
+                               ((RT(a, RT_RMED, i) * TRR[q] - RT(a, RT_RMED, i - 1) * TRR[q - nsec]) *
+                                    RT(a, RT_INVDIFFRMED, i) +
+                                (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])),
+                           (T)0.5 * (D[q] + D[q - nsec]));
   }
   // (not in a padded substep, dt = 0: the edge rings keep the velocities the last
   // transport gave them)
@@ -919,11 +921,11 @@ __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
   const T c2 = (T)(CVNR * CVNR);
   auto qr = [&](size_t k) -> T {
     T dv = VR[k + nsec] - VR[k];
-    return (dv < (T)0.0) ? c2 * D[k] * dv * dv : (T)0.0;
+    return lt0(dv) ? c2 * D[k] * dv * dv : (T)0.0;
   };
   auto qt = [&](size_t k, size_t kp) -> T {
     T dv = VT[kp] - VT[k];
-    return (dv < (T)0.0) ? c2 * D[k] * dv * dv : (T)0.0;
+    return lt0(dv) ? c2 * D[k] * dv * dv : (T)0.0;
   };
   const T qr0 = qr(q), qt0 = qt(q, qp);
   T vrnew = (T)0.0;
@@ -931,13 +933,13 @@ __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
     const T qr1 = qr(q - nsec);
     const T dens = D[q] + D[q - nsec];
     const T densint = qr0 - qr1;
-    vrnew = VR[q] - dt * (T)2.0 / dens * densint * RT(a, RT_INVDIFFRMED, i);
+    vrnew = VR[q] - qdiv(dt * (T)2.0, dens) * densint * RT(a, RT_INVDIFFRMED, i);
   }
   const T qtm = qt(qm, q);
   const T dens2 = D[q] + D[qm];
   const T tempint = qt0 - qtm;
   const T idx = RT(a, RT_INVDXTHETA, i);
-  const T vtnew = VT[q] - dt * (T)2.0 / dens2 * tempint * idx;
+  const T vtnew = VT[q] - qdiv(dt * (T)2.0, dens2) * tempint * idx;
   if (a.P.adiabatic) {
     a.d.energyint[q] = a.d.energy[q] - dt * qr0 * (VR[q + nsec] - VR[q]) * RT(a, RT_INVDIFFRSUP, i) -
                        dt * qt0 * (VT[qp] - VT[q]) * idx;
@@ -964,7 +966,8 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
     const size_t k = (size_t)ii * nsec + j;
     const T nu = a.d.nu[ii];
     if (nu != (T)0.0) {
-      T qp = (T)0.5 / nu / D[k] * (a.d.taurr[k] * a.d.taurr[k] + a.d.taurp[k] * a.d.taurp[k] + a.d.taupp[k] * a.d.taupp[k]);
+      T qp = qdiv(qdiv((T)0.5, nu), D[k]) *
+             (a.d.taurr[k] * a.d.taurr[k] + a.d.taurp[k] * a.d.taurp[k] + a.d.taupp[k] * a.d.taupp[k]);
       qp += (T)(2.0 / 9.0) * nu * D[k] * a.d.divv[k] * a.d.divv[k];
       return qp;
     }
@@ -986,12 +989,12 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
   if (!a.P.cooling) {
     T num = dt * qp + ei;
     T den = (T)1.0 + KC(T, a, KC_GM1) * dt * dv;
-    enew = num / den;
+    enew = qdiv(num, den);
   } else {
     const T em = RT(a, RT_ENERGYMED, i), sm = RT(a, RT_SIGMAMED, i), ct = RT(a, RT_COOLTIME, i), qm = RT(a, RT_QPLUSMED, i);
-    T num = em * dt * D[q] / sm + ct * ei + dt * ct * (qp - qm * D[q] / sm);
+    T num = qdiv(em * dt * D[q], sm) + ct * ei + dt * ct * (qp - qdiv(qm * D[q], sm));
     T den = dt + ct + KC(T, a, KC_GM1) * dt * ct * dv;
-    enew = num / den;
+    enew = qdiv(num, den);
     if (dt == (T)0.0) enew = ei;  // a padded substep: (ct ei) / ct is not exactly ei
   }
   a.d.energy[q] = enew;
@@ -1055,7 +1058,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
       q[3] = d * (a.d.vtheta[qk] + rm * Om) * rm;
       q[4] = P.adiabatic ? a.d.energy[qk] : (T)0.0;
       q[5] = d;
-      inv = (T)1.0 / (d + (T)1e-20);
+      inv = qdiv((T)1.0, d + (T)1e-20);
       vr = v0;
     } else if (col && k == nrad) {
       vr = a.d.vrad[(size_t)k * nsec + j];
@@ -1083,7 +1086,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
         const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
         const T dqm = (w0 - wm) * idm0;
         const T dqp = (wp - w0) * idm1;
-        v = (dqp * dqm > (T)0.0) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+        v = gt0(dqp * dqm) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
       }
       sD[f][dd][x] = v;
     }
@@ -1096,7 +1099,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
     const T v = sV[ss][x];
     // the upwind side and the coefficient of its slope, the same for every stream:
     // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise
-    const bool up = v > (T)0.0;
+    const bool up = gt0(v);
     T coef = (T)0.0;
     if (in) {
       const T lo = sRT[1][ss + 1] - sRT[1][ss] - v * dt;
@@ -1190,7 +1193,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
     for (int j = tid; j < nsec; j += nt) {
       const T dqm = q[j] - q[jm1(j, nsec)];
       const T dqp = q[jp1(j, nsec)] - q[j];
-      dq[j] = (dqp * dqm > (T)0.0) ? dqp * dqm / (dqp + dqm) * invdx : (T)0.0;
+      dq[j] = gt0(dqp * dqm) ? qdiv(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
     }
   };
   // StarThetaKernel2: upwind interface value
@@ -1199,7 +1202,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
       const T v = vel ? vel[j] : vconst;
       const T ksi = v * tdt;
       const int jm = jm1(j, nsec);
-      qs[j] = (ksi > (T)0.0) ? q[jm] + (dxtheta - ksi) * dq[jm] : q[j] - (dxtheta + ksi) * dq[j];
+      qs[j] = gt0(ksi) ? q[jm] + (dxtheta - ksi) * dq[jm] : q[j] - (dxtheta + ksi) * dq[j];
     }
   };
   // QuantitiesAdvection with velocity vel[] (or the constant vconst)
@@ -1207,7 +1210,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
     slope(Dn, B);
     // DivisePolarGrid with the density's reciprocal, formed once per cell for every
     // quantity (one divide per cell instead of one per quantity, within an ulp)
-    for (int j = tid; j < nsec; j += nt) ID[j] = (T)1.0 / (Dn[j] + (T)1e-20);
+    for (int j = tid; j < nsec; j += nt) ID[j] = qdiv((T)1.0, Dn[j] + (T)1e-20);
     __syncthreads();
     star(Dn, B, DS, vel, vconst);
     __syncthreads();
@@ -1402,12 +1405,12 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
-      dq[k] = (dqp * dqm > (T)0.0) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+      dq[k] = gt0(dqp * dqm) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
     }
 #pragma unroll
     for (int c = 0; c < 5; c++) {
       const T ksi = v[c] * tdt;
-      upw[c] = ksi > (T)0.0;
+      upw[c] = gt0(ksi);
       // x + (dxtheta - ksi) q' upwind from the left, x - (dxtheta + ksi) q' from the right
       coef[c] = upw[c] ? dxtheta - ksi : -(dxtheta + ksi);
       const T ds = (upw[c] ? d[c + 1] : d[c + 2]) + coef[c] * (upw[c] ? dq[c] : dq[c + 1]);
@@ -1435,7 +1438,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
 #pragma unroll
       for (int k = 0; k < 6; k++) {
         const T dqm = wv[k + 1] - wv[k], dqp = wv[k + 2] - wv[k + 1];
-        dw[k] = (dqp * dqm > (T)0.0) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+        dw[k] = gt0(dqp * dqm) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
       }
 #pragma unroll
       for (int c = 0; c < 5; c++) sw[c] = (upw[c] ? wv[c + 1] : wv[c + 2]) + coef[c] * (upw[c] ? dw[c] : dw[c + 1]);
@@ -1479,9 +1482,9 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
   const int jm = jm1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens;
-  const T vr = (i == 0) ? (T)0.0 : (a.d.radmomp[q - nsec] + a.d.radmomm[q]) / (D[q] + D[q - nsec] + (T)1e-20);
+  const T vr = (i == 0) ? (T)0.0 : qdiv(a.d.radmomp[q - nsec] + a.d.radmomm[q], D[q] + D[q - nsec] + (T)1e-20);
   const T rm = RT(a, RT_RMED, i);
-  const T vt = (a.d.thetamomp[qm] + a.d.thetamomm[q]) / (D[q] + D[qm] + (T)1e-15) / rm - rm * Om;
+  const T vt = qdiv(qdiv(a.d.thetamomp[qm] + a.d.thetamomm[q], D[q] + D[qm] + (T)1e-15), rm) - rm * Om;
   // a substep with dt = 0 (a padded one) keeps the velocities: re-deriving them
   // from the momenta is not exact
   if (dt != (T)0.0) {
@@ -1489,8 +1492,8 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
     a.d.vtheta[q] = vt;
   }
   if (with_temperature) {
-    if (!a.P.adiabatic) a.d.temperature[q] = a.d.pressure[q] / D[q];
-    else a.d.temperature[q] = KC(T, a, KC_GM1) * a.d.energy[q] / D[q];
+    if (!a.P.adiabatic) a.d.temperature[q] = qdiv(a.d.pressure[q], D[q]);
+    else a.d.temperature[q] = qdiv(KC(T, a, KC_GM1) * a.d.energy[q], D[q]);
   }
   if (!isfinite(D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
 }
