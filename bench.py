@@ -60,6 +60,7 @@ WORKLOADS = {"c1": "isothermal disk 128x384, 1 planet (fixed orbit)",
 # as the first substeps of a run take a smaller CFL step)
 SAMPLE_DT_DIVISOR = {"c1": 30, "c2": 54, "c3": 220, "wide": 200}
 REF_EXE = os.path.join(ROOT, "oracle", "_ref", "fargo_ref_cpu")
+REF_CUDA_EXE = os.path.join(ROOT, "oracle", "_ref", "fargoGPU_sm103a")
 
 
 def parse():
@@ -71,6 +72,9 @@ def parse():
     ap.add_argument("--config", default="c3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the 256x768 self-gravitating disk extra")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip the reference's own CUDA build on the isothermal 128x384 disk")
+    ap.add_argument("--no-drift", action="store_true", help="skip the 100-orbit FP32-bulk drift measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-correction measurement")
     ap.add_argument("--profile", choices=["fp32", "fp64"], default=None,
@@ -415,28 +419,30 @@ def _par_values(text):
     return vals
 
 
-def reference_cpu_sample(cfg, ndt, threads, sample_divisor=None):
-    """Runs the reference's main() (CPU build) on the workload's .par with the DT
-    shortened to about one hydro substep, for ndt DTs, on `threads` host threads
-    (blocks of each launch in parallel).  Returns (substeps, AlgoGas seconds,
-    cells) over all DTs, from the binary's REFSTEP lines.  Reads no product code."""
-    if not os.path.exists(REF_EXE):
-        raise RuntimeError(f"{REF_EXE} is missing (build(): oracle/ref_emul/build_ref.py)")
+def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=1000000000, outdir=None):
+    """Runs a build of the reference's main() (oracle/_ref: its CPU build or its own
+    CUDA build) on the workload's .par for ndt DTs (Ntot = ndt - 1: the reference
+    runs Ntot + 1), the DT divided by dt_divisor, dumps every `ninterm` DTs into
+    outdir (a temporary directory when None), the seeded noise of the .par's
+    SigmaNoise / EnergyNoise / NoiseSeed keys through the build's link-time
+    wrappers.  Returns ([(substeps, AlgoGas seconds) per DT], cells) from the
+    binary's REFSTEP lines.  Reads no product code."""
+    if not os.path.exists(exe):
+        raise RuntimeError(f"{exe} is missing (built by build(): oracle/ref_emul, oracle/ref_cuda)")
     src = os.path.join(CONFIG_DIR, CONFIG_FILES[cfg])
     text = open(src).read()
     vals = _par_values(text)
-    divisor = sample_divisor or SAMPLE_DT_DIVISOR.get(cfg, 100)
     with tempfile.TemporaryDirectory() as d:
-        out = os.path.join(d, "out")
-        os.makedirs(out)
+        out = outdir or os.path.join(d, "out")
+        os.makedirs(out, exist_ok=True)
         keep = []
         for line in text.splitlines():
             k = line.split()[0].upper() if line.split() else ""
             if k in ("NTOT", "NINTERM", "DT", "OUTPUTDIR", "PLANETCONFIG"):
                 continue
             keep.append(line)
-        keep += [f"Ntot {ndt - 1}", "Ninterm 1000000000",
-                 f"DT {float(vals.get('DT', '0.314159265359')) / divisor!r}", f"OutputDir {out}/"]
+        keep += [f"Ntot {ndt - 1}", f"Ninterm {int(ninterm)}",
+                 f"DT {float(vals.get('DT', '0.314159265359')) / dt_divisor!r}", f"OutputDir {out}/"]
         if "PLANETCONFIG" in vals:
             # the reference keeps the planet file's path in a fixed-size buffer
             # (src/Main.cu:248-249): a short copy beside the run
@@ -447,19 +453,53 @@ def reference_cpu_sample(cfg, ndt, threads, sample_divisor=None):
         par = os.path.join(d, "run.par")
         open(par, "w").write("\n".join(keep) + "\n")
         env = dict(os.environ)
-        env["FARGO_REF_THREADS"] = str(threads)
-        env["OMP_NUM_THREADS"] = str(threads)
+        env.update(env_extra or {})
         for key, var in (("SIGMANOISE", "FARGO_REF_SIGMA_NOISE"), ("ENERGYNOISE", "FARGO_REF_ENERGY_NOISE"),
                          ("NOISESEED", "FARGO_REF_NOISE_SEED")):
             if key in vals:
                 env[var] = vals[key]
-        r = subprocess.run([REF_EXE, par], input="0\n", capture_output=True, text=True, env=env, cwd=d,
+        r = subprocess.run([exe, par], input="0\n", capture_output=True, text=True, env=env, cwd=d,
                            timeout=3600)
         if r.returncode != 0:
-            raise RuntimeError(f"reference CPU build failed ({r.returncode}): {(r.stdout + r.stderr)[-600:]}")
+            raise RuntimeError(f"{os.path.basename(exe)} failed ({r.returncode}): {(r.stdout + r.stderr)[-600:]}")
         steps = [m.groups() for m in re.finditer(r"REFSTEP (\d+) (\d+) ([0-9.eE+-]+)", r.stderr)]
     cells = int(vals["NRAD"]) * int(vals["NSEC"])
-    return [(int(s), float(t)) for _, s, t in steps], cells, divisor
+    return [(int(s), float(t)) for _, s, t in steps], cells
+
+
+def reference_cpu_sample(cfg, ndt, threads, sample_divisor=None):
+    """The reference's CPU build on a bounded sample of the workload: the DT
+    shortened to about one hydro substep, on `threads` host threads (blocks of
+    each launch in parallel).  Returns ([(substeps, seconds) per DT], cells, divisor)."""
+    divisor = sample_divisor or SAMPLE_DT_DIVISOR.get(cfg, 100)
+    steps, cells = run_reference_exe(REF_EXE, cfg, ndt, {"FARGO_REF_THREADS": str(threads),
+                                                         "OMP_NUM_THREADS": str(threads)}, dt_divisor=divisor)
+    return steps, cells, divisor
+
+
+def reference_cuda(fg, stream, flush):
+    """The reference's own CUDA build (oracle/_ref/fargoGPU_sm103a, sm_103a, two
+    source-compat fixes) on the isothermal 128 x 384 disk -- the one configuration
+    whose kernels were read for out-of-bounds access -- for 15 DTs (about 220 hydro
+    substeps, the first DT untimed), timed by the AlgoGas wrapper; beside it, this
+    code's FP64 mode on the same disk and DTs, device-resident and through the C-ABI."""
+    if not os.path.exists(REF_CUDA_EXE):
+        err = REF_CUDA_EXE + ".build_error"
+        return {"unavailable": open(err).read()[-300:] if os.path.exists(err) else f"{REF_CUDA_EXE} not built"}
+    steps, cells = run_reference_exe(REF_CUDA_EXE, "c1", 15)
+    n, t = sum(s for s, _ in steps[1:]), sum(x for _, x in steps[1:])
+    p1, pl1, _ = workload("c1")
+    r = measure_mode(fg, p1, pl1, fg.FARGO_FP64, stream, flush, 14, 1)
+    w, ne, _, _ = r["e2e"]
+    own = r["substeps"] * cells / (r["ms"] * 1e-3)
+    return {"workload": WORKLOADS["c1"], "config_file": "configs/" + CONFIG_FILES["c1"],
+            "build": "the reference's src/*.cu with nvcc 13 for sm_103a (Makefile flags; __shfl_down_sync and "
+                     "::array compat fixes), seeded noise and AlgoGas timing through link-time wrappers",
+            "value": n * cells / t, "unit": METRIC, "dtype": "f64", "substeps": n, "seconds": t,
+            "timing": "host clock around each AlgoGas call (the reference synchronises the device after every "
+                      "launch), DTs 2..15",
+            "gb300_fp64_same_disk": {"value": own, "e2e": ne * cells / w, "unit": METRIC,
+                                     "ms_per_dt": r["ms"] / 14}}
 
 
 def cpu_baselines(cfg, params, planets):
@@ -596,6 +636,11 @@ def run_own(args, world, rank, local):
     }
     if not args.no_cpu_baseline:
         line.update(cpu_baselines(args.config, params, planets))
+    if not args.no_reference_cuda and world == 1:
+        try:
+            line["reference_cuda"] = reference_cuda(fg, stream, flush)
+        except Exception as e:  # reported, never fatal to the own arm
+            line["reference_cuda"] = {"unavailable": str(e)[-300:]}
     if not args.no_extra and world == 1 and args.config != "c2":
         p2, pl2, n2 = workload("c2")
         e = {"workload": n2, "config_file": "configs/c2_selfgravity.par"}
@@ -608,6 +653,15 @@ def run_own(args, world, rank, local):
                 e[key]["e2e"] = ne * p2.nrad * p2.nsec / w
         e["fp32_error_vs_fp64"] = fp32_errors(fg, p2, pl2, stream)
         line["c2"] = e
+    if not args.no_drift and world == 1:
+        from cudaprotoplanetarydisks_gb300.drift import drift
+        dr = drift("c2", 100, every=25)
+        line["fp32_drift_100_orbits"] = {
+            "workload": WORKLOADS["c2"], "against": "FP64 mode of this code from the same initial state",
+            "dts": dr["dts"], "dens_rel_l2": dr["final_dens_rel_l2"],
+            "fields_after_100_orbits": {k: dr["by_orbit"][-1][k] for k in ("dens", "vrad", "vtheta")},
+            "dens_rel_l2_by_orbit": {r["orbits"]: r["dens"]["rel_l2"] for r in dr["by_orbit"]},
+            "target": 1e-5, "seconds": dr["seconds_fp64"] + dr["seconds_fp32"]}
     if not args.no_batch and world == 1:
         line["batch_c4"] = batch_ensemble()
     if not args.no_learned and world == 1:

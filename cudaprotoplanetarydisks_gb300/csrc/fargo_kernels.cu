@@ -1153,8 +1153,8 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x, nt = blockDim.x;
   T *base = a.az_smem ? (T *)az_smem : a.d.az_scratch + (size_t)i * AZ_NARR * nsec;
   T *V = base, *Dn = base + nsec, *En = base + 2 * nsec, *M0 = base + 3 * nsec, *M1 = base + 4 * nsec,
-    *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *S = base + 9 * nsec,
-    *DS = base + 10 * nsec, *ID = base + 11 * nsec;
+    *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *FL = base + 9 * nsec,
+    *F = base + 10 * nsec, *ID = base + 11 * nsec;
   const Ctl *c = a.d.ctl;
   const double dt = c->dt;
   const size_t row = (size_t)i * nsec;
@@ -1188,48 +1188,63 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
   const T dxrad = RT(a, RT_DRAD, i) * (T)dt, isurf = RT(a, RT_INVSURF, i);
   const T tdt = (T)dt;
-  // StarThetaKernel: harmonic slope of q into dq
-  auto slope = [&](const T *q, T *dq) {
-    for (int j = tid; j < nsec; j += nt) {
-      const T dqm = q[j] - q[jm1(j, nsec)];
-      const T dqp = q[jp1(j, nsec)] - q[j];
-      dq[j] = gt0(dqp * dqm) ? qdiv(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
-    }
+  // StarThetaKernel: harmonic slope of q at cell j
+  auto slope_at = [&](const T *q, int j) -> T {
+    const T dqm = q[j] - q[jm1(j, nsec)];
+    const T dqp = q[jp1(j, nsec)] - q[j];
+    return gt0(dqp * dqm) ? qdiv(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
   };
-  // StarThetaKernel2: upwind interface value
-  auto star = [&](const T *q, const T *dq, T *qs, const T *vel, T vconst) {
+  // QuantitiesAdvection with velocity vel[] (or the constant vconst).  Per
+  // interface j (between cells j-1 and j) the upwind side, its slope coefficient
+  // and the mass flux dxrad Dstar v are the same for every quantity: ksi = v dt is
+  // kept in KS (the velocity's slot) and the flux factor in F, formed once per
+  // sweep; each quantity then needs its W = Q / rho, its slopes, one upwind value
+  // and flux per interface and its update (StarThetaKernel/2, DivisePolarGrid,
+  // VanLeerThetaKernel, src/Kernels.cu:1049-1170).  Three barriers per quantity:
+  // the update of one quantity and W of the next share a phase.
+  T *const KS = V;
+  auto advect = [&](const T *vel, T vconst) {
+    for (int j = tid; j < nsec; j += nt) {
+      B[j] = slope_at(Dn, j);
+      // DivisePolarGrid with the density's reciprocal, formed once per cell for every
+      // quantity (one divide per cell instead of one per quantity, within an ulp)
+      ID[j] = qdiv((T)1.0, Dn[j] + (T)1e-20);
+    }
+    __syncthreads();
     for (int j = tid; j < nsec; j += nt) {
       const T v = vel ? vel[j] : vconst;
       const T ksi = v * tdt;
+      const bool up = gt0(ksi);
       const int jm = jm1(j, nsec);
-      qs[j] = gt0(ksi) ? q[jm] + (dxtheta - ksi) * dq[jm] : q[j] - (dxtheta + ksi) * dq[j];
+      const T cf = up ? dxtheta - ksi : -(dxtheta + ksi);
+      const T ds = (up ? Dn[jm] : Dn[j]) + cf * (up ? B[jm] : B[j]);
+      F[j] = dxrad * ds * v;
+      KS[j] = ksi;  // vel[j] (== KS[j] in the first sweep) is read by this thread only
     }
-  };
-  // QuantitiesAdvection with velocity vel[] (or the constant vconst)
-  auto advect = [&](const T *vel, T vconst) {
-    slope(Dn, B);
-    // DivisePolarGrid with the density's reciprocal, formed once per cell for every
-    // quantity (one divide per cell instead of one per quantity, within an ulp)
-    for (int j = tid; j < nsec; j += nt) ID[j] = qdiv((T)1.0, Dn[j] + (T)1e-20);
-    __syncthreads();
-    star(Dn, B, DS, vel, vconst);
-    __syncthreads();
     T *qs[6] = {M0, M1, M2, M3, En, Dn};
-    for (int f = 0; f < 6; f++) {
-      if (f == 4 && !P.adiabatic) continue;
-      T *Q = qs[f];
-      for (int j = tid; j < nsec; j += nt) W[j] = Q[j] * ID[j];
-      __syncthreads();
-      slope(W, B);
-      __syncthreads();
-      star(W, B, S, vel, vconst);
+    int nf = 0, fs[6];
+    for (int f = 0; f < 6; f++)
+      if (f != 4 || P.adiabatic) fs[nf++] = f;
+    __syncthreads();
+    for (int j = tid; j < nsec; j += nt) W[j] = qs[fs[0]][j] * ID[j];
+    __syncthreads();
+    for (int k = 0; k < nf; k++) {
+      T *Q = qs[fs[k]];
+      for (int j = tid; j < nsec; j += nt) B[j] = slope_at(W, j);
       __syncthreads();
       for (int j = tid; j < nsec; j += nt) {
-        const int jp = jp1(j, nsec);
-        const T v0 = vel ? vel[j] : vconst, v1 = vel ? vel[jp] : vconst;
-        T varq = dxrad * S[j] * DS[j] * v0;
-        varq -= dxrad * S[jp] * DS[jp] * v1;
+        const T ksi = KS[j];
+        const bool up = gt0(ksi);
+        const int jm = jm1(j, nsec);
+        const T cf = up ? dxtheta - ksi : -(dxtheta + ksi);
+        FL[j] = ((up ? W[jm] : W[j]) + cf * (up ? B[jm] : B[j])) * F[j];
+      }
+      __syncthreads();
+      T *Qn = k + 1 < nf ? qs[fs[k + 1]] : nullptr;
+      for (int j = tid; j < nsec; j += nt) {
+        const T varq = FL[j] - FL[jp1(j, nsec)];
         Q[j] += varq * isurf;
+        if (Qn) W[j] = Qn[j] * ID[j];
       }
       __syncthreads();
     }

@@ -1,0 +1,44 @@
+"""The reference's own CUDA build on the GB300 against this code's FP64 mode.
+
+oracle/_ref/fargoGPU_sm103a is the reference's src/*.cu compiled by nvcc for
+sm_103a with two source-compat fixes (oracle/ref_cuda/build_ref_cuda.py).  It runs
+the isothermal 128 x 384 disk (configs/c1_isothermal.par: WALL boundaries, no
+self-gravity -- the configuration whose kernels were read for out-of-bounds access)
+for three DTs with a dump before each.  The same disk advanced by this code in FP64
+must take the same number of hydro substeps in every DT and match the reference's
+gasdens / gasvrad / gasvtheta dumps after one and two DTs within 1e-9 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import bench
+import cudaprotoplanetarydisks_gb300 as fg
+from tests.helpers import rel_l2, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_cuda_build_matches_fp64_path(tmp_path):
+    if not os.path.exists(bench.REF_CUDA_EXE):
+        err = bench.REF_CUDA_EXE + ".build_error"
+        pytest.fail(open(err).read() if os.path.exists(err) else "the reference's CUDA build is missing")
+    out = str(tmp_path / "out")
+    steps, cells = bench.run_reference_exe(bench.REF_CUDA_EXE, "c1", 3, ninterm=1, outdir=out)
+    assert len(steps) == 3
+    params, planets = fg.load_config("c1")
+    disk = fg.Disk(params, planets, fg.FARGO_FP64)
+    try:
+        shape = (params.nrad, params.nsec)
+        for k in (1, 2):
+            assert disk.step_DT() == steps[k - 1][0], (k, steps[k - 1])
+            for name in ("dens", "vrad", "vtheta"):
+                ref = np.fromfile(os.path.join(out, name, f"{name}{k}.dat"), dtype=np.float64).reshape(shape)
+                mine = disk.field(name)[:-1]
+                full_ref = np.vstack([ref, np.zeros((1, params.nsec))])
+                full_mine = np.vstack([mine, np.zeros((1, params.nsec))])
+                err = rel_linf(full_mine, full_ref)
+                assert err < 1e-9, (name, k, err, rel_l2(full_mine, full_ref))
+    finally:
+        disk.close()
