@@ -201,6 +201,7 @@ def kernel_bytes(name, params, esize):
         "k_artvisc": (3 + ad) + (2 + ad),
         "k_energy": 8 + 2,
         "k_transport_radial": (3 + ad) + (5 + ad),
+        "k_transport_radial_tma": (3 + ad) + (5 + ad),
         "k_transport_azimuthal": (6 + ad) + (5 + ad),
         "k_velocities": (5 + 1) + 3,
         "k_temperature": 3,

@@ -103,6 +103,7 @@ SIGNATURES = [
     ("fargo_get_fields", _I, [_P, _DP, _DP, _DP, _DP, _DP]),
     ("fargo_set_fields", _I, [_P, _DP, _DP, _DP, _DP]),
     ("fargo_get_field", _I, [_P, _I, _DP]),
+    ("fargo_get_field_device", _I, [_P, _I, _P]),
     ("fargo_get_planets", _I, [_P, ctypes.POINTER(FargoPlanet), _I, ctypes.POINTER(_I)]),
     ("fargo_get_scalars", _I, [_P, ctypes.POINTER(FargoScalars)]),
     ("fargo_get_mesh", _I, [_P, _DP, _DP, _DP, _DP]),

@@ -6,6 +6,8 @@
 // (DT start, sound speed of the energy equation) followed by a conditional WHILE
 // node whose body is one hydro substep; the substep's last kernel sets the loop
 // condition from the device-side dtemp, so a DT runs without any host sync.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -68,11 +70,48 @@ struct fargo_ctx {
   bool use_pad = true;        // two substeps per loop body, the second padded (dt = 0) after the DT's last
   bool sg_generic = false;    // run-time FFT plans only (the compile-time ones compared in the tests)
   bool az_generic = false;    // barrier-per-phase azimuthal kernel instead of the register-blocked one
+  // radial transport with TMA-staged tiles (k_transport_radial_tma): its tensor maps
+  // and persistent grid; off when the rows are not 16-byte strided or FARGO_NO_TMA=1
+  RadMaps rad_maps;
+  bool use_tma = false;
+  int rad_grid = 0;
 };
 
 namespace {
 // ring buffers of the barrier-per-phase azimuthal kernel (AZ_NARR in fargo_kernels.cu)
 constexpr int AZ_NARR_HOST = 12;
+
+// 2D tensor maps (sectors x rings 0..nrad, one box = RAD_BW sectors x RAD_BR rings,
+// zero fill outside) of the density, Vrad, Vtheta and (energy equation) energy,
+// for k_transport_radial_tma.  TMA needs 16-byte row strides (nsec * element size).
+// The encoder is the driver's cuTensorMapEncodeTiled, reached through the runtime.
+template <class T>
+void make_rad_maps(fargo_ctx *c) {
+  c->use_tma = false;
+  const size_t E = sizeof(T);
+  if (((size_t)c->P.nsec * E) % 16 != 0) return;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void **)&enc, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !enc)
+    return;
+  const cuuint64_t dims[2] = {(cuuint64_t)c->P.nsec, (cuuint64_t)c->P.nrad + 1};
+  const cuuint64_t strides[1] = {(cuuint64_t)c->P.nsec * E};
+  const cuuint32_t box[2] = {(cuuint32_t)RAD_BW(T), (cuuint32_t)RAD_BR};
+  const cuuint32_t es[2] = {1, 1};
+  const CUtensorMapDataType dt = E == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  void *src[4] = {c->dens, c->vrad, c->vtheta, c->P.adiabatic ? c->energy : c->dens};
+  CUtensorMap *dst[4] = {&c->rad_maps.dens, &c->rad_maps.vrad, &c->rad_maps.vtheta, &c->rad_maps.energy};
+  for (int f = 0; f < 4; f++) {
+    if (!src[f]) return;
+    if (enc(dst[f], dt, 2, src[f], dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return;
+  }
+  c->rad_grid = rad_tma_grid<T>(c->P.nrad, c->P.nsec);
+  c->use_tma = c->rad_grid > 0;
+}
 
 int set_err(fargo_ctx *c, int code, const std::string &msg) {
   if (c) c->err = msg;
@@ -154,6 +193,8 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.az_regs = c->az_regs;
   a.pdl = c->use_pdl ? 1 : 0;
   a.sg_generic = c->sg_generic ? 1 : 0;
+  a.rad_maps = c->use_tma ? &c->rad_maps : nullptr;
+  a.rad_grid = c->rad_grid;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -406,6 +447,11 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
       CK(prepare_kernels<T>(0, 0));
       if ((rc = dev_alloc(c, &c->az_scratch, (size_t)p.nrad * AZ_NARR_HOST * p.nsec * E))) return rc;
     }
+  }
+  // TMA maps of the radial transport's input fields
+  {
+    const char *nt = std::getenv("FARGO_NO_TMA");
+    if (!(nt && nt[0] == '1')) make_rad_maps<T>(c);
   }
   CK(cudaStreamSynchronize(c->stream));
   // density first: self-gravity set-up needs it
@@ -852,6 +898,22 @@ int fargo_get_field(fargo_ctx *c, int which, double *host) {
       pot -= ix * x + iy * y;
       host[(size_t)i * c->P.nsec + j] += pot;
     }
+  return FARGO_OK;
+}
+
+int fargo_get_field_device(fargo_ctx *c, int which, double *dev) {
+  if (!c || !dev) return FARGO_ERR_STATE;
+  void *p = field_ptr(c, which);
+  if (!p || which == FARGO_FIELD_POTENTIAL)
+    return set_err(c, FARGO_ERR_INVALID, "field not held on the device in this configuration");
+  const size_t n = c->h.size_grid;
+  if (c->esize == 8) {
+    CK(cudaMemcpyAsync(dev, p, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+  } else {
+    launch_convert_to_f64(p, dev, n, (int)c->esize, c->stream);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(c->stream));
   return FARGO_OK;
 }
 

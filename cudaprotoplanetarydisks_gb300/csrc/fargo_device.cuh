@@ -1,5 +1,6 @@
 // fargo_device.cuh -- device-side argument block and helpers for the step kernels.
 #pragma once
+#include <cuda.h>
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -48,6 +49,12 @@ struct SgDev {
   int M;                        // nsec / 2 + 1
 };
 
+// TMA descriptors of the fields the radial transport reads (k_transport_radial_tma):
+// 2D maps (sectors x rings 0..nrad) of the density, Vrad, Vtheta and energy.
+struct RadMaps {
+  CUtensorMap dens, vrad, vtheta, energy;
+};
+
 template <class T>
 struct KArgs {
   DevParams P;
@@ -69,6 +76,8 @@ struct KArgs {
   int pdl;                         // launch with programmatic dependent launch
   int guard;                       // 1: return at once when the DT loop is done (a next substep's kernels)
   int sg_generic;                  // self-gravity FFTs with the run-time plan at every length
+  const RadMaps *rad_maps;         // host copy of the radial transport's TMA maps (nullptr: plain loads)
+  int rad_grid;                    // CTAs of the persistent TMA radial transport
   SgDev sg;
 };
 

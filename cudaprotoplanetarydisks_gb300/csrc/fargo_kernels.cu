@@ -1009,60 +1009,29 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
 // memory, then the slopes dq(k) of the rings, the upwind values at the
 // interfaces and the cell updates are each formed once, one barrier between
 // the phases.
-#define RAD_TR 16
 #define RAD_NY 10  // thread rows: at most two rows per phase for every warp
 #define RAD_NS 7   // streams: rmp, rmm, tmp, tmm, energy, density (as q/rho), raw density
 #define RAD_SMEM(T) \
   (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 2) + RAD_NS * (RAD_TR + 1)))
+
+// The radial tile's shared arrays (32 sectors x RAD_TR rings and their halos).
 template <class T>
-__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
-  pdl_enter();
-  constexpr int TW = 32, TR = RAD_TR, NS = RAD_NS;
-  extern __shared__ __align__(16) unsigned char rad_smem[];
-  T(*sW)[TR + 4][TW] = reinterpret_cast<T(*)[TR + 4][TW]>(rad_smem);    // q/rho, rings i0-2 .. i0+TR+1
-  T(*sQ)[TR][TW] = reinterpret_cast<T(*)[TR][TW]>(sW + NS);              // raw quantities of the tile's rings
-  T(*sV)[TW] = reinterpret_cast<T(*)[TW]>(sQ + 6);                       // Vrad at interfaces i0 .. i0+TR
-  T(*sD)[TR + 2][TW] = reinterpret_cast<T(*)[TR + 2][TW]>(sV + TR + 1);  // slopes of rings i0-1 .. i0+TR
-  T(*sS)[TR + 1][TW] = reinterpret_cast<T(*)[TR + 1][TW]>(sD + NS);      // interface values at i0 .. i0+TR
-  const DevParams &P = a.P;
-  const int nrad = P.nrad, nsec = P.nsec;
-  constexpr int ny = RAD_NY;
-  const int x = threadIdx.x, y = threadIdx.y;
-  const int j = blockIdx.x * TW + x, i0 = blockIdx.y * TR;
-  const bool col = j < nsec;
-  const int jp = col ? jp1(j, nsec) : 0;
-  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT), Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
-  // ring-table rows of rings i0-1 .. i0+TR+1 (zero outside 0 .. nrad), staged with
-  // the tile so that no phase after a barrier loads from global memory
-  __shared__ T sRT[5][TR + 3];  // INVDIFFRMED, RMED, RINF, RSUP, INVSURF
-  if (y == 0 && x < TR + 3) {
-    const int k = i0 - 1 + x;
-    const bool ok = k >= 0 && k <= nrad;
-    sRT[0][x] = ok ? RT(a, RT_INVDIFFRMED, k) : (T)0;
-    sRT[1][x] = ok ? RT(a, RT_RMED, k) : (T)0;
-    sRT[2][x] = ok ? RT(a, RT_RINF, k) : (T)0;
-    sRT[3][x] = ok ? RT(a, RT_RSUP, k) : (T)0;
-    sRT[4][x] = ok ? RT(a, RT_INVSURF, k) : (T)0;
+struct RadTile {
+  static constexpr int TW = 32, TR = RAD_TR, NS = RAD_NS;
+  T (*sW)[TR + 4][TW];  // q/rho, rings i0-2 .. i0+TR+1
+  T (*sQ)[TR][TW];      // raw quantities of the tile's rings
+  T (*sV)[TW];          // Vrad at interfaces i0 .. i0+TR
+  T (*sD)[TR + 2][TW];  // slopes of rings i0-1 .. i0+TR
+  T (*sS)[TR + 1][TW];  // interface values at i0 .. i0+TR
+  __device__ __forceinline__ explicit RadTile(unsigned char *smem) {
+    sW = reinterpret_cast<T(*)[TR + 4][TW]>(smem);
+    sQ = reinterpret_cast<T(*)[TR][TW]>(sW + NS);
+    sV = reinterpret_cast<T(*)[TW]>(sQ + 6);
+    sD = reinterpret_cast<T(*)[TR + 2][TW]>(sV + TR + 1);
+    sS = reinterpret_cast<T(*)[TR + 1][TW]>(sD + NS);
   }
-  // LRMomenta and DivisePolarGrid over the tile and its halo (zero outside the grid)
-  for (int rr = y; rr < TR + 4; rr += ny) {
-    const int k = i0 - 2 + rr;
-    T q[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0}, inv = (T)0.0, vr = (T)0.0;
-    if (col && k >= 0 && k < nrad) {
-      const size_t qk = (size_t)k * nsec + j;
-      const T rm = RT(a, RT_RMED, k);
-      const T d = a.d.dens[qk], v0 = a.d.vrad[qk], v1 = a.d.vrad[qk + nsec];
-      q[0] = d * v1;
-      q[1] = d * v0;
-      q[2] = d * (a.d.vtheta[(size_t)k * nsec + jp] + rm * Om) * rm;
-      q[3] = d * (a.d.vtheta[qk] + rm * Om) * rm;
-      q[4] = P.adiabatic ? a.d.energy[qk] : (T)0.0;
-      q[5] = d;
-      inv = qdiv((T)1.0, d + (T)1e-20);
-      vr = v0;
-    } else if (col && k == nrad) {
-      vr = a.d.vrad[(size_t)k * nsec + j];
-    }
+  // LRMomenta + DivisePolarGrid of one cell of row rr (ring i0-2+rr) into the tile
+  __device__ __forceinline__ void put(int rr, int x, const T (&q)[6], T inv, T vr) const {
 #pragma unroll
     for (int f = 0; f < 6; f++) sW[f][rr][x] = q[f] * inv;
     sW[6][rr][x] = q[5];
@@ -1072,7 +1041,35 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
     }
     if (rr >= 2 && rr <= TR + 2) sV[rr - 2][x] = vr;
   }
-  __syncthreads();
+};
+
+// ring-table rows of rings i0-1 .. i0+TR+1 (zero outside 0 .. nrad), staged with the
+// tile so that no phase after a barrier loads from global memory
+template <class T>
+__device__ __forceinline__ void rad_stage_rt(const KArgs<T> &a, T (*sRT)[RAD_TR + 3], int i0, int x, int y) {
+  const int nrad = a.P.nrad;
+  if (y == 0 && x < RAD_TR + 3) {
+    const int k = i0 - 1 + x;
+    const bool ok = k >= 0 && k <= nrad;
+    sRT[0][x] = ok ? RT(a, RT_INVDIFFRMED, k) : (T)0;
+    sRT[1][x] = ok ? RT(a, RT_RMED, k) : (T)0;
+    sRT[2][x] = ok ? RT(a, RT_RINF, k) : (T)0;
+    sRT[3][x] = ok ? RT(a, RT_RSUP, k) : (T)0;
+    sRT[4][x] = ok ? RT(a, RT_INVSURF, k) : (T)0;
+  }
+}
+
+// StarRadKernel, StarRadKernel2 and VanLeerRadialKernel on a filled tile: the
+// slopes of every stream, the upwind interface values and the cell updates, one
+// barrier between the phases.
+template <class T>
+__device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile<T> &t, T (*sRT)[RAD_TR + 3],
+                                                int i0, int j, int x, int y) {
+  constexpr int TR = RAD_TR, NS = RAD_NS, ny = RAD_NY;
+  const DevParams &P = a.P;
+  const int nrad = P.nrad, nsec = P.nsec;
+  const bool col = j < nsec;
+  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
   // StarRadKernel: slopes of rings k = i0-1 .. i0+TR (zero at the first and last
   // ring), the seven streams of a ring together
   for (int dd = y; dd < TR + 2; dd += ny) {
@@ -1083,12 +1080,12 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
     for (int f = 0; f < NS; f++) {
       T v = (T)0.0;
       if (in) {
-        const T wm = sW[f][dd][x], w0 = sW[f][dd + 1][x], wp = sW[f][dd + 2][x];
+        const T wm = t.sW[f][dd][x], w0 = t.sW[f][dd + 1][x], wp = t.sW[f][dd + 2][x];
         const T dqm = (w0 - wm) * idm0;
         const T dqp = (wp - w0) * idm1;
         v = gt0(dqp * dqm) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
       }
-      sD[f][dd][x] = v;
+      t.sD[f][dd][x] = v;
     }
   }
   __syncthreads();
@@ -1096,7 +1093,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
   for (int ss = y; ss < TR + 1; ss += ny) {
     const int m = i0 + ss;
     const bool in = m > 0 && m < nrad;
-    const T v = sV[ss][x];
+    const T v = t.sV[ss][x];
     // the upwind side and the coefficient of its slope, the same for every stream:
     // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise
     const bool up = gt0(v);
@@ -1108,29 +1105,211 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
     }
     const int rw = up ? ss + 1 : ss + 2, rd = up ? ss : ss + 1;
 #pragma unroll
-    for (int f = 0; f < NS; f++) sS[f][ss][x] = in ? sW[f][rw][x] + coef * sD[f][rd][x] : (T)0.0;
+    for (int f = 0; f < NS; f++) t.sS[f][ss][x] = in ? t.sW[f][rw][x] + coef * t.sD[f][rd][x] : (T)0.0;
   }
   __syncthreads();
   if (!col) return;
   // VanLeerRadialKernel
   const T dtheta = KC(T, a, KC_DTHETA);
-  for (int t = y; t < TR; t += ny) {
-    const int i = i0 + t;
+  for (int r = y; r < TR; r += ny) {
+    const int i = i0 + r;
     if (i >= nrad) break;
     const size_t q = (size_t)i * nsec + j;
-    const T rinf = sRT[2][t + 1], rsup = sRT[3][t + 1], isurf = sRT[4][t + 1];
-    const T v0 = sV[t][x], v1 = sV[t + 1][x];
-    const T ds0 = sS[6][t][x], ds1 = sS[6][t + 1][x];
+    const T rinf = sRT[2][r + 1], rsup = sRT[3][r + 1], isurf = sRT[4][r + 1];
+    const T v0 = t.sV[r][x], v1 = t.sV[r + 1][x];
+    const T ds0 = t.sS[6][r][x], ds1 = t.sS[6][r + 1][x];
     // the mass fluxes through the two interfaces, the same for every stream
     const T F0 = dt * dtheta * rinf * ds0 * v0, F1 = dt * dtheta * rsup * ds1 * v1;
     T *out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
 #pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
-      const T varq = sS[f][t][x] * F0 - sS[f][t + 1][x] * F1;
-      out[f][q] = sQ[f][t][x] + varq * isurf;
+      const T varq = t.sS[f][r][x] * F0 - t.sS[f][r + 1][x] * F1;
+      out[f][q] = t.sQ[f][r][x] + varq * isurf;
       if (f == 5 && i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq;
     }
+  }
+}
+
+// LRMomenta and DivisePolarGrid of one cell (ring k, sector j) from its inputs
+template <class T>
+__device__ __forceinline__ void rad_cell(const KArgs<T> &a, int k, T d, T v0, T v1, T vtp, T vt, T e, T (&q)[6],
+                                         T &inv) {
+  const T rm = RT(a, RT_RMED, k);
+  const T Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA);
+  q[0] = d * v1;
+  q[1] = d * v0;
+  q[2] = d * (vtp + rm * Om) * rm;
+  q[3] = d * (vt + rm * Om) * rm;
+  q[4] = a.P.adiabatic ? e : (T)0.0;
+  q[5] = d;
+  inv = qdiv((T)1.0, d + (T)1e-20);
+}
+
+// Radial transport: LRMomentaKernel (src/Kernels.cu:774-787) + OneWindRad
+// (src/TransportEuler.cu:60-156: StarRadKernel/2, DivisePolarGridKernel,
+// VanLeerRadialKernel for every conserved quantity, density last), with no
+// intermediate field in memory.  One CTA per 32 sectors x RAD_TR rings: the
+// transported quantities of the tile and a halo of two rings go to shared
+// memory, then the slopes dq(k) of the rings, the upwind values at the
+// interfaces and the cell updates are each formed once, one barrier between
+// the phases.
+template <class T>
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
+  pdl_enter();
+  constexpr int TR = RAD_TR, ny = RAD_NY;
+  extern __shared__ __align__(16) unsigned char rad_smem[];
+  const RadTile<T> t(rad_smem);
+  const DevParams &P = a.P;
+  const int nrad = P.nrad, nsec = P.nsec;
+  const int x = threadIdx.x, y = threadIdx.y;
+  const int j = blockIdx.x * 32 + x, i0 = blockIdx.y * TR;
+  const bool col = j < nsec;
+  const int jp = col ? jp1(j, nsec) : 0;
+  __shared__ T sRT[5][TR + 3];  // INVDIFFRMED, RMED, RINF, RSUP, INVSURF
+  rad_stage_rt(a, sRT, i0, x, y);
+  // LRMomenta and DivisePolarGrid over the tile and its halo (zero outside the grid)
+  for (int rr = y; rr < TR + 4; rr += ny) {
+    const int k = i0 - 2 + rr;
+    T q[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0}, inv = (T)0.0, vr = (T)0.0;
+    if (col && k >= 0 && k < nrad) {
+      const size_t qk = (size_t)k * nsec + j;
+      const T v0 = a.d.vrad[qk];
+      rad_cell(a, k, a.d.dens[qk], v0, a.d.vrad[qk + nsec], a.d.vtheta[(size_t)k * nsec + jp], a.d.vtheta[qk],
+               P.adiabatic ? a.d.energy[qk] : (T)0.0, q, inv);
+      vr = v0;
+    } else if (col && k == nrad) {
+      vr = a.d.vrad[(size_t)k * nsec + j];
+    }
+    t.put(rr, x, q, inv, vr);
+  }
+  __syncthreads();
+  rad_tile_update(a, t, sRT, i0, j, x, y);
+}
+
+// ---------------------------------------------------------------------------
+// The same radial transport with its input tiles fetched by the Tensor Memory
+// Accelerator.  A persistent CTA walks the 32-sector x RAD_TR-ring tiles of the
+// grid (tile b, b + gridDim.x, ...).  Per tile, one thread issues four
+// cp.async.bulk.tensor.2d copies (density, Vrad, Vtheta, energy: rings i0-2 ..
+// i0+RAD_TR+2, sectors j0 .. j0+RAD_BW-1, zero-filled outside the field) into one
+// of two shared-memory stages, completing on that stage's mbarrier, so the next
+// tile streams in while this one is computed.  The cells are then formed from the
+// staged tile exactly as k_transport_radial forms them from global memory (the
+// azimuthal wrap of Vtheta at the last sector is the one plain load), and the
+// phases after it are the same code: the results are bitwise equal.
+#define RAD_FIELD_BYTES(T) (((size_t)RAD_BR * RAD_BW(T) * sizeof(T) + 127) / 128 * 128)
+#define RAD_STAGE_BYTES(T) (4 * RAD_FIELD_BYTES(T))
+#define RAD_TMA_SMEM(T) (((RAD_SMEM(T) + 127) / 128 * 128) + 2 * RAD_STAGE_BYTES(T) + 128)
+// bounded waits: iterations of mbarrier.try_wait (each suspends the thread for a
+// while in hardware) before the kernel gives up, flags the error and returns
+#define TMA_WAIT_LIMIT (1u << 24)
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// waits for the phase `parity` of the mbarrier at `bar`; false after TMA_WAIT_LIMIT tries
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+  for (unsigned n = 0; n < TMA_WAIT_LIMIT; n++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, unsigned bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      :
+      : "r"(smem_u32(dst)), "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+template <class T>
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(KArgs<T> a, const __grid_constant__ RadMaps maps) {
+  pdl_enter();
+  constexpr int TR = RAD_TR, ny = RAD_NY, BW = RAD_BW(T), BR = RAD_BR;
+  extern __shared__ __align__(128) unsigned char rad_smem[];
+  const RadTile<T> t(rad_smem);
+  // the two stages start at the first 128-byte boundary after the tile's arrays
+  // (RAD_TMA_SMEM holds 128 bytes of slack for it); each field box inside a stage
+  // is a multiple of 128 bytes
+  const unsigned smem_base = smem_u32(rad_smem);
+  unsigned char *stage0 = rad_smem + ((((smem_base + (unsigned)RAD_SMEM(T)) + 127u) & ~127u) - smem_base);
+  __shared__ __align__(8) unsigned long long bar[2];
+  __shared__ T sRT[5][TR + 3];
+  const DevParams &P = a.P;
+  const int nrad = P.nrad, nsec = P.nsec;
+  const int x = threadIdx.x, y = threadIdx.y, tid = y * 32 + x;
+  const int ntx = (nsec + 31) / 32, nty = (nrad + TR - 1) / TR, ntiles = ntx * nty;
+  const unsigned bytes = (unsigned)((P.adiabatic ? 4 : 3) * (size_t)BR * BW * sizeof(T));
+  const CUtensorMap *fmaps[4] = {&maps.dens, &maps.vrad, &maps.vtheta, &maps.energy};
+  auto field = [&](int s, int f) -> T(*)[BW] {
+    return reinterpret_cast<T(*)[BW]>(stage0 + (size_t)s * RAD_STAGE_BYTES(T) + (size_t)f * RAD_FIELD_BYTES(T));
+  };
+  auto issue = [&](int tile, int s) {
+    const unsigned b = smem_u32(&bar[s]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    const int j0 = (tile % ntx) * 32, k0 = (tile / ntx) * TR - 2;
+    for (int f = 0; f < 4; f++)
+      if (f != 3 || P.adiabatic) tma_load_2d(field(s, f), fmaps[f], b, j0, k0);
+  };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  }
+  __syncthreads();
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+    const int s = it & 1;
+    if (tid == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x, s ^ 1);
+    const int j0 = (tile % ntx) * 32, i0 = (tile / ntx) * TR;
+    const int j = j0 + x;
+    const bool col = j < nsec;
+    const int jp = col ? jp1(j, nsec) : 0;
+    rad_stage_rt(a, sRT, i0, x, y);
+    // every thread observes the stage's completion; the decision to give up is the
+    // CTA's together (no thread leaves while others wait at a barrier)
+    const bool ok = mbar_wait_bounded(smem_u32(&bar[s]), (unsigned)(it >> 1) & 1u);
+    if (__syncthreads_or(!ok)) {
+      // a copy did not complete: flag it, let the other stage's copy (if any) land
+      // within the same bound, and stop
+      if (tid == 0) {
+        atomicOr(&a.d.ctl->err, FARGO_DEVERR_WAIT);
+        if (tile + (int)gridDim.x < ntiles) mbar_wait_bounded(smem_u32(&bar[s ^ 1]), (unsigned)((it + 1) >> 1) & 1u);
+      }
+      return;
+    }
+    const T(*D)[BW] = field(s, 0);
+    const T(*VR)[BW] = field(s, 1);
+    const T(*VT)[BW] = field(s, 2);
+    const T(*E)[BW] = field(s, 3);
+    for (int rr = y; rr < TR + 4; rr += ny) {
+      const int k = i0 - 2 + rr;
+      T q[6] = {(T)0, (T)0, (T)0, (T)0, (T)0, (T)0}, inv = (T)0.0, vr = (T)0.0;
+      if (col && k >= 0 && k < nrad) {
+        const T v0 = VR[rr][x];
+        // Vtheta at j+1: the next staged column, or sector 0 across the wrap
+        const T vtp = (jp == j + 1) ? VT[rr][x + 1] : a.d.vtheta[(size_t)k * nsec];
+        rad_cell(a, k, D[rr][x], v0, VR[rr + 1][x], vtp, VT[rr][x], P.adiabatic ? E[rr][x] : (T)0.0, q, inv);
+        vr = v0;
+      } else if (col && k == nrad) {
+        vr = VR[rr][x];
+      }
+      t.put(rr, x, q, inv, vr);
+    }
+    __syncthreads();
+    rad_tile_update(a, t, sRT, i0, j, x, y);
+    __syncthreads();  // the tile and this stage are free for the next tiles
   }
 }
 
@@ -1647,8 +1826,15 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
-    launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR), dim3(32, RAD_NY), RAD_SMEM(T), s, a);
-    MARK("k_transport_radial");
+    if (a.rad_maps) {
+      launch_k(a.pdl, k_transport_radial_tma<T>, dim3(a.rad_grid), dim3(32, RAD_NY), RAD_TMA_SMEM(T), s, a,
+               *a.rad_maps);
+      MARK("k_transport_radial_tma");
+    } else {
+      launch_k(a.pdl, k_transport_radial<T>, dim3((P.nsec + 31) / 32, (P.nrad + RAD_TR - 1) / RAD_TR),
+               dim3(32, RAD_NY), RAD_SMEM(T), s, a);
+      MARK("k_transport_radial");
+    }
     if (a.az_regs) {
       const int nt4 = az4_threads<T>(P.nsec);
       if (P.nsec / 4 > nt4)
@@ -1792,6 +1978,18 @@ void launch_cfl_only(const KArgs<T> &a0, cudaStream_t s) {
 }
 
 template <class T>
+int rad_tma_grid(int nrad, int nsec) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_transport_radial_tma<T>, 32 * RAD_NY,
+                                                    RAD_TMA_SMEM(T)) != cudaSuccess || per < 1)
+    return 0;
+  const int tiles = ((nsec + 31) / 32) * ((nrad + RAD_TR - 1) / RAD_TR);
+  return tiles < sms * per ? tiles : sms * per;
+}
+
+template <class T>
 cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
   // One shared-memory carveout for every step kernel: an SM changes its L1 /
   // shared split only when idle, so kernels that run side by side (the CFL/force
@@ -1812,6 +2010,12 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs) {
     if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) != cudaSuccess)
       return e;
   e = cudaFuncSetAttribute(k_transport_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RAD_SMEM(T));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_transport_radial_tma<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           FARGO_SMEM_CARVEOUT);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_transport_radial_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)RAD_TMA_SMEM(T));
   if (e != cudaSuccess) return e;
   if (az_smem_bytes == 0) return cudaSuccess;
   if (az_regs) {
@@ -1876,6 +2080,7 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
   template void launch_dt_prefix<T>(const KArgs<T> &, cudaStream_t);                                    \
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
   template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \
-  template cudaError_t prepare_kernels<T>(size_t, int);
+  template cudaError_t prepare_kernels<T>(size_t, int); \
+  template int rad_tma_grid<T>(int, int);
 INSTANTIATE(double)
 INSTANTIATE(float)

@@ -117,6 +117,14 @@ template <class T>
 void launch_boundaries(const KArgs<T> &a, cudaStream_t s);
 template <class T>
 cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
+// CTAs of the persistent TMA radial transport on this device (0: not launchable)
+template <class T>
+int rad_tma_grid(int nrad, int nsec);
+// TMA box of the radial transport's staged tiles: sectors (33 rounded up to 16
+// bytes) x rings (the tile's RAD_TR rings, two below, three above)
+#define RAD_TR 16
+#define RAD_BW(T) (sizeof(T) == 4 ? 36 : 34)
+#define RAD_BR (RAD_TR + 5)
 
 // self-gravity (fargo_sg.cu)
 template <class T>

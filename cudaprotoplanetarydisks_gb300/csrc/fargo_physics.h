@@ -27,6 +27,7 @@
 #define FARGO_DEVERR_CFL 1        // non-finite or non-positive CFL time step
 #define FARGO_DEVERR_CAP 2        // too many substeps in one DT
 #define FARGO_DEVERR_NAN 4        // non-finite density found
+#define FARGO_DEVERR_WAIT 8       // a bounded wait on an asynchronous copy gave up
 
 struct DevParams {
   int nrad, nsec, nb, nsec2pot;

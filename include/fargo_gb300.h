@@ -197,6 +197,13 @@ int  fargo_set_fields(fargo_ctx *ctx, const double *dens, const double *vrad,
                       const double *vtheta, const double *energy);
 /* One named field (FARGO_FIELD_*), (nrad+1)*nsec doubles. */
 int  fargo_get_field(fargo_ctx *ctx, int which, double *host);
+/* The same field copied device to device into the caller's FP64 array dev
+   ((nrad+1)*nsec doubles, the reference's layout; FP32-bulk fields widened), on the
+   context's stream, then synchronised.  For a host driver that keeps device arrays
+   of its own: the reference's DeviceToHostcudaMemcpy (src/Main.cu:605-616) reads
+   Dens_d, Vrad_d, Vtheta_d, Energy_d, Temperature_d, Qplus_d.  Fields held on the
+   host or completed there (isothermal sound speed, potential): FARGO_ERR_INVALID. */
+int  fargo_get_field_device(fargo_ctx *ctx, int which, double *dev);
 int  fargo_get_planets(fargo_ctx *ctx, fargo_planet *out, int cap, int *nb);
 int  fargo_get_scalars(fargo_ctx *ctx, fargo_scalars *s);
 /* 1D mesh arrays (FillPolar1DArrays src/SourceEuler.cu:66-162): Rinf, Rmed, Rsup,

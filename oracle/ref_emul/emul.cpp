@@ -80,11 +80,15 @@ void emu_syncthreads() {
   swapcontext(&g_cur->ctx, &g_sched);
 }
 
-// Host threads over the blocks of a launch (FARGO_REF_THREADS, default 1).  No
-// reference kernel but DeviceReduceKernel (run in order, below) uses shared
-// memory, barriers or atomics, and none reads in one launch what another block
-// of the same launch writes, so the blocks' order does not change the result
-// (checked bitwise against the one-thread fixtures by tests/test_ref_cpu.py).
+// Host threads over the blocks of a launch (FARGO_REF_THREADS, default 1), for
+// two-dimensional grids only.  No reference kernel but DeviceReduceKernel (run in
+// order, below) uses shared memory, barriers or atomics, and every kernel launched
+// on a 2D grid guards i < nrad, j < nsec and reads nothing another block of the same
+// launch writes, so their blocks' order does not change the result.  The 1D launches
+// (boundary kernels over sectors, ring loops) stay in block order: one of them,
+// NonReflectingBoundaryKernel2 (src/Kernels.cu:575-589), lets its padded threads
+// write into the next ring, and which write lands last depends on that order.
+// tests/test_ref_cpu.py checks the one-thread fixtures bitwise on four threads.
 int emu_ref_threads() {
   static int n = [] {
     const char *s = std::getenv("FARGO_REF_THREADS");
@@ -100,7 +104,7 @@ void emu_run(const EmuCfg &c, void (*fn)(void *), void *body) {
   const unsigned nthr = c.b.x * c.b.y * c.b.z;
   if (!c.sync) {
     const long nblk = (long)c.g.x * c.g.y * c.g.z;
-#pragma omp parallel for schedule(static) num_threads(emu_ref_threads()) if (emu_ref_threads() > 1 && nblk > 1)
+#pragma omp parallel for schedule(static) num_threads(emu_ref_threads()) if (emu_ref_threads() > 1 && c.g.y > 1)
     for (long b = 0; b < nblk; b++) {
       gridDim = c.g;
       blockDim = c.b;
