@@ -75,6 +75,9 @@ struct fargo_ctx {
   RadMaps rad_maps;
   bool use_tma = false;
   int rad_grid = 0;
+  bool want_tma = true;       // the variant asks for the TMA radial transport
+  int cell_block = 0;         // per-cell kernels' CTA shape (fargo_variant.cell_block)
+  int az_chunks = 1;          // chunks per thread of the register azimuthal sweep
 };
 
 namespace {
@@ -195,6 +198,12 @@ KArgs<T> make_args(const fargo_ctx *c) {
   a.sg_generic = c->sg_generic ? 1 : 0;
   a.rad_maps = c->use_tma ? &c->rad_maps : nullptr;
   a.rad_grid = c->rad_grid;
+  {
+    static const int bx[4] = {64, 32, 128, 256}, by[4] = {4, 8, 2, 1};
+    a.cell_bx = bx[c->cell_block];
+    a.cell_by = by[c->cell_block];
+  }
+  a.az_chunks = c->az_chunks;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -449,10 +458,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
     }
   }
   // TMA maps of the radial transport's input fields
-  {
-    const char *nt = std::getenv("FARGO_NO_TMA");
-    if (!(nt && nt[0] == '1')) make_rad_maps<T>(c);
-  }
+  if (c->want_tma) make_rad_maps<T>(c);
   CK(cudaStreamSynchronize(c->stream));
   // density first: self-gravity set-up needs it
   if ((rc = upload(c, c->dens, h.Dens.data(), sg))) return rc;
@@ -727,6 +733,10 @@ void fargo_variant_default(fargo_variant *v) {
   v->az_generic = env_on("FARGO_AZ_GENERIC") ? 1 : 0;
   const char *pr = std::getenv("FARGO_PRIO");
   v->priority = pr ? std::atoi(pr) : 0;
+  const char *cb = std::getenv("FARGO_CELL_BLOCK");
+  v->cell_block = cb ? std::atoi(cb) : 0;
+  v->rad_tma = env_on("FARGO_NO_TMA") ? 0 : 1;
+  v->az_chunks = env_on("FARGO_AZ_CHUNKS2") ? 2 : 1;
 }
 
 int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb, int precision, void *stream,
@@ -741,6 +751,7 @@ int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets,
   if (variant) v = *variant;
   else fargo_variant_default(&v);
   if (v.priority < 0 || v.priority > 2) return FARGO_ERR_INVALID;
+  if (v.cell_block < 0 || v.cell_block > 3 || v.az_chunks < 1 || v.az_chunks > 2) return FARGO_ERR_INVALID;
   if (precision != FARGO_FP64 && precision != FARGO_FP32_BULK) return FARGO_ERR_INVALID;
   if (p->nrad < 8 || p->nsec < 8 || !p->is_disk || !(p->dt > 0.0)) return FARGO_ERR_INVALID;
   fargo_ctx *c = new fargo_ctx();
@@ -755,6 +766,9 @@ int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets,
   c->use_sg_ahead = v.sg_ahead != 0;
   c->use_pad = v.pad != 0;
   c->az_generic = v.az_generic != 0;
+  c->want_tma = v.rad_tma != 0;
+  c->cell_block = v.cell_block;
+  c->az_chunks = v.az_chunks;
   c->sg_generic = env_on("FARGO_SG_GENERIC");  // a parity-test switch, not a variant
   // stream priorities: 0 all equal; 1 the hydro chain and the planets above the
   // self-gravity transforms; 2 the transforms above the rest.  The caller's

@@ -78,6 +78,8 @@ struct KArgs {
   int sg_generic;                  // self-gravity FFTs with the run-time plan at every length
   const RadMaps *rad_maps;         // host copy of the radial transport's TMA maps (nullptr: plain loads)
   int rad_grid;                    // CTAs of the persistent TMA radial transport
+  int cell_bx, cell_by;            // CTA shape (sectors x rings) of the per-cell kernels
+  int az_chunks;                   // four-cell chunks per thread of the register azimuthal sweep
   SgDev sg;
 };
 

@@ -1758,8 +1758,8 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
                             const SideBranch *side, unsigned rot) {
   KArgs<T> a = a0;
   const DevParams &P = a.P;
-  const dim3 b2(64, 4);
-  const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
+  const dim3 b2(a.cell_bx, a.cell_by);
+  const dim3 g2((P.nsec + a.cell_bx - 1) / a.cell_bx, (P.nrad + a.cell_by - 1) / a.cell_by);
   bool joined = true;
   const bool head_done = rot & ROT_HEAD_DONE;
   const bool bc1 = (which_mask & SUBK_BC1) && (P.open_inner || P.non_reflecting || P.evanescent);
@@ -1836,7 +1836,9 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
       MARK("k_transport_radial");
     }
     if (a.az_regs) {
-      const int nt4 = az4_threads<T>(P.nsec);
+      // one chunk of four cells per thread up to the CTA's size, or (az_chunks = 2)
+      // half the threads with two chunks each
+      const int nt4 = az4_threads<T>(a.az_chunks == 2 ? P.nsec / 2 : P.nsec);
       if (P.nsec / 4 > nt4)
         launch_k(a.pdl, k_transport_azimuthal4<T, true>, dim3(P.nrad), dim3(nt4), az_smem_bytes, s, a);
       else
@@ -1946,8 +1948,8 @@ void launch_boundaries(const KArgs<T> &a, cudaStream_t s) {
     MARK("k_bc_nr_adjust");
   }
   if (P.evanescent) {
-    const dim3 b2(64, 4);
-    const dim3 g2((P.nsec + 63) / 64, (P.nrad + 3) / 4);
+    const dim3 b2(a.cell_bx, a.cell_by);
+    const dim3 g2((P.nsec + a.cell_bx - 1) / a.cell_bx, (P.nrad + a.cell_by - 1) / a.cell_by);
     launch_k(a.pdl, k_bc_evanescent<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_bc_evanescent");
   }

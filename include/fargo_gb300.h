@@ -175,6 +175,12 @@ typedef struct {
   int rotate;      /* rotated DT loop (self-gravity of each substep launched by the previous one) */
   int az_generic;  /* barrier-per-phase azimuthal transport instead of the register-blocked one */
   int priority;    /* 0 equal stream priorities; 1 hydro chain above self-gravity; 2 the reverse */
+  /* tile and launch shapes (each cell's arithmetic unchanged) */
+  int cell_block;  /* CTA of the per-cell kernels: 0 64x4 sectors x rings, 1 32x8, 2 128x2, 3 256x1 */
+  int rad_tma;     /* 1: radial transport on TMA-staged tiles in a persistent grid (when the rows
+                      are 16-byte strided); 0: per-thread loads, one CTA per tile */
+  int az_chunks;   /* four-cell chunks per thread of the register azimuthal sweep: 1 (one per
+                      thread, up to the CTA size) or 2 (half the threads, two chunks each) */
 } fargo_variant;
 /* The default variant, with the FARGO_NO_GRAPH, FARGO_NO_PDL, FARGO_NO_PAD,
    FARGO_NO_SG_AHEAD, FARGO_ROTATE, FARGO_AZ_GENERIC and FARGO_PRIO switches

@@ -69,5 +69,27 @@ def test_autotune_keeps_a_variant_at_least_as_fast():
     disks = small_ensemble(4)
     v, best, default = fg.autotune(disks, fg.FARGO_FP32_BULK, ndt=1)
     assert best >= default > 0
-    assert set(v.as_dict()) == {"graph", "pdl", "pad", "sg_ahead", "rotate", "az_generic", "priority"}
+    assert set(v.as_dict()) == {"graph", "pdl", "pad", "sg_ahead", "rotate", "az_generic", "priority",
+                                "cell_block", "rad_tma", "az_chunks"}
     assert v.priority in (0, 1, 2) and v.pad in (0, 1) and v.pdl in (0, 1)
+    assert v.cell_block in (0, 1, 2, 3) and v.rad_tma in (0, 1) and v.az_chunks in (1, 2)
+
+
+@pytest.mark.parametrize("cell_block,rad_tma,az_chunks", [(1, 0, 2), (2, 1, 2), (3, 0, 1)])
+@pytest.mark.parametrize("precision", [fg.FARGO_FP32_BULK, fg.FARGO_FP64])
+def test_tile_shapes_are_bitwise_the_default(cell_block, rad_tma, az_chunks, precision):
+    # the autotuner's tile and launch shapes change which thread forms a cell, never
+    # its arithmetic: fields bitwise equal to the default shapes
+    disks = small_ensemble(3)
+    v = fg.default_variant()
+    v.cell_block, v.rad_tma, v.az_chunks = cell_block, rad_tma, az_chunks
+    a = fg.Batch(disks, precision)
+    b = fg.Batch(disks, precision, variant=v)
+    for x in (a, b):
+        x.run_async(2)
+        x.sync()
+    for k in range(len(disks)):
+        for name in ("dens", "vrad", "vtheta"):
+            assert np.array_equal(a.disk(k).field(name), b.disk(k).field(name)), (k, name, cell_block)
+    a.close()
+    b.close()
