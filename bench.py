@@ -710,7 +710,7 @@ def run_reference(args, world, rank):
 
 
 # ---------------------------------------------------------------------------
-def batch_ensemble(ndt=2, n=64):
+def batch_ensemble(ndt=4, n=64):
     """The batched ensemble (64 seeded disks, Nrad in {128..512}, Nsec = 3 Nrad):
     FP32-bulk disks advanced side by side (fargo_batch) against the same disks in
     plain FP64 one after another, after one warm-up DT each; the FP32 density
@@ -722,8 +722,10 @@ def batch_ensemble(ndt=2, n=64):
     disks = fg.c4_disks(n)
     cells = [p.nrad * p.nsec for p, _ in disks]
 
-    def batched(variant):
+    def batched(variant, fused=False):
         b = fg.Batch(disks, fg.FARGO_FP32_BULK, variant=variant)
+        if fused:
+            b.fuse()
         b.run_async(1)
         b.sync()
         s0 = [d.scalars().substeps for d in b.disks]
@@ -734,8 +736,13 @@ def batch_ensemble(ndt=2, n=64):
         t = time.perf_counter() - t0
         cu = sum((d.scalars().substeps - s0[k]) * cells[k] for k, d in enumerate(b.disks))
         dens = [d.field("dens")[:-1] for d in b.disks]
-        launches = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
-                       for k, d in enumerate(b.disks))
+        if fused:
+            per_sub, per_dt = b.fused_launches()
+            nsub_max = max(d.scalars().substeps - s0[k] for k, d in enumerate(b.disks))
+            launches = ndt * per_dt + nsub_max * per_sub  # at least: the loop runs to the slowest disk
+        else:
+            launches = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
+                           for k, d in enumerate(b.disks))
         b.close()
         return t, cu, dens, launches
 
@@ -746,6 +753,9 @@ def batch_ensemble(ndt=2, n=64):
     t_tune = time.perf_counter() - t_tune
     tt, cut, dens_t, _ = batched(variant)
     assert all(np.array_equal(x, y) for x, y in zip(dens32, dens_t))  # variants change speed only
+    # the fused form: each substep kernel launched once for the whole ensemble
+    tf, cuf, dens_f, launches_f = batched(None, fused=True)
+    assert all(np.array_equal(x, y) for x, y in zip(dens32, dens_f))  # bitwise the disks alone
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     t64, cu64, err = 0.0, 0, []
     for k, (p, pl) in enumerate(disks):
@@ -768,6 +778,10 @@ def batch_ensemble(ndt=2, n=64):
             "fp32_batched": {"value": v32, "unit": METRIC, "seconds": t32, "gpu_launches_approx": launches32},
             "fp32_batched_autotuned": {"value": cut / tt, "unit": METRIC, "seconds": tt, "variant": variant.as_dict(),
                                        "search": {"seconds": t_tune, "rate_default": r_default, "rate_kept": r_best}},
+            "fp32_fused": {"value": cuf / tf, "unit": METRIC, "seconds": tf, "gpu_launches_approx": launches_f,
+                           "form": "one launch of each substep kernel for all disks, one graph per DT round, "
+                                   "masked subcycling (fargo_batch_fuse)",
+                           "speedup_over_per_disk_graphs": (cuf / tf) / v32},
             "fp64_plain_sequential": {"value": v64, "unit": METRIC, "seconds": t64},
             "ratio_fp32_batched_to_fp64_plain": v32 / v64,
             "fp32_dens_rel_l2_vs_fp64_max": max(err), "fp32_dens_rel_l2_vs_fp64_median": float(np.median(err)),

@@ -217,6 +217,23 @@ class Batch:
         if rc != _capi.FARGO_OK:
             raise FargoError(f"fargo_batch_sync: status {rc}")
 
+    def fuse(self):
+        """fargo_batch_fuse: from now on every substep kernel runs once for the whole
+        ensemble (one graph per DT round, masked subcycling); raises with the reason
+        when a disk uses a path the fused form does not carry."""
+        rc = self.lib.fargo_batch_fuse(self.h)
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_fuse: status {rc}: {self.lib.fargo_batch_last_error(self.h).decode()}")
+        return self
+
+    def fused_launches(self):
+        """(launches per substep of the whole ensemble, launches per DT round)."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        rc = self.lib.fargo_batch_fused_launches(self.h, ctypes.byref(a), ctypes.byref(b))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_fused_launches: status {rc}")
+        return a.value, b.value
+
     def advance(self, t_end):
         """Every disk to physical time t_end (whole DTs of its own); returns the
         substeps of all disks."""

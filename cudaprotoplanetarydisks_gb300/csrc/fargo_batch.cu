@@ -14,11 +14,16 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "fargo_gb300.h"
+#include "fargo_internal.h"
 
 struct fargo_batch {
   std::vector<fargo_ctx *> disks;
-  std::vector<double> dt;  // DT of each disk (its parameter file's DT)
+  std::vector<double> dt;           // DT of each disk (its parameter file's DT)
+  fargo_fused *fused = nullptr;     // the fused form (fargo_batch_fuse), or none
+  std::string err;
 };
 
 extern "C" {
@@ -56,6 +61,7 @@ int fargo_batch_create_variant(int n, const fargo_params *params, const fargo_pl
 
 void fargo_batch_destroy(fargo_batch *b) {
   if (!b) return;
+  fused_destroy(b->fused);
   for (fargo_ctx *c : b->disks) fargo_ctx_destroy(c);
   delete b;
 }
@@ -83,11 +89,30 @@ static int enqueue(fargo_batch *b, const int *ndt, int ndt_all) {
 
 int fargo_batch_run_async(fargo_batch *b, int ndt) {
   if (!b || ndt < 0) return FARGO_ERR_STATE;
+  if (b->fused) return fused_run(b->fused, ndt);
   return enqueue(b, nullptr, ndt);
+}
+
+int fargo_batch_fuse(fargo_batch *b) {
+  if (!b) return FARGO_ERR_STATE;
+  if (b->fused) return FARGO_OK;
+  b->err.clear();
+  return fused_create(b->disks.data(), (int)b->disks.size(), &b->fused, &b->err);
+}
+
+const char *fargo_batch_last_error(const fargo_batch *b) { return b ? b->err.c_str() : ""; }
+
+int fargo_batch_fused_launches(const fargo_batch *b, int *per_substep, int *per_dt) {
+  if (!b || !b->fused) return FARGO_ERR_STATE;
+  return fused_launches(b->fused, per_substep, per_dt);
 }
 
 int fargo_batch_sync(fargo_batch *b) {
   if (!b) return FARGO_ERR_STATE;
+  if (b->fused) {
+    const int rc = fused_sync(b->fused);
+    if (rc != FARGO_OK) return rc;
+  }
   for (fargo_ctx *c : b->disks) {
     const int rc = fargo_sync(c);
     if (rc != FARGO_OK) return rc;
@@ -113,7 +138,10 @@ int fargo_batch_advance(fargo_batch *b, double t_end, long long *nsub, int *fail
     const double left = (t_end - s.physical_time) / b->dt[k];
     ndt[k] = left > 1e-9 ? (int)std::ceil(left - 1e-9) : 0;
   }
-  int rc = enqueue(b, ndt.data(), 0);
+  bool same = true;
+  for (size_t k = 1; k < n; k++) same = same && ndt[k] == ndt[0];
+  int rc = (b->fused && same) ? fused_run(b->fused, n ? ndt[0] : 0) : enqueue(b, ndt.data(), 0);
+  if (rc == FARGO_OK && b->fused) rc = fused_sync(b->fused);
   if (rc != FARGO_OK) return rc;
   long long tot = 0;
   for (size_t k = 0; k < n; k++) {

@@ -10,6 +10,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1195,3 +1196,240 @@ int fargo_restart(fargo_ctx *c, int index) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Fused ensembles.  Every disk keeps its own context (fields, control block, ring
+// tables); the plan gathers their kernel arguments in one device array and, for
+// each substep kernel, one launch group: the members that run it, each member's
+// own grid (the single-disk launch's), one block size (the largest member's, for
+// the kernels whose block follows the ring width) and shared memory (the largest).
+// One graph per DT round: the DT start of every disk, then a conditional while
+// node whose body is one substep of every disk not yet done.  A disk is done when
+// its own DT is (k_end's test, src/SourceEuler.cu:222); its blocks then return at
+// once, and the loop ends with the last disk.  Each disk runs the single-disk
+// kernel bodies in the single-disk order, so its results are bitwise those of the
+// disk run alone.
+struct fargo_fused {
+  int precision = FARGO_FP64;
+  int n = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void *> bufs;  // device: arguments, control-block table, group tables
+  int per_substep = 0, per_dt = 0;
+};
+
+namespace {
+struct FusedGroup {
+  int kernel;
+  std::vector<int> member, first, gx;
+  dim3 block;
+  size_t smem = 0;
+  int extra = 0;
+};
+
+template <class T>
+int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why) {
+  std::vector<KArgs<T>> args(n);
+  size_t az_smem = 0;
+  for (int k = 0; k < n; k++) {
+    const fargo_ctx *c = disks[k];
+    const fargo_params &p = c->P;
+    const char *no = p.self_gravity ? "self-gravity"
+                   : (p.open_inner || p.non_reflecting || p.evanescent) ? "an open, non-reflecting or evanescent boundary"
+                   : p.sloppy_cfl ? "the sloppy CFL (-c)"
+                   : !c->az_regs ? "a ring too wide for the register azimuthal sweep"
+                   : nullptr;
+    if (no) {
+      *why = "disk " + std::to_string(k) + " uses " + no + ", which the fused form does not carry";
+      return FARGO_ERR_INVALID;
+    }
+    KArgs<T> a = make_args<T>(c);
+    a.use_cond = 0;
+    a.guard = 0;
+    a.mode = 0;
+    a.pdl = 1;
+    a.rad_maps = nullptr;
+    a.cell_bx = 64;
+    a.cell_by = 4;
+    args[k] = a;
+    az_smem = std::max(az_smem, c->az_smem);
+  }
+  auto dev = [&](const void *src, size_t bytes) -> void * {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    f->bufs.push_back(p);
+    if (cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return p;
+  };
+  const KArgs<T> *args_dev = (const KArgs<T> *)dev(args.data(), n * sizeof(KArgs<T>));
+  std::vector<Ctl *> ctls(n);
+  for (int k = 0; k < n; k++) ctls[k] = disks[k]->d_ctl;
+  Ctl *const *ctls_dev = (Ctl *const *)dev(ctls.data(), n * sizeof(Ctl *));
+  if (!args_dev || !ctls_dev) {
+    *why = "device allocation of the fused plan failed";
+    return FARGO_ERR_CUDA;
+  }
+  // launch groups in substep order
+  auto group = [&](int kernel, auto pred, auto grid, dim3 block, size_t smem, int extra) {
+    FusedGroup g;
+    g.kernel = kernel;
+    g.block = block;
+    g.smem = smem;
+    g.extra = extra;
+    g.first.push_back(0);
+    for (int k = 0; k < n; k++) {
+      if (!pred(disks[k]->P, disks[k])) continue;
+      const int2 gd = grid(disks[k]->P, disks[k]);
+      g.member.push_back(k);
+      g.gx.push_back(gd.x);
+      g.first.push_back(g.first.back() + gd.x * gd.y);
+    }
+    return g;
+  };
+  auto all = [](const fargo_params &, const fargo_ctx *) { return true; };
+  auto one = [](const fargo_params &, const fargo_ctx *) { return make_int2(1, 1); };
+  auto rings = [](const fargo_params &p, const fargo_ctx *) { return make_int2(p.nrad, 1); };
+  auto cells = [](const fargo_params &p, const fargo_ctx *) { return make_int2((p.nsec + 63) / 64, (p.nrad + 3) / 4); };
+  auto tiles = [](const fargo_params &p, const fargo_ctx *) {
+    return make_int2((p.nsec + 31) / 32, (p.nrad + RAD_TR - 1) / RAD_TR);
+  };
+  auto v4 = [](const fargo_params &p, const fargo_ctx *) { return p.nsec % 4 == 0 && p.nsec >= 260 && p.nsec <= 1024; };
+  auto not_v4 = [&](const fargo_params &p, const fargo_ctx *c) { return !v4(p, c); };
+  auto adiabatic = [](const fargo_params &p, const fargo_ctx *) { return p.adiabatic != 0; };
+  auto corot = [](const fargo_params &p, const fargo_ctx *) { return p.corotating != 0; };
+  auto az_mc = [](const fargo_params &p, const fargo_ctx *) { return p.nsec / 4 > az4_threads_host<T>(p.nsec); };
+  auto az_one = [&](const fargo_params &p, const fargo_ctx *c) { return !az_mc(p, c); };
+  int v4_threads = 32, az_threads = 32;
+  for (int k = 0; k < n; k++) {
+    const fargo_params &p = disks[k]->P;
+    if (v4(p, disks[k])) v4_threads = std::max(v4_threads, (p.nsec / 4 + 31) / 32 * 32);
+    az_threads = std::max(az_threads, az4_threads_host<T>(p.nsec));
+  }
+  const dim3 b2(64, 4);
+  std::vector<FusedGroup> head = {group(BK_DT_BEGIN, all, one, dim3(32), 0, 0),
+                                  group(BK_SOUNDSPEED, adiabatic, rings, dim3(256), 0, 0)};
+  std::vector<FusedGroup> body = {
+      group(BK_CFL_V4, v4, rings, dim3(v4_threads), 0, 0),
+      group(BK_CFL, not_v4, rings, dim3(256), 0, 0),
+      group(BK_PLANETS, all, one, dim3(64), 0, 0),
+      group(BK_COROT, corot, cells, b2, 0, 0),
+      group(BK_SOURCE, all, cells, b2, 0, 0),
+      group(BK_VISC_TAU, all, cells, b2, 0, 0),
+      group(BK_VISC_UPDATE, all, cells, b2, 0, 0),
+      group(BK_ARTVISC, all, cells, b2, 0, 0),
+      group(BK_VISC_TAU, adiabatic, cells, b2, 0, 1),
+      group(BK_ENERGY, adiabatic, cells, b2, 0, 0),
+      group(BK_RADIAL, all, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
+      group(BK_AZ4, az_one, rings, dim3(az_threads), az_smem, 0),
+      group(BK_AZ4_MC, az_mc, rings, dim3(sizeof(T) == 8 ? 512 : 768), az_smem, 0),
+      group(BK_VELOCITIES, all, cells, b2, 0, 1),
+      group(BK_END, all, one, dim3(256), 0, 0)};
+  if (prepare_batched<T>(rad_smem_bytes(sizeof(T)), az_smem) != cudaSuccess) {
+    *why = "cudaFuncSetAttribute on the batched kernels failed";
+    return FARGO_ERR_CUDA;
+  }
+  auto to_dev = [&](const FusedGroup &g, BatchGroup<T> &G) -> bool {
+    G.args = args_dev;
+    G.ng = (int)g.member.size();
+    G.extra = g.extra;
+    G.member = (const int *)dev(g.member.data(), g.member.size() * sizeof(int));
+    G.first = (const int *)dev(g.first.data(), g.first.size() * sizeof(int));
+    G.gx = (const int *)dev(g.gx.data(), g.gx.size() * sizeof(int));
+    return G.member && G.first && G.gx;
+  };
+  std::vector<BatchGroup<T>> hg(head.size()), bg(body.size());
+  for (size_t q = 0; q < head.size(); q++)
+    if (!head[q].member.empty() && !to_dev(head[q], hg[q])) return FARGO_ERR_CUDA;
+  for (size_t q = 0; q < body.size(); q++)
+    if (!body[q].member.empty() && !to_dev(body[q], bg[q])) return FARGO_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess) return FARGO_ERR_CUDA;
+  // the graph: the DT start of every disk, then the while loop of substeps
+  cudaGraph_t g = nullptr, gp = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return FARGO_ERR_CUDA;
+  f->graph = g;
+  LaunchProbe probe;
+  std::memset(&probe, 0, sizeof(probe));
+  g_probe = &probe;
+  if (cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return FARGO_ERR_CUDA;
+  for (size_t q = 0; q < head.size(); q++)
+    if (!head[q].member.empty())
+      launch_batched<T>(head[q].kernel, hg[q], head[q].first.back(), head[q].block, head[q].smem, 1, f->stream);
+  g_probe = nullptr;
+  if (cudaStreamEndCapture(f->stream, &gp) != cudaSuccess) return FARGO_ERR_CUDA;
+  f->per_dt = probe.count;
+  cudaGraphNode_t np, nc;
+  if (cudaGraphAddChildGraphNode(&np, g, nullptr, 0, gp) != cudaSuccess) return FARGO_ERR_CUDA;
+  cudaGraphDestroy(gp);
+  cudaGraphConditionalHandle h;
+  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) return FARGO_ERR_CUDA;
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  if (cudaGraphAddNode(&nc, g, &np, nullptr, 1, &cp) != cudaSuccess) return FARGO_ERR_CUDA;
+  cudaGraph_t loop = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(f->stream, loop, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess)
+    return FARGO_ERR_CUDA;
+  probe.count = 0;
+  g_probe = &probe;
+  for (size_t q = 0; q < body.size(); q++)
+    if (!body[q].member.empty())
+      launch_batched<T>(body[q].kernel, bg[q], body[q].first.back(), body[q].block, body[q].smem, 1, f->stream);
+  launch_loop_cond(ctls_dev, n, (unsigned long long)h, 1, f->stream);
+  g_probe = nullptr;
+  if (cudaStreamEndCapture(f->stream, &loop) != cudaSuccess) return FARGO_ERR_CUDA;
+  f->per_substep = probe.count;
+  if (cudaGraphInstantiate(&f->exec, g, 0) != cudaSuccess) return FARGO_ERR_CUDA;
+  return FARGO_OK;
+}
+}  // namespace
+
+int fused_create(fargo_ctx *const *disks, int n, fargo_fused **out, std::string *why) {
+  *out = nullptr;
+  if (!disks || n <= 0) return FARGO_ERR_INVALID;
+  for (int k = 0; k < n; k++)
+    if (disks[k]->precision != disks[0]->precision) {
+      *why = "the disks of a fused ensemble share one precision";
+      return FARGO_ERR_INVALID;
+    }
+  // every disk's own queue is drained first: the plan reads their control blocks
+  for (int k = 0; k < n; k++)
+    if (cudaStreamSynchronize(disks[k]->stream) != cudaSuccess) return FARGO_ERR_CUDA;
+  fargo_fused *f = new fargo_fused();
+  f->precision = disks[0]->precision;
+  f->n = n;
+  const int rc = f->precision == FARGO_FP64 ? fused_build<double>(f, disks, n, why) : fused_build<float>(f, disks, n, why);
+  if (rc != FARGO_OK) {
+    if (why->empty()) *why = std::string("building the fused plan: ") + cudaGetErrorString(cudaGetLastError());
+    fused_destroy(f);
+    return rc;
+  }
+  *out = f;
+  return FARGO_OK;
+}
+
+int fused_run(fargo_fused *f, int ndt) {
+  for (int k = 0; k < ndt; k++)
+    if (cudaGraphLaunch(f->exec, f->stream) != cudaSuccess) return FARGO_ERR_CUDA;
+  return FARGO_OK;
+}
+
+int fused_sync(fargo_fused *f) { return cudaStreamSynchronize(f->stream) == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA; }
+
+int fused_launches(const fargo_fused *f, int *per_substep, int *per_dt) {
+  if (per_substep) *per_substep = f->per_substep;
+  if (per_dt) *per_dt = f->per_dt;
+  return FARGO_OK;
+}
+
+void fused_destroy(fargo_fused *f) {
+  if (!f) return;
+  if (f->stream) cudaStreamSynchronize(f->stream);
+  if (f->exec) cudaGraphExecDestroy(f->exec);
+  if (f->graph) cudaGraphDestroy(f->graph);
+  for (void *p : f->bufs) cudaFree(p);
+  if (f->stream) cudaStreamDestroy(f->stream);
+  delete f;
+}

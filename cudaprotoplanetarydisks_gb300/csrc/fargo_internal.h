@@ -89,3 +89,13 @@ int host_read_planet_row(const std::string &outdir, int k, int index, fargo_plan
                          double *physical_time, double *omega_frame);
 int host_truncate_planet_file(const std::string &outdir, int k, int index);
 int host_append_row(const std::string &outdir, const std::string &file, int index, const double *v, int nv);
+
+// Fused execution of an ensemble (fargo_ctx.cu): one launch of each substep kernel
+// for all disks, one CUDA graph per DT round (the DT start of every disk, then a
+// conditional while loop of substeps that runs until the last disk's DT is done).
+struct fargo_fused;
+int fused_create(fargo_ctx *const *disks, int n, fargo_fused **out, std::string *why);
+int fused_run(fargo_fused *f, int ndt);
+int fused_sync(fargo_fused *f);
+void fused_destroy(fargo_fused *f);
+int fused_launches(const fargo_fused *f, int *per_substep, int *per_dt);

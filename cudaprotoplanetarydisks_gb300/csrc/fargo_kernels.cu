@@ -157,14 +157,14 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
 // of the largest argument: the last CTA takes one sqrt and two divides of the two
 // words it reads, and no other CTA waits on an FP64 divide.
 template <class T, int V4>
-__global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
-  pdl_enter();
+__device__ __forceinline__ void cfl_forces_body(const KArgs<T> &a, const uint3 bid) {
+  
   if (a.guard && a.d.ctl->done) return;  // the next substep's, after the DT's last
   constexpr int NW = 8;                       // most warps of a CTA (96 to 256 threads)
   constexpr int NV = 2 * (FARGO_MAXPL + 1);   // force components, body-major
   constexpr int NC = V4 ? 4 : 1;
   const DevParams &P = a.P;
-  const int i = blockIdx.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
+  const int i = bid.x, nsec = P.nsec, nrad = P.nrad, tid = threadIdx.x;
   const int lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
   Ctl *c = a.d.ctl;
   __shared__ SumAcc<T> s_part[NW][NV];
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
   // last block: CFL decision, force totals
   __threadfence();
   __syncthreads();
-  if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == gridDim.x - 1);
+  if (tid == 0) s_last = (atomicAdd(&c->ticket, 1u) == bid.z - 1);
   if (own && do_forces && P.nb > 0) store4(pot + j0, ph);
   __syncthreads();
   if (!s_last) return;
@@ -505,6 +505,11 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
       a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
   }
 }
+template <class T, int V4>
+__global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
+  pdl_enter();
+  cfl_forces_body<T, V4>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // The CFL/force kernel for a ring of nsec cells: four contiguous cells per
 // thread when nsec % 4 == 0 and 260 <= nsec <= 1024 (96 to 256 threads: every
@@ -526,8 +531,8 @@ void launch_cfl_forces(const KArgs<T> &a, cudaStream_t s) {
 // next substep's planet parameters, which no hydro kernel of the substep reads,
 // so it may run beside them; in a corotating frame the hydro kernels need the
 // new frame rate and it runs before them.
-__global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const double *__restrict__ ring_force, int fp32) {
-  pdl_enter();
+__device__ __forceinline__ void planets_body(const DevParams &P, Ctl *c, const double *__restrict__ ring_force,
+                                             int fp32) {
   constexpr int NV = 2 * (FARGO_MAXPL + 1);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nrad = P.nrad;
   // the disk's force on each planet feeling it (bodies 1.. of k_cfl_forces)
@@ -542,14 +547,18 @@ __global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const doubl
   __syncthreads();
   if (threadIdx.x == 0) fargo_planets_substep(*c, P, c->dt, c->t_sub);
 }
+__global__ void __launch_bounds__(64) k_planets(DevParams P, Ctl *c, const double *__restrict__ ring_force, int fp32) {
+  pdl_enter();
+  planets_body(P, c, ring_force, fp32);
+}
 
 // ---------------------------------------------------------------------------
 // ComputeSoundSpeed (energy equation) + Make1Dprofile(1) ring means; one CTA per ring.
 template <class T>
-__global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
-  pdl_enter();
+__device__ __forceinline__ void soundspeed_body(const KArgs<T> &a, const uint3 bid) {
+  
   __shared__ SumAcc<T> s_red[8];
-  const int i = blockIdx.x, nsec = a.P.nsec;
+  const int i = bid.x, nsec = a.P.nsec;
   const double g = a.P.adiabaticindex;
   SumAcc<T> s;
   s.zero();
@@ -574,15 +583,25 @@ __global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
     }
   }
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
+  pdl_enter();
+  soundspeed_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // CorrectVthetaKernel src/Kernels.cu:1256-1263 (corotating frame)
 template <class T>
-__global__ void k_correct_vtheta(KArgs<T> a) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void correct_vtheta_body(const KArgs<T> &a, const uint3 bid) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const size_t q = (size_t)i * a.P.nsec + j;
   a.d.vtheta[q] = a.d.vtheta[q] - CTL_T(T, a.d.ctl, domega, CTL_F_DOMEGA) * RT(a, RT_RMED, i);
+}
+template <class T>
+__global__ void k_correct_vtheta(KArgs<T> a) {
+  pdl_enter();
+  correct_vtheta_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -834,9 +853,9 @@ __device__ __forceinline__ T subkeplerian_edge(const KArgs<T> &a, int i) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void source_body(const KArgs<T> &a, const uint3 bid) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   if (i >= a.P.nrad || j >= a.P.nsec) return;
   const SrcCell<T> o = source_cell(a, i, j);
   const size_t q = (size_t)i * a.P.nsec + j;
@@ -844,12 +863,17 @@ __global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
   a.d.vthetaint[q] = o.vt;
   a.d.pressure[q] = o.p;
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
+  pdl_enter();
+  source_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
 template <class T>
-__global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restrict__ vr, const T *__restrict__ vt) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void visc_tau_body(const KArgs<T> &a, const uint3 bid, const T *__restrict__ vr, const T *__restrict__ vt) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
@@ -871,13 +895,18 @@ __global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restric
     a.d.taurp[q] = (T)(2.0 * 0.25) * (D[q] + D[q - nsec] + D[qm] + D[qm - nsec]) * nu * drp;
   }
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restrict__ vr, const T *__restrict__ vt) {
+  pdl_enter();
+  visc_tau_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y), vr, vt);
+}
 
 // UpdateVelocitiesKernel src/Kernels.cu:118-150 + ApplySubKeplerianBoundaryKernel
 // src/Kernels.cu:1416-1430 (skipped with the evanescent boundary, src/SourceEuler.cu:338).
 template <class T>
-__global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void visc_update_body(const KArgs<T> &a, const uint3 bid) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const Ctl *c = a.d.ctl;
@@ -904,14 +933,19 @@ __global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
   // transport gave them)
   if (!a.P.evanescent && (i == 0 || i == nrad - 1) && dt != (T)0.0) a.d.vthetaint[q] = subkeplerian_edge(a, i);
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
+  pdl_enter();
+  visc_update_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // Substep2Kernel (src/Kernels.cu:409-434) + kernel (src/Kernels.cu:438-479) +
 // ActualiseGasVrad/Vtheta: the artificial-viscosity pressures are evaluated where
 // they are needed and the new velocities are written to Vrad/Vtheta directly.
 template <class T>
-__global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void artvisc_body(const KArgs<T> &a, const uint3 bid) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
@@ -951,12 +985,17 @@ __global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
     a.d.vtheta[q + nsec] = (T)0.0;
   }
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
+  pdl_enter();
+  artvisc_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // Substep3Kernel + Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
 template <class T>
-__global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const double g = a.P.adiabaticindex;
@@ -998,6 +1037,11 @@ __global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
     if (dt == (T)0.0) enew = ei;  // a padded substep: (ct ei) / ct is not exactly ei
   }
   a.d.energy[q] = enew;
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
+  pdl_enter();
+  energy_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -1155,15 +1199,15 @@ __device__ __forceinline__ void rad_cell(const KArgs<T> &a, int k, T d, T v0, T 
 // interfaces and the cell updates are each formed once, one barrier between
 // the phases.
 template <class T>
-__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
-  pdl_enter();
+__device__ __forceinline__ void radial_body(const KArgs<T> &a, const uint3 bid) {
+  
   constexpr int TR = RAD_TR, ny = RAD_NY;
   extern __shared__ __align__(16) unsigned char rad_smem[];
   const RadTile<T> t(rad_smem);
   const DevParams &P = a.P;
   const int nrad = P.nrad, nsec = P.nsec;
   const int x = threadIdx.x, y = threadIdx.y;
-  const int j = blockIdx.x * 32 + x, i0 = blockIdx.y * TR;
+  const int j = bid.x * 32 + x, i0 = bid.y * TR;
   const bool col = j < nsec;
   const int jp = col ? jp1(j, nsec) : 0;
   __shared__ T sRT[5][TR + 3];  // INVDIFFRMED, RMED, RINF, RSUP, INVSURF
@@ -1185,6 +1229,11 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
   }
   __syncthreads();
   rad_tile_update(a, t, sRT, i0, j, x, y);
+}
+template <class T>
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
+  pdl_enter();
+  radial_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -1467,16 +1516,21 @@ inline int az4_threads(int nsec) {
   const int n = nsec / 4 < most ? nsec / 4 : most;
   return (n + 31) / 32 * 32;
 }
-template <class T, bool MC>  // MC: several chunks per thread (rings wider than the CTA)
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
-  pdl_enter();
+template <class T>
+int az4_threads_host(int nsec) {
+  return az4_threads<T>(nsec);
+}
+size_t rad_smem_bytes(int esize) { return esize == 8 ? RAD_SMEM(double) : RAD_SMEM(float); }
+template <class T, bool MC>
+__device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 bid) {
+  
   extern __shared__ __align__(16) unsigned char az_smem[];
   __shared__ SumAcc<T> s_part[32];
   __shared__ RingMean<T> s_vm;
   __shared__ T s_vct;
   __shared__ int s_shift;
   const DevParams &P = a.P;
-  const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x;
+  const int i = bid.x, nsec = P.nsec, tid = threadIdx.x;
   const int lane = tid & 31, w = tid >> 5, nw = (blockDim.x + 31) >> 5;
   const int nchunk = nsec >> 2;
   // body(j0) for the thread's chunks: one chunk in straight-line code when !MC
@@ -1663,13 +1717,18 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimut
     each_chunk([&](int j0) { sweep(QA, nullptr, false, j0); });
   }
 }
+template <class T, bool MC>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
+  pdl_enter();
+  azimuthal4_body<T, MC>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // ComputeVelocitiesKernel src/Kernels.cu:1193-1210 (+ ComputeTemperatureFieldKernel
 // src/Kernels.cu:203-213 when no boundary runs in between).
 template <class T>
-__global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_temperature) {
-  pdl_enter();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void velocities_body(const KArgs<T> &a, const uint3 bid, int with_temperature) {
+  
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
   const T Om = CTL_T(T, a.d.ctl, OmegaFrame, CTL_F_OMEGA), dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
@@ -1691,6 +1750,11 @@ __global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_tempera
   }
   if (!isfinite(D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_temperature) {
+  pdl_enter();
+  velocities_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y), with_temperature);
+}
 
 // ComputeTemperatureFieldKernel src/Kernels.cu:203-213 (after a boundary condition)
 template <class T>
@@ -1706,8 +1770,8 @@ __global__ void k_temperature(KArgs<T> a) {
 // End of a substep: LostMass (src/TransportEuler.cu:77), PhysicalTime += dt
 // (src/SourceEuler.cu:302) and the while-loop condition of AlgoGas (line 222).
 template <class T>
-__global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
-  pdl_enter();
+__device__ __forceinline__ void end_body(const KArgs<T> &a, const uint3 bid) {
+  
   __shared__ double s_red[32];
   Ctl *c = a.d.ctl;
   if (a.P.open_inner) {
@@ -1734,10 +1798,14 @@ __global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
     if (a.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_handle, done ? 0u : 1u);
   }
 }
+template <class T>
+__global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
+  pdl_enter();
+  end_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+}
 
 // Start of a DT (AlgoGas entry, src/SourceEuler.cu:202-221).
-__global__ void k_dt_begin(Ctl *c) {
-  pdl_enter();
+__device__ __forceinline__ void dt_begin_body(Ctl *c) {
   c->dtemp = 0.0;
   c->nsub_dt = 0;
   c->done = 0;
@@ -1745,6 +1813,150 @@ __global__ void k_dt_begin(Ctl *c) {
   c->ticket = 0u;
   c->padding = 0;
   c->ring_max[0] = c->ring_max[1] = FARGO_RING_NO_LIMIT;
+}
+__global__ void k_dt_begin(Ctl *c) {
+  pdl_enter();
+  dt_begin_body(c);
+}
+
+// ---------------------------------------------------------------------------
+// Fused ensembles (fargo_batch_fuse): one launch of each substep kernel for a
+// group of disks.  Member g of a group owns the launch's blocks first[g] ..
+// first[g+1]-1, its own grid laid out gx[g] blocks wide; a block finds its disk by
+// binary search, skips it when that disk's DT is over (masked subcycling: every
+// disk keeps its own CFL step and substep count, and the loop runs until the last
+// disk is done), and runs the kernel body of the single-disk launch with the
+// disk's arguments and its own block index.
+template <class T>
+__device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, uint3 &bid, bool masked = true) {
+  const int b = (int)blockIdx.x;
+  int lo = 0, hi = G.ng - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (G.first[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const KArgs<T> *a = &G.args[G.member[lo]];
+  if (masked && a->d.ctl->done) return nullptr;
+  const int local = b - G.first[lo];
+  bid = make_uint3((unsigned)(local % G.gx[lo]), (unsigned)(local / G.gx[lo]),
+                   (unsigned)(G.first[lo + 1] - G.first[lo]));
+  return a;
+}
+
+#define FARGO_BATCHED(kname, bounds, call)                                       \
+  template <class T>                                                             \
+  __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
+    pdl_enter();                                                                 \
+    uint3 bid;                                                                   \
+    const KArgs<T> *a = batch_block(G, bid);                                     \
+    if (a) call;                                                                 \
+  }
+FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body<T>(*a, bid))
+FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body<T>(*a, bid))
+FARGO_BATCHED(kb_source, 256, source_body<T>(*a, bid))
+FARGO_BATCHED(kb_visc_tau, 256,
+              visc_tau_body<T>(*a, bid, G.extra ? a->d.vrad : a->d.vradint, G.extra ? a->d.vtheta : a->d.vthetaint))
+FARGO_BATCHED(kb_visc_update, 256, visc_update_body<T>(*a, bid))
+FARGO_BATCHED(kb_artvisc, 256, artvisc_body<T>(*a, bid))
+FARGO_BATCHED(kb_energy, 256, energy_body<T>(*a, bid))
+FARGO_BATCHED(kb_radial, 32 * RAD_NY, radial_body<T>(*a, bid))
+FARGO_BATCHED(kb_velocities, 256, velocities_body<T>(*a, bid, G.extra))
+FARGO_BATCHED(kb_end, 256, end_body<T>(*a, bid))
+FARGO_BATCHED(kb_planets, 64, planets_body(a->P, a->d.ctl, a->d.ring_force, sizeof(T) == 4))
+#undef FARGO_BATCHED
+
+template <class T, int V4>
+__global__ void __launch_bounds__(256, V4 ? 1 : 2) kb_cfl_forces(BatchGroup<T> G) {
+  pdl_enter();
+  uint3 bid;
+  const KArgs<T> *a = batch_block(G, bid);
+  if (a) cfl_forces_body<T, V4>(*a, bid);
+}
+template <class T, bool MC>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(BatchGroup<T> G) {
+  pdl_enter();
+  uint3 bid;
+  const KArgs<T> *a = batch_block(G, bid);
+  if (a) azimuthal4_body<T, MC>(*a, bid);
+}
+// the start of a DT on every member (not masked: it clears the done flag)
+template <class T>
+__global__ void kb_dt_begin(BatchGroup<T> G) {
+  pdl_enter();
+  uint3 bid;
+  const KArgs<T> *a = batch_block(G, bid, false);
+  if (threadIdx.x == 0) dt_begin_body(a->d.ctl);
+}
+// the condition of the fused DT loop: another substep while any disk is not done
+__global__ void kb_loop_cond(Ctl *const *ctls, int n, unsigned long long handle) {
+  pdl_enter();
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    if (!ctls[k]->done) any = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) cudaGraphSetConditional((cudaGraphConditionalHandle)handle, any ? 1u : 0u);
+}
+
+template <class T>
+void launch_batched(int kernel, const BatchGroup<T> &G, int nblocks, dim3 block, size_t smem, int pdl,
+                    cudaStream_t s) {
+  const dim3 g(nblocks);
+  switch (kernel) {
+    case BK_DT_BEGIN: launch_k(pdl, kb_dt_begin<T>, g, block, smem, s, G); probe_mark(s, "kb_dt_begin"); break;
+    case BK_SOUNDSPEED: launch_k(pdl, kb_soundspeed<T>, g, block, smem, s, G); probe_mark(s, "kb_soundspeed"); break;
+    case BK_CFL_V4: launch_k(pdl, kb_cfl_forces<T, 1>, g, block, smem, s, G); probe_mark(s, "kb_cfl_forces"); break;
+    case BK_CFL: launch_k(pdl, kb_cfl_forces<T, 0>, g, block, smem, s, G); probe_mark(s, "kb_cfl_forces"); break;
+    case BK_PLANETS: launch_k(pdl, kb_planets<T>, g, block, smem, s, G); probe_mark(s, "kb_planets"); break;
+    case BK_COROT: launch_k(pdl, kb_correct_vtheta<T>, g, block, smem, s, G); probe_mark(s, "kb_correct_vtheta"); break;
+    case BK_SOURCE: launch_k(pdl, kb_source<T>, g, block, smem, s, G); probe_mark(s, "kb_source"); break;
+    case BK_VISC_TAU: launch_k(pdl, kb_visc_tau<T>, g, block, smem, s, G); probe_mark(s, "kb_visc_tau"); break;
+    case BK_VISC_UPDATE: launch_k(pdl, kb_visc_update<T>, g, block, smem, s, G); probe_mark(s, "kb_visc_update"); break;
+    case BK_ARTVISC: launch_k(pdl, kb_artvisc<T>, g, block, smem, s, G); probe_mark(s, "kb_artvisc"); break;
+    case BK_ENERGY: launch_k(pdl, kb_energy<T>, g, block, smem, s, G); probe_mark(s, "kb_energy"); break;
+    case BK_RADIAL: launch_k(pdl, kb_radial<T>, g, block, smem, s, G); probe_mark(s, "kb_radial"); break;
+    case BK_AZ4: launch_k(pdl, kb_azimuthal4<T, false>, g, block, smem, s, G); probe_mark(s, "kb_azimuthal4"); break;
+    case BK_AZ4_MC: launch_k(pdl, kb_azimuthal4<T, true>, g, block, smem, s, G); probe_mark(s, "kb_azimuthal4"); break;
+    case BK_VELOCITIES: launch_k(pdl, kb_velocities<T>, g, block, smem, s, G); probe_mark(s, "kb_velocities"); break;
+    case BK_END: launch_k(pdl, kb_end<T>, g, block, smem, s, G); probe_mark(s, "kb_end"); break;
+    default: break;
+  }
+}
+
+void launch_loop_cond(Ctl *const *ctls, int n, unsigned long long handle, int pdl, cudaStream_t s) {
+  launch_k(pdl, kb_loop_cond, dim3(1), dim3(256), 0, s, ctls, n, handle);
+  probe_mark(s, "kb_loop_cond");
+}
+
+// prepares the batched kernels that take more than 48 KB of shared memory
+template <class T>
+cudaError_t prepare_batched(size_t rad_smem, size_t az_smem) {
+  cudaError_t e;
+  const void *all[] = {(const void *)kb_dt_begin<T>, (const void *)kb_soundspeed<T>,
+                       (const void *)kb_cfl_forces<T, 1>, (const void *)kb_cfl_forces<T, 0>,
+                       (const void *)kb_planets<T>, (const void *)kb_correct_vtheta<T>, (const void *)kb_source<T>,
+                       (const void *)kb_visc_tau<T>, (const void *)kb_visc_update<T>, (const void *)kb_artvisc<T>,
+                       (const void *)kb_energy<T>, (const void *)kb_radial<T>, (const void *)kb_azimuthal4<T, false>,
+                       (const void *)kb_azimuthal4<T, true>, (const void *)kb_velocities<T>, (const void *)kb_end<T>,
+                       (const void *)kb_loop_cond};
+  for (const void *f : all)
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, FARGO_SMEM_CARVEOUT)) !=
+        cudaSuccess)
+      return e;
+  if ((e = cudaFuncSetAttribute(kb_radial<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rad_smem)) !=
+      cudaSuccess)
+    return e;
+  if (az_smem > 0) {
+    if ((e = cudaFuncSetAttribute(kb_azimuthal4<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)az_smem)) != cudaSuccess)
+      return e;
+    if ((e = cudaFuncSetAttribute(kb_azimuthal4<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)az_smem)) != cudaSuccess)
+      return e;
+  }
+  return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------
@@ -2083,6 +2295,9 @@ void launch_convert_to_f64(const void *in, double *out, size_t n, int esize, cud
   template void launch_cfl_only<T>(const KArgs<T> &, cudaStream_t);                                     \
   template void launch_boundaries<T>(const KArgs<T> &, cudaStream_t);                                   \
   template cudaError_t prepare_kernels<T>(size_t, int); \
-  template int rad_tma_grid<T>(int, int);
+  template int rad_tma_grid<T>(int, int);                                                              \
+  template void launch_batched<T>(int, const BatchGroup<T> &, int, dim3, size_t, int, cudaStream_t);   \
+  template cudaError_t prepare_batched<T>(size_t, size_t);                                                \
+  template int az4_threads_host<T>(int);
 INSTANTIATE(double)
 INSTANTIATE(float)

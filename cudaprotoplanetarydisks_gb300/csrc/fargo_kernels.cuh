@@ -117,6 +117,31 @@ template <class T>
 void launch_boundaries(const KArgs<T> &a, cudaStream_t s);
 template <class T>
 cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
+// Fused ensembles: one launch of a substep kernel over a group of disks
+// (fargo_kernels.cu, kb_*); the plan is built by fargo_fused.cu.
+template <class T>
+struct BatchGroup {
+  const KArgs<T> *args;  // every disk's kernel arguments (device array, indexed by disk)
+  const int *member;     // [ng] disk index of each member of the group
+  const int *first;      // [ng + 1] first block of each member in the launch (prefix sums)
+  const int *gx;         // [ng] width (blocks along x) of each member's own grid
+  int ng;
+  int extra;             // kb_visc_tau: 1 = the new velocities; kb_velocities: with temperature
+};
+enum BatchKernel {
+  BK_DT_BEGIN, BK_SOUNDSPEED, BK_CFL_V4, BK_CFL, BK_PLANETS, BK_COROT, BK_SOURCE, BK_VISC_TAU,
+  BK_VISC_UPDATE, BK_ARTVISC, BK_ENERGY, BK_RADIAL, BK_AZ4, BK_AZ4_MC, BK_VELOCITIES, BK_END
+};
+template <class T>
+void launch_batched(int kernel, const BatchGroup<T> &G, int nblocks, dim3 block, size_t smem, int pdl,
+                    cudaStream_t s);
+void launch_loop_cond(Ctl *const *ctls, int n, unsigned long long handle, int pdl, cudaStream_t s);
+template <class T>
+cudaError_t prepare_batched(size_t rad_smem, size_t az_smem);
+template <class T>
+int az4_threads_host(int nsec);
+#define RAD_NY_HOST 10
+size_t rad_smem_bytes(int esize);
 // CTAs of the persistent TMA radial transport on this device (0: not launchable)
 template <class T>
 int rad_tma_grid(int nrad, int nsec);

@@ -93,3 +93,59 @@ def test_tile_shapes_are_bitwise_the_default(cell_block, rad_tma, az_chunks, pre
             assert np.array_equal(a.disk(k).field(name), b.disk(k).field(name)), (k, name, cell_block)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", [fg.FARGO_FP32_BULK, fg.FARGO_FP64])
+def test_fused_ensemble_is_bitwise_the_disks_alone(precision):
+    # one launch per substep kernel for the whole ensemble, masked subcycling: every
+    # disk still takes its own substeps and ends bitwise where it ends alone
+    # widths that take both forms of the CFL kernel (four cells per thread at 288
+    # and 384 sectors, the streamed form at 96)
+    disks = fg.c4_disks(5, seed=7, nrad_choices=(32, 96, 128))
+    assert len({p.nsec for p, _ in disks}) > 1
+    b = fg.Batch(disks, precision).fuse()
+    per_substep, per_dt = b.fused_launches()
+    assert per_substep <= 16 and per_dt <= 2
+    b.run_async(2)
+    b.sync()
+    for k, (p, pl) in enumerate(disks):
+        d = fg.Disk(p, pl, precision)
+        d.run(2)
+        assert d.scalars().substeps == b.disk(k).scalars().substeps
+        for name in ("dens", "vrad", "vtheta"):
+            assert np.array_equal(d.field(name), b.disk(k).field(name)), (k, name)
+        pa, pb = d.planets()[0], b.disk(k).planets()[0]
+        assert (pa.x, pa.y, pa.vx, pa.vy) == (pb.x, pb.y, pb.vx, pb.vy)
+        d.close()
+    b.close()
+
+
+def test_fused_ensemble_adiabatic_and_corotating_disks():
+    # the energy equation (sound speed at the DT start, heating and cooling) and a
+    # corotating frame (frame correction before the hydro) ride in the same launches
+    base = small_ensemble(2)
+    disks = []
+    for k, (p, pl) in enumerate(base):
+        p3, pl3 = fg.load_config("c3", nrad=p.nrad, nsec=p.nsec)
+        disks.append((p3, pl3))
+        q = fg.FargoParams.from_buffer_copy(p)
+        q.corotating = 1
+        disks.append((q, pl))
+    b = fg.Batch(disks, fg.FARGO_FP64).fuse()
+    b.run_async(2)
+    b.sync()
+    for k, (p, pl) in enumerate(disks):
+        d = fg.Disk(p, pl, fg.FARGO_FP64)
+        d.run(2)
+        for name in ("dens", "vrad", "vtheta", "energy"):
+            assert np.array_equal(d.field(name), b.disk(k).field(name)), (k, name)
+        d.close()
+    b.close()
+
+
+def test_fuse_rejects_self_gravity():
+    p, pl = fg.load_config("c2", nrad=32, nsec=96)
+    b = fg.Batch([(p, pl)], fg.FARGO_FP64)
+    with pytest.raises(fg.FargoError, match="self-gravity"):
+        b.fuse()
+    b.close()
