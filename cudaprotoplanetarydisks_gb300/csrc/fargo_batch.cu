@@ -202,23 +202,23 @@ int fargo_batch_autotune(int n, const fargo_params *params, const fargo_planet *
   // one knob at a time: every other value of the knob on the best variant so far
   struct Knob {
     int fargo_variant::*field;
-    int nvals;  // values 0 .. nvals - 1 (az_chunks: 1 .. nvals)
+    int nvals;  // values 0 .. nvals - 1
     bool on;
   } knobs[] = {{&fargo_variant::pad, 2, true},
                {&fargo_variant::priority, 3, true},
                {&fargo_variant::sg_ahead, 2, sg},
                {&fargo_variant::pdl, 2, true},
                // tile and launch shapes: the per-cell kernels' CTA (64x4, 32x8, 128x2,
-               // 256x1), the radial transport's TMA-staged persistent form, the
-               // azimuthal sweep's chunks per thread
+               // 256x1) and the radial transport's TMA-staged persistent form (the
+               // azimuthal sweep's chunks per thread change the ring mean's summation
+               // order, so that knob is not searched: every candidate here is bitwise
+               // the default)
                {&fargo_variant::cell_block, 4, true},
-               {&fargo_variant::rad_tma, 2, true},
-               {&fargo_variant::az_chunks, 2, true}};
+               {&fargo_variant::rad_tma, 2, true}};
   for (const Knob &kn : knobs) {
     if (!kn.on) continue;
     const fargo_variant base = v;
-    const int lo = kn.field == &fargo_variant::az_chunks ? 1 : 0;
-    for (int val = lo; val < lo + kn.nvals; val++) {
+    for (int val = 0; val < kn.nvals; val++) {
       if (val == base.*kn.field) continue;
       fargo_variant cand = base;
       cand.*kn.field = val;

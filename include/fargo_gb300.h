@@ -166,7 +166,8 @@ int  fargo_planets_read(const char *cfgfile, const fargo_params *p,
 int  fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb,
                       int precision, void *stream, fargo_ctx **out);
 /* Execution variants of a context: every combination gives bitwise the same
-   results (the step's schedule changes, not its arithmetic). */
+   results (the step's schedule changes, not its arithmetic), except az_chunks = 2
+   and az_generic = 1, which sum the azimuthal ring mean in another order. */
 typedef struct {
   int graph;       /* 1: one CUDA graph per DT, CFL loop on the device; 0: host loop */
   int pdl;         /* programmatic dependent launch between the step kernels */
@@ -180,7 +181,9 @@ typedef struct {
   int rad_tma;     /* 1: radial transport on TMA-staged tiles in a persistent grid (when the rows
                       are 16-byte strided); 0: per-thread loads, one CTA per tile */
   int az_chunks;   /* four-cell chunks per thread of the register azimuthal sweep: 1 (one per
-                      thread, up to the CTA size) or 2 (half the threads, two chunks each) */
+                      thread, up to the CTA size) or 2 (half the threads, two chunks each; the
+                      ring mean is summed in another order, so results agree to rounding,
+                      not bitwise) */
 } fargo_variant;
 /* The default variant, with the FARGO_NO_GRAPH, FARGO_NO_PDL, FARGO_NO_PAD,
    FARGO_NO_SG_AHEAD, FARGO_ROTATE, FARGO_AZ_GENERIC and FARGO_PRIO switches
