@@ -1202,7 +1202,7 @@ template <class T>
 __device__ __forceinline__ void radial_body(const KArgs<T> &a, const uint3 bid) {
   
   constexpr int TR = RAD_TR, ny = RAD_NY;
-  extern __shared__ __align__(16) unsigned char rad_smem[];
+  extern __shared__ __align__(128) unsigned char rad_smem[];
   const RadTile<T> t(rad_smem);
   const DevParams &P = a.P;
   const int nrad = P.nrad, nsec = P.nsec;
@@ -1844,13 +1844,19 @@ __device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, u
   return a;
 }
 
+// The body runs on a private copy of the disk's arguments: like the single-disk
+// kernel's parameters, no store of the body can alias it, so the compiler sees the
+// same invariant values and forms the same arithmetic (multiply-adds included).
 #define FARGO_BATCHED(kname, bounds, call)                                       \
   template <class T>                                                             \
   __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
     pdl_enter();                                                                 \
     uint3 bid;                                                                   \
-    const KArgs<T> *a = batch_block(G, bid);                                     \
-    if (a) call;                                                                 \
+    const KArgs<T> *ap = batch_block(G, bid);                                    \
+    if (!ap) return;                                                             \
+    const KArgs<T> la = *ap;                                                     \
+    const KArgs<T> *a = &la;                                                     \
+    call;                                                                        \
   }
 FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body<T>(*a, bid))
 FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body<T>(*a, bid))
@@ -1870,15 +1876,19 @@ template <class T, int V4>
 __global__ void __launch_bounds__(256, V4 ? 1 : 2) kb_cfl_forces(BatchGroup<T> G) {
   pdl_enter();
   uint3 bid;
-  const KArgs<T> *a = batch_block(G, bid);
-  if (a) cfl_forces_body<T, V4>(*a, bid);
+  const KArgs<T> *ap = batch_block(G, bid);
+  if (!ap) return;
+  const KArgs<T> la = *ap;
+  cfl_forces_body<T, V4>(la, bid);
 }
 template <class T, bool MC>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(BatchGroup<T> G) {
   pdl_enter();
   uint3 bid;
-  const KArgs<T> *a = batch_block(G, bid);
-  if (a) azimuthal4_body<T, MC>(*a, bid);
+  const KArgs<T> *ap = batch_block(G, bid);
+  if (!ap) return;
+  const KArgs<T> la = *ap;
+  azimuthal4_body<T, MC>(la, bid);
 }
 // the start of a DT on every member (not masked: it clears the done flag)
 template <class T>
