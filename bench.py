@@ -235,14 +235,16 @@ def _profile_rows(cfg, mode):
 def ncu_traffic(kernel, cfg, mode="fp32"):
     """DRAM bytes (read + write) of one launch of `kernel` from the committed ncu
     summary profiles/kernels_<cfg>_<mode>.md (one cold-cache capture), or None."""
-    cells = _profile_rows(cfg, mode).get(kernel)
+    rows = _profile_rows(cfg, mode)
+    # the substep timer names both azimuthal forms k_transport_azimuthal; ncu names
+    # the register form k_transport_azimuthal4
+    cells = rows.get(kernel) or rows.get(kernel + "4")
     if cells is None:
         return None
-    if mode == "fp64":  # columns: launches, avg us, read MB, write MB, ...
-        try:
-            return (float(cells[3]) + float(cells[4])) * 1e6
-        except (ValueError, IndexError):
-            return None
+    try:  # columns: kernel, launches, avg us, read MB, write MB, ...
+        return (float(cells[3]) + float(cells[4])) * 1e6
+    except (ValueError, IndexError):
+        pass
     scale = {"B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
     try:
         rd, ru = cells[2].split()
@@ -612,7 +614,7 @@ def run_own(args, world, rank, local):
                      "traffic": ncu_traffic(dname, args.config, "fp64"),
                      "traffic_source": f"profiles/kernels_{args.config}_fp64.md (ncu, one cold-cache launch)",
                      "fp64_pipe": fp64_pipe,
-                     "note": "the FP64 kernels are bound by the FP64 pipe (83-90% busy in ncu), not by HBM; "
+                     "note": "the FP64 kernels are bound by the FP64 pipe (81-89% busy in ncu), not by HBM; "
                              "fp64_pipe.frac is the roofline fraction that applies"},
         "step_roofline": {"alg_bytes_per_cell_update": sb64, "achieved_GBs": value * sb64 / 1e9,
                           "frac": value * sb64 / 1e9 / hbm_peak},
@@ -722,10 +724,10 @@ def batch_ensemble(ndt=4, n=64):
     disks = fg.c4_disks(n)
     cells = [p.nrad * p.nsec for p, _ in disks]
 
-    def batched(variant, fused=False):
+    def batched(variant, fused=None):
         b = fg.Batch(disks, fg.FARGO_FP32_BULK, variant=variant)
         if fused:
-            b.fuse()
+            b.fuse(by_width=(fused == "width"))
         b.run_async(1)
         b.sync()
         s0 = [d.scalars().substeps for d in b.disks]
@@ -740,6 +742,12 @@ def batch_ensemble(ndt=4, n=64):
             per_sub, per_dt = b.fused_launches()
             nsub_max = max(d.scalars().substeps - s0[k] for k, d in enumerate(b.disks))
             launches = ndt * per_dt + nsub_max * per_sub  # at least: the loop runs to the slowest disk
+            if fused == "width":
+                # per-group device times of one substep (lanes one after another)
+                groups = {}
+                for name, ms in b.fused_kernel_times(reps=3):
+                    groups[name] = groups.get(name, 0.0) + ms
+                launches = (launches, {k: round(v, 4) for k, v in sorted(groups.items(), key=lambda kv: -kv[1])})
         else:
             launches = sum(d.scalars().launches_per_substep * (d.scalars().substeps - s0[k] + d.scalars().padded_substeps)
                            for k, d in enumerate(b.disks))
@@ -753,9 +761,12 @@ def batch_ensemble(ndt=4, n=64):
     t_tune = time.perf_counter() - t_tune
     tt, cut, dens_t, _ = batched(variant)
     assert all(np.array_equal(x, y) for x, y in zip(dens32, dens_t))  # variants change speed only
-    # the fused form: each substep kernel launched once for the whole ensemble
-    tf, cuf, dens_f, launches_f = batched(None, fused=True)
+    # the fused forms: each substep kernel launched once per ring width (lanes side
+    # by side), and once for the whole ensemble
+    tf, cuf, dens_f, (launches_f, groups_ms) = batched(None, fused="width")
     fused_diff = max(float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(dens_f, dens32))
+    tf1, cuf1, dens_f1, launches_f1 = batched(None, fused="one")
+    fused_diff = max(fused_diff, max(float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(dens_f1, dens32)))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     t64, cu64, err = 0.0, 0, []
     for k, (p, pl) in enumerate(disks):
@@ -779,9 +790,15 @@ def batch_ensemble(ndt=4, n=64):
             "fp32_batched_autotuned": {"value": cut / tt, "unit": METRIC, "seconds": tt, "variant": variant.as_dict(),
                                        "search": {"seconds": t_tune, "rate_default": r_default, "rate_kept": r_best}},
             "fp32_fused": {"value": cuf / tf, "unit": METRIC, "seconds": tf, "gpu_launches_approx": launches_f,
-                           "form": "one launch of each substep kernel for all disks, one graph per DT round, "
-                                   "masked subcycling (fargo_batch_fuse)",
+                           "form": "one launch of each substep kernel per ring width, the width lanes side by side, "
+                                   "one graph per DT round, masked subcycling (fargo_batch_fuse)",
                            "speedup_over_per_disk_graphs": (cuf / tf) / v32,
+                           "group_ms_per_substep": groups_ms,
+                           "one_lane": {"value": cuf1 / tf1, "unit": METRIC, "seconds": tf1,
+                                        "gpu_launches_approx": launches_f1,
+                                        "form": "one launch of each substep kernel for the whole ensemble "
+                                                "(fargo_batch_fuse_by_width(b, 0))",
+                                        "speedup_over_per_disk_graphs": (cuf1 / tf1) / v32},
                            "dens_max_rel_diff_vs_per_disk": fused_diff},
             "fp64_plain_sequential": {"value": v64, "unit": METRIC, "seconds": t64},
             "ratio_fp32_batched_to_fp64_plain": v32 / v64,

@@ -217,14 +217,33 @@ class Batch:
         if rc != _capi.FARGO_OK:
             raise FargoError(f"fargo_batch_sync: status {rc}")
 
-    def fuse(self):
-        """fargo_batch_fuse: from now on every substep kernel runs once for the whole
-        ensemble (one graph per DT round, masked subcycling); raises with the reason
-        when a disk uses a path the fused form does not carry."""
-        rc = self.lib.fargo_batch_fuse(self.h)
+    def fuse(self, by_width=True):
+        """fargo_batch_fuse / fargo_batch_fuse_by_width: from now on every substep
+        kernel runs once per lane of disks (one lane per ring width, or with
+        by_width=False one for the whole ensemble; one graph per DT round, masked
+        subcycling); raises with the reason when a disk uses a path the fused form
+        does not carry."""
+        rc = self.lib.fargo_batch_fuse_by_width(self.h, 1 if by_width else 0)
         if rc != _capi.FARGO_OK:
             raise FargoError(f"fargo_batch_fuse: status {rc}: {self.lib.fargo_batch_last_error(self.h).decode()}")
         return self
+
+    def fused_lanes(self):
+        n = ctypes.c_int(0)
+        rc = self.lib.fargo_batch_fused_lanes(self.h, ctypes.byref(n))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_fused_lanes: status {rc}")
+        return n.value
+
+    def fused_kernel_times(self, reps=4):
+        """[(kernel, mean ms)] of every launch group of one fused substep
+        (fargo_batch_fused_time_kernels: starts a DT round, runs reps substeps)."""
+        ms = (ctypes.c_double * 1024)()
+        n = ctypes.c_int(0)
+        rc = self.lib.fargo_batch_fused_time_kernels(self.h, reps, ms, 1024, ctypes.byref(n))
+        if rc != _capi.FARGO_OK:
+            raise FargoError(f"fargo_batch_fused_time_kernels: status {rc}")
+        return [(self.lib.fargo_batch_fused_kernel_name(self.h, k).decode(), ms[k]) for k in range(n.value)]
 
     def fused_launches(self):
         """(launches per substep of the whole ensemble, launches per DT round)."""

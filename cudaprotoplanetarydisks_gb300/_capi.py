@@ -141,6 +141,10 @@ SIGNATURES = [
     ("fargo_batch_fuse", _I, [_P]),
     ("fargo_batch_last_error", ctypes.c_char_p, [_P]),
     ("fargo_batch_fused_launches", _I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("fargo_batch_fuse_by_width", _I, [_P, _I]),
+    ("fargo_batch_fused_lanes", _I, [_P, ctypes.POINTER(_I)]),
+    ("fargo_batch_fused_time_kernels", _I, [_P, _I, ctypes.POINTER(_D), _I, ctypes.POINTER(_I)]),
+    ("fargo_batch_fused_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_batch_advance", _I, [_P, _D, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)]),
     ("fargo_mlp_create", _I, [_I, ctypes.POINTER(_P)]),
     ("fargo_mlp_destroy", None, [_P]),

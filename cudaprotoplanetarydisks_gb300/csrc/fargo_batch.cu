@@ -93,11 +93,35 @@ int fargo_batch_run_async(fargo_batch *b, int ndt) {
   return enqueue(b, nullptr, ndt);
 }
 
-int fargo_batch_fuse(fargo_batch *b) {
+int fargo_batch_fuse_by_width(fargo_batch *b, int by_width) {
   if (!b) return FARGO_ERR_STATE;
-  if (b->fused) return FARGO_OK;
+  by_width = by_width ? 1 : 0;
+  if (b->fused && (fused_lanes(b->fused) > 1) == (by_width == 1)) return FARGO_OK;
+  if (b->fused) {
+    const int rc = fused_sync(b->fused);
+    fused_destroy(b->fused);
+    b->fused = nullptr;
+    if (rc != FARGO_OK) return rc;
+  }
   b->err.clear();
-  return fused_create(b->disks.data(), (int)b->disks.size(), &b->fused, &b->err);
+  return fused_create(b->disks.data(), (int)b->disks.size(), by_width, &b->fused, &b->err);
+}
+
+int fargo_batch_fuse(fargo_batch *b) { return fargo_batch_fuse_by_width(b, 1); }
+
+int fargo_batch_fused_lanes(const fargo_batch *b, int *lanes) {
+  if (!b || !b->fused || !lanes) return FARGO_ERR_STATE;
+  *lanes = fused_lanes(b->fused);
+  return FARGO_OK;
+}
+
+int fargo_batch_fused_time_kernels(fargo_batch *b, int reps, double *ms_per_group, int cap, int *ngroups) {
+  if (!b || !b->fused) return FARGO_ERR_STATE;
+  return fused_time_kernels(b->fused, reps, ms_per_group, cap, ngroups);
+}
+
+const char *fargo_batch_fused_kernel_name(const fargo_batch *b, int k) {
+  return b && b->fused ? fused_kernel_name(b->fused, k) : nullptr;
 }
 
 const char *fargo_batch_last_error(const fargo_batch *b) { return b ? b->err.c_str() : ""; }

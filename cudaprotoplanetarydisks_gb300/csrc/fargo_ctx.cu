@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -1212,11 +1213,20 @@ int fargo_restart(fargo_ctx *c, int index) {
 struct fargo_fused {
   int precision = FARGO_FP64;
   int n = 0;
+  int lanes = 1;
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<void *> bufs;  // device: arguments, control-block table, group tables
   int per_substep = 0, per_dt = 0;
+  // the launches of the plan, for fused_time_kernels: the DT start, then the
+  // substep groups (lane by lane)
+  struct Launch {
+    const char *name;
+    std::function<void(cudaStream_t, int)> fn;  // (stream, programmatic launch)
+  };
+  std::vector<Launch> head, body;
+  std::vector<std::string> names;  // of the last fused_time_kernels
 };
 
 namespace {
@@ -1228,10 +1238,18 @@ struct FusedGroup {
   int extra = 0;
 };
 
+const char *batch_kernel_name(int k) {
+  static const char *const names[BK_END + 1] = {
+      "kb_dt_begin", "kb_soundspeed", "kb_cfl_forces (4 cells/thread)", "kb_cfl_forces", "kb_planets",
+      "kb_correct_vtheta", "kb_source", "kb_visc_tau", "kb_visc_update", "kb_artvisc", "kb_energy", "kb_radial",
+      "kb_azimuthal4", "kb_azimuthal4 (chunks/thread)", "kb_velocities", "kb_end"};
+  return k >= 0 && k <= BK_END ? names[k] : "?";
+}
+
 template <class T>
-int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why) {
+int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, std::string *why) {
   std::vector<KArgs<T>> args(n);
-  size_t az_smem = 0;
+  size_t az_smem_all = 0;
   for (int k = 0; k < n; k++) {
     const fargo_ctx *c = disks[k];
     const fargo_params &p = c->P;
@@ -1253,7 +1271,7 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
     a.cell_bx = 64;
     a.cell_by = 4;
     args[k] = a;
-    az_smem = std::max(az_smem, c->az_smem);
+    az_smem_all = std::max(az_smem_all, c->az_smem);
   }
   auto dev = [&](const void *src, size_t bytes) -> void * {
     void *p = nullptr;
@@ -1270,8 +1288,17 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
     *why = "device allocation of the fused plan failed";
     return FARGO_ERR_CUDA;
   }
+  // lanes: one per ring width (by_width), or one for every disk.  Width 0 = any.
+  std::vector<int> widths;
+  if (by_width) {
+    for (int k = 0; k < n; k++) widths.push_back(disks[k]->P.nsec);
+    std::sort(widths.begin(), widths.end());
+    widths.erase(std::unique(widths.begin(), widths.end()), widths.end());
+  } else {
+    widths.push_back(0);
+  }
   // launch groups in substep order
-  auto group = [&](int kernel, auto pred, auto grid, dim3 block, size_t smem, int extra) {
+  auto group = [&](int kernel, int width, auto pred, auto grid, dim3 block, size_t smem, int extra) {
     FusedGroup g;
     g.kernel = kernel;
     g.block = block;
@@ -1279,6 +1306,7 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
     g.extra = extra;
     g.first.push_back(0);
     for (int k = 0; k < n; k++) {
+      if (width && disks[k]->P.nsec != width) continue;
       if (!pred(disks[k]->P, disks[k])) continue;
       const int2 gd = grid(disks[k]->P, disks[k]);
       g.member.push_back(k);
@@ -1300,32 +1328,38 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
   auto corot = [](const fargo_params &p, const fargo_ctx *) { return p.corotating != 0; };
   auto az_mc = [](const fargo_params &p, const fargo_ctx *) { return p.nsec / 4 > az4_threads_host<T>(p.nsec); };
   auto az_one = [&](const fargo_params &p, const fargo_ctx *c) { return !az_mc(p, c); };
-  int v4_threads = 32, az_threads = 32;
-  for (int k = 0; k < n; k++) {
-    const fargo_params &p = disks[k]->P;
-    if (v4(p, disks[k])) v4_threads = std::max(v4_threads, (p.nsec / 4 + 31) / 32 * 32);
-    az_threads = std::max(az_threads, az4_threads_host<T>(p.nsec));
-  }
   const dim3 b2(64, 4);
-  std::vector<FusedGroup> head = {group(BK_DT_BEGIN, all, one, dim3(32), 0, 0),
-                                  group(BK_SOUNDSPEED, adiabatic, rings, dim3(256), 0, 0)};
-  std::vector<FusedGroup> body = {
-      group(BK_CFL_V4, v4, rings, dim3(v4_threads), 0, 0),
-      group(BK_CFL, not_v4, rings, dim3(256), 0, 0),
-      group(BK_PLANETS, all, one, dim3(64), 0, 0),
-      group(BK_COROT, corot, cells, b2, 0, 0),
-      group(BK_SOURCE, all, cells, b2, 0, 0),
-      group(BK_VISC_TAU, all, cells, b2, 0, 0),
-      group(BK_VISC_UPDATE, all, cells, b2, 0, 0),
-      group(BK_ARTVISC, all, cells, b2, 0, 0),
-      group(BK_VISC_TAU, adiabatic, cells, b2, 0, 1),
-      group(BK_ENERGY, adiabatic, cells, b2, 0, 0),
-      group(BK_RADIAL, all, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
-      group(BK_AZ4, az_one, rings, dim3(az_threads), az_smem, 0),
-      group(BK_AZ4_MC, az_mc, rings, dim3(sizeof(T) == 8 ? 512 : 768), az_smem, 0),
-      group(BK_VELOCITIES, all, cells, b2, 0, 1),
-      group(BK_END, all, one, dim3(256), 0, 0)};
-  if (prepare_batched<T>(rad_smem_bytes(sizeof(T)), az_smem) != cudaSuccess) {
+  std::vector<FusedGroup> head = {group(BK_DT_BEGIN, 0, all, one, dim3(32), 0, 0),
+                                  group(BK_SOUNDSPEED, 0, adiabatic, rings, dim3(256), 0, 0)};
+  std::vector<std::vector<FusedGroup>> body;  // per lane
+  for (const int w : widths) {
+    // the blocks that follow the ring width take the lane's widest member
+    int v4_threads = 32, az_threads = 32;
+    size_t az_smem = 0;
+    for (int k = 0; k < n; k++) {
+      const fargo_params &p = disks[k]->P;
+      if (w && p.nsec != w) continue;
+      if (v4(p, disks[k])) v4_threads = std::max(v4_threads, (p.nsec / 4 + 31) / 32 * 32);
+      az_threads = std::max(az_threads, az4_threads_host<T>(p.nsec));
+      az_smem = std::max(az_smem, disks[k]->az_smem);
+    }
+    body.push_back({group(BK_CFL_V4, w, v4, rings, dim3(v4_threads), 0, 0),
+                    group(BK_CFL, w, not_v4, rings, dim3(256), 0, 0),
+                    group(BK_PLANETS, w, all, one, dim3(64), 0, 0),
+                    group(BK_COROT, w, corot, cells, b2, 0, 0),
+                    group(BK_SOURCE, w, all, cells, b2, 0, 0),
+                    group(BK_VISC_TAU, w, all, cells, b2, 0, 0),
+                    group(BK_VISC_UPDATE, w, all, cells, b2, 0, 0),
+                    group(BK_ARTVISC, w, all, cells, b2, 0, 0),
+                    group(BK_VISC_TAU, w, adiabatic, cells, b2, 0, 1),
+                    group(BK_ENERGY, w, adiabatic, cells, b2, 0, 0),
+                    group(BK_RADIAL, w, all, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
+                    group(BK_AZ4, w, az_one, rings, dim3(az_threads), az_smem, 0),
+                    group(BK_AZ4_MC, w, az_mc, rings, dim3(sizeof(T) == 8 ? 512 : 768), az_smem, 0),
+                    group(BK_VELOCITIES, w, all, cells, b2, 0, 1),
+                    group(BK_END, w, all, one, dim3(256), 0, 0)});
+  }
+  if (prepare_batched<T>(rad_smem_bytes(sizeof(T)), az_smem_all) != cudaSuccess) {
     *why = "cudaFuncSetAttribute on the batched kernels failed";
     return FARGO_ERR_CUDA;
   }
@@ -1338,11 +1372,26 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
     G.gx = (const int *)dev(g.gx.data(), g.gx.size() * sizeof(int));
     return G.member && G.first && G.gx;
   };
-  std::vector<BatchGroup<T>> hg(head.size()), bg(body.size());
-  for (size_t q = 0; q < head.size(); q++)
-    if (!head[q].member.empty() && !to_dev(head[q], hg[q])) return FARGO_ERR_CUDA;
-  for (size_t q = 0; q < body.size(); q++)
-    if (!body[q].member.empty() && !to_dev(body[q], bg[q])) return FARGO_ERR_CUDA;
+  auto add = [&](std::vector<fargo_fused::Launch> &to, const FusedGroup &g) -> bool {
+    if (g.member.empty()) return true;
+    BatchGroup<T> G;
+    if (!to_dev(g, G)) return false;
+    const int kernel = g.kernel, nb = g.first.back();
+    const dim3 block = g.block;
+    const size_t smem = g.smem;
+    to.push_back({batch_kernel_name(kernel),
+                  [=](cudaStream_t s, int pdl) { launch_batched<T>(kernel, G, nb, block, smem, pdl, s); }});
+    return true;
+  };
+  for (const FusedGroup &g : head)
+    if (!add(f->head, g)) return FARGO_ERR_CUDA;
+  std::vector<size_t> lane_end;  // f->body index after each lane
+  for (const auto &lane : body) {
+    for (const FusedGroup &g : lane)
+      if (!add(f->body, g)) return FARGO_ERR_CUDA;
+    lane_end.push_back(f->body.size());
+  }
+  f->lanes = (int)body.size();
   if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess) return FARGO_ERR_CUDA;
   // the graph: the DT start of every disk, then the while loop of substeps
   cudaGraph_t g = nullptr, gp = nullptr;
@@ -1352,9 +1401,7 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
   std::memset(&probe, 0, sizeof(probe));
   g_probe = &probe;
   if (cudaStreamBeginCapture(f->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return FARGO_ERR_CUDA;
-  for (size_t q = 0; q < head.size(); q++)
-    if (!head[q].member.empty())
-      launch_batched<T>(head[q].kernel, hg[q], head[q].first.back(), head[q].block, head[q].smem, 1, f->stream);
+  for (const auto &l : f->head) l.fn(f->stream, 1);
   g_probe = nullptr;
   if (cudaStreamEndCapture(f->stream, &gp) != cudaSuccess) return FARGO_ERR_CUDA;
   f->per_dt = probe.count;
@@ -1369,24 +1416,58 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, std::string *why
   cp.conditional.size = 1;
   if (cudaGraphAddNode(&nc, g, &np, nullptr, 1, &cp) != cudaSuccess) return FARGO_ERR_CUDA;
   cudaGraph_t loop = cp.conditional.phGraph_out[0];
-  if (cudaStreamBeginCaptureToGraph(f->stream, loop, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
-      cudaSuccess)
+  // the loop body: each lane's substep on a stream of its own (lane 0 on the plan's
+  // stream), forked from and joined back into the plan's stream; every lane's first
+  // launch and the loop condition after the join are plain launches
+  const int L = f->lanes;
+  std::vector<cudaStream_t> ls(L, f->stream);
+  std::vector<cudaEvent_t> ev(L, nullptr);
+  bool ok = true;
+  for (int l = 0; l < L && ok; l++) {
+    ok = cudaEventCreateWithFlags(&ev[l], cudaEventDisableTiming) == cudaSuccess;
+    if (ok && l > 0) ok = cudaStreamCreateWithFlags(&ls[l], cudaStreamNonBlocking) == cudaSuccess;
+  }
+  auto cleanup = [&]() {
+    for (int l = 0; l < L; l++) {
+      if (ev[l]) cudaEventDestroy(ev[l]);
+      if (l > 0 && ls[l] != f->stream && ls[l]) cudaStreamDestroy(ls[l]);
+    }
+  };
+  if (!ok) {
+    cleanup();
     return FARGO_ERR_CUDA;
+  }
+  if (cudaStreamBeginCaptureToGraph(f->stream, loop, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess) {
+    cleanup();
+    return FARGO_ERR_CUDA;
+  }
   probe.count = 0;
   g_probe = &probe;
-  for (size_t q = 0; q < body.size(); q++)
-    if (!body[q].member.empty())
-      launch_batched<T>(body[q].kernel, bg[q], body[q].first.back(), body[q].block, body[q].smem, 1, f->stream);
-  launch_loop_cond(ctls_dev, n, (unsigned long long)h, 1, f->stream);
+  if (L > 1) {
+    cudaEventRecord(ev[0], f->stream);
+    for (int l = 1; l < L; l++) cudaStreamWaitEvent(ls[l], ev[0], 0);
+  }
+  for (int l = 0; l < L; l++) {
+    const size_t b0 = l ? lane_end[l - 1] : 0;
+    for (size_t q = b0; q < lane_end[l]; q++) f->body[q].fn(ls[l], L > 1 && q == b0 ? 0 : 1);
+  }
+  for (int l = 1; l < L; l++) {
+    cudaEventRecord(ev[l], ls[l]);
+    cudaStreamWaitEvent(f->stream, ev[l], 0);
+  }
+  launch_loop_cond(ctls_dev, n, (unsigned long long)h, L > 1 ? 0 : 1, f->stream);
   g_probe = nullptr;
-  if (cudaStreamEndCapture(f->stream, &loop) != cudaSuccess) return FARGO_ERR_CUDA;
+  const cudaError_t ce = cudaStreamEndCapture(f->stream, &loop);
+  cleanup();
+  if (ce != cudaSuccess) return FARGO_ERR_CUDA;
   f->per_substep = probe.count;
   if (cudaGraphInstantiate(&f->exec, g, 0) != cudaSuccess) return FARGO_ERR_CUDA;
   return FARGO_OK;
 }
 }  // namespace
 
-int fused_create(fargo_ctx *const *disks, int n, fargo_fused **out, std::string *why) {
+int fused_create(fargo_ctx *const *disks, int n, int by_width, fargo_fused **out, std::string *why) {
   *out = nullptr;
   if (!disks || n <= 0) return FARGO_ERR_INVALID;
   for (int k = 0; k < n; k++)
@@ -1400,7 +1481,8 @@ int fused_create(fargo_ctx *const *disks, int n, fargo_fused **out, std::string 
   fargo_fused *f = new fargo_fused();
   f->precision = disks[0]->precision;
   f->n = n;
-  const int rc = f->precision == FARGO_FP64 ? fused_build<double>(f, disks, n, why) : fused_build<float>(f, disks, n, why);
+  const int rc = f->precision == FARGO_FP64 ? fused_build<double>(f, disks, n, by_width, why)
+                                             : fused_build<float>(f, disks, n, by_width, why);
   if (rc != FARGO_OK) {
     if (why->empty()) *why = std::string("building the fused plan: ") + cudaGetErrorString(cudaGetLastError());
     fused_destroy(f);
@@ -1422,6 +1504,51 @@ int fused_launches(const fargo_fused *f, int *per_substep, int *per_dt) {
   if (per_substep) *per_substep = f->per_substep;
   if (per_dt) *per_dt = f->per_dt;
   return FARGO_OK;
+}
+
+int fused_lanes(const fargo_fused *f) { return f->lanes; }
+
+int fused_time_kernels(fargo_fused *f, int reps, double *ms, int cap, int *ngroups) {
+  if (reps <= 0 || !ms || !ngroups) return FARGO_ERR_INVALID;
+  const int G = (int)f->body.size();
+  if (cap < G) return FARGO_ERR_INVALID;
+  if (cudaStreamSynchronize(f->stream) != cudaSuccess) return FARGO_ERR_CUDA;
+  std::vector<cudaEvent_t> ev(G + 1, nullptr);
+  for (auto &e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+      return FARGO_ERR_CUDA;
+    }
+  for (const auto &l : f->head) l.fn(f->stream, 0);
+  std::vector<double> acc(G, 0.0);
+  int rc = FARGO_OK;
+  for (int r = 0; r < reps && rc == FARGO_OK; r++) {
+    cudaEventRecord(ev[0], f->stream);
+    for (int q = 0; q < G; q++) {
+      f->body[q].fn(f->stream, 0);
+      cudaEventRecord(ev[q + 1], f->stream);
+    }
+    if (cudaStreamSynchronize(f->stream) != cudaSuccess) rc = FARGO_ERR_CUDA;
+    for (int q = 0; q < G && rc == FARGO_OK; q++) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+      acc[q] += t;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc != FARGO_OK) return rc;
+  f->names.clear();
+  for (int q = 0; q < G; q++) {
+    ms[q] = acc[q] / reps;
+    f->names.push_back(f->body[q].name);
+  }
+  *ngroups = G;
+  return FARGO_OK;
+}
+
+const char *fused_kernel_name(const fargo_fused *f, int k) {
+  return k >= 0 && k < (int)f->names.size() ? f->names[k].c_str() : nullptr;
 }
 
 void fused_destroy(fargo_fused *f) {

@@ -94,8 +94,11 @@ int host_append_row(const std::string &outdir, const std::string &file, int inde
 // for all disks, one CUDA graph per DT round (the DT start of every disk, then a
 // conditional while loop of substeps that runs until the last disk's DT is done).
 struct fargo_fused;
-int fused_create(fargo_ctx *const *disks, int n, fargo_fused **out, std::string *why);
+int fused_create(fargo_ctx *const *disks, int n, int by_width, fargo_fused **out, std::string *why);
 int fused_run(fargo_fused *f, int ndt);
 int fused_sync(fargo_fused *f);
 void fused_destroy(fargo_fused *f);
 int fused_launches(const fargo_fused *f, int *per_substep, int *per_dt);
+int fused_lanes(const fargo_fused *f);
+int fused_time_kernels(fargo_fused *f, int reps, double *ms, int cap, int *ngroups);
+const char *fused_kernel_name(const fargo_fused *f, int k);

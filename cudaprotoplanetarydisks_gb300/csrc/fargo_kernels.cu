@@ -142,6 +142,31 @@ __device__ __forceinline__ void cell_force(T xc, T yc, T cellmass, T x, T y, T r
   fy.add(cellmass * dy * InvDist3);
 }
 
+// FP64 step bodies run out of line.  Each step body below is a template that the
+// single-disk kernel (k_*) and the fused-ensemble kernel (kb_*) both run.  Inlined
+// into two kernels, the same FP64 source can come out with different multiply-add
+// pairs contracted into fused multiply-adds (every FP64 divide branches to the
+// IEEE divide outside its safe exponent range, and the optimiser arranges those
+// blocks per kernel), which moves the last bits.  For T = double the kernels
+// therefore call one out-of-line instance of each body, so that both run the same
+// machine code and the fused ensemble is bitwise the disks run alone; the FP32
+// bodies stay inlined (their kernels agree bitwise inlined, tested).  The
+// single-disk kernels take their arguments as __grid_constant__ so that the
+// out-of-line call reads them in place.
+#define FARGO_F64_BODY(body)                                                                    \
+  template <class... X>                                                                         \
+  __device__ __noinline__ void body##_f64(const KArgs<double> &a, const uint3 bid, X... x) {    \
+    body<double>(a, bid, x...);                                                                 \
+  }
+#define FARGO_RUN_BODY(T, body, a, bid, ...)                                                   \
+  do {                                                                                          \
+    if constexpr (sizeof(T) == 8)                                                               \
+      body##_f64(a, bid, ##__VA_ARGS__);                                                        \
+    else                                                                                        \
+      body<T>(a, bid, ##__VA_ARGS__);                                                           \
+  } while (0)
+#define FARGO_BID make_uint3(blockIdx.x, blockIdx.y, gridDim.x *gridDim.y)
+
 // V4 = 1 (nsec % 4 == 0, 260 <= nsec <= 1024): thread t holds the inputs of cells
 // 4t..4t+3 in registers, each stream read with one 16-byte load, in one batch
 // ahead of the ring mean (one memory latency, a few load instructions).  V4 = 0:
@@ -505,10 +530,21 @@ __device__ __forceinline__ void cfl_forces_body(const KArgs<T> &a, const uint3 b
       a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
   }
 }
+template <int V4>
+__device__ __noinline__ void cfl_forces_body_f64(const KArgs<double> &a, const uint3 bid) {
+  cfl_forces_body<double, V4>(a, bid);
+}
 template <class T, int V4>
-__global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(KArgs<T> a) {
+__device__ __forceinline__ void cfl_forces_run(const KArgs<T> &a, const uint3 bid) {
+  if constexpr (sizeof(T) == 8)
+    cfl_forces_body_f64<V4>(a, bid);
+  else
+    cfl_forces_body<T, V4>(a, bid);
+}
+template <class T, int V4>
+__global__ void __launch_bounds__(256, V4 ? 1 : 2) k_cfl_forces(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  cfl_forces_body<T, V4>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  cfl_forces_run<T, V4>(a, FARGO_BID);
 }
 
 // The CFL/force kernel for a ring of nsec cells: four contiguous cells per
@@ -583,10 +619,11 @@ __device__ __forceinline__ void soundspeed_body(const KArgs<T> &a, const uint3 b
     }
   }
 }
+FARGO_F64_BODY(soundspeed_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_soundspeed(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_soundspeed(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  soundspeed_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, soundspeed_body, a, FARGO_BID);
 }
 
 // CorrectVthetaKernel src/Kernels.cu:1256-1263 (corotating frame)
@@ -598,10 +635,11 @@ __device__ __forceinline__ void correct_vtheta_body(const KArgs<T> &a, const uin
   const size_t q = (size_t)i * a.P.nsec + j;
   a.d.vtheta[q] = a.d.vtheta[q] - CTL_T(T, a.d.ctl, domega, CTL_F_DOMEGA) * RT(a, RT_RMED, i);
 }
+FARGO_F64_BODY(correct_vtheta_body)
 template <class T>
-__global__ void k_correct_vtheta(KArgs<T> a) {
+__global__ void k_correct_vtheta(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  correct_vtheta_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, correct_vtheta_body, a, FARGO_BID);
 }
 
 // ---------------------------------------------------------------------------
@@ -863,10 +901,11 @@ __device__ __forceinline__ void source_body(const KArgs<T> &a, const uint3 bid) 
   a.d.vthetaint[q] = o.vt;
   a.d.pressure[q] = o.p;
 }
+FARGO_F64_BODY(source_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_source(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_source(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  source_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, source_body, a, FARGO_BID);
 }
 
 // ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
@@ -895,10 +934,12 @@ __device__ __forceinline__ void visc_tau_body(const KArgs<T> &a, const uint3 bid
     a.d.taurp[q] = (T)(2.0 * 0.25) * (D[q] + D[q - nsec] + D[qm] + D[qm - nsec]) * nu * drp;
   }
 }
+FARGO_F64_BODY(visc_tau_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_visc_tau(KArgs<T> a, const T *__restrict__ vr, const T *__restrict__ vt) {
+__global__ void __launch_bounds__(256) k_visc_tau(const __grid_constant__ KArgs<T> a, const T *__restrict__ vr,
+                                                  const T *__restrict__ vt) {
   pdl_enter();
-  visc_tau_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y), vr, vt);
+  FARGO_RUN_BODY(T, visc_tau_body, a, FARGO_BID, vr, vt);
 }
 
 // UpdateVelocitiesKernel src/Kernels.cu:118-150 + ApplySubKeplerianBoundaryKernel
@@ -933,10 +974,11 @@ __device__ __forceinline__ void visc_update_body(const KArgs<T> &a, const uint3 
   // transport gave them)
   if (!a.P.evanescent && (i == 0 || i == nrad - 1) && dt != (T)0.0) a.d.vthetaint[q] = subkeplerian_edge(a, i);
 }
+FARGO_F64_BODY(visc_update_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_visc_update(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_visc_update(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  visc_update_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, visc_update_body, a, FARGO_BID);
 }
 
 // Substep2Kernel (src/Kernels.cu:409-434) + kernel (src/Kernels.cu:438-479) +
@@ -985,10 +1027,11 @@ __device__ __forceinline__ void artvisc_body(const KArgs<T> &a, const uint3 bid)
     a.d.vtheta[q + nsec] = (T)0.0;
   }
 }
+FARGO_F64_BODY(artvisc_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_artvisc(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_artvisc(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  artvisc_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, artvisc_body, a, FARGO_BID);
 }
 
 // Substep3Kernel + Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
@@ -1038,10 +1081,11 @@ __device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) 
   }
   a.d.energy[q] = enew;
 }
+FARGO_F64_BODY(energy_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_energy(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_energy(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  energy_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, energy_body, a, FARGO_BID);
 }
 
 // ---------------------------------------------------------------------------
@@ -1190,6 +1234,44 @@ __device__ __forceinline__ void rad_cell(const KArgs<T> &a, int k, T d, T v0, T 
   inv = qdiv((T)1.0, d + (T)1e-20);
 }
 
+// out-of-line FP64 instances of the radial helpers, shared by the plain, the
+// TMA-staged and the fused-ensemble radial kernels (see FARGO_F64_BODY)
+template <class T>
+struct RadCellOut {
+  T q[6];
+  T inv;
+};
+__device__ __noinline__ RadCellOut<double> rad_cell_f64(const KArgs<double> &a, int k, double d, double v0,
+                                                        double v1, double vtp, double vt, double e) {
+  RadCellOut<double> r;
+  rad_cell<double>(a, k, d, v0, v1, vtp, vt, e, r.q, r.inv);
+  return r;
+}
+template <class T>
+__device__ __forceinline__ void rad_cell_run(const KArgs<T> &a, int k, T d, T v0, T v1, T vtp, T vt, T e,
+                                             T (&q)[6], T &inv) {
+  if constexpr (sizeof(T) == 8) {
+    const RadCellOut<double> r = rad_cell_f64(a, k, d, v0, v1, vtp, vt, e);
+#pragma unroll
+    for (int f = 0; f < 6; f++) q[f] = r.q[f];
+    inv = r.inv;
+  } else {
+    rad_cell<T>(a, k, d, v0, v1, vtp, vt, e, q, inv);
+  }
+}
+__device__ __noinline__ void rad_tile_update_f64(const KArgs<double> &a, const RadTile<double> t,
+                                                 double (*sRT)[RAD_TR + 3], int i0, int j, int x, int y) {
+  rad_tile_update<double>(a, t, sRT, i0, j, x, y);
+}
+template <class T>
+__device__ __forceinline__ void rad_tile_update_run(const KArgs<T> &a, const RadTile<T> &t, T (*sRT)[RAD_TR + 3],
+                                                    int i0, int j, int x, int y) {
+  if constexpr (sizeof(T) == 8)
+    rad_tile_update_f64(a, t, sRT, i0, j, x, y);
+  else
+    rad_tile_update<T>(a, t, sRT, i0, j, x, y);
+}
+
 // Radial transport: LRMomentaKernel (src/Kernels.cu:774-787) + OneWindRad
 // (src/TransportEuler.cu:60-156: StarRadKernel/2, DivisePolarGridKernel,
 // VanLeerRadialKernel for every conserved quantity, density last), with no
@@ -1219,7 +1301,7 @@ __device__ __forceinline__ void radial_body(const KArgs<T> &a, const uint3 bid) 
     if (col && k >= 0 && k < nrad) {
       const size_t qk = (size_t)k * nsec + j;
       const T v0 = a.d.vrad[qk];
-      rad_cell(a, k, a.d.dens[qk], v0, a.d.vrad[qk + nsec], a.d.vtheta[(size_t)k * nsec + jp], a.d.vtheta[qk],
+      rad_cell_run(a, k, a.d.dens[qk], v0, a.d.vrad[qk + nsec], a.d.vtheta[(size_t)k * nsec + jp], a.d.vtheta[qk],
                P.adiabatic ? a.d.energy[qk] : (T)0.0, q, inv);
       vr = v0;
     } else if (col && k == nrad) {
@@ -1228,10 +1310,10 @@ __device__ __forceinline__ void radial_body(const KArgs<T> &a, const uint3 bid) 
     t.put(rr, x, q, inv, vr);
   }
   __syncthreads();
-  rad_tile_update(a, t, sRT, i0, j, x, y);
+  rad_tile_update_run(a, t, sRT, i0, j, x, y);
 }
 template <class T>
-__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(KArgs<T> a) {
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
   radial_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
 }
@@ -1282,7 +1364,8 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
 }
 
 template <class T>
-__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(KArgs<T> a, const __grid_constant__ RadMaps maps) {
+__global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(const __grid_constant__ KArgs<T> a,
+                                                                    const __grid_constant__ RadMaps maps) {
   pdl_enter();
   constexpr int TR = RAD_TR, ny = RAD_NY, BW = RAD_BW(T), BR = RAD_BR;
   extern __shared__ __align__(128) unsigned char rad_smem[];
@@ -1349,7 +1432,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(KArgs<T> a
         const T v0 = VR[rr][x];
         // Vtheta at j+1: the next staged column, or sector 0 across the wrap
         const T vtp = (jp == j + 1) ? VT[rr][x + 1] : a.d.vtheta[(size_t)k * nsec];
-        rad_cell(a, k, D[rr][x], v0, VR[rr + 1][x], vtp, VT[rr][x], P.adiabatic ? E[rr][x] : (T)0.0, q, inv);
+        rad_cell_run(a, k, D[rr][x], v0, VR[rr + 1][x], vtp, VT[rr][x], P.adiabatic ? E[rr][x] : (T)0.0, q, inv);
         vr = v0;
       } else if (col && k == nrad) {
         vr = VR[rr][x];
@@ -1357,7 +1440,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(KArgs<T> a
       t.put(rr, x, q, inv, vr);
     }
     __syncthreads();
-    rad_tile_update(a, t, sRT, i0, j, x, y);
+    rad_tile_update_run(a, t, sRT, i0, j, x, y);
     __syncthreads();  // the tile and this stage are free for the next tiles
   }
 }
@@ -1717,10 +1800,21 @@ __device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 b
     each_chunk([&](int j0) { sweep(QA, nullptr, false, j0); });
   }
 }
+template <bool MC>
+__device__ __noinline__ void azimuthal4_body_f64(const KArgs<double> &a, const uint3 bid) {
+  azimuthal4_body<double, MC>(a, bid);
+}
 template <class T, bool MC>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(KArgs<T> a) {
+__device__ __forceinline__ void azimuthal4_run(const KArgs<T> &a, const uint3 bid) {
+  if constexpr (sizeof(T) == 8)
+    azimuthal4_body_f64<MC>(a, bid);
+  else
+    azimuthal4_body<T, MC>(a, bid);
+}
+template <class T, bool MC>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) k_transport_azimuthal4(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  azimuthal4_body<T, MC>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  azimuthal4_run<T, MC>(a, FARGO_BID);
 }
 
 // ComputeVelocitiesKernel src/Kernels.cu:1193-1210 (+ ComputeTemperatureFieldKernel
@@ -1750,10 +1844,11 @@ __device__ __forceinline__ void velocities_body(const KArgs<T> &a, const uint3 b
   }
   if (!isfinite(D[q])) atomicOr(&a.d.ctl->err, FARGO_DEVERR_NAN);
 }
+FARGO_F64_BODY(velocities_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_velocities(KArgs<T> a, int with_temperature) {
+__global__ void __launch_bounds__(256) k_velocities(const __grid_constant__ KArgs<T> a, int with_temperature) {
   pdl_enter();
-  velocities_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y), with_temperature);
+  FARGO_RUN_BODY(T, velocities_body, a, FARGO_BID, with_temperature);
 }
 
 // ComputeTemperatureFieldKernel src/Kernels.cu:203-213 (after a boundary condition)
@@ -1798,10 +1893,11 @@ __device__ __forceinline__ void end_body(const KArgs<T> &a, const uint3 bid) {
     if (a.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)a.cond_handle, done ? 0u : 1u);
   }
 }
+FARGO_F64_BODY(end_body)
 template <class T>
-__global__ void __launch_bounds__(256) k_end(KArgs<T> a) {
+__global__ void __launch_bounds__(256) k_end(const __grid_constant__ KArgs<T> a) {
   pdl_enter();
-  end_body<T>(a, make_uint3(blockIdx.x, blockIdx.y, gridDim.x * gridDim.y));
+  FARGO_RUN_BODY(T, end_body, a, FARGO_BID);
 }
 
 // Start of a DT (AlgoGas entry, src/SourceEuler.cu:202-221).
@@ -1847,29 +1943,53 @@ __device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, u
 // The body runs on a private copy of the disk's arguments: like the single-disk
 // kernel's parameters, no store of the body can alias it, so the compiler sees the
 // same invariant values and forms the same arithmetic (multiply-adds included).
-#define FARGO_BATCHED(kname, bounds, call)                                       \
+#define FARGO_BATCHED(kname, bounds, body, ...)                                  \
   template <class T>                                                             \
   __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
     pdl_enter();                                                                 \
     uint3 bid;                                                                   \
     const KArgs<T> *ap = batch_block(G, bid);                                    \
     if (!ap) return;                                                             \
-    const KArgs<T> la = *ap;                                                     \
-    const KArgs<T> *a = &la;                                                     \
-    call;                                                                        \
+    if constexpr (sizeof(T) == 8) {                                              \
+      const KArgs<T> *a = ap;                                                    \
+      body##_f64(*a, bid, ##__VA_ARGS__);                                        \
+    } else {                                                                     \
+      const KArgs<T> la = *ap;                                                   \
+      const KArgs<T> *a = &la;                                                   \
+      body<T>(*a, bid, ##__VA_ARGS__);                                           \
+    }                                                                            \
   }
-FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body<T>(*a, bid))
-FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body<T>(*a, bid))
-FARGO_BATCHED(kb_source, 256, source_body<T>(*a, bid))
-FARGO_BATCHED(kb_visc_tau, 256,
-              visc_tau_body<T>(*a, bid, G.extra ? a->d.vrad : a->d.vradint, G.extra ? a->d.vtheta : a->d.vthetaint))
-FARGO_BATCHED(kb_visc_update, 256, visc_update_body<T>(*a, bid))
-FARGO_BATCHED(kb_artvisc, 256, artvisc_body<T>(*a, bid))
-FARGO_BATCHED(kb_energy, 256, energy_body<T>(*a, bid))
-FARGO_BATCHED(kb_radial, 32 * RAD_NY, radial_body<T>(*a, bid))
-FARGO_BATCHED(kb_velocities, 256, velocities_body<T>(*a, bid, G.extra))
-FARGO_BATCHED(kb_end, 256, end_body<T>(*a, bid))
-FARGO_BATCHED(kb_planets, 64, planets_body(a->P, a->d.ctl, a->d.ring_force, sizeof(T) == 4))
+FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body)
+FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body)
+FARGO_BATCHED(kb_source, 256, source_body)
+FARGO_BATCHED(kb_visc_tau, 256, visc_tau_body, G.extra ? a->d.vrad : a->d.vradint,
+              G.extra ? a->d.vtheta : a->d.vthetaint)
+FARGO_BATCHED(kb_visc_update, 256, visc_update_body)
+FARGO_BATCHED(kb_artvisc, 256, artvisc_body)
+FARGO_BATCHED(kb_energy, 256, energy_body)
+FARGO_BATCHED(kb_velocities, 256, velocities_body, G.extra)
+FARGO_BATCHED(kb_end, 256, end_body)
+template <class T>
+__global__ void __launch_bounds__(32 * RAD_NY) kb_radial(BatchGroup<T> G) {
+  pdl_enter();
+  uint3 bid;
+  const KArgs<T> *ap = batch_block(G, bid);
+  if (!ap) return;
+  if constexpr (sizeof(T) == 8) {
+    radial_body<T>(*ap, bid);
+  } else {
+    const KArgs<T> la = *ap;
+    radial_body<T>(la, bid);
+  }
+}
+template <class T>
+__global__ void __launch_bounds__(64) kb_planets(BatchGroup<T> G) {
+  pdl_enter();
+  uint3 bid;
+  const KArgs<T> *ap = batch_block(G, bid);
+  if (!ap) return;
+  planets_body(ap->P, ap->d.ctl, ap->d.ring_force, sizeof(T) == 4);
+}
 #undef FARGO_BATCHED
 
 template <class T, int V4>
@@ -1878,8 +1998,12 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) kb_cfl_forces(BatchGroup<T> G
   uint3 bid;
   const KArgs<T> *ap = batch_block(G, bid);
   if (!ap) return;
-  const KArgs<T> la = *ap;
-  cfl_forces_body<T, V4>(la, bid);
+  if constexpr (sizeof(T) == 8) {
+    cfl_forces_body_f64<V4>(*ap, bid);
+  } else {
+    const KArgs<T> la = *ap;
+    cfl_forces_body<T, V4>(la, bid);
+  }
 }
 template <class T, bool MC>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(BatchGroup<T> G) {
@@ -1887,8 +2011,12 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(Batc
   uint3 bid;
   const KArgs<T> *ap = batch_block(G, bid);
   if (!ap) return;
-  const KArgs<T> la = *ap;
-  azimuthal4_body<T, MC>(la, bid);
+  if constexpr (sizeof(T) == 8) {
+    azimuthal4_body_f64<MC>(*ap, bid);
+  } else {
+    const KArgs<T> la = *ap;
+    azimuthal4_body<T, MC>(la, bid);
+  }
 }
 // the start of a DT on every member (not masked: it clears the done flag)
 template <class T>

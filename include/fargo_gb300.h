@@ -324,21 +324,36 @@ int  fargo_batch_create(int n, const fargo_params *params, const fargo_planet *p
 /* The same with every disk in variant v (NULL: the default). */
 int  fargo_batch_create_variant(int n, const fargo_params *params, const fargo_planet *planets,
                                 const int *nplanets, int precision, const fargo_variant *v, fargo_batch **out);
-/* Fused execution of the batch (the spec ensemble form): from this call on,
-   fargo_batch_run_async advances every disk by launching each substep kernel
-   once for the whole ensemble -- one CUDA graph per DT round: every disk's DT
-   start, then a conditional while loop whose body is one substep of every disk
-   whose DT is not yet over (masked subcycling: each disk keeps its own CFL step,
-   substep count and DT; finished disks' blocks return at once) -- instead of one
-   graph per disk.  Bitwise the results of the disks run alone.  FARGO_ERR_INVALID
-   (reason in fargo_batch_last_error) when a disk uses self-gravity, an open,
-   non-reflecting or evanescent boundary, the sloppy CFL or a ring too wide for the
-   register azimuthal sweep. */
+/* Fused execution of the batch: from this call on, fargo_batch_run_async
+   advances every disk by launching each substep kernel once per lane of disks
+   instead of running one graph per disk -- one CUDA graph per DT round: every
+   disk's DT start, then a conditional while loop whose body is one substep of
+   every disk whose DT is not yet over (masked subcycling: each disk keeps its own
+   CFL step, substep count and DT; finished disks' blocks return at once).
+   fargo_batch_fuse gathers the disks of each ring width into a lane (one launch
+   per kernel per width, the lanes side by side in the loop body, every block
+   shaped for its width); fargo_batch_fuse_by_width(b, 0) puts every disk in one
+   lane (one launch per kernel for the whole ensemble, blocks shaped for the
+   widest ring).  Bitwise the results of the disks run alone.
+   FARGO_ERR_INVALID (reason in fargo_batch_last_error) when a disk uses
+   self-gravity, an open, non-reflecting or evanescent boundary, the sloppy CFL
+   or a ring too wide for the register azimuthal sweep. */
 int  fargo_batch_fuse(fargo_batch *b);
+int  fargo_batch_fuse_by_width(fargo_batch *b, int by_width);
 /* The reason of the last failed fargo_batch_fuse ("" if none). */
 const char *fargo_batch_last_error(const fargo_batch *b);
 /* Kernel launches of the fused form: per substep (all disks) and per DT round. */
 int  fargo_batch_fused_launches(const fargo_batch *b, int *per_substep, int *per_dt);
+/* Lanes of the fused form. */
+int  fargo_batch_fused_lanes(const fargo_batch *b, int *lanes);
+/* Starts a DT round of the fused form, then runs reps substeps of it launch by
+   launch (lanes one after another, a CUDA event after every launch) and returns
+   the mean device time (ms) of each launch group of one substep, in launch order;
+   *ngroups = groups per substep.  Advances the disks like reps substeps of a
+   round (a disk whose DT ends sooner stops there). */
+int  fargo_batch_fused_time_kernels(fargo_batch *b, int reps, double *ms_per_group, int cap, int *ngroups);
+/* Kernel of group k of the last fargo_batch_fused_time_kernels call (NULL if none). */
+const char *fargo_batch_fused_kernel_name(const fargo_batch *b, int k);
 /* Autotuner of the ensemble's schedule: starting from the default variant, tries
    the alternatives of one knob at a time (padding, stream priorities, the
    self-gravity schedule when a disk has self-gravity, programmatic launch), each

@@ -62,8 +62,11 @@ def test_fp64_profile_columns():
     n = bench.ncu_fp64_instructions("k_transport_azimuthal", "c3")
     assert n is not None and n > 3145728 * 100  # hundreds of FP64 instructions per cell
     assert bench.ncu_fp64_instructions("no_such_kernel", "c3") is None
-    t = bench.ncu_traffic("k_transport_radial", "c3", "fp64")
+    t = bench.ncu_traffic("k_transport_radial_tma", "c3", "fp64")
     assert t is not None and 1e8 < t < 1e9
+    # the FP32 summary; the timer's generic azimuthal name finds the register form
+    t = bench.ncu_traffic("k_transport_azimuthal", "c3", "fp32")
+    assert t is not None and 1e7 < t < 1e9
 
 
 def test_step_algorithmic_bytes():

@@ -95,17 +95,20 @@ def test_tile_shapes_are_bitwise_the_default(cell_block, rad_tma, az_chunks, pre
     b.close()
 
 
+@pytest.mark.parametrize("by_width", [True, False])
 @pytest.mark.parametrize("precision", [fg.FARGO_FP32_BULK, fg.FARGO_FP64])
-def test_fused_ensemble_is_bitwise_the_disks_alone(precision):
+def test_fused_ensemble_is_bitwise_the_disks_alone(precision, by_width):
     # one launch per substep kernel for the whole ensemble, masked subcycling: every
     # disk still takes its own substeps and ends bitwise where it ends alone
     # widths that take both forms of the CFL kernel (four cells per thread at 288
     # and 384 sectors, the streamed form at 96)
     disks = fg.c4_disks(5, seed=7, nrad_choices=(32, 96, 128))
     assert len({p.nsec for p, _ in disks}) > 1
-    b = fg.Batch(disks, precision).fuse()
+    b = fg.Batch(disks, precision).fuse(by_width=by_width)
     per_substep, per_dt = b.fused_launches()
-    assert per_substep <= 16 and per_dt <= 2
+    lanes = b.fused_lanes()
+    assert lanes == (len({p.nsec for p, _ in disks}) if by_width else 1)
+    assert per_substep <= 15 * lanes + 1 and per_dt <= 2
     b.run_async(2)
     b.sync()
     for k, (p, pl) in enumerate(disks):
@@ -169,4 +172,15 @@ def test_two_azimuthal_chunks_per_thread_agree_to_rounding():
             x, y = a.disk(k).field(name), b.disk(k).field(name)
             assert np.abs(x - y).max() <= 1e-11 * np.abs(x).max(), (k, name)
     a.close()
+    b.close()
+
+
+def test_fused_kernel_times_cover_every_group():
+    disks = fg.c4_disks(6, seed=11, nrad_choices=(32, 64))
+    b = fg.Batch(disks, fg.FARGO_FP32_BULK).fuse()
+    times = b.fused_kernel_times(reps=2)
+    per_substep, _ = b.fused_launches()
+    assert len(times) == per_substep - 1  # every group but the loop condition
+    assert all(ms > 0.0 for _, ms in times)
+    assert {"kb_cfl_forces", "kb_radial", "kb_azimuthal4", "kb_end"} <= {name for name, _ in times}
     b.close()
