@@ -202,6 +202,7 @@ def kernel_bytes(name, params, esize):
         "k_energy": 8 + 2,
         "k_transport_radial": (3 + ad) + (5 + ad),
         "k_transport_radial_tma": (3 + ad) + (5 + ad),
+        "k_transport_radial_col": (3 + ad) + (5 + ad),
         "k_transport_azimuthal": (6 + ad) + (5 + ad),
         "k_velocities": (5 + 1) + 3,
         "k_temperature": 3,
@@ -658,15 +659,24 @@ def run_own(args, world, rank, local):
         line["c2"] = e
     if not args.no_drift and world == 1:
         from cudaprotoplanetarydisks_gb300.drift import drift
-        dr = drift("c2", 100, every=25)
+
+        def drift_obj(cfg):
+            dr = drift(cfg, 100, every=25, control=True)
+            return {"workload": WORKLOADS[cfg], "dts": dr["dts"], "dens_rel_l2": dr["final_dens_rel_l2"],
+                    "fields_after_100_orbits": {k: dr["by_orbit"][-1][k] for k in ("dens", "vrad", "vtheta")},
+                    "dens_rel_l2_by_orbit": {r["orbits"]: r["dens"]["rel_l2"] for r in dr["by_orbit"]},
+                    "control_dens_rel_l2_by_orbit": {r["orbits"]: r["control_dens"]["rel_l2"]
+                                                     for r in dr["by_orbit"]},
+                    "seconds": dr["seconds_fp64"] + dr["seconds_fp32"]}
+        d2 = drift_obj("c2")
         line["fp32_drift_100_orbits"] = {
-            "workload": WORKLOADS["c2"], "against": "FP64 mode of this code from the same initial state",
-            "dts": dr["dts"], "dens_rel_l2": dr["final_dens_rel_l2"],
-            "fields_after_100_orbits": {k: dr["by_orbit"][-1][k] for k in ("dens", "vrad", "vtheta")},
-            "dens_rel_l2_by_orbit": {r["orbits"]: r["dens"]["rel_l2"] for r in dr["by_orbit"]},
-            "target": 1e-5, "seconds": dr["seconds_fp64"] + dr["seconds_fp32"]}
+            "against": "FP64 mode of this code from the same initial state",
+            "control": "FP64 from the same state with the density perturbed by one unit in the last place: "
+                       "how much the flow itself amplifies the smallest perturbation",
+            "target": 1e-5, "dens_rel_l2": d2["dens_rel_l2"], "c2": d2, "c1": drift_obj("c1")}
     if not args.no_batch and world == 1:
         line["batch_c4"] = batch_ensemble()
+        line["batch_small"] = batch_small()
     if not args.no_learned and world == 1:
         line["learned_c5"] = learned_c5()
     print(json.dumps(line), flush=True)
@@ -712,6 +722,46 @@ def run_reference(args, world, rank):
 
 
 # ---------------------------------------------------------------------------
+def batch_small(ndt=4, n=256):
+    """An ensemble of many small disks (256 seeded disks of the C4 distribution at
+    Nrad in {32, 48, 64}), where a disk's kernels are a few CTAs each and the
+    per-disk graphs are bound by launch and scheduling overheads: per-disk graphs
+    against the fused form (one launch per kernel per ring width, and one for the
+    whole ensemble), FP32-bulk, after one warm-up DT, host wall clock."""
+    import numpy as np
+    import torch
+    import cudaprotoplanetarydisks_gb300 as fg
+    disks = fg.c4_disks(n, seed=5, nrad_choices=(32, 48, 64))
+    cells = [p.nrad * p.nsec for p, _ in disks]
+
+    def run(fused):
+        b = fg.Batch(disks, fg.FARGO_FP32_BULK)
+        if fused:
+            b.fuse(by_width=(fused == "width"))
+        b.run_async(1)
+        b.sync()
+        s0 = [d.scalars().substeps for d in b.disks]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run_async(ndt)
+        b.sync()
+        t = time.perf_counter() - t0
+        cu = sum((d.scalars().substeps - s0[k]) * cells[k] for k, d in enumerate(b.disks))
+        dens = [d.field("dens")[:-1] for d in b.disks]
+        b.close()
+        return cu / t, dens
+
+    v0, d0 = run(None)
+    vw, dw = run("width")
+    v1, d1 = run("one")
+    same = all(np.array_equal(x, y) for x, y in zip(d0, dw)) and all(np.array_equal(x, y) for x, y in zip(d0, d1))
+    return {"workload": f"{n} seeded disks of the C4 distribution, Nrad in {{32,48,64}}, Nsec = 3 Nrad",
+            "cells": sum(cells), "dts_per_disk": ndt, "unit": METRIC,
+            "per_disk_graphs": v0, "fused_by_width": vw, "fused_one_lane": v1,
+            "speedup_fused_by_width": vw / v0, "speedup_fused_one_lane": v1 / v0,
+            "bitwise_equal": same, "timing": "host wall clock around run + sync"}
+
+
 def batch_ensemble(ndt=4, n=64):
     """The batched ensemble (64 seeded disks, Nrad in {128..512}, Nsec = 3 Nrad):
     FP32-bulk disks advanced side by side (fargo_batch) against the same disks in

@@ -75,7 +75,8 @@ class FargoVariant(ctypes.Structure):
     """fargo_variant: the execution variant of a context (bitwise-equal results)."""
     _fields_ = [("graph", ctypes.c_int), ("pdl", ctypes.c_int), ("pad", ctypes.c_int), ("sg_ahead", ctypes.c_int),
                 ("rotate", ctypes.c_int), ("az_generic", ctypes.c_int), ("priority", ctypes.c_int),
-                ("cell_block", ctypes.c_int), ("rad_tma", ctypes.c_int), ("az_chunks", ctypes.c_int)]
+                ("cell_block", ctypes.c_int), ("rad_tma", ctypes.c_int), ("az_chunks", ctypes.c_int),
+                ("rad_col", ctypes.c_int)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -233,12 +233,14 @@ int fargo_batch_autotune(int n, const fargo_params *params, const fargo_planet *
                {&fargo_variant::sg_ahead, 2, sg},
                {&fargo_variant::pdl, 2, true},
                // tile and launch shapes: the per-cell kernels' CTA (64x4, 32x8, 128x2,
-               // 256x1) and the radial transport's TMA-staged persistent form (the
+               // 256x1), the radial transport's TMA-staged persistent form and its
+               // column march (the
                // azimuthal sweep's chunks per thread change the ring mean's summation
                // order, so that knob is not searched: every candidate here is bitwise
                // the default)
                {&fargo_variant::cell_block, 4, true},
-               {&fargo_variant::rad_tma, 2, true}};
+               {&fargo_variant::rad_tma, 2, true},
+               {&fargo_variant::rad_col, 2, true}};
   for (const Knob &kn : knobs) {
     if (!kn.on) continue;
     const fargo_variant base = v;

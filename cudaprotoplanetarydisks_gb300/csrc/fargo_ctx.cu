@@ -80,6 +80,7 @@ struct fargo_ctx {
   bool want_tma = true;       // the variant asks for the TMA radial transport
   int cell_block = 0;         // per-cell kernels' CTA shape (fargo_variant.cell_block)
   int az_chunks = 1;          // chunks per thread of the register azimuthal sweep
+  bool rad_col = false;       // column-march radial transport
 };
 
 namespace {
@@ -206,6 +207,7 @@ KArgs<T> make_args(const fargo_ctx *c) {
     a.cell_by = by[c->cell_block];
   }
   a.az_chunks = c->az_chunks;
+  a.rad_col = c->rad_col ? 1 : 0;
   a.cond_handle = 0;
   a.use_cond = 0;
   a.sg.spec_r = c->spec_r;
@@ -739,6 +741,8 @@ void fargo_variant_default(fargo_variant *v) {
   v->cell_block = cb ? std::atoi(cb) : 0;
   v->rad_tma = env_on("FARGO_NO_TMA") ? 0 : 1;
   v->az_chunks = env_on("FARGO_AZ_CHUNKS2") ? 2 : 1;
+  const char *rc = std::getenv("FARGO_RAD_COL");
+  v->rad_col = rc ? (std::atoi(rc) ? 1 : 0) : -1;
 }
 
 int fargo_ctx_create(const fargo_params *p, const fargo_planet *planets, int nb, int precision, void *stream,
@@ -754,6 +758,7 @@ int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets,
   else fargo_variant_default(&v);
   if (v.priority < 0 || v.priority > 2) return FARGO_ERR_INVALID;
   if (v.cell_block < 0 || v.cell_block > 3 || v.az_chunks < 1 || v.az_chunks > 2) return FARGO_ERR_INVALID;
+  if (v.rad_col < -1 || v.rad_col > 1) return FARGO_ERR_INVALID;
   if (precision != FARGO_FP64 && precision != FARGO_FP32_BULK) return FARGO_ERR_INVALID;
   if (p->nrad < 8 || p->nsec < 8 || !p->is_disk || !(p->dt > 0.0)) return FARGO_ERR_INVALID;
   fargo_ctx *c = new fargo_ctx();
@@ -771,6 +776,7 @@ int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets,
   c->want_tma = v.rad_tma != 0;
   c->cell_block = v.cell_block;
   c->az_chunks = v.az_chunks;
+  c->rad_col = v.rad_col < 0 ? precision == FARGO_FP32_BULK : v.rad_col != 0;
   c->sg_generic = env_on("FARGO_SG_GENERIC");  // a parity-test switch, not a variant
   // stream priorities: 0 all equal; 1 the hydro chain and the planets above the
   // self-gravity transforms; 2 the transforms above the rest.  The caller's
@@ -1242,7 +1248,7 @@ const char *batch_kernel_name(int k) {
   static const char *const names[BK_END + 1] = {
       "kb_dt_begin", "kb_soundspeed", "kb_cfl_forces (4 cells/thread)", "kb_cfl_forces", "kb_planets",
       "kb_correct_vtheta", "kb_source", "kb_visc_tau", "kb_visc_update", "kb_artvisc", "kb_energy", "kb_radial",
-      "kb_azimuthal4", "kb_azimuthal4 (chunks/thread)", "kb_velocities", "kb_end"};
+      "kb_radial_col", "kb_azimuthal4", "kb_azimuthal4 (chunks/thread)", "kb_velocities", "kb_end"};
   return k >= 0 && k <= BK_END ? names[k] : "?";
 }
 
@@ -1322,6 +1328,11 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
   auto tiles = [](const fargo_params &p, const fargo_ctx *) {
     return make_int2((p.nsec + 31) / 32, (p.nrad + RAD_TR - 1) / RAD_TR);
   };
+  auto columns = [](const fargo_params &p, const fargo_ctx *) {
+    return make_int2((p.nsec + RADC_THREADS - 1) / RADC_THREADS, (p.nrad + RADC_RINGS - 1) / RADC_RINGS);
+  };
+  auto rad_col = [](const fargo_params &, const fargo_ctx *c) { return c->rad_col; };
+  auto rad_tile = [](const fargo_params &, const fargo_ctx *c) { return !c->rad_col; };
   auto v4 = [](const fargo_params &p, const fargo_ctx *) { return p.nsec % 4 == 0 && p.nsec >= 260 && p.nsec <= 1024; };
   auto not_v4 = [&](const fargo_params &p, const fargo_ctx *c) { return !v4(p, c); };
   auto adiabatic = [](const fargo_params &p, const fargo_ctx *) { return p.adiabatic != 0; };
@@ -1353,7 +1364,8 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
                     group(BK_ARTVISC, w, all, cells, b2, 0, 0),
                     group(BK_VISC_TAU, w, adiabatic, cells, b2, 0, 1),
                     group(BK_ENERGY, w, adiabatic, cells, b2, 0, 0),
-                    group(BK_RADIAL, w, all, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
+                    group(BK_RADIAL, w, rad_tile, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
+                    group(BK_RADIAL_COL, w, rad_col, columns, dim3(RADC_THREADS), 0, 0),
                     group(BK_AZ4, w, az_one, rings, dim3(az_threads), az_smem, 0),
                     group(BK_AZ4_MC, w, az_mc, rings, dim3(sizeof(T) == 8 ? 512 : 768), az_smem, 0),
                     group(BK_VELOCITIES, w, all, cells, b2, 0, 1),
@@ -1367,10 +1379,14 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
     G.args = args_dev;
     G.ng = (int)g.member.size();
     G.extra = g.extra;
-    G.member = (const int *)dev(g.member.data(), g.member.size() * sizeof(int));
-    G.first = (const int *)dev(g.first.data(), g.first.size() * sizeof(int));
-    G.gx = (const int *)dev(g.gx.data(), g.gx.size() * sizeof(int));
-    return G.member && G.first && G.gx;
+    std::vector<int4> blk;
+    blk.reserve(g.first.back());
+    for (size_t m = 0; m < g.member.size(); m++) {
+      const int nb = g.first[m + 1] - g.first[m];
+      for (int b = 0; b < nb; b++) blk.push_back(make_int4(g.member[m], b % g.gx[m], b / g.gx[m], nb));
+    }
+    G.blk = (const int4 *)dev(blk.data(), blk.size() * sizeof(int4));
+    return G.blk != nullptr;
   };
   auto add = [&](std::vector<fargo_fused::Launch> &to, const FusedGroup &g) -> bool {
     if (g.member.empty()) return true;

@@ -80,6 +80,7 @@ struct KArgs {
   int rad_grid;                    // CTAs of the persistent TMA radial transport
   int cell_bx, cell_by;            // CTA shape (sectors x rings) of the per-cell kernels
   int az_chunks;                   // four-cell chunks per thread of the register azimuthal sweep
+  int rad_col;                     // radial transport as a column march (k_transport_radial_col)
   SgDev sg;
 };
 

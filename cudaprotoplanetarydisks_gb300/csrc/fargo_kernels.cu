@@ -1319,6 +1319,173 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial(const __grid_c
 }
 
 // ---------------------------------------------------------------------------
+// The same radial transport as a column march.  The radial sweep couples a cell
+// only to the cells of its own sector (and V_theta of the next sector), so one
+// thread takes one sector and walks a chunk of RADC_RINGS rings upward, keeping
+// the few rings its stencil needs in registers: the quantities over density of
+// rings r-2, r-1, r, the slopes of rings r-2, r-1 and the upwind interface
+// values at r-2, r-1.  No shared memory and no barrier: a warp's loads are 32
+// consecutive sectors of one ring (coalesced), and the work per cell is the
+// tile kernel's arithmetic in the same order (slopes, upwind values, updates).
+// Each chunk re-reads the two rings on either side of it.
+template <class T>
+struct RadColRing {
+  T w[RAD_NS];  // q / (rho + 1e-20) for the six transported quantities, and rho itself
+  T q[6];       // the raw quantities
+  T v;          // Vrad at the ring's inner interface
+};
+// the loads of one cell (ring k): issued a few rings ahead of their use
+template <class T>
+struct RadColRaw {
+  T d, v0, v1, vtp, vt, e;
+};
+template <class T>
+__device__ __forceinline__ void radc_raw(const KArgs<T> &a, int k, int j, int jp, RadColRaw<T> &x) {
+  const DevParams &P = a.P;
+  const int nrad = P.nrad, nsec = P.nsec;
+  x.d = x.v0 = x.v1 = x.vtp = x.vt = x.e = (T)0.0;
+  if (k >= 0 && k < nrad) {
+    const size_t qk = (size_t)k * nsec + j;
+    x.d = a.d.dens[qk];
+    x.v0 = a.d.vrad[qk];
+    x.v1 = a.d.vrad[qk + nsec];
+    x.vtp = a.d.vtheta[(size_t)k * nsec + jp];
+    x.vt = a.d.vtheta[qk];
+    if (P.adiabatic) x.e = a.d.energy[qk];
+  } else if (k == nrad) {
+    x.v0 = a.d.vrad[(size_t)k * nsec + j];
+  }
+}
+// LRMomenta and DivisePolarGrid of ring k from its loads (zero outside the grid)
+template <class T>
+__device__ __forceinline__ void radc_form(const KArgs<T> &a, int k, const RadColRaw<T> &x, RadColRing<T> &c) {
+  const int nrad = a.P.nrad;
+#pragma unroll
+  for (int f = 0; f < 6; f++) c.q[f] = (T)0;
+  T inv = (T)0.0;
+  c.v = (T)0.0;
+  if (k >= 0 && k < nrad) {
+    rad_cell_run(a, k, x.d, x.v0, x.v1, x.vtp, x.vt, a.P.adiabatic ? x.e : (T)0.0, c.q, inv);
+    c.v = x.v0;
+  } else if (k == nrad) {
+    c.v = x.v0;
+  }
+#pragma unroll
+  for (int f = 0; f < 6; f++) c.w[f] = c.q[f] * inv;
+  c.w[6] = c.q[5];
+}
+// StarRadKernel at ring k from rings k-1, k, k+1 (zero at the first and last ring)
+template <class T>
+__device__ __forceinline__ void radc_slope(const KArgs<T> &a, int k, const RadColRing<T> &m, const RadColRing<T> &c,
+                                           const RadColRing<T> &p, T (&d)[RAD_NS]) {
+  const int nrad = a.P.nrad;
+  const bool in = k > 0 && k < nrad - 1;
+  const T idm0 = in ? RT(a, RT_INVDIFFRMED, k) : (T)0.0, idm1 = in ? RT(a, RT_INVDIFFRMED, k + 1) : (T)0.0;
+#pragma unroll
+  for (int f = 0; f < RAD_NS; f++) {
+    T v = (T)0.0;
+    if (in) {
+      const T wm = m.w[f], w0 = c.w[f], wp = p.w[f];
+      const T dqm = (w0 - wm) * idm0;
+      const T dqp = (wp - w0) * idm1;
+      v = gt0(dqp * dqm) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+    }
+    d[f] = v;
+  }
+}
+// StarRadKernel2 at interface m between rings m-1 (lo) and m (hi)
+template <class T>
+__device__ __forceinline__ void radc_iface(const KArgs<T> &a, int m, T dt, const RadColRing<T> &lo,
+                                           const RadColRing<T> &hi, const T (&dlo)[RAD_NS], const T (&dhi)[RAD_NS],
+                                           T (&sv)[RAD_NS]) {
+  const int nrad = a.P.nrad;
+  const bool in = m > 0 && m < nrad;
+  const T v = hi.v;
+  const bool up = gt0(v);
+  T coef = (T)0.0;
+  if (in) {
+    const T r0 = RT(a, RT_RMED, m - 1), r1 = RT(a, RT_RMED, m), r2 = RT(a, RT_RMED, m + 1);
+    const T l = r1 - r0 - v * dt;
+    const T h = r2 - r1 + v * dt;
+    coef = up ? l * (T)0.5 : -(h * (T)0.5);
+  }
+#pragma unroll
+  for (int f = 0; f < RAD_NS; f++) sv[f] = in ? (up ? lo.w[f] + coef * dlo[f] : hi.w[f] + coef * dhi[f]) : (T)0.0;
+}
+template <class T>
+__device__ __forceinline__ void radial_col_body(const KArgs<T> &a, const uint3 bid) {
+  const DevParams &P = a.P;
+  const int nrad = P.nrad, nsec = P.nsec;
+  const int j = bid.x * RADC_THREADS + threadIdx.x;
+  if (j >= nsec) return;
+  const int jp = jp1(j, nsec);
+  const int i0 = bid.y * RADC_RINGS, i1 = min(i0 + RADC_RINGS, nrad);
+  const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
+  const T dtheta = KC(T, a, KC_DTHETA);
+  T *const out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
+  // rings r-2, r-1, r; slopes of rings r-2, r-1; interface values at r-2, r-1
+  RadColRing<T> c0, c1, c2;
+  T d0[RAD_NS], d1[RAD_NS], s0[RAD_NS], s1[RAD_NS];
+  // the loads of rings r+1 and r+2 are in flight while ring r is formed
+  RadColRaw<T> x0, x1, x2, x3;
+  radc_raw(a, i0 - 2, j, jp, x0);
+  radc_raw(a, i0 - 1, j, jp, x1);
+  radc_raw(a, i0, j, jp, x2);
+  radc_raw(a, i0 + 1, j, jp, x3);
+  RadColRaw<T> n1, n2;
+  radc_raw(a, i0 + 2, j, jp, n1);
+  radc_raw(a, i0 + 3, j, jp, n2);
+  radc_form(a, i0 - 2, x0, c0);
+  radc_form(a, i0 - 1, x1, c1);
+  radc_form(a, i0, x2, c2);
+  radc_slope(a, i0 - 1, c0, c1, c2, d1);  // slope of ring i0-1
+  // ring i0+1: slope of ring i0, interface value at i0
+#pragma unroll
+  for (int f = 0; f < RAD_NS; f++) d0[f] = d1[f];
+  c0 = c1;
+  c1 = c2;
+  radc_form(a, i0 + 1, x3, c2);
+  radc_slope(a, i0, c0, c1, c2, d1);
+  radc_iface(a, i0, dt, c0, c1, d0, d1, s1);
+  // steady state: form ring r, slope of ring r-1, interface at r-1, update of cell r-2
+  for (int r = i0 + 2; r <= i1 + 1; r++) {
+    const RadColRaw<T> cur = n1;
+    n1 = n2;
+    if (r + 2 <= i1 + 1) radc_raw(a, r + 2, j, jp, n2);
+#pragma unroll
+    for (int f = 0; f < RAD_NS; f++) {
+      d0[f] = d1[f];
+      s0[f] = s1[f];
+    }
+    c0 = c1;
+    c1 = c2;
+    radc_form(a, r, cur, c2);
+    radc_slope(a, r - 1, c0, c1, c2, d1);
+    radc_iface(a, r - 1, dt, c0, c1, d0, d1, s1);
+    // VanLeerRadialKernel of cell i = r - 2 (ring c0)
+    const int i = r - 2;
+    const size_t q = (size_t)i * nsec + j;
+    const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
+    // the cell's own interfaces: inner at i (s0), outer at i+1 (s1); Vrad at both
+    const T v0 = c0.v, v1 = c1.v;
+    const T F0 = dt * dtheta * rinf * s0[6] * v0, F1 = dt * dtheta * rsup * s1[6] * v1;
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      if (f == 4 && !P.adiabatic) continue;
+      const T varq = s0[f] * F0 - s1[f] * F1;
+      out[f][q] = c0.q[f] + varq * isurf;
+      if (f == 5 && i == 0 && P.open_inner) a.d.lostbydisk[j] = (double)varq;
+    }
+  }
+}
+FARGO_F64_BODY(radial_col_body)
+template <class T>
+__global__ void __launch_bounds__(RADC_THREADS) k_transport_radial_col(const __grid_constant__ KArgs<T> a) {
+  pdl_enter();
+  FARGO_RUN_BODY(T, radial_col_body, a, FARGO_BID);
+}
+
+// ---------------------------------------------------------------------------
 // The same radial transport with its input tiles fetched by the Tensor Memory
 // Accelerator.  A persistent CTA walks the 32-sector x RAD_TR-ring tiles of the
 // grid (tile b, b + gridDim.x, ...).  Per tile, one thread issues four
@@ -1918,46 +2085,33 @@ __global__ void k_dt_begin(Ctl *c) {
 // ---------------------------------------------------------------------------
 // Fused ensembles (fargo_batch_fuse): one launch of each substep kernel for a
 // group of disks.  Member g of a group owns the launch's blocks first[g] ..
-// first[g+1]-1, its own grid laid out gx[g] blocks wide; a block finds its disk by
-// binary search, skips it when that disk's DT is over (masked subcycling: every
+// first[g+1]-1, its own grid laid out gx[g] blocks wide; a block reads its disk and
+// its place in that disk's grid from a per-block table, skips it when that disk's DT is over (masked subcycling: every
 // disk keeps its own CFL step and substep count, and the loop runs until the last
 // disk is done), and runs the kernel body of the single-disk launch with the
 // disk's arguments and its own block index.
 template <class T>
 __device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, uint3 &bid, bool masked = true) {
-  const int b = (int)blockIdx.x;
-  int lo = 0, hi = G.ng - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (G.first[mid] <= b) lo = mid;
-    else hi = mid - 1;
-  }
-  const KArgs<T> *a = &G.args[G.member[lo]];
+  const int4 r = __ldg(&G.blk[blockIdx.x]);
+  const KArgs<T> *a = &G.args[r.x];
   if (masked && a->d.ctl->done) return nullptr;
-  const int local = b - G.first[lo];
-  bid = make_uint3((unsigned)(local % G.gx[lo]), (unsigned)(local / G.gx[lo]),
-                   (unsigned)(G.first[lo + 1] - G.first[lo]));
+  bid = make_uint3((unsigned)r.y, (unsigned)r.z, (unsigned)r.w);
   return a;
 }
 
-// The body runs on a private copy of the disk's arguments: like the single-disk
-// kernel's parameters, no store of the body can alias it, so the compiler sees the
-// same invariant values and forms the same arithmetic (multiply-adds included).
+// The body reads the disk's arguments in place (for T = double through the
+// out-of-line body shared with the single-disk kernel).
 #define FARGO_BATCHED(kname, bounds, body, ...)                                  \
   template <class T>                                                             \
   __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
     pdl_enter();                                                                 \
     uint3 bid;                                                                   \
-    const KArgs<T> *ap = batch_block(G, bid);                                    \
-    if (!ap) return;                                                             \
-    if constexpr (sizeof(T) == 8) {                                              \
-      const KArgs<T> *a = ap;                                                    \
+    const KArgs<T> *a = batch_block(G, bid);                                     \
+    if (!a) return;                                                              \
+    if constexpr (sizeof(T) == 8)                                                \
       body##_f64(*a, bid, ##__VA_ARGS__);                                        \
-    } else {                                                                     \
-      const KArgs<T> la = *ap;                                                   \
-      const KArgs<T> *a = &la;                                                   \
+    else                                                                         \
       body<T>(*a, bid, ##__VA_ARGS__);                                           \
-    }                                                                            \
   }
 FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body)
 FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body)
@@ -1975,13 +2129,9 @@ __global__ void __launch_bounds__(32 * RAD_NY) kb_radial(BatchGroup<T> G) {
   uint3 bid;
   const KArgs<T> *ap = batch_block(G, bid);
   if (!ap) return;
-  if constexpr (sizeof(T) == 8) {
-    radial_body<T>(*ap, bid);
-  } else {
-    const KArgs<T> la = *ap;
-    radial_body<T>(la, bid);
-  }
+  radial_body<T>(*ap, bid);
 }
+FARGO_BATCHED(kb_radial_col, RADC_THREADS, radial_col_body)
 template <class T>
 __global__ void __launch_bounds__(64) kb_planets(BatchGroup<T> G) {
   pdl_enter();
@@ -1998,12 +2148,7 @@ __global__ void __launch_bounds__(256, V4 ? 1 : 2) kb_cfl_forces(BatchGroup<T> G
   uint3 bid;
   const KArgs<T> *ap = batch_block(G, bid);
   if (!ap) return;
-  if constexpr (sizeof(T) == 8) {
-    cfl_forces_body_f64<V4>(*ap, bid);
-  } else {
-    const KArgs<T> la = *ap;
-    cfl_forces_body<T, V4>(la, bid);
-  }
+  cfl_forces_run<T, V4>(*ap, bid);
 }
 template <class T, bool MC>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(BatchGroup<T> G) {
@@ -2011,12 +2156,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768) kb_azimuthal4(Batc
   uint3 bid;
   const KArgs<T> *ap = batch_block(G, bid);
   if (!ap) return;
-  if constexpr (sizeof(T) == 8) {
-    azimuthal4_body_f64<MC>(*ap, bid);
-  } else {
-    const KArgs<T> la = *ap;
-    azimuthal4_body<T, MC>(la, bid);
-  }
+  azimuthal4_run<T, MC>(*ap, bid);
 }
 // the start of a DT on every member (not masked: it clears the done flag)
 template <class T>
@@ -2055,6 +2195,7 @@ void launch_batched(int kernel, const BatchGroup<T> &G, int nblocks, dim3 block,
     case BK_ARTVISC: launch_k(pdl, kb_artvisc<T>, g, block, smem, s, G); probe_mark(s, "kb_artvisc"); break;
     case BK_ENERGY: launch_k(pdl, kb_energy<T>, g, block, smem, s, G); probe_mark(s, "kb_energy"); break;
     case BK_RADIAL: launch_k(pdl, kb_radial<T>, g, block, smem, s, G); probe_mark(s, "kb_radial"); break;
+    case BK_RADIAL_COL: launch_k(pdl, kb_radial_col<T>, g, block, smem, s, G); probe_mark(s, "kb_radial_col"); break;
     case BK_AZ4: launch_k(pdl, kb_azimuthal4<T, false>, g, block, smem, s, G); probe_mark(s, "kb_azimuthal4"); break;
     case BK_AZ4_MC: launch_k(pdl, kb_azimuthal4<T, true>, g, block, smem, s, G); probe_mark(s, "kb_azimuthal4"); break;
     case BK_VELOCITIES: launch_k(pdl, kb_velocities<T>, g, block, smem, s, G); probe_mark(s, "kb_velocities"); break;
@@ -2176,7 +2317,12 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   }
   const bool bc = P.open_inner || P.non_reflecting || P.evanescent;
   if (which_mask & SUBK_TRANSPORT) {
-    if (a.rad_maps) {
+    if (a.rad_col) {
+      launch_k(a.pdl, k_transport_radial_col<T>,
+               dim3((P.nsec + RADC_THREADS - 1) / RADC_THREADS, (P.nrad + RADC_RINGS - 1) / RADC_RINGS),
+               dim3(RADC_THREADS), 0, s, a);
+      MARK("k_transport_radial_col");
+    } else if (a.rad_maps) {
       launch_k(a.pdl, k_transport_radial_tma<T>, dim3(a.rad_grid), dim3(32, RAD_NY), RAD_TMA_SMEM(T), s, a,
                *a.rad_maps);
       MARK("k_transport_radial_tma");

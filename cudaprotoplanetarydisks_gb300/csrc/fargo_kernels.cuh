@@ -122,16 +122,17 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
 template <class T>
 struct BatchGroup {
   const KArgs<T> *args;  // every disk's kernel arguments (device array, indexed by disk)
-  const int *member;     // [ng] disk index of each member of the group
-  const int *first;      // [ng + 1] first block of each member in the launch (prefix sums)
-  const int *gx;         // [ng] width (blocks along x) of each member's own grid
+  const int4 *blk;       // [blocks of the launch] disk, block x and y in the disk's own grid, its blocks
   int ng;
   int extra;             // kb_visc_tau: 1 = the new velocities; kb_velocities: with temperature
 };
 enum BatchKernel {
   BK_DT_BEGIN, BK_SOUNDSPEED, BK_CFL_V4, BK_CFL, BK_PLANETS, BK_COROT, BK_SOURCE, BK_VISC_TAU,
-  BK_VISC_UPDATE, BK_ARTVISC, BK_ENERGY, BK_RADIAL, BK_AZ4, BK_AZ4_MC, BK_VELOCITIES, BK_END
+  BK_VISC_UPDATE, BK_ARTVISC, BK_ENERGY, BK_RADIAL, BK_RADIAL_COL, BK_AZ4, BK_AZ4_MC, BK_VELOCITIES, BK_END
 };
+// column-march radial transport: threads (sectors) per CTA, rings per thread
+#define RADC_THREADS 128
+#define RADC_RINGS 32
 template <class T>
 void launch_batched(int kernel, const BatchGroup<T> &G, int nblocks, dim3 block, size_t smem, int pdl,
                     cudaStream_t s);

@@ -184,6 +184,11 @@ typedef struct {
                       thread, up to the CTA size) or 2 (half the threads, two chunks each; the
                       ring mean is summed in another order, so results agree to rounding,
                       not bitwise) */
+  int rad_col;     /* radial transport as a column march (one thread per sector walks a chunk
+                      of rings with its stencil in registers; no shared memory, no barrier):
+                      1 on, 0 off (rad_tma decides), -1 (default) on in FP32-bulk, off in FP64,
+                      where it measured slower than the TMA-staged tiles; FP32 results are
+                      bitwise those of the tiles, FP64 agree to rounding */
 } fargo_variant;
 /* The default variant, with the FARGO_NO_GRAPH, FARGO_NO_PDL, FARGO_NO_PAD,
    FARGO_NO_SG_AHEAD, FARGO_ROTATE, FARGO_AZ_GENERIC and FARGO_PRIO switches

@@ -76,12 +76,12 @@ def test_variant_layout_and_default_switches(monkeypatch):
     assert size == ctypes.sizeof(_capi.FargoVariant)
     lib = _capi.load()
     for name in ("FARGO_NO_GRAPH", "FARGO_NO_PDL", "FARGO_NO_PAD", "FARGO_NO_SG_AHEAD", "FARGO_ROTATE",
-                 "FARGO_AZ_GENERIC", "FARGO_PRIO", "FARGO_CELL_BLOCK", "FARGO_NO_TMA", "FARGO_AZ_CHUNKS2"):
+                 "FARGO_AZ_GENERIC", "FARGO_PRIO", "FARGO_CELL_BLOCK", "FARGO_NO_TMA", "FARGO_AZ_CHUNKS2", "FARGO_RAD_COL"):
         monkeypatch.delenv(name, raising=False)
     v = _capi.FargoVariant()
     lib.fargo_variant_default(ctypes.byref(v))
     assert v.as_dict() == {"graph": 1, "pdl": 1, "pad": 1, "sg_ahead": 1, "rotate": 0, "az_generic": 0,
-                           "priority": 0, "cell_block": 0, "rad_tma": 1, "az_chunks": 1}
+                           "priority": 0, "cell_block": 0, "rad_tma": 1, "az_chunks": 1, "rad_col": -1}
     monkeypatch.setenv("FARGO_NO_PAD", "1")
     monkeypatch.setenv("FARGO_ROTATE", "1")
     monkeypatch.setenv("FARGO_PRIO", "2")
@@ -97,7 +97,7 @@ def test_variant_layout_and_default_switches(monkeypatch):
                                         ctypes.byref(h)) == _capi.FARGO_ERR_INVALID
     # so are unknown tile shapes
     lib.fargo_variant_default(ctypes.byref(v))
-    for field, bad in (("cell_block", 4), ("az_chunks", 3), ("az_chunks", 0)):
+    for field, bad in (("cell_block", 4), ("az_chunks", 3), ("az_chunks", 0), ("rad_col", 2)):
         w = _capi.FargoVariant.from_buffer_copy(v)
         setattr(w, field, bad)
         assert lib.fargo_ctx_create_variant(ctypes.byref(p), None, 0, 0, None, ctypes.byref(w),

@@ -70,7 +70,7 @@ def test_autotune_keeps_a_variant_at_least_as_fast():
     v, best, default = fg.autotune(disks, fg.FARGO_FP32_BULK, ndt=1)
     assert best >= default > 0
     assert set(v.as_dict()) == {"graph", "pdl", "pad", "sg_ahead", "rotate", "az_generic", "priority",
-                                "cell_block", "rad_tma", "az_chunks"}
+                                "cell_block", "rad_tma", "az_chunks", "rad_col"}
     assert v.priority in (0, 1, 2) and v.pad in (0, 1) and v.pdl in (0, 1)
     assert v.cell_block in (0, 1, 2, 3) and v.rad_tma in (0, 1) and v.az_chunks in (1, 2)
 

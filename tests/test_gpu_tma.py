@@ -1,5 +1,6 @@
 """The radial transport with TMA-staged tiles (k_transport_radial_tma) against the
-same transport with per-thread loads (k_transport_radial, FARGO_NO_TMA=1).
+same transport with per-thread loads (k_transport_radial, FARGO_NO_TMA=1), and the
+column march (k_transport_radial_col, variant rad_col) against both.
 
 Both form every cell from the same inputs with the same arithmetic; only the way
 the tile reaches shared memory differs (cp.async.bulk.tensor into a double-buffered
@@ -30,22 +31,15 @@ CASES = [
 
 
 def run(params, planets, prec, ndt, no_tma):
-    old = os.environ.get("FARGO_NO_TMA")
-    if no_tma:
-        os.environ["FARGO_NO_TMA"] = "1"
-    else:
-        os.environ.pop("FARGO_NO_TMA", None)
-    try:
-        d = fg.Disk(params, planets, prec)
-    finally:
-        if old is None:
-            os.environ.pop("FARGO_NO_TMA", None)
-        else:
-            os.environ["FARGO_NO_TMA"] = old
+    v = fg.default_variant()
+    v.rad_col = 0  # the tile forms (FP32-bulk would take the column march by default)
+    v.rad_tma = 0 if no_tma else 1
+    b = fg.Batch([(params, planets)], prec, variant=v)
+    d = b.disk(0)
     n = [d.step_DT() for _ in range(ndt)]
     out = {k: d.field(k) for k in ("dens", "vrad", "vtheta", "energy")}
     s = d.scalars()
-    d.close()
+    b.close()
     return n, out, s
 
 
@@ -72,3 +66,37 @@ def test_tma_kernel_is_the_one_launched():
     names = [d.lib.fargo_substep_kernel_name(d.h, k).decode() for k in range(nk.value)]
     d.close()
     assert "k_transport_radial_tma" in names and "k_transport_radial" not in names
+
+
+def run_variant(params, planets, prec, ndt, **fields):
+    v = fg.default_variant()
+    for k, x in fields.items():
+        setattr(v, k, x)
+    b = fg.Batch([(params, planets)], prec, variant=v)
+    d = b.disk(0)
+    n = [d.step_DT() for _ in range(ndt)]
+    out = {k: d.field(k) for k in ("dens", "vrad", "vtheta", "energy")}
+    s = d.scalars()
+    b.close()
+    return n, out, s
+
+
+@pytest.mark.parametrize("cfg,prec,nrad,nsec,extra", CASES)
+def test_column_march_radial_transport(cfg, prec, nrad, nsec, extra):
+    # the column march forms every cell with the tile kernel's arithmetic in the
+    # same order: FP32 fields are bitwise the tile kernel's; FP64 (out-of-line
+    # bodies, compiled apart from the tile kernel's) within rounding
+    params, planets = small(cfg, nrad=nrad, nsec=nsec)
+    for k, v in extra.items():
+        setattr(params, k, v)
+    n1, f1, s1 = run_variant(params, planets, prec, 2, rad_col=1)
+    n0, f0, s0 = run_variant(params, planets, prec, 2, rad_col=0)
+    assert n1 == n0
+    for k in f0:
+        if prec == fg.FARGO_FP32_BULK:
+            assert np.array_equal(f1[k], f0[k]), k
+        else:
+            scale = max(float(np.abs(f0[k]).max()), 1e-300)
+            assert float(np.abs(f1[k] - f0[k]).max()) <= 1e-13 * scale, k
+    if prec == fg.FARGO_FP32_BULK:
+        assert s1.lost_mass == s0.lost_mass
