@@ -124,6 +124,7 @@ SIGNATURES = [
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_fp64_pipe_peak", _I, [ctypes.POINTER(_D)]),
+    ("fargo_tc_selftest", _I, [_P, _P, _I, _I, _I, _P]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),
     ("fargo_batch_create", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),
                                 _I, ctypes.POINTER(_P)]),
@@ -153,6 +154,8 @@ SIGNATURES = [
     ("fargo_mlp_get_params", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
     ("fargo_mlp_get_grad", _I, [_P, ctypes.POINTER(ctypes.c_float)]),
     ("fargo_mlp_forward", _I, [_P, _P, _I, _P, _I, _P]),
+    ("fargo_mlp_set_tensor_path", _I, [_P, _I]),
+    ("fargo_mlp_status", _I, [_P]),
     ("fargo_mlp_backward", _I, [_P, _P, _I, _P, _P]),
     ("fargo_mlp_adam", _I, [_P, ctypes.c_float, _P]),
     ("fargo_learned_features", _I, [_I, _P, _P, _P, _P, _I, _I, _D, ctypes.POINTER(ctypes.c_float), _P, _P]),

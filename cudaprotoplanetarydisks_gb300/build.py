@@ -28,7 +28,7 @@ CUFLAGS = ARCH + COMMON + ["--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 LIB_SOURCES = ["params.cpp", "setup.cpp", "fargo_kernels.cu", "fargo_sg.cu", "fargo_ctx.cu", "output.cpp",
                "fargo_noalloc.cu", "fargo_batch.cu", "fargo_mlp.cu", "fargo_learned.cu",
-               "fargo_force_diag.cu", "fargo_peak.cu"]
+               "fargo_force_diag.cu", "fargo_peak.cu", "fargo_tc.cu"]
 EXE_SOURCES = ["driver.cpp"]
 HEADERS = ["fargo_internal.h", "fargo_device.cuh"]
 

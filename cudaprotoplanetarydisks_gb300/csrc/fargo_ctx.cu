@@ -776,7 +776,12 @@ int fargo_ctx_create_variant(const fargo_params *p, const fargo_planet *planets,
   c->want_tma = v.rad_tma != 0;
   c->cell_block = v.cell_block;
   c->az_chunks = v.az_chunks;
-  c->rad_col = v.rad_col < 0 ? precision == FARGO_FP32_BULK : v.rad_col != 0;
+  // the column march by default where it measured faster: FP32-bulk grids with at
+  // least 65536 column chunks (3072 sectors x 1024 rings: 64 against 85 us); a
+  // 768 x 256 grid gives it 48 CTAs, and FP64 is bound by its pipe either way
+  c->rad_col = v.rad_col < 0 ? (precision == FARGO_FP32_BULK &&
+                                (long)p->nsec * ((p->nrad + RADC_RINGS - 1) / RADC_RINGS) >= 65536)
+                             : v.rad_col != 0;
   c->sg_generic = env_on("FARGO_SG_GENERIC");  // a parity-test switch, not a variant
   // stream priorities: 0 all equal; 1 the hydro chain and the planets above the
   // self-gravity transforms; 2 the transforms above the rest.  The caller's

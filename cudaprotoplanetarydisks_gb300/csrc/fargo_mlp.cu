@@ -35,6 +35,7 @@
 #include <cstring>
 
 #include "fargo_gb300.h"
+#include "fargo_tc.cuh"
 
 #define MLP_IN 128
 #define MLP_H 64
@@ -317,6 +318,177 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float *__restrict__ P
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// Forward on the 5th-generation tensor cores (tcgen05): a persistent CTA of eight
+// warps takes 128-row tiles.  Per tile, one thread issues each layer's MMAs
+// (M = 128 rows, N = 64, 64, 16; K = 128, 64, 64 in steps of 16) with BF16
+// operands in shared memory and the FP32 accumulators in tensor memory.  Row m of
+// an accumulator is read (tcgen05.ld) by the two warps of lane quarter m / 32,
+// one per half of the columns; each adds the bias, rounds z to BF16, applies GELU
+// and writes BF16 h into shared memory as the next layer's A operand -- the same
+// arithmetic per value as the mma.sync kernel.  The next tile's X streams in by
+// cp.async as soon as the current tile's first layer has read its buffer, behind
+// the two hidden-layer epilogues.  Three CTAs fit an SM (74 KB of shared memory,
+// 128 tensor-memory columns each).
+//
+// Shared-memory operands use the no-swizzle K-major layout of fargo_tc.cuh with
+// the rows of a K chunk packed together: element (r, k) of an R-row operand at
+// (k / 8) * (R * 16) + r * 16 + (k % 8) * 2, i.e. LBO = R * 16 (along K) and
+// SBO = 128 (8-row groups), so that consecutive threads (rows) write consecutive
+// 16-byte slots (no bank conflicts).
+#define TCF_ROWS 128
+#define TCF_THREADS 256
+#define TCF_X_BYTES (TCF_ROWS * MLP_IN * 2)       // 32 KB
+#define TCF_W1_BYTES (MLP_H * MLP_IN * 2)         // 16 KB
+#define TCF_W2_BYTES (MLP_H * MLP_H * 2)          // 8 KB
+#define TCF_N3 16                                 // the last layer's N (the 2 outputs, zero-padded)
+#define TCF_W3_BYTES (TCF_N3 * MLP_H * 2)         // 2 KB
+#define TCF_H_BYTES (TCF_ROWS * MLP_H * 2)        // 16 KB
+#define TCF_SMEM (TCF_X_BYTES + TCF_W1_BYTES + TCF_W2_BYTES + TCF_W3_BYTES + TCF_H_BYTES)
+#define TCF_TMEM_COLS 128                         // layers 1 and 2 at columns 0..63, layer 3 at 64..79
+
+__device__ __forceinline__ uint32_t tcf_off(int r, int k, int rows) {
+  return (uint32_t)(k >> 3) * (uint32_t)(rows * 16) + (uint32_t)r * 16u + (uint32_t)(k & 7) * 2u;
+}
+
+__global__ void __launch_bounds__(TCF_THREADS) k_mlp_forward_tc(const float *__restrict__ P,
+                                                                const bf16 *__restrict__ X, int n,
+                                                                float *__restrict__ y, int *err) {
+  extern __shared__ __align__(128) unsigned char tcf_raw[];
+  __shared__ uint32_t tslot;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ float b1[MLP_H], b2[MLP_H], b3[2];
+  unsigned char *xs = tcf_raw, *w1 = xs + TCF_X_BYTES, *w2 = w1 + TCF_W1_BYTES, *w3 = w2 + TCF_W2_BYTES;
+  unsigned char *hs = w3 + TCF_W3_BYTES;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2, m = 32 * quarter + lane;  // accumulator row and column half
+  const int ntile = (n + TCF_ROWS - 1) / TCF_ROWS;
+  // the weights as B operands (N rows = outputs, K = inputs), BF16
+  for (int e = tid; e < MLP_IN * MLP_H; e += blockDim.x) {
+    const int k = e / MLP_H, o = e % MLP_H;
+    *reinterpret_cast<bf16 *>(w1 + tcf_off(o, k, MLP_H)) = __float2bfloat16_rn(P[MLP_OFF_W1 + e]);
+  }
+  for (int e = tid; e < MLP_H * MLP_H; e += blockDim.x) {
+    const int k = e / MLP_H, o = e % MLP_H;
+    *reinterpret_cast<bf16 *>(w2 + tcf_off(o, k, MLP_H)) = __float2bfloat16_rn(P[MLP_OFF_W2 + e]);
+  }
+  for (int e = tid; e < MLP_H * TCF_N3; e += blockDim.x) {
+    const int k = e / TCF_N3, o = e % TCF_N3;
+    *reinterpret_cast<bf16 *>(w3 + tcf_off(o, k, TCF_N3)) =
+        __float2bfloat16_rn(o < MLP_OUT ? P[MLP_OFF_W3 + k * MLP_OUTP + o] : 0.0f);
+  }
+  for (int e = tid; e < MLP_H; e += blockDim.x) {
+    b1[e] = P[MLP_OFF_B1 + e];
+    b2[e] = P[MLP_OFF_B2 + e];
+  }
+  if (tid < 2) b3[tid] = P[MLP_OFF_B3 + tid];
+  // row (tid % 128) of a tile, its half (tid / 128) of the 16 chunks of 16 bytes;
+  // rows >= n as zeros
+  auto stage = [&](int tile) {
+    const int rr = tid & (TCF_ROWS - 1), c0 = (tid >> 7) * 8, r = tile * TCF_ROWS + rr;
+    const bool valid = r < n;
+    const bf16 *src = X + (size_t)(valid ? r : 0) * MLP_IN;
+#pragma unroll
+    for (int c = c0; c < c0 + 8; c++)
+      cp_async16(reinterpret_cast<bf16 *>(xs + tcf_off(rr, 8 * c, TCF_ROWS)), src + 8 * c, valid);
+    cp_async_commit();
+  };
+  int tile = blockIdx.x;
+  if (tile < ntile) stage(tile);
+  if (warp == 0) tc::alloc(&tslot, TCF_TMEM_COLS);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tslot, lane_addr = tmem + ((uint32_t)(32 * quarter) << 16);
+  const uint32_t id64 = tc::idesc_bf16_f32(TCF_ROWS, MLP_H), id16 = tc::idesc_bf16_f32(TCF_ROWS, TCF_N3);
+  uint32_t phase = 0;
+  bool ok = true;
+  // one layer: D (columns col..) = A (shared, 128 rows, K = k) * B^T.  Thread 0
+  // issues the MMAs and alone polls their completion (false if it gave up); the
+  // others wait at the barrier that follows, which costs them no issue slots
+  auto layer = [&](const unsigned char *a, const unsigned char *b, int brows, int k, uint32_t col, uint32_t idesc) {
+    bool done = true;
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int s = 0; s < k / 16; s++) {
+        const uint64_t ad = tc::smem_desc(tc::smem_addr(a) + (uint32_t)s * 2 * TCF_ROWS * 16, TCF_ROWS * 16, 128);
+        const uint64_t bd = tc::smem_desc(tc::smem_addr(b) + (uint32_t)s * 2 * brows * 16, brows * 16, 128);
+        tc::mma_bf16(tmem + col, ad, bd, idesc, s > 0);
+      }
+      tc::commit(&bar);
+      done = tc::mbar_wait(&bar, phase);
+    }
+    phase ^= 1;
+    return done;
+  };
+  // bias, BF16 z, GELU, BF16 h of this thread's row and column half into the next
+  // layer's A operand
+  auto hidden = [&](const float *bias) {
+    float acc[2][16];  // both loads in flight before one wait
+    tc::ld16(lane_addr + (uint32_t)(half * 32), acc[0]);
+    tc::ld16(lane_addr + (uint32_t)(half * 32 + 16), acc[1]);
+    tc::wait_ld();
+#pragma unroll
+    for (int cc = 0; cc < 2; cc++) {
+      const int c0 = half * 32 + cc * 16;
+      uint32_t h[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float2 z =
+            unpack2(pack2(acc[cc][2 * i] + bias[c0 + 2 * i], acc[cc][2 * i + 1] + bias[c0 + 2 * i + 1]));
+        h[i] = pack2(gelu(z.x), gelu(z.y));
+      }
+      *reinterpret_cast<uint4 *>(hs + tcf_off(m, c0, TCF_ROWS)) = make_uint4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<uint4 *>(hs + tcf_off(m, c0 + 8, TCF_ROWS)) = make_uint4(h[4], h[5], h[6], h[7]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::fence_before_sync();
+    __syncthreads();
+  };
+  for (; tile < ntile; tile += gridDim.x) {
+    cp_async_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::fence_before_sync();
+    __syncthreads();
+    ok = layer(xs, w1, MLP_H, MLP_IN, 0, id64);
+    if (!__syncthreads_and(ok)) break;
+    tc::fence_after_sync();
+    // the first layer has read X: the next tile streams in behind the epilogues
+    if (tile + (int)gridDim.x < ntile) stage(tile + gridDim.x);
+    hidden(b1);
+    ok = layer(hs, w2, MLP_H, MLP_H, 0, id64);
+    if (!__syncthreads_and(ok)) break;
+    tc::fence_after_sync();
+    hidden(b2);
+    ok = layer(hs, w3, TCF_N3, MLP_H, 64, id16);
+    if (!__syncthreads_and(ok)) break;
+    tc::fence_after_sync();
+    if (half == 0) {
+      float v[16];
+      tc::ld16(lane_addr + 64u, v);
+      tc::wait_ld();
+      const int r = tile * TCF_ROWS + m;
+      if (r < n) *reinterpret_cast<float2 *>(y + (size_t)r * MLP_OUT) = make_float2(v[0] + b3[0], v[1] + b3[1]);
+    }
+    tc::fence_before_sync();
+  }
+  cp_async_wait<0>();
+  if (!ok) {
+    // an MMA did not complete in time (thread 0 saw it): flag it, give it one more
+    // bounded wait, and free the tensor memory all the same
+    atomicOr(err, 1);
+    tc::mbar_wait(&bar, phase ^ 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::dealloc(tmem, TCF_TMEM_COLS);
+}
+
 // Backward: dL/dparameters of sum over rows of dy . y, per CTA (FP32 partial
 // blob to part[blockIdx.x]).  dy: FP32 [n][2].
 struct MlpBwdSmem {
@@ -532,6 +704,9 @@ struct fargo_mlp {
   float *m1 = nullptr, *m2 = nullptr;
   float *part = nullptr;            // per-CTA gradient partials of the backward pass
   int fwd_ctas = 0, bwd_ctas = 0;   // persistent grids: the device's resident CTAs
+  int tc_ctas = 0;                  // the tcgen05 forward's persistent grid
+  int *err = nullptr;               // device flag: an MMA of the tcgen05 forward did not complete
+  int path = FARGO_MLP_TCGEN05;     // fargo_mlp_set_tensor_path
   int steps = 0;
 };
 
@@ -557,6 +732,14 @@ int fargo_mlp_create(int max_rows, fargo_mlp **out) {
   if (e == cudaSuccess && (per_fwd < 1 || per_bwd < 1)) e = cudaErrorInvalidConfiguration;
   m->fwd_ctas = sms * per_fwd;
   m->bwd_ctas = sms * per_bwd;
+  int per_tc = 0;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TCF_SMEM);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_tc, k_mlp_forward_tc, TCF_THREADS, TCF_SMEM);
+  // tensor memory: TCF_TMEM_COLS columns per CTA, 512 per SM
+  m->tc_ctas = sms * std::max(1, std::min(per_tc, 512 / TCF_TMEM_COLS));
+  if (e == cudaSuccess) e = cudaMalloc(&m->err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&m->P, MLP_NPARAM * 4);
   if (e == cudaSuccess) e = cudaMalloc(&m->grad, MLP_NPARAM * 4);
   if (e == cudaSuccess) e = cudaMalloc(&m->m1, MLP_NPARAM * 4);
@@ -575,7 +758,7 @@ int fargo_mlp_create(int max_rows, fargo_mlp **out) {
 
 void fargo_mlp_destroy(fargo_mlp *m) {
   if (!m) return;
-  for (void *p : {(void *)m->P, (void *)m->grad, (void *)m->m1, (void *)m->m2, (void *)m->part})
+  for (void *p : {(void *)m->P, (void *)m->grad, (void *)m->m1, (void *)m->m2, (void *)m->part, (void *)m->err})
     if (p) cudaFree(p);
   delete m;
 }
@@ -608,9 +791,27 @@ static bool rows_ok(const fargo_mlp *m, const void *x, int n, const void *v) {
 int fargo_mlp_forward(fargo_mlp *m, const void *x, int n, float *y, int train, void *stream) {
   (void)train;  // the backward pass recomputes what it needs
   if (!rows_ok(m, x, n, y)) return FARGO_ERR_INVALID;
-  const int warps = (n + 15) / 16, ctas = std::min(m->fwd_ctas, (warps + 3) / 4);
-  k_mlp_forward<<<ctas, 128, fwd_smem(), (cudaStream_t)stream>>>(m->P, (const bf16 *)x, n, y);
+  if (m->path == FARGO_MLP_TCGEN05) {
+    const int ctas = std::min(m->tc_ctas, (n + TCF_ROWS - 1) / TCF_ROWS);
+    k_mlp_forward_tc<<<ctas, TCF_THREADS, TCF_SMEM, (cudaStream_t)stream>>>(m->P, (const bf16 *)x, n, y, m->err);
+  } else {
+    const int warps = (n + 15) / 16, ctas = std::min(m->fwd_ctas, (warps + 3) / 4);
+    k_mlp_forward<<<ctas, 128, fwd_smem(), (cudaStream_t)stream>>>(m->P, (const bf16 *)x, n, y);
+  }
   return cudaGetLastError() == cudaSuccess ? FARGO_OK : FARGO_ERR_CUDA;
+}
+
+int fargo_mlp_set_tensor_path(fargo_mlp *m, int path) {
+  if (!m || (path != FARGO_MLP_TCGEN05 && path != FARGO_MLP_MMA_SYNC)) return FARGO_ERR_INVALID;
+  m->path = path;
+  return FARGO_OK;
+}
+
+int fargo_mlp_status(fargo_mlp *m) {
+  if (!m) return FARGO_ERR_INVALID;
+  int e = 0;
+  if (cudaMemcpy(&e, m->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FARGO_ERR_CUDA;
+  return e ? FARGO_ERR_NUMERIC : FARGO_OK;
 }
 
 int fargo_mlp_backward(fargo_mlp *m, const void *x, int n, const float *dy, void *stream) {

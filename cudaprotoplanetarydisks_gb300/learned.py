@@ -66,6 +66,15 @@ class MLP:
         self._ok(self.lib.fargo_mlp_get_params(self.h, P.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "get_params")
         return P
 
+    def set_tensor_path(self, path):
+        """"tcgen05" (default) or "mma.sync": the forward pass's tensor-core kernel."""
+        code = {"tcgen05": 0, "mma.sync": 1}[path]
+        self._ok(self.lib.fargo_mlp_set_tensor_path(self.h, code), "set_tensor_path")
+
+    def status(self):
+        """Raises if an MMA of a tcgen05 forward pass did not complete in time."""
+        self._ok(self.lib.fargo_mlp_status(self.h), "mlp status")
+
     def grad(self):
         G = np.empty(NPARAM, dtype=np.float32)
         self._ok(self.lib.fargo_mlp_get_grad(self.h, G.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "get_grad")
@@ -221,7 +230,7 @@ def restrict(fine, coarse, factor):
 IDENTITY_NORM = np.concatenate([np.zeros(125), np.ones(125)]).astype(np.float32)
 
 
-def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None, reset_every=1):
+def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None, reset_every=1, sample_every=1):
     """Training pairs from the plain solver: for every (params, planets) of a
     coarse disk, its fine teacher runs `spinup` DTs, then the coarse disk starts
     from the restricted fine state and both take `ndt` DTs; after each, the inputs
@@ -229,7 +238,9 @@ def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None, reset_
     coarse one.  The coarse disk restarts from the restricted fine state every
     `reset_every` DTs: with 1 every pair starts on the teacher's trajectory, with
     more the later pairs start from states the coarse solver drifted to, and their
-    targets pull back to the teacher.  Returns samples
+    targets pull back to the teacher.  With sample_every = s > 1 the pairs spread
+    along the teacher's trajectory: the teacher runs s - 1 DTs alone between two
+    pairs, and every pair starts from the restricted teacher state.  Returns samples
     [(x, target, surf, nrad, nsec)] on the GPU."""
     import torch
     from . import Disk, FARGO_FP32_BULK
@@ -247,6 +258,9 @@ def generate(disks, factor=4, spinup=4, ndt=8, norm=None, precision=None, reset_
         restrict(fine, coarse, factor)
         corr = Correction(None, norm, 1.0)
         for k in range(ndt):
+            if sample_every > 1:
+                fine.run(sample_every - 1)
+                restrict(fine, coarse, factor)
             x = torch.empty((n, NIN), dtype=torch.bfloat16, device="cuda")
             coarse.step_DT()
             fine.step_DT()
@@ -364,7 +378,8 @@ def evaluate_loss(mlp, samples, scale, var=None, ring_neutral=False):
 
 
 def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, ndt_eval=10, epochs=40, lr=1e-3,
-               seed=2025, sigma_noise=1e-4, reset_every=4, ring_neutral=True, limiter=0.5):
+               seed=2025, sigma_noise=1e-4, reset_every=4, ring_neutral=True, limiter=0.5, sample_every=1,
+               eval_every=1, ndt_time=10):
     """Coarse disks of nrad x 3 nrad drawn from the ensemble distribution, a
     factor-x finer plain run of each as teacher: train on n_train disks, then on
     n_test held-out disks report the one-DT loss with and without the network and
@@ -379,7 +394,7 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
     te_disks = c4_disks(n_test, seed=seed + 1, nrad_choices=(nrad,), sigma_noise=sigma_noise)
     t0 = time.perf_counter()
     norm = feature_norm(generate(tr_disks[:2], factor, spinup, 2))
-    tr = generate(tr_disks, factor, spinup, ndt_train, norm, reset_every=reset_every)
+    tr = generate(tr_disks, factor, spinup, ndt_train, norm, reset_every=reset_every, sample_every=sample_every)
     ho = generate(te_disks, factor, spinup, 4, norm)
     t_gen = time.perf_counter() - t0
     scale, var = target_stats(tr)
@@ -401,23 +416,29 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
             restrict(fine, d, factor)
         work = workspace(learn)
         err = {"plain": [], "learned": []}
-        for _ in range(ndt_eval):
+        perr = {"plain": [], "learned": []}
+        for k in range(ndt_eval):
             fine.step_DT()
             plain.step_DT()
             corr.step_DT(learn, work)
-            restrict(fine, ref, factor)
-            r = ref.field("dens")[:-1]
-            err["plain"].append(rel(plain.field("dens")[:-1], r))
-            err["learned"].append(rel(learn.field("dens")[:-1], r))
+            if (k + 1) % eval_every == 0:
+                restrict(fine, ref, factor)
+                r = ref.field("dens")[:-1]
+                rp = r.mean(axis=1)
+                for name, d in (("plain", plain), ("learned", learn)):
+                    x = d.field("dens")[:-1]
+                    err[name].append(rel(x, r))
+                    perr[name].append(rel(x.mean(axis=1), rp))
+        restrict(fine, ref, factor)
         prof = {k: d.field("dens")[:-1].mean(axis=1) for k, d in (("ref", ref), ("plain", plain), ("learned", learn))}
         t = {}
-        for name, run in (("fine", lambda: fine.run(ndt_eval)), ("plain", lambda: plain.run(ndt_eval)),
-                          ("learned", lambda: [corr.step_DT(learn, work) for _ in range(ndt_eval)])):
+        for name, run in (("fine", lambda: fine.run(ndt_time)), ("plain", lambda: plain.run(ndt_time)),
+                          ("learned", lambda: [corr.step_DT(learn, work) for _ in range(ndt_time)])):
             t0 = time.perf_counter()
             run()
-            t[name] = (time.perf_counter() - t0) / ndt_eval
+            t[name] = (time.perf_counter() - t0) / ndt_time
         roll.append({"field_err": err, "profile_err": {k: rel(prof[k], prof["ref"]) for k in ("plain", "learned")},
-                     "s_per_dt": t})
+                     "profile_err_per_eval": perr, "s_per_dt": t})
         for d in (fine, plain, learn, ref):
             d.close()
     avg = lambda get: float(np.mean([get(r) for r in roll]))  # noqa: E731
@@ -431,8 +452,13 @@ def experiment(n_train=12, n_test=4, nrad=256, factor=4, spinup=8, ndt_train=8, 
                   "seconds_data": t_gen, "seconds_training": t_train},
         "held_out_one_dt_loss": {"with_network": with_net, "without": without},
         "rollout_dts": ndt_eval,
-        "field_err_rel_per_dt": {k: [avg(lambda r, i=i, k=k: r["field_err"][k][i]) for i in range(ndt_eval)]
+        "eval_every_dts": eval_every,
+        "field_err_rel_per_dt": {k: [avg(lambda r, i=i, k=k: r["field_err"][k][i]) for i in range(ndt_eval // eval_every)]
                                  for k in ("plain", "learned")},
+        "profile_err_rel_per_eval": {k: [avg(lambda r, i=i, k=k: r["profile_err_per_eval"][k][i])
+                                         for i in range(ndt_eval // eval_every)] for k in ("plain", "learned")},
+        "profile_err_rel_max_over_disks": {k: float(max(r["profile_err"][k] for r in roll))
+                                           for k in ("plain", "learned")},
         "profile_err_rel": {k: avg(lambda r, k=k: r["profile_err"][k]) for k in ("plain", "learned")},
         "s_per_dt": {k: avg(lambda r, k=k: r["s_per_dt"][k]) for k in ("fine", "plain", "learned")},
         "corrections": {"accepted": corr.accepted, "rejected": corr.rejected,
@@ -470,7 +496,11 @@ def kernel_timing(nrad=256, reps=50, seed=5):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps * 1e3
 
+    mlp.set_tensor_path("mma.sync")
+    fwd_ms_us = ev(lambda: mlp.forward(x, y))
+    mlp.set_tensor_path("tcgen05")
     fwd_us, bwd_us = ev(lambda: mlp.forward(x, y)), ev(lambda: mlp.backward(x, dy))
+    mlp.status()
     corr = Correction(mlp, IDENTITY_NORM, 1.0)
     corr.features(disk, x)
     t0 = time.perf_counter()
@@ -481,8 +511,12 @@ def kernel_timing(nrad=256, reps=50, seed=5):
     disk.close()
     f_fwd = 2 * (128 * 64 + 64 * 64 + 64 * 2)
     f_bwd = 2 * (128 * 64 + 64 * 64) + 2 * (2 * 64 + 64 * 64) + 2 * (128 * 64 + 64 * 64 + 64 * 2)
-    return {"rows": n, "tensor_path": "mma.sync m16n8k16 BF16, FP32 accumulate",
+    return {"rows": n,
+            "forward_path": "tcgen05.mma kind::f16 (BF16, FP32 accumulators in tensor memory), 128-row tiles",
             "forward_us": fwd_us, "forward_tflops": f_fwd * n / fwd_us * 1e-6,
+            "forward_mma_sync_us": fwd_ms_us, "forward_mma_sync_tflops": f_fwd * n / fwd_ms_us * 1e-6,
+            "x_bytes_per_forward": n * NIN * 2, "forward_x_GBs": n * NIN * 2 / fwd_us * 1e-3,
+            "backward_path": "mma.sync m16n8k16 BF16, FP32 accumulate",
             "backward_us": bwd_us, "backward_tflops": f_bwd * n / bwd_us * 1e-6,
             "backward_includes": "forward recompute and the per-CTA gradient reduction",
             "features_wall_us": feat_us}

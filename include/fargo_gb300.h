@@ -186,9 +186,11 @@ typedef struct {
                       not bitwise) */
   int rad_col;     /* radial transport as a column march (one thread per sector walks a chunk
                       of rings with its stencil in registers; no shared memory, no barrier):
-                      1 on, 0 off (rad_tma decides), -1 (default) on in FP32-bulk, off in FP64,
-                      where it measured slower than the TMA-staged tiles; FP32 results are
-                      bitwise those of the tiles, FP64 agree to rounding */
+                      1 on, 0 off (rad_tma decides), -1 (default) on in FP32-bulk on grids
+                      of at least 65536 sectors x ring chunks of 32 (off on smaller grids,
+                      where it has too few threads, and in FP64, where it measured slower
+                      than the TMA-staged tiles); FP32 results are bitwise those of the
+                      tiles, FP64 agree to rounding */
 } fargo_variant;
 /* The default variant, with the FARGO_NO_GRAPH, FARGO_NO_PDL, FARGO_NO_PAD,
    FARGO_NO_SG_AHEAD, FARGO_ROTATE, FARGO_AZ_GENERIC and FARGO_PRIO switches
@@ -296,6 +298,17 @@ const char *fargo_substep_kernel_name(const fargo_ctx *ctx, int k);
    filling every SM, timed with CUDA events after a warm-up launch.  The roofline
    of the FP64 mode, whose kernels are bound by this pipe.  Synchronous. */
 int  fargo_fp64_pipe_peak(double *dfma_per_s);
+/* Self-test of the 5th-generation tensor-core path (tcgen05, sm_100 family): one
+   CTA computes d (128 x n, FP32, row-major) = a (128 x k, BF16 bit patterns,
+   row-major) x b (n x k, BF16, row-major)^T with k / 16 MMAs accumulating in
+   tensor memory, read back with tcgen05.ld.  n in 16..256 and k in 16..128,
+   multiples of 16.  The operands are staged in the no-swizzle K-major layout with
+   the core matrices adjacent along K packed together (mode 0) or those adjacent
+   along the rows (mode 1); mode 2 stages as mode 0 but swaps the two stride fields
+   of the descriptors (the other reading of the descriptor; its product is not
+   expected to be the matrix product).  Synchronous; FARGO_ERR_NUMERIC if an MMA did
+   not complete within its bounded wait. */
+int  fargo_tc_selftest(const unsigned short *a, const unsigned short *b, int n, int k, int mode, float *d);
 
 /* ---- allocation-free CFL (no counterpart in the reference) --------------- */
 /* The CFL integer of ConditionCFL for callers that cannot call cudaMalloc
@@ -402,6 +415,15 @@ int  fargo_mlp_get_grad(fargo_mlp *m, float *host);
 /* y = f(x) on n rows.  train is accepted for compatibility and ignored: the
    backward pass recomputes the forward pass of its rows. */
 int  fargo_mlp_forward(fargo_mlp *m, const void *x_bf16, int n, float *y, int train, void *stream);
+/* The forward pass's tensor-core path: FARGO_MLP_TCGEN05 (default: 128-row tiles,
+   tcgen05.mma with the accumulators in tensor memory) or FARGO_MLP_MMA_SYNC
+   (16-row warp tiles, mma.sync m16n8k16).  The two agree to FP32 summation order. */
+#define FARGO_MLP_TCGEN05 0
+#define FARGO_MLP_MMA_SYNC 1
+int  fargo_mlp_set_tensor_path(fargo_mlp *m, int path);
+/* FARGO_ERR_NUMERIC if an MMA of a tcgen05 forward pass did not complete within
+   its bounded wait (the pass then leaves its rows unwritten).  Synchronous. */
+int  fargo_mlp_status(fargo_mlp *m);
 /* dL/dparameters from dL/dy (FP32 [n][2]) of the rows x; summed over the rows in
    a fixed order (deterministic on a given device). */
 int  fargo_mlp_backward(fargo_mlp *m, const void *x_bf16, int n, const float *dy, void *stream);
