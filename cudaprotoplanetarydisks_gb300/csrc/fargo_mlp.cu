@@ -706,7 +706,7 @@ struct fargo_mlp {
   int fwd_ctas = 0, bwd_ctas = 0;   // persistent grids: the device's resident CTAs
   int tc_ctas = 0;                  // the tcgen05 forward's persistent grid
   int *err = nullptr;               // device flag: an MMA of the tcgen05 forward did not complete
-  int path = FARGO_MLP_TCGEN05;     // fargo_mlp_set_tensor_path
+  int path = FARGO_MLP_MMA_SYNC;    // fargo_mlp_set_tensor_path (the faster, measured)
   int steps = 0;
 };
 
@@ -734,10 +734,19 @@ int fargo_mlp_create(int max_rows, fargo_mlp **out) {
   m->bwd_ctas = sms * per_bwd;
   int per_tc = 0;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TCF_SMEM);
+  // the largest shared-memory carveout, so that three CTAs fit an SM
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_tc, k_mlp_forward_tc, TCF_THREADS, TCF_SMEM);
-  // tensor memory: TCF_TMEM_COLS columns per CTA, 512 per SM
-  m->tc_ctas = sms * std::max(1, std::min(per_tc, 512 / TCF_TMEM_COLS));
+  // CTAs that fit an SM by shared memory (the occupancy query reported one CTA per
+  // SM for this kernel on GB300, where ncu shows three resident), and by tensor
+  // memory: TCF_TMEM_COLS columns per CTA, 512 per SM
+  int smem_sm = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  const int per_smem = smem_sm / (TCF_SMEM + 2048);  // + static shared memory and the per-CTA reserve
+  m->tc_ctas = sms * std::max(1, std::min(std::max(per_tc, per_smem), 512 / TCF_TMEM_COLS));
   if (e == cudaSuccess) e = cudaMalloc(&m->err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&m->P, MLP_NPARAM * 4);

@@ -415,9 +415,12 @@ int  fargo_mlp_get_grad(fargo_mlp *m, float *host);
 /* y = f(x) on n rows.  train is accepted for compatibility and ignored: the
    backward pass recomputes the forward pass of its rows. */
 int  fargo_mlp_forward(fargo_mlp *m, const void *x_bf16, int n, float *y, int train, void *stream);
-/* The forward pass's tensor-core path: FARGO_MLP_TCGEN05 (default: 128-row tiles,
-   tcgen05.mma with the accumulators in tensor memory) or FARGO_MLP_MMA_SYNC
-   (16-row warp tiles, mma.sync m16n8k16).  The two agree to FP32 summation order. */
+/* The forward pass's tensor-core path: FARGO_MLP_MMA_SYNC (default: 16-row warp
+   tiles, mma.sync m16n8k16, every activation in registers) or FARGO_MLP_TCGEN05
+   (128-row tiles, tcgen05.mma with the accumulators in tensor memory, each hidden
+   layer's GELU epilogue through shared memory).  Their outputs are bitwise equal on
+   GB300; the mma.sync path measured faster (31.8 against 41.1 us on 196,608 rows:
+   the GELU epilogue, not the tensor pipe, bounds both). */
 #define FARGO_MLP_TCGEN05 0
 #define FARGO_MLP_MMA_SYNC 1
 int  fargo_mlp_set_tensor_path(fargo_mlp *m, int path);
