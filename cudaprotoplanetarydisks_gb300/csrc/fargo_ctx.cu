@@ -1243,11 +1243,14 @@ struct fargo_fused {
 namespace {
 struct FusedGroup {
   int kernel;
-  std::vector<int> member, first, gx;
+  std::vector<int> member, first, gx, gy;  // first: prefix sums of the launched blocks
   dim3 block;
   size_t smem = 0;
   int extra = 0;
+  int merge = 1;  // consecutive blocks of a disk's grid along x per launched block
 };
+// launched blocks of the per-cell kernels cover this many blocks of their disk
+constexpr int FUSED_CELL_MERGE = 4;
 
 const char *batch_kernel_name(int k) {
   static const char *const names[BK_END + 1] = {
@@ -1309,12 +1312,13 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
     widths.push_back(0);
   }
   // launch groups in substep order
-  auto group = [&](int kernel, int width, auto pred, auto grid, dim3 block, size_t smem, int extra) {
+  auto group = [&](int kernel, int width, auto pred, auto grid, dim3 block, size_t smem, int extra, int merge = 1) {
     FusedGroup g;
     g.kernel = kernel;
     g.block = block;
     g.smem = smem;
     g.extra = extra;
+    g.merge = merge;
     g.first.push_back(0);
     for (int k = 0; k < n; k++) {
       if (width && disks[k]->P.nsec != width) continue;
@@ -1322,7 +1326,8 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
       const int2 gd = grid(disks[k]->P, disks[k]);
       g.member.push_back(k);
       g.gx.push_back(gd.x);
-      g.first.push_back(g.first.back() + gd.x * gd.y);
+      g.gy.push_back(gd.y);
+      g.first.push_back(g.first.back() + (gd.x + merge - 1) / merge * gd.y);
     }
     return g;
   };
@@ -1362,18 +1367,18 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
     body.push_back({group(BK_CFL_V4, w, v4, rings, dim3(v4_threads), 0, 0),
                     group(BK_CFL, w, not_v4, rings, dim3(256), 0, 0),
                     group(BK_PLANETS, w, all, one, dim3(64), 0, 0),
-                    group(BK_COROT, w, corot, cells, b2, 0, 0),
-                    group(BK_SOURCE, w, all, cells, b2, 0, 0),
-                    group(BK_VISC_TAU, w, all, cells, b2, 0, 0),
-                    group(BK_VISC_UPDATE, w, all, cells, b2, 0, 0),
-                    group(BK_ARTVISC, w, all, cells, b2, 0, 0),
-                    group(BK_VISC_TAU, w, adiabatic, cells, b2, 0, 1),
-                    group(BK_ENERGY, w, adiabatic, cells, b2, 0, 0),
+                    group(BK_COROT, w, corot, cells, b2, 0, 0, FUSED_CELL_MERGE),
+                    group(BK_SOURCE, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
+                    group(BK_VISC_TAU, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
+                    group(BK_VISC_UPDATE, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
+                    group(BK_ARTVISC, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
+                    group(BK_VISC_TAU, w, adiabatic, cells, b2, 0, 1, FUSED_CELL_MERGE),
+                    group(BK_ENERGY, w, adiabatic, cells, b2, 0, 0, FUSED_CELL_MERGE),
                     group(BK_RADIAL, w, rad_tile, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
                     group(BK_RADIAL_COL, w, rad_col, columns, dim3(RADC_THREADS), 0, 0),
                     group(BK_AZ4, w, az_one, rings, dim3(az_threads), az_smem, 0),
                     group(BK_AZ4_MC, w, az_mc, rings, dim3(sizeof(T) == 8 ? 512 : 768), az_smem, 0),
-                    group(BK_VELOCITIES, w, all, cells, b2, 0, 1),
+                    group(BK_VELOCITIES, w, all, cells, b2, 0, 1, FUSED_CELL_MERGE),
                     group(BK_END, w, all, one, dim3(256), 0, 0)});
   }
   if (prepare_batched<T>(rad_smem_bytes(sizeof(T)), az_smem_all) != cudaSuccess) {
@@ -1387,8 +1392,12 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
     std::vector<int4> blk;
     blk.reserve(g.first.back());
     for (size_t m = 0; m < g.member.size(); m++) {
-      const int nb = g.first[m + 1] - g.first[m];
-      for (int b = 0; b < nb; b++) blk.push_back(make_int4(g.member[m], b % g.gx[m], b / g.gx[m], nb));
+      const int gx = g.gx[m], gy = g.gy[m], nb = gx * gy;
+      for (int by = 0; by < gy; by++)
+        for (int bx = 0; bx < gx; bx += g.merge) {
+          const int cnt = std::min(g.merge, gx - bx);
+          blk.push_back(make_int4(g.member[m] | (cnt << 20), bx, by, nb));
+        }
     }
     G.blk = (const int4 *)dev(blk.data(), blk.size() * sizeof(int4));
     return G.blk != nullptr;
@@ -1490,7 +1499,7 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
 
 int fused_create(fargo_ctx *const *disks, int n, int by_width, fargo_fused **out, std::string *why) {
   *out = nullptr;
-  if (!disks || n <= 0) return FARGO_ERR_INVALID;
+  if (!disks || n <= 0 || n >= (1 << 20)) return FARGO_ERR_INVALID;  // disk index: 20 bits of a table entry
   for (int k = 0; k < n; k++)
     if (disks[k]->precision != disks[0]->precision) {
       *why = "the disks of a fused ensemble share one precision";

@@ -2092,27 +2092,35 @@ __global__ void k_dt_begin(Ctl *c) {
 // disk is done), and runs the kernel body of the single-disk launch with the
 // disk's arguments and its own block index.
 template <class T>
-__device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, uint3 &bid, bool masked = true) {
+__device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, uint3 &bid, bool masked = true,
+                                                       int *count = nullptr) {
   const int4 r = __ldg(&G.blk[blockIdx.x]);
-  const KArgs<T> *a = &G.args[r.x];
+  const KArgs<T> *a = &G.args[r.x & 0xFFFFF];
   if (masked && a->d.ctl->done) return nullptr;
   bid = make_uint3((unsigned)r.y, (unsigned)r.z, (unsigned)r.w);
+  if (count) *count = r.x >> 20;
   return a;
 }
 
 // The body reads the disk's arguments in place (for T = double through the
-// out-of-line body shared with the single-disk kernel).
+// out-of-line body shared with the single-disk kernel).  A launched block may
+// cover several consecutive blocks of its disk's grid along x (the per-cell
+// kernels: the table read and the done test are paid once for all of them).
 #define FARGO_BATCHED(kname, bounds, body, ...)                                  \
   template <class T>                                                             \
   __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
     pdl_enter();                                                                 \
     uint3 bid;                                                                   \
-    const KArgs<T> *a = batch_block(G, bid);                                     \
+    int cnt = 1;                                                                 \
+    const KArgs<T> *a = batch_block(G, bid, true, &cnt);                         \
     if (!a) return;                                                              \
-    if constexpr (sizeof(T) == 8)                                                \
-      body##_f64(*a, bid, ##__VA_ARGS__);                                        \
-    else                                                                         \
-      body<T>(*a, bid, ##__VA_ARGS__);                                           \
+    for (int k = 0; k < cnt; k++) {                                              \
+      const uint3 b = make_uint3(bid.x + k, bid.y, bid.z);                       \
+      if constexpr (sizeof(T) == 8)                                              \
+        body##_f64(*a, b, ##__VA_ARGS__);                                        \
+      else                                                                       \
+        body<T>(*a, b, ##__VA_ARGS__);                                           \
+    }                                                                            \
   }
 FARGO_BATCHED(kb_soundspeed, 256, soundspeed_body)
 FARGO_BATCHED(kb_correct_vtheta, 256, correct_vtheta_body)

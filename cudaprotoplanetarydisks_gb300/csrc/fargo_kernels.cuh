@@ -122,7 +122,8 @@ cudaError_t prepare_kernels(size_t az_smem_bytes, int az_regs);
 template <class T>
 struct BatchGroup {
   const KArgs<T> *args;  // every disk's kernel arguments (device array, indexed by disk)
-  const int4 *blk;       // [blocks of the launch] disk, block x and y in the disk's own grid, its blocks
+  const int4 *blk;       // [blocks of the launch] disk + (blocks covered << 20), the first block's x and
+                         // y in the disk's own grid, the disk's blocks
   int ng;
   int extra;             // kb_visc_tau: 1 = the new velocities; kb_velocities: with temperature
 };
