@@ -423,18 +423,28 @@ def _par_values(text):
     return vals
 
 
-def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=1000000000, outdir=None):
+def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=1000000000, outdir=None, overrides=None):
     """Runs a build of the reference's main() (oracle/_ref: its CPU build or its own
     CUDA build) on the workload's .par for ndt DTs (Ntot = ndt - 1: the reference
     runs Ntot + 1), the DT divided by dt_divisor, dumps every `ninterm` DTs into
     outdir (a temporary directory when None), the seeded noise of the .par's
     SigmaNoise / EnergyNoise / NoiseSeed keys through the build's link-time
-    wrappers.  Returns ([(substeps, AlgoGas seconds) per DT], cells) from the
-    binary's REFSTEP lines.  Reads no product code."""
+    wrappers; overrides replaces .par keys (e.g. {"NRAD": 128, "NSEC": 384}).
+    Returns ([(substeps, AlgoGas seconds) per DT], cells) from the binary's
+    REFSTEP lines.  Reads no product code."""
     if not os.path.exists(exe):
         raise RuntimeError(f"{exe} is missing (built by build(): oracle/ref_emul, oracle/ref_cuda)")
     src = os.path.join(CONFIG_DIR, CONFIG_FILES[cfg])
     text = open(src).read()
+    over = {k.upper(): v for k, v in (overrides or {}).items()}
+    if over:
+        lines, seen = [], set()
+        for line in text.splitlines():
+            k = line.split()[0].upper() if line.split() else ""
+            lines.append(f"{k} {over[k]}" if k in over else line)
+            seen.add(k)
+        lines += [f"{k} {v}" for k, v in over.items() if k not in seen]
+        text = "\n".join(lines) + "\n"
     vals = _par_values(text)
     with tempfile.TemporaryDirectory() as d:
         out = outdir or os.path.join(d, "out")
@@ -496,14 +506,23 @@ def reference_cuda(fg, stream, flush):
     r = measure_mode(fg, p1, pl1, fg.FARGO_FP64, stream, flush, 14, 1)
     w, ne, _, _ = r["e2e"]
     own = r["substeps"] * cells / (r["ms"] * 1e-3)
-    return {"workload": WORKLOADS["c1"], "config_file": "configs/" + CONFIG_FILES["c1"],
-            "build": "the reference's src/*.cu with nvcc 13 for sm_103a (Makefile flags; __shfl_down_sync and "
-                     "::array compat fixes), seeded noise and AlgoGas timing through link-time wrappers",
-            "value": n * cells / t, "unit": METRIC, "dtype": "f64", "substeps": n, "seconds": t,
-            "timing": "host clock around each AlgoGas call (the reference synchronises the device after every "
-                      "launch), DTs 2..15",
-            "gb300_fp64_same_disk": {"value": own, "e2e": ne * cells / w, "unit": METRIC,
-                                     "ms_per_dt": r["ms"] / 14}}
+    out = {"workload": WORKLOADS["c1"], "config_file": "configs/" + CONFIG_FILES["c1"],
+           "build": "the reference's src/*.cu with nvcc 13 for sm_103a (Makefile flags; __shfl_down_sync and "
+                    "::array compat fixes), seeded noise and AlgoGas timing through link-time wrappers",
+           "value": n * cells / t, "unit": METRIC, "dtype": "f64", "substeps": n, "seconds": t,
+           "timing": "host clock around each AlgoGas call (the reference synchronises the device after every "
+                     "launch), DTs 2..15",
+           "gb300_fp64_same_disk": {"value": own, "e2e": ne * cells / w, "unit": METRIC,
+                                    "ms_per_dt": r["ms"] / 14}}
+    # the headline disk (1024 x 3072 adiabatic with cooling, WALL boundaries, no
+    # self-gravity: its kernels read for out-of-bounds access too), 3 DTs, the
+    # first untimed; this code's FP64 on the same disk is the headline value
+    steps3, cells3 = run_reference_exe(REF_CUDA_EXE, "c3", 3)
+    n3, t3 = sum(s for s, _ in steps3[1:]), sum(x for _, x in steps3[1:])
+    out["c3"] = {"workload": WORKLOADS["c3"], "config_file": "configs/" + CONFIG_FILES["c3"],
+                 "value": n3 * cells3 / t3, "unit": METRIC, "dtype": "f64", "substeps": n3, "seconds": t3,
+                 "timing": "host clock around each AlgoGas call, DTs 2..3"}
+    return out
 
 
 def cpu_baselines(cfg, params, planets):
@@ -774,8 +793,8 @@ def batch_ensemble(ndt=4, n=64):
     disks = fg.c4_disks(n)
     cells = [p.nrad * p.nsec for p, _ in disks]
 
-    def batched(variant, fused=None):
-        b = fg.Batch(disks, fg.FARGO_FP32_BULK, variant=variant)
+    def batched(variant, fused=None, precision=None):
+        b = fg.Batch(disks, fg.FARGO_FP32_BULK if precision is None else precision, variant=variant)
         if fused:
             b.fuse(by_width=(fused == "width"))
         b.run_async(1)
@@ -816,6 +835,8 @@ def batch_ensemble(ndt=4, n=64):
     tf, cuf, dens_f, (launches_f, groups_ms) = batched(None, fused="width")
     fused_diff = max(float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(dens_f, dens32))
     tf1, cuf1, dens_f1, launches_f1 = batched(None, fused="one")
+    # FP64 at the same batching (per-disk graphs side by side)
+    t64b, cu64b, _, _ = batched(None, precision=fg.FARGO_FP64)
     fused_diff = max(fused_diff, max(float(np.abs(x - y).max() / np.abs(y).max()) for x, y in zip(dens_f1, dens32)))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     t64, cu64, err = 0.0, 0, []
@@ -851,7 +872,10 @@ def batch_ensemble(ndt=4, n=64):
                                         "speedup_over_per_disk_graphs": (cuf1 / tf1) / v32},
                            "dens_max_rel_diff_vs_per_disk": fused_diff},
             "fp64_plain_sequential": {"value": v64, "unit": METRIC, "seconds": t64},
+            "fp64_batched": {"value": cu64b / t64b, "unit": METRIC, "seconds": t64b,
+                             "form": "the same per-disk graphs side by side, FP64"},
             "ratio_fp32_batched_to_fp64_plain": v32 / v64,
+            "ratio_fp32_batched_to_fp64_batched": v32 / (cu64b / t64b),
             "fp32_dens_rel_l2_vs_fp64_max": max(err), "fp32_dens_rel_l2_vs_fp64_median": float(np.median(err)),
             "timing": "host wall clock around run + sync (many streams: one per disk)"}
 

@@ -22,10 +22,16 @@ synchronises the device after every launch, so host time is its device time).
 Output: oracle/_ref/fargoGPU_sm103a, run as `echo 0 | fargoGPU_sm103a file.par`.
 
 Only configurations whose kernels were read for out-of-bounds access may run on a
-GPU: the isothermal disk with closed (WALL) boundaries and no self-gravity (every
-kernel on that path guards i < nrad, j < nsec and indexes inside its allocation;
-DeviceReduce never sees N = 1).  The non-reflecting boundary
-(NonReflectingBoundaryKernel2, src/Kernels.cu:575, no j < nsec guard) and
+GPU: disks with closed (WALL) boundaries and no self-gravity, isothermal (C1) or
+adiabatic with cooling and alpha viscosity (C3).  Every kernel on those paths
+guards i < nrad, j < nsec and indexes inside its allocation; DeviceReduce never
+sees N = 1.  The energy path adds ComputeSoundSpeedKernel, Substep3Kernel
+(i > 0), Substep3Kernel2 (i == 0 reads rings 1 and 2; the update guards i < nrad),
+ComputeTemperatureFieldKernel and Make1DprofileKernel (i < nrad into an NRAD-long
+profile), and the host arrays EnergyMed, SigmaMed, CoolingTimeMed, QplusMed and
+viscosity_array_d are NRAD + 1 long (src/Kernels.cu:56-115, 167-215, 610-646;
+src/Main.cu:623-630, 729-732; src/SourceEuler.cu:412).  The non-reflecting
+boundary (NonReflectingBoundaryKernel2, src/Kernels.cu:575, no j < nsec guard) and
 self-gravity (Update_sgvelocityKernel, src/Kernels.cu:930, index -1) are not run.
 """
 import concurrent.futures as cf

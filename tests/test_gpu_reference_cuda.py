@@ -2,11 +2,13 @@
 
 oracle/_ref/fargoGPU_sm103a is the reference's src/*.cu compiled by nvcc for
 sm_103a with two source-compat fixes (oracle/ref_cuda/build_ref_cuda.py).  It runs
-the isothermal 128 x 384 disk (configs/c1_isothermal.par: WALL boundaries, no
-self-gravity -- the configuration whose kernels were read for out-of-bounds access)
-for three DTs with a dump before each.  The same disk advanced by this code in FP64
-must take the same number of hydro substeps in every DT and match the reference's
-gasdens / gasvrad / gasvtheta dumps after one and two DTs within 1e-9 relative.
+the configurations whose kernels were read for out-of-bounds access (WALL
+boundaries, no self-gravity): the isothermal 128 x 384 disk
+(configs/c1_isothermal.par) and the adiabatic disk with cooling and alpha viscosity
+(configs/c3_adiabatic.par) at 128 x 384, for three DTs with a dump before each.
+The same disk advanced by this code in FP64 must take the same number of hydro
+substeps in every DT and match the reference's gasdens / gasvrad / gasvtheta (and
+gasenergy) dumps after one and two DTs within 1e-9 relative.
 """
 import os
 
@@ -20,20 +22,23 @@ from tests.helpers import rel_l2, rel_linf
 pytestmark = pytest.mark.gpu
 
 
-def test_reference_cuda_build_matches_fp64_path(tmp_path):
+@pytest.mark.parametrize("cfg,size", [("c1", None), ("c3", (128, 384))])
+def test_reference_cuda_build_matches_fp64_path(tmp_path, cfg, size):
     if not os.path.exists(bench.REF_CUDA_EXE):
         err = bench.REF_CUDA_EXE + ".build_error"
         pytest.fail(open(err).read() if os.path.exists(err) else "the reference's CUDA build is missing")
     out = str(tmp_path / "out")
-    steps, cells = bench.run_reference_exe(bench.REF_CUDA_EXE, "c1", 3, ninterm=1, outdir=out)
+    over = {"NRAD": size[0], "NSEC": size[1], "WRITEENERGY": "YES"} if size else None
+    steps, cells = bench.run_reference_exe(bench.REF_CUDA_EXE, cfg, 3, ninterm=1, outdir=out, overrides=over)
     assert len(steps) == 3
-    params, planets = fg.load_config("c1")
+    params, planets = fg.load_config(cfg, **({"nrad": size[0], "nsec": size[1]} if size else {}))
     disk = fg.Disk(params, planets, fg.FARGO_FP64)
+    names = ("dens", "vrad", "vtheta") + (("energy",) if params.adiabatic else ())
     try:
         shape = (params.nrad, params.nsec)
         for k in (1, 2):
             assert disk.step_DT() == steps[k - 1][0], (k, steps[k - 1])
-            for name in ("dens", "vrad", "vtheta"):
+            for name in names:
                 ref = np.fromfile(os.path.join(out, name, f"{name}{k}.dat"), dtype=np.float64).reshape(shape)
                 mine = disk.field(name)[:-1]
                 full_ref = np.vstack([ref, np.zeros((1, params.nsec))])
