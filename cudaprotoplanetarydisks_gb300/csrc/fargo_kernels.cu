@@ -2105,10 +2105,10 @@ __device__ __forceinline__ const KArgs<T> *batch_block(const BatchGroup<T> &G, u
 // The body reads the disk's arguments in place (for T = double through the
 // out-of-line body shared with the single-disk kernel).  (Copying them into
 // shared memory first measured 5% faster on the 64-disk ensemble but changed the
-// last bits of the inlined FP32 bodies against the single-disk kernels.)
- A launched block may
-// cover several consecutive blocks of its disk's grid along x (the per-cell
-// kernels: the table read and the done test are paid once for all of them).
+// last bits of the inlined FP32 bodies against the single-disk kernels.)  A
+// launched block may cover several consecutive blocks of its disk's grid along x
+// (the per-cell kernels: the table read and the done test are paid once for all
+// of them).
 #define FARGO_BATCHED(kname, bounds, body, ...)                                  \
   template <class T>                                                             \
   __global__ void __launch_bounds__(bounds) kname(BatchGroup<T> G) {             \
