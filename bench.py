@@ -199,7 +199,7 @@ def kernel_bytes(name, params, esize):
         "k_visc_tau": 3 + 4,
         "k_visc_update": 6 + 2,
         "k_artvisc": (3 + ad) + (2 + ad),
-        "k_energy": 8 + 2,
+        "k_energy": 4 + 3,  # vrad, vtheta, dens, energyint in; divv, qplus, energy out
         "k_transport_radial": (3 + ad) + (5 + ad),
         "k_transport_radial_tma": (3 + ad) + (5 + ad),
         "k_transport_radial_col": (3 + ad) + (5 + ad),
@@ -686,12 +686,16 @@ def run_own(args, world, rank, local):
                     "dens_rel_l2_by_orbit": {r["orbits"]: r["dens"]["rel_l2"] for r in dr["by_orbit"]},
                     "control_dens_rel_l2_by_orbit": {r["orbits"]: r["control_dens"]["rel_l2"]
                                                      for r in dr["by_orbit"]},
+                    "control32_dens_rel_l2_by_orbit": {r["orbits"]: r["control32_dens"]["rel_l2"]
+                                                       for r in dr["by_orbit"]},
                     "seconds": dr["seconds_fp64"] + dr["seconds_fp32"]}
         d2 = drift_obj("c2")
         line["fp32_drift_100_orbits"] = {
             "against": "FP64 mode of this code from the same initial state",
             "control": "FP64 from the same state with the density perturbed by one unit in the last place: "
                        "how much the flow itself amplifies the smallest perturbation",
+            "control32": "FP64 from the same state with the density perturbed by one FP32 rounding (2^-24): "
+                         "how much the flow amplifies a single FP32-sized error",
             "target": 1e-5, "dens_rel_l2": d2["dens_rel_l2"], "c2": d2, "c1": drift_obj("c1")}
     if not args.no_batch and world == 1:
         line["batch_c4"] = batch_ensemble()

@@ -1372,7 +1372,6 @@ int fused_build(fargo_fused *f, fargo_ctx *const *disks, int n, int by_width, st
                     group(BK_VISC_TAU, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
                     group(BK_VISC_UPDATE, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
                     group(BK_ARTVISC, w, all, cells, b2, 0, 0, FUSED_CELL_MERGE),
-                    group(BK_VISC_TAU, w, adiabatic, cells, b2, 0, 1, FUSED_CELL_MERGE),
                     group(BK_ENERGY, w, adiabatic, cells, b2, 0, 0, FUSED_CELL_MERGE),
                     group(BK_RADIAL, w, rad_tile, tiles, dim3(32, RAD_NY_HOST), rad_smem_bytes(sizeof(T)), 0),
                     group(BK_RADIAL_COL, w, rad_col, columns, dim3(RADC_THREADS), 0, 0),

@@ -11,8 +11,10 @@
 //   k_visc_tau          ViscousTermsKernel
 //   k_visc_update       UpdateVelocitiesKernel + ApplySubKeplerianBoundaryKernel
 //   k_artvisc           Substep2Kernel + kernel + ActualiseGasVrad/Vtheta
-//   [k_visc_tau, k_energy]  Substep3 (energy equation)
+//   [k_energy]          ViscousTermsKernel on the new velocities + Substep3 (energy
+//                       equation): the stresses stay in registers
 //   k_transport_radial  LRMomenta + OneWindRad (all conserved quantities at once)
+//                       (or k_transport_radial_tma / k_transport_radial_col)
 //   k_transport_azimuthal  OneWindTheta: ring mean, FARGO split, two van Leer
 //                       sweeps and the integer shift, one CTA per ring
 //   k_velocities        ComputeVelocities (+ ComputeTemperatureField)
@@ -908,13 +910,16 @@ __global__ void __launch_bounds__(256) k_source(const __grid_constant__ KArgs<T>
   FARGO_RUN_BODY(T, source_body, a, FARGO_BID);
 }
 
-// ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens.
+// ViscousTermsKernel src/Kernels.cu:733-771 on (vr, vt) with the density dens, for
+// one cell: the velocity divergence and the stresses (tau_rphi only for i > 0)
 template <class T>
-__device__ __forceinline__ void visc_tau_body(const KArgs<T> &a, const uint3 bid, const T *__restrict__ vr, const T *__restrict__ vt) {
-  
-  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
-  const int nrad = a.P.nrad, nsec = a.P.nsec;
-  if (i >= nrad || j >= nsec) return;
+struct ViscCell {
+  T divv, trr, tpp, trp;
+};
+template <class T>
+__device__ __forceinline__ ViscCell<T> visc_tau_cell(const KArgs<T> &a, int i, int j, const T *__restrict__ vr,
+                                                     const T *__restrict__ vt) {
+  const int nsec = a.P.nsec;
   const int jm = jm1(j, nsec), jp = jp1(j, nsec);
   const size_t q = (size_t)i * nsec + j, qp = (size_t)i * nsec + jp, qm = (size_t)i * nsec + jm;
   const T *D = a.d.dens;
@@ -925,14 +930,29 @@ __device__ __forceinline__ void visc_tau_body(const KArgs<T> &a, const uint3 bid
   T divv = (vr[q + nsec] * RT(a, RT_RSUP, i) - vr[q] * RT(a, RT_RINF, i)) * idrs * irm;
   divv += (vt[qp] - vt[q]) * invdphi * irm;
   const T nu = a.d.nu[i];
-  a.d.divv[q] = divv;
-  a.d.taurr[q] = (T)2.0 * D[q] * nu * (drr - onethird * divv);
-  a.d.taupp[q] = (T)2.0 * D[q] * nu * (dpp - onethird * divv);
+  ViscCell<T> c;
+  c.divv = divv;
+  c.trr = (T)2.0 * D[q] * nu * (drr - onethird * divv);
+  c.tpp = (T)2.0 * D[q] * nu * (dpp - onethird * divv);
+  c.trp = (T)0.0;
   if (i > 0) {
     const T drp = (T)0.5 * (RT(a, RT_RINF, i) * (vt[q] * irm - vt[q - nsec] * RT(a, RT_INVRMED, i - 1)) * RT(a, RT_INVDIFFRMED, i) +
                             (vr[q] - vr[qm]) * invdphi * RT(a, RT_INVRINF, i));
-    a.d.taurp[q] = (T)(2.0 * 0.25) * (D[q] + D[q - nsec] + D[qm] + D[qm - nsec]) * nu * drp;
+    c.trp = (T)(2.0 * 0.25) * (D[q] + D[q - nsec] + D[qm] + D[qm - nsec]) * nu * drp;
   }
+  return c;
+}
+template <class T>
+__device__ __forceinline__ void visc_tau_body(const KArgs<T> &a, const uint3 bid, const T *__restrict__ vr, const T *__restrict__ vt) {
+  const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
+  const int nrad = a.P.nrad, nsec = a.P.nsec;
+  if (i >= nrad || j >= nsec) return;
+  const ViscCell<T> c = visc_tau_cell(a, i, j, vr, vt);
+  const size_t q = (size_t)i * nsec + j;
+  a.d.divv[q] = c.divv;
+  a.d.taurr[q] = c.trr;
+  a.d.taupp[q] = c.tpp;
+  if (i > 0) a.d.taurp[q] = c.trp;
 }
 FARGO_F64_BODY(visc_tau_body)
 template <class T>
@@ -1034,39 +1054,43 @@ __global__ void __launch_bounds__(256) k_artvisc(const __grid_constant__ KArgs<T
   FARGO_RUN_BODY(T, artvisc_body, a, FARGO_BID);
 }
 
-// Substep3Kernel + Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
+// ViscousTermsKernel (src/Kernels.cu:733-771) on the new velocities + Substep3Kernel +
+// Substep3Kernel2 (src/Kernels.cu:56-115) + ActualiseGasEnergy.
 template <class T>
 __device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) {
   
   const int j = bid.x * blockDim.x + threadIdx.x, i = bid.y * blockDim.y + threadIdx.y;
   const int nrad = a.P.nrad, nsec = a.P.nsec;
   if (i >= nrad || j >= nsec) return;
-  const double g = a.P.adiabaticindex;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
   const T *D = a.d.dens;
-  auto qplus = [&](int ii) -> T {
+  // ViscousTermsKernel on the new velocities (src/SourceEuler.cu:362-375), cell by
+  // cell in registers: no stress field goes through memory
+  const ViscCell<T> c0 = visc_tau_cell(a, i, j, a.d.vrad, a.d.vtheta);
+  auto qplus = [&](int ii, const ViscCell<T> &c) -> T {
     const size_t k = (size_t)ii * nsec + j;
     const T nu = a.d.nu[ii];
     if (nu != (T)0.0) {
-      T qp = qdiv(qdiv((T)0.5, nu), D[k]) *
-             (a.d.taurr[k] * a.d.taurr[k] + a.d.taurp[k] * a.d.taurp[k] + a.d.taupp[k] * a.d.taupp[k]);
-      qp += (T)(2.0 / 9.0) * nu * D[k] * a.d.divv[k] * a.d.divv[k];
+      T qp = qdiv(qdiv((T)0.5, nu), D[k]) * (c.trr * c.trr + c.trp * c.trp + c.tpp * c.tpp);
+      qp += (T)(2.0 / 9.0) * nu * D[k] * c.divv * c.divv;
       return qp;
     }
     return (T)0.0;
   };
   T qp;
   if (i > 0) {
-    qp = qplus(i);
+    qp = qplus(i, c0);
   } else if (a.d.nu[nrad - 1] != (T)0.0) {
-    const T q1 = qplus(1), q2 = qplus(2);
+    const T q1 = qplus(1, visc_tau_cell(a, 1, j, a.d.vrad, a.d.vtheta));
+    const T q2 = qplus(2, visc_tau_cell(a, 2, j, a.d.vrad, a.d.vtheta));
     qp = q1 * exp(log(q1 / q2) * (T)a.lr01 / (T)a.lr12);
   } else {
     qp = (T)0.0;
   }
   const size_t q = (size_t)i * nsec + j;
+  a.d.divv[q] = c0.divv;
   a.d.qplus[q] = qp;
-  const T ei = a.d.energyint[q], dv = a.d.divv[q];
+  const T ei = a.d.energyint[q], dv = c0.divv;
   T enew;
   if (!a.P.cooling) {
     T num = dt * qp + ei;
@@ -2322,8 +2346,7 @@ void launch_substep_kernels(const KArgs<T> &a0, cudaStream_t s, unsigned which_m
   }
   if (which_mask & SUBK_BC2) launch_boundaries(a, s);
   if ((which_mask & SUBK_ENERGY) && P.adiabatic) {
-    launch_k(a.pdl, k_visc_tau<T>, dim3(g2), dim3(b2), 0, s, a, a.d.vrad, a.d.vtheta);
-    MARK("k_visc_tau");
+    // the viscous stresses of the new velocities are formed inside k_energy
     launch_k(a.pdl, k_energy<T>, dim3(g2), dim3(b2), 0, s, a);
     MARK("k_energy");
   }
