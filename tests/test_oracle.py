@@ -6,7 +6,7 @@ import pytest
 
 import cudaprotoplanetarydisks_gb300 as fg
 from oracle import oracle as orc
-from tests.helpers import disk_mass, small
+from tests.helpers import disk_mass, sg_direct_sum, small
 
 
 @pytest.mark.parametrize("shape", [(8, 6), (16, 12), (64, 48), (256, 384), (10, 7), (128, 66)])
@@ -116,3 +116,19 @@ def test_cfl_count_and_time():
     s = o.scalars()
     assert n >= 1 and s.substeps == n
     assert abs(s.physical_time - p.dt) <= 1e-12
+
+
+def test_self_gravity_matches_a_direct_convolution():
+    # the oracle's FFT self-gravity of the initial 16 x 32 self-gravitating disk
+    # against the direct sum of its kernels
+    params, planets = small("c2", nrad=16, nsec=32)
+    o = orc.OracleDisk(params, planets)
+    try:
+        rinf, rmed, _, _ = o.mesh()
+        accr, acct = sg_direct_sum(params, rinf, rmed, o.field("dens"))
+        n = params.nrad
+        er = float(np.abs(o.field("sg_accr")[:n] - accr).max() / np.abs(accr).max())
+        et = float(np.abs(o.field("sg_acct")[:n] - acct).max() / np.abs(acct).max())
+    finally:
+        o.close()
+    assert er < 1e-6 and et < 1e-6, (er, et)
