@@ -423,13 +423,15 @@ def _par_values(text):
     return vals
 
 
-def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=1000000000, outdir=None, overrides=None):
+def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=1000000000, outdir=None, overrides=None,
+                      planet_mass=None):
     """Runs a build of the reference's main() (oracle/_ref: its CPU build or its own
     CUDA build) on the workload's .par for ndt DTs (Ntot = ndt - 1: the reference
     runs Ntot + 1), the DT divided by dt_divisor, dumps every `ninterm` DTs into
     outdir (a temporary directory when None), the seeded noise of the .par's
     SigmaNoise / EnergyNoise / NoiseSeed keys through the build's link-time
-    wrappers; overrides replaces .par keys (e.g. {"NRAD": 128, "NSEC": 384}).
+    wrappers; overrides replaces .par keys (e.g. {"NRAD": 128, "NSEC": 384}) and
+    planet_mass the mass column of the planet file.
     Returns ([(substeps, AlgoGas seconds) per DT], cells) from the binary's
     REFSTEP lines.  Reads no product code."""
     if not os.path.exists(exe):
@@ -462,7 +464,12 @@ def run_reference_exe(exe, cfg, ndt, env_extra=None, dt_divisor=1.0, ninterm=100
             # (src/Main.cu:248-249): a short copy beside the run
             cfg_path = os.path.join(d, "planet.cfg")
             with open(os.path.join(CONFIG_DIR, vals["PLANETCONFIG"])) as f_in, open(cfg_path, "w") as f_out:
-                f_out.write(f_in.read())
+                for line in f_in.read().splitlines():
+                    tok = line.split()
+                    if planet_mass is not None and tok and not tok[0].startswith("#") and len(tok) >= 3:
+                        tok[2] = repr(float(planet_mass))
+                        line = "  ".join(tok)
+                    f_out.write(line + "\n")
             keep.append(f"PlanetConfig {cfg_path}")
         par = os.path.join(d, "run.par")
         open(par, "w").write("\n".join(keep) + "\n")
@@ -522,7 +529,37 @@ def reference_cuda(fg, stream, flush):
     out["c3"] = {"workload": WORKLOADS["c3"], "config_file": "configs/" + CONFIG_FILES["c3"],
                  "value": n3 * cells3 / t3, "unit": METRIC, "dtype": "f64", "substeps": n3, "seconds": t3,
                  "timing": "host clock around each AlgoGas call, DTs 2..3"}
+    out["c4_sequential"] = reference_cuda_c4()
     return out
+
+
+def c4_overrides(d):
+    """.par keys of an ensemble disk (config.c4_draws) over the isothermal c1 file."""
+    return {"NRAD": d["nrad"], "NSEC": d["nsec"], "VISCOSITY": 0.0, "ALPHAVISCOSITY": repr(d["alpha"]),
+            "ASPECTRATIO": repr(d["h"]), "SIGMASLOPE": repr(d["slope"]), "SIGMA0": 6.3662e-4,
+            "SIGMANOISE": 1e-4, "NOISESEED": d["noise_seed"]}
+
+
+def reference_cuda_c4(n=64, ndt=2):
+    """The ensemble's baseline: the 64 disks of the batched workload as 64
+    sequential runs of the reference's own CUDA build (isothermal, alpha viscosity,
+    WALL boundaries, no self-gravity: the kernels read for out-of-bounds access),
+    one process each, ndt DTs with the first untimed.  The disks' draws come from
+    config.c4_draws; .par keys per disk, the planet file's mass per disk."""
+    from cudaprotoplanetarydisks_gb300.config import c4_draws
+    tot_n = tot_t = 0.0
+    subs = 0
+    for d in c4_draws(n):
+        steps, cells = run_reference_exe(REF_CUDA_EXE, "c1", ndt, overrides=c4_overrides(d), planet_mass=d["q"])
+        ns = sum(s for s, _ in steps[1:])
+        subs += ns
+        tot_n += ns * cells
+        tot_t += sum(x for _, x in steps[1:])
+    return {"workload": f"the {n} seeded disks of batch_c4 (Nrad 128-512, Nsec = 3 Nrad, isothermal, alpha, one "
+                        "planet each), one reference process per disk, one after another",
+            "value": tot_n / tot_t, "unit": METRIC, "dtype": "f64", "substeps": subs, "seconds": tot_t,
+            "timing": f"host clock around each AlgoGas call, DTs 2..{ndt} of every disk (process start-up and "
+                      "set-up not counted)"}
 
 
 def cpu_baselines(cfg, params, planets):

@@ -77,6 +77,16 @@ def load_config(name_or_path, **overrides):
         if isinstance(v, str):
             v = v.encode()
         setattr(params, k, v)
+    # the switches the .par reader derives from these values (fargo_params_read's
+    # last step, after src/Interpret.cu's checks)
+    if "alphaviscosity" in overrides or "viscosity" in overrides:
+        if params.alphaviscosity != 0.0 and params.viscosity != 0.0:
+            raise ValueError("VISCOSITY and ALPHAVISCOSITY cannot both be set")
+        params.viscosity_alpha = 1 if params.alphaviscosity != 0.0 else 0
+    if "rochesmoothing" in overrides or "thicknesssmoothing" in overrides:
+        if params.thicknesssmoothing != 0.0 and params.rochesmoothing != 0.0:
+            raise ValueError("THICKNESSSMOOTHING and ROCHESMOOTHING cannot both be set")
+        params.roche_smoothing = 1 if params.rochesmoothing != 0.0 else 0
     return params, planets
 
 
@@ -84,14 +94,11 @@ def load_config(name_or_path, **overrides):
 C4_NRAD = (128, 192, 256, 384, 512)
 
 
-def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD, sigma_noise=1e-4):
-    """(params, planets) of n seeded disks: the isothermal c1 setup (log grid on
-    [0.4, 2.5], one planet on a fixed circular orbit at r = 1, FARGO transport)
-    with per-disk draws: Nrad uniform in nrad_choices, Nsec = 3 Nrad; planet mass
-    ratio q log-uniform in [1e-5, 3e-3]; alpha viscosity log-uniform in
-    [1e-4, 1e-2]; aspect ratio h uniform in [0.03, 0.08]; Sigma slope uniform in
-    [0, 1.5]; Sigma0 = 6.3662e-4; density noise of relative amplitude sigma_noise
-    seeded per disk."""
+def c4_draws(n=64, seed=2024, nrad_choices=C4_NRAD):
+    """The seeded per-disk draws of the ensemble workload, one dict per disk:
+    nrad uniform in nrad_choices (nsec = 3 nrad); planet mass ratio q log-uniform in
+    [1e-5, 3e-3]; alpha viscosity log-uniform in [1e-4, 1e-2]; aspect ratio h
+    uniform in [0.03, 0.08]; Sigma slope uniform in [0, 1.5]; the disk's noise seed."""
     import numpy as np
     rng = np.random.Generator(np.random.PCG64(seed))
     out = []
@@ -101,9 +108,34 @@ def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD, sigma_noise=1e-4):
         alpha = float(10 ** rng.uniform(-4.0, -2.0))
         h = float(rng.uniform(0.03, 0.08))
         slope = float(rng.uniform(0.0, 1.5))
-        params, planets = load_config("c1", nrad=nrad, nsec=3 * nrad, viscosity=0.0, alphaviscosity=alpha,
-                                      aspectratio=h, sigmaslope=slope, sigma0=6.3662e-4,
-                                      noise_seed=seed * 1000 + k + 1, sigma_noise=sigma_noise)
-        planets[0].mass = q
+        out.append({"nrad": nrad, "nsec": 3 * nrad, "q": q, "alpha": alpha, "h": h, "slope": slope,
+                    "noise_seed": seed * 1000 + k + 1})
+    return out
+
+
+def c4_disks(n=64, seed=2024, nrad_choices=C4_NRAD, sigma_noise=1e-4):
+    """(params, planets) of n seeded disks: the isothermal c1 setup (log grid on
+    [0.4, 2.5], one planet on a fixed circular orbit at r = 1, FARGO transport)
+    with the per-disk draws of c4_draws, no uniform viscosity, Sigma0 = 6.3662e-4
+    and density noise of relative amplitude sigma_noise seeded per disk."""
+    out = []
+    for d in c4_draws(n, seed, nrad_choices):
+        params, planets = load_config("c1", nrad=d["nrad"], nsec=d["nsec"], viscosity=0.0, alphaviscosity=d["alpha"],
+                                      aspectratio=d["h"], sigmaslope=d["slope"], sigma0=6.3662e-4,
+                                      noise_seed=d["noise_seed"], sigma_noise=sigma_noise)
+        set_planet_mass(params, planets[0], d["q"])
         out.append((params, planets))
     return out
+
+
+def set_planet_mass(params, planet, mass):
+    """A planet of the planet file read with another mass: the mass and the initial
+    velocity that InitPlanetarySystem derives from it (src/Psys.cu: vy =
+    sqrt((1 + m) / d) sqrt((1 - e) / (1 + e)), vx = -1e-10 vy, d the file's
+    distance, here x / (1 + e), exact for the circular orbits of the workloads)."""
+    import math
+    e = params.eccentricity
+    dist = planet.x / (1.0 + e)
+    planet.mass = mass
+    planet.vy = math.sqrt(1.0 * (1.0 + mass) / dist) * math.sqrt((1.0 - e) / (1.0 + e))
+    planet.vx = -0.0000000001 * planet.vy

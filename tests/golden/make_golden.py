@@ -74,6 +74,19 @@ Rmax 3.0
 Frame FIXED
 EnergyNoise 1e-4
 """, PLANET_FIXED),
+    # an ensemble disk: isothermal with alpha viscosity and a Sigma slope away from
+    # 1/2 (the initial viscous drift is not zero), a low-mass planet
+    "iso_alpha": ("""AspectRatio 0.0788
+Sigma0 6.3662e-4
+AlphaViscosity 8.5e-4
+SigmaSlope 1.2
+ForcedCircular YES
+ThicknessSmoothing 0.6
+Rmin 0.4
+Rmax 2.5
+Frame FIXED
+InnerBoundary WALL
+""", "Earthlike 1.0 1.0267e-05 0.0 NO NO\n"),
     "corotating_rk5": ("""AspectRatio 0.05
 Sigma0 8.84194128288308e-4
 AlphaViscosity 1e-3

@@ -6,7 +6,7 @@ order on one host thread and DeviceReduceKernel's blocks run as cooperative fibe
 The build now restates DeviceReduce's summation order without fibers
 (oracle/ref_emul/reduce_wrap.cpp) and may run the blocks of a launch on several
 host threads (FARGO_REF_THREADS).  Neither may change a bit: every dumped field
-and planet row of the seven cases must be reproduced exactly, on one thread and on
+and planet row of the eight cases must be reproduced exactly, on one thread and on
 four.  This build is bench.py's reference arm.
 """
 import os
@@ -26,7 +26,7 @@ pytestmark = pytest.mark.skipif(not os.path.exists(EXE), reason="the CPU build o
 
 @pytest.mark.parametrize("threads", ["1", "4"])
 @pytest.mark.parametrize("name", ["iso", "open", "evanescent", "nonreflecting", "adiabatic_cooling",
-                                  "corotating_rk5", "selfgravity"])
+                                  "corotating_rk5", "selfgravity", "iso_alpha"])
 def test_reference_cpu_build_reproduces_fixture(name, threads, monkeypatch):
     import make_golden as mg
     rec_file = dict(np.load(os.path.join(HERE, "golden", f"ref_{name}.npz")))
