@@ -60,3 +60,81 @@ def sg_direct_sum(params, rinf, rmed, dens):
     accr = -gr * rstep * tstep / np.sqrt(div) + dens * rstep * tstep / eps
     acct = -gt * rstep * tstep / (div * np.sqrt(div))
     return accr, acct
+
+
+def lbp_profile(r, tau, nu, mass=1.0, r0=1.0):
+    """Lynden-Bell & Pringle (1974) spreading ring: Sigma(x, tau) = (M / (pi R0^2))
+    tau^-1 x^-1/4 exp(-(1 + x^2) / tau) I_1/4(2 x / tau), x = r / R0, tau = 12 nu t / R0^2."""
+    import math
+    from scipy.special import ive
+    x = r / r0
+    z = 2 * x / tau
+    # I_1/4(z) exp(-(1 + x^2)/tau) = ive(z) exp(z - (1 + x^2)/tau) = ive(z) exp(-(1 - x)^2 / tau)
+    return mass / (math.pi * r0 ** 2) / tau * x ** -0.25 * np.exp(-(1 - x) ** 2 / tau) * ive(0.25, z)
+
+
+def _massless_planet(cfg, **kw):
+    from cudaprotoplanetarydisks_gb300.config import set_planet_mass
+    params, planets = fg.load_config(cfg, **kw)
+    set_planet_mass(params, planets[0], 0.0)
+    return params, planets
+
+
+def rest_state(make):
+    """One orbit of the c1 disk without viscosity, noise or planet mass, from
+    make(params, planets) (an FP64 disk with field / step_DT / close).  Returns
+    (max |dSigma| / max Sigma, max |v_r| of the inner interfaces, the largest
+    departure from axisymmetry relative to max Sigma, c_s / v_K)."""
+    import math
+    params, planets = _massless_planet("c1", sigma_noise=0.0, viscosity=0.0)
+    disk = make(params, planets)
+    try:
+        s0 = disk.field("dens")[:-1].copy()
+        for _ in range(int(round(2 * math.pi / params.dt))):
+            disk.step_DT()
+        s1 = disk.field("dens")[:-1]
+        vr = disk.field("vrad")[1:-1]
+        return (float(np.abs(s1 - s0).max() / np.abs(s0).max()), float(np.abs(vr).max()),
+                float(np.abs(s1 - s1.mean(axis=1, keepdims=True)).max() / np.abs(s1).max()), params.aspectratio)
+    finally:
+        disk.close()
+
+
+def lbp_ring(make, nu=1e-4, tau0=0.016, tau1=0.032):
+    """A Lynden-Bell & Pringle ring (constant nu, aspect ratio 1e-3, 256 x 384 on
+    [0.4, 2.5], WALL boundaries) started from the solution at tau0 -- Keplerian
+    rotation, v_r = -3 / (Sigma r^1/2) d(nu Sigma r^1/2) / dr at the interfaces --
+    and advanced whole DTs to about tau1.  Returns (relative L2 error of the ring
+    means against the solution where it exceeds 1e-3 of its peak, relative mass
+    change, DTs, reached tau)."""
+    params, planets = _massless_planet("c1", sigma_noise=0.0, viscosity=nu, aspectratio=1e-3, nrad=256, nsec=384,
+                                       rmin=0.4, rmax=2.5)
+    disk = make(params, planets)
+    try:
+        rinf, rmed, rsup, surf = disk.mesh()
+        n, ns = params.nrad, params.nsec
+        sig = np.zeros((n + 1, ns))
+        sig[:n] = lbp_profile(rmed[:n], tau0, nu)[:, None]
+        floor = 1e-10 * sig.max()
+        sig[:n] += floor
+        ri = rinf[:n]
+        h = 1e-6
+        g = lambda r: nu * (lbp_profile(r, tau0, nu) + floor) * np.sqrt(r)  # noqa: E731
+        vr_i = -3.0 / ((lbp_profile(ri, tau0, nu) + floor) * np.sqrt(ri)) * (g(ri * (1 + h)) - g(ri * (1 - h))) / (2 * h * ri)
+        vr = np.zeros((n + 1, ns))
+        vr[1:n] = vr_i[1:, None]  # the wall rings keep v_r = 0
+        vt = np.zeros((n + 1, ns))
+        vt[:n] = (rmed[:n] ** -0.5)[:, None]
+        disk.set_fields(dens=sig, vrad=vr, vtheta=vt)
+        m0 = float((disk.field("dens")[:n] * surf[:n, None]).sum())
+        ndt = int(round((tau1 - tau0) / (12 * nu) / params.dt))
+        for _ in range(ndt):
+            disk.step_DT()
+        tau = tau0 + 12 * nu * ndt * params.dt
+        got = disk.field("dens")[:n].mean(axis=1) - floor
+        ref = lbp_profile(rmed[:n], tau, nu)
+        m1 = float((disk.field("dens")[:n] * surf[:n, None]).sum())
+        mask = ref > 1e-3 * ref.max()
+        return float(np.linalg.norm((got - ref)[mask]) / np.linalg.norm(ref[mask])), abs(m1 - m0) / m0, ndt, tau
+    finally:
+        disk.close()

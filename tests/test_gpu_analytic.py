@@ -1,6 +1,11 @@
 """Analytic checks of the FP64 step, independent of the oracle.
 
-* Rest state: a disk without planet, viscosity or noise starts in the
+Both hydro checks keep the planet file's planet with zero mass: the star's potential
+enters the reference's potential together with the first planet
+(FillForcesArrays / FillForcesArraysKernel, src/Pframeforce.cu:67-80,
+src/Kernels.cu:1246-1251), so a disk with no planet at all feels no gravity.
+
+* Rest state: a disk with a massless planet, no viscosity and no noise starts in the
   equilibrium the set-up builds (pressure-supported rotation, no radial flow) and
   stays there: over one orbit the density changes, and the radial velocity grows,
   only at the level of the discretisation error of that equilibrium.
@@ -16,84 +21,37 @@
   from them).
 * Self-gravity: the FFT convolution against a direct sum of the same kernels.
 """
-import math
-
 import numpy as np
 import pytest
 
 import cudaprotoplanetarydisks_gb300 as fg
-from tests.helpers import sg_direct_sum
+from tests.helpers import lbp_ring, rest_state, sg_direct_sum
 
 pytestmark = pytest.mark.gpu
 
 
+def _fp64(params, planets):
+    return fg.Disk(params, planets, fg.FARGO_FP64)
+
+
 def test_rest_state_stays_steady():
-    params, _ = fg.load_config("c1", sigma_noise=0.0, viscosity=0.0)
-    disk = fg.Disk(params, [], fg.FARGO_FP64)
-    try:
-        s0 = disk.field("dens")[:-1].copy()
-        cs = params.aspectratio  # cs / v_K
-        orbit = int(round(2 * math.pi / params.dt))
-        disk.run(orbit)
-        s1 = disk.field("dens")[:-1]
-        vr = disk.field("vrad")[1:-1]
-        ds = float(np.abs(s1 - s0).max() / np.abs(s0).max())
-        vr_max = float(np.abs(vr).max())
-        print(f"one orbit at rest: max |dSigma|/Sigma {ds:.2e}, max |v_r| {vr_max:.2e} (c_s/v_K = {cs})")
-        # axisymmetric to rounding, and steady to well below the sound speed's level
-        assert float(np.abs(s1 - s1.mean(axis=1, keepdims=True)).max() / np.abs(s1).max()) < 1e-12
-        assert ds < 1e-3
-        assert vr_max < 1e-2 * cs
-    finally:
-        disk.close()
-
-
-def _lbp(r, tau, nu, mass=1.0, r0=1.0):
-    from scipy.special import ive
-    x = r / r0
-    z = 2 * x / tau
-    # I_1/4(z) exp(-(1 + x^2)/tau) = ive(z) exp(z - (1 + x^2)/tau) = ive(z) exp(-(1 - x)^2 / tau)
-    return mass / (math.pi * r0 ** 2) / tau * x ** -0.25 * np.exp(-(1 - x) ** 2 / tau) * ive(0.25, z)
+    ds, vr_max, axi, cs = rest_state(_fp64)
+    print(f"one orbit at rest: max |dSigma|/Sigma {ds:.2e}, max |v_r| {vr_max:.2e} (c_s/v_K = {cs})")
+    # axisymmetric to rounding, and steady: the FP64 oracle gives 1.0e-3 and 1.0e-4
+    # (the set-up's rotation balances the analytic pressure gradient, not the
+    # discrete one)
+    assert axi < 1e-12
+    assert ds < 3e-3
+    assert vr_max < 1e-2 * cs
 
 
 def test_viscous_ring_spreading_matches_lynden_bell_pringle():
     pytest.importorskip("scipy")
-    nu, tau0, tau1 = 1e-4, 0.016, 0.032
-    params, _ = fg.load_config("c1", sigma_noise=0.0, viscosity=nu, aspectratio=1e-3, nrad=256, nsec=384,
-                               rmin=0.4, rmax=2.5)
-    disk = fg.Disk(params, [], fg.FARGO_FP64)
-    try:
-        rinf, rmed, rsup, surf = disk.mesh()
-        n, ns = params.nrad, params.nsec
-        sig = np.zeros((n + 1, ns))
-        sig[:n] = _lbp(rmed[:n], tau0, nu)[:, None]
-        floor = 1e-10 * sig.max()
-        sig[:n] += floor
-        # v_r at the interfaces r = rinf[i]: -3 / (Sigma r^1/2) d(nu Sigma r^1/2)/dr, from the solution
-        ri = rinf[:n]
-        h = 1e-6
-        g = lambda r: nu * (_lbp(r, tau0, nu) + floor) * np.sqrt(r)  # noqa: E731
-        vr_i = -3.0 / ((_lbp(ri, tau0, nu) + floor) * np.sqrt(ri)) * (g(ri * (1 + h)) - g(ri * (1 - h))) / (2 * h * ri)
-        vr = np.zeros((n + 1, ns))
-        vr[1:n] = vr_i[1:, None]  # the wall rings keep v_r = 0
-        vt = np.zeros((n + 1, ns))
-        vt[:n] = (rmed[:n] ** -0.5)[:, None]
-        disk.set_fields(dens=sig, vrad=vr, vtheta=vt)
-        m0 = float((disk.field("dens")[:n] * surf[:n, None]).sum())
-        t1 = (tau1 - tau0) / (12 * nu)
-        ndt = int(round(t1 / params.dt))
-        disk.run(ndt)
-        tau = tau0 + 12 * nu * ndt * params.dt
-        got = disk.field("dens")[:n].mean(axis=1) - floor
-        ref = _lbp(rmed[:n], tau, nu)
-        m1 = float((disk.field("dens")[:n] * surf[:n, None]).sum())
-        mask = ref > 1e-3 * ref.max()
-        err = float(np.linalg.norm((got - ref)[mask]) / np.linalg.norm(ref[mask]))
-        print(f"LBP ring, tau {tau0} -> {tau:.4f} ({ndt} DTs): relative L2 {err:.2e}, mass change {abs(m1 - m0) / m0:.1e}")
-        assert abs(m1 - m0) <= 1e-12 * m0
-        assert err < 0.05
-    finally:
-        disk.close()
+    err, dm, ndt, tau = lbp_ring(_fp64)
+    print(f"LBP ring to tau {tau:.4f} ({ndt} DTs): relative L2 {err:.2e}, mass change {dm:.1e}")
+    # the FP64 oracle gives 8.3e-4 over these 42 DTs (262 substeps)
+    assert dm <= 1e-12
+    assert err < 5e-3
 
 
 def test_self_gravity_matches_a_direct_convolution():

@@ -6,7 +6,7 @@ import pytest
 
 import cudaprotoplanetarydisks_gb300 as fg
 from oracle import oracle as orc
-from tests.helpers import disk_mass, sg_direct_sum, small
+from tests.helpers import disk_mass, lbp_ring, rest_state, sg_direct_sum, small
 
 
 @pytest.mark.parametrize("shape", [(8, 6), (16, 12), (64, 48), (256, 384), (10, 7), (128, 66)])
@@ -132,3 +132,14 @@ def test_self_gravity_matches_a_direct_convolution():
     finally:
         o.close()
     assert er < 1e-6 and et < 1e-6, (er, et)
+
+
+def test_rest_state_stays_steady():
+    ds, vr_max, axi, cs = rest_state(orc.OracleDisk)
+    assert axi < 1e-12 and ds < 3e-3 and vr_max < 1e-2 * cs, (axi, ds, vr_max)
+
+
+def test_viscous_ring_spreading_matches_lynden_bell_pringle():
+    pytest.importorskip("scipy")
+    err, dm, ndt, tau = lbp_ring(orc.OracleDisk)
+    assert dm <= 1e-12 and err < 5e-3, (dm, err)
