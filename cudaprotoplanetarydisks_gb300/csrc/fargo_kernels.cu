@@ -1195,7 +1195,7 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
         const T wm = t.sW[f][dd][x], w0 = t.sW[f][dd + 1][x], wp = t.sW[f][dd + 2][x];
         const T dqm = (w0 - wm) * idm0;
         const T dqp = (wp - w0) * idm1;
-        v = gt0(dqp * dqm) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+        v = gt0(dqp * dqm) ? lim_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
       }
       t.sD[f][dd][x] = v;
     }
@@ -1414,7 +1414,7 @@ __device__ __forceinline__ void radc_slope(const KArgs<T> &a, int k, const RadCo
       const T wm = m.w[f], w0 = c.w[f], wp = p.w[f];
       const T dqm = (w0 - wm) * idm0;
       const T dqp = (wp - w0) * idm1;
-      v = gt0(dqp * dqm) ? bulk_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+      v = gt0(dqp * dqm) ? lim_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
     }
     d[f] = v;
   }
@@ -1695,7 +1695,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   auto slope_at = [&](const T *q, int j) -> T {
     const T dqm = q[j] - q[jm1(j, nsec)];
     const T dqp = q[jp1(j, nsec)] - q[j];
-    return gt0(dqp * dqm) ? qdiv(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+    return gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
   };
   // QuantitiesAdvection with velocity vel[] (or the constant vconst).  Per
   // interface j (between cells j-1 and j) the upwind side, its slope coefficient
@@ -1928,7 +1928,7 @@ __device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 b
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
-      dq[k] = gt0(dqp * dqm) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+      dq[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
     }
 #pragma unroll
     for (int c = 0; c < 5; c++) {
@@ -1961,7 +1961,7 @@ __device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 b
 #pragma unroll
       for (int k = 0; k < 6; k++) {
         const T dqm = wv[k + 1] - wv[k], dqp = wv[k + 2] - wv[k + 1];
-        dw[k] = gt0(dqp * dqm) ? bulk_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+        dw[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
       }
 #pragma unroll
       for (int c = 0; c < 5; c++) sw[c] = (upw[c] ? wv[c + 1] : wv[c + 2]) + coef[c] * (upw[c] ? dw[c] : dw[c + 1]);
