@@ -1644,7 +1644,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(const __gr
 // and AdvectSHIFT (src/Kernels.cu:1049-1190).  The ring lives in shared memory
 // (or in global scratch when it does not fit); the FARGO shift is applied as an
 // index rotation when the ring is stored.
-#define AZ_NARR 12
+#define AZ_NARR 13
 template <class T>
 __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   pdl_enter();
@@ -1657,7 +1657,7 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   T *base = a.az_smem ? (T *)az_smem : a.d.az_scratch + (size_t)i * AZ_NARR * nsec;
   T *V = base, *Dn = base + nsec, *En = base + 2 * nsec, *M0 = base + 3 * nsec, *M1 = base + 4 * nsec,
     *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *FL = base + 9 * nsec,
-    *F = base + 10 * nsec, *ID = base + 11 * nsec;
+    *F = base + 10 * nsec, *ID = base + 11 * nsec, *CF = base + 12 * nsec;
   const Ctl *c = a.d.ctl;
   const double dt = c->dt;
   const size_t row = (size_t)i * nsec;
@@ -1691,20 +1691,25 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   const T dxtheta = RT(a, RT_DXTHETA, i), invdx = RT(a, RT_INVDXTHETA, i);
   const T dxrad = RT(a, RT_DRAD, i) * (T)dt, isurf = RT(a, RT_INVSURF, i);
   const T tdt = (T)dt;
-  // StarThetaKernel: harmonic slope of q at cell j
+  // StarThetaKernel: harmonic slope of q at cell j, times dxtheta (the 1/dxtheta
+  // of the slope is carried by the upwind coefficient CF)
   auto slope_at = [&](const T *q, int j) -> T {
     const T dqm = q[j] - q[jm1(j, nsec)];
     const T dqp = q[jp1(j, nsec)] - q[j];
-    return gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+    return gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;
   };
   // QuantitiesAdvection with velocity vel[] (or the constant vconst).  Per
   // interface j (between cells j-1 and j) the upwind side, its slope coefficient
   // and the mass flux dxrad Dstar v are the same for every quantity: ksi = v dt is
-  // kept in KS (the velocity's slot) and the flux factor in F, formed once per
-  // sweep; each quantity then needs its W = Q / rho, its slopes, one upwind value
-  // and flux per interface and its update (StarThetaKernel/2, DivisePolarGrid,
+  // kept in KS (the velocity's slot), the slope coefficient (dxtheta -+ ksi) /
+  // dxtheta in CF and the flux factor in F, formed once per sweep; each quantity
+  // then needs its W = Q / rho, its slopes, one upwind value and flux per
+  // interface and its update (StarThetaKernel/2, DivisePolarGrid,
   // VanLeerThetaKernel, src/Kernels.cu:1049-1170).  Three barriers per quantity:
-  // the update of one quantity and W of the next share a phase.
+  // the update of one quantity and W of the next share a phase.  (The slope
+  // times its coefficient is formed as coefficient x (dxtheta slope) instead of
+  // (dxtheta -+ ksi) x slope: the same product to within an ulp of the
+  // interface correction.)
   T *const KS = V;
   auto advect = [&](const T *vel, T vconst) {
     for (int j = tid; j < nsec; j += nt) {
@@ -1719,10 +1724,11 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
       const T ksi = v * tdt;
       const bool up = gt0(ksi);
       const int jm = jm1(j, nsec);
-      const T cf = up ? dxtheta - ksi : -(dxtheta + ksi);
+      const T cf = (up ? dxtheta - ksi : -(dxtheta + ksi)) * invdx;
       const T ds = (up ? Dn[jm] : Dn[j]) + cf * (up ? B[jm] : B[j]);
       F[j] = dxrad * ds * v;
       KS[j] = ksi;  // vel[j] (== KS[j] in the first sweep) is read by this thread only
+      CF[j] = cf;
     }
     T *qs[6] = {M0, M1, M2, M3, En, Dn};
     int nf = 0, fs[6];
@@ -1736,11 +1742,9 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
       for (int j = tid; j < nsec; j += nt) B[j] = slope_at(W, j);
       __syncthreads();
       for (int j = tid; j < nsec; j += nt) {
-        const T ksi = KS[j];
-        const bool up = gt0(ksi);
+        const bool up = gt0(KS[j]);
         const int jm = jm1(j, nsec);
-        const T cf = up ? dxtheta - ksi : -(dxtheta + ksi);
-        FL[j] = ((up ? W[jm] : W[j]) + cf * (up ? B[jm] : B[j])) * F[j];
+        FL[j] = ((up ? W[jm] : W[j]) + CF[j] * (up ? B[jm] : B[j])) * F[j];
       }
       __syncthreads();
       T *Qn = k + 1 < nf ? qs[fs[k + 1]] : nullptr;
@@ -1925,17 +1929,18 @@ __device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 b
     halo8(Q + 5 * nsec, d);
 #pragma unroll
     for (int c = 0; c < 8; c++) id[c] = bulk_div((T)1.0, d[c] + (T)1e-20);  // DivisePolarGrid: one reciprocal per cell
+    // slopes times dxtheta; the upwind coefficient carries the 1/dxtheta
 #pragma unroll
     for (int k = 0; k < 6; k++) {
       const T dqm = d[k + 1] - d[k], dqp = d[k + 2] - d[k + 1];
-      dq[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+      dq[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;
     }
 #pragma unroll
     for (int c = 0; c < 5; c++) {
       const T ksi = v[c] * tdt;
       upw[c] = gt0(ksi);
       // x + (dxtheta - ksi) q' upwind from the left, x - (dxtheta + ksi) q' from the right
-      coef[c] = upw[c] ? dxtheta - ksi : -(dxtheta + ksi);
+      coef[c] = (upw[c] ? dxtheta - ksi : -(dxtheta + ksi)) * invdx;
       const T ds = (upw[c] ? d[c + 1] : d[c + 2]) + coef[c] * (upw[c] ? dq[c] : dq[c + 1]);
       F[c] = dxrad * ds * v[c];
     }
@@ -1961,7 +1966,7 @@ __device__ __forceinline__ void azimuthal4_body(const KArgs<T> &a, const uint3 b
 #pragma unroll
       for (int k = 0; k < 6; k++) {
         const T dqm = wv[k + 1] - wv[k], dqp = wv[k + 2] - wv[k + 1];
-        dw[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) * invdx : (T)0.0;
+        dw[k] = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;
       }
 #pragma unroll
       for (int c = 0; c < 5; c++) sw[c] = (upw[c] ? wv[c + 1] : wv[c + 2]) + coef[c] * (upw[c] ? dw[c] : dw[c + 1]);
