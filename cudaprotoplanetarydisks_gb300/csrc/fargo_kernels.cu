@@ -1195,7 +1195,7 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
         const T wm = t.sW[f][dd][x], w0 = t.sW[f][dd + 1][x], wp = t.sW[f][dd + 2][x];
         const T dqm = (w0 - wm) * idm0;
         const T dqp = (wp - w0) * idm1;
-        v = gt0(dqp * dqm) ? lim_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+        v = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;  // half the van Leer slope
       }
       t.sD[f][dd][x] = v;
     }
@@ -1207,13 +1207,15 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
     const bool in = m > 0 && m < nrad;
     const T v = t.sV[ss][x];
     // the upwind side and the coefficient of its slope, the same for every stream:
-    // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise
+    // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise, formed as
+    // lo (q'/2) and hi (q'/2) with the halved slopes the slope pass stores (the same
+    // products: the factors 2 and 1/2 are exact)
     const bool up = gt0(v);
     T coef = (T)0.0;
     if (in) {
       const T lo = sRT[1][ss + 1] - sRT[1][ss] - v * dt;
       const T hi = sRT[1][ss + 2] - sRT[1][ss + 1] + v * dt;
-      coef = up ? lo * (T)0.5 : -(hi * (T)0.5);
+      coef = up ? lo : -hi;
     }
     const int rw = up ? ss + 1 : ss + 2, rd = up ? ss : ss + 1;
 #pragma unroll
@@ -1414,7 +1416,7 @@ __device__ __forceinline__ void radc_slope(const KArgs<T> &a, int k, const RadCo
       const T wm = m.w[f], w0 = c.w[f], wp = p.w[f];
       const T dqm = (w0 - wm) * idm0;
       const T dqp = (wp - w0) * idm1;
-      v = gt0(dqp * dqm) ? lim_div((T)2.0 * dqp * dqm, dqp + dqm) : (T)0.0;
+      v = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;  // half the van Leer slope
     }
     d[f] = v;
   }
@@ -1433,7 +1435,7 @@ __device__ __forceinline__ void radc_iface(const KArgs<T> &a, int m, T dt, const
     const T r0 = RT(a, RT_RMED, m - 1), r1 = RT(a, RT_RMED, m), r2 = RT(a, RT_RMED, m + 1);
     const T l = r1 - r0 - v * dt;
     const T h = r2 - r1 + v * dt;
-    coef = up ? l * (T)0.5 : -(h * (T)0.5);
+    coef = up ? l : -h;  // times the halved slope: l/2 q', -h/2 q'
   }
 #pragma unroll
   for (int f = 0; f < RAD_NS; f++) sv[f] = in ? (up ? lo.w[f] + coef * dlo[f] : hi.w[f] + coef * dhi[f]) : (T)0.0;
