@@ -671,7 +671,7 @@ def run_own(args, world, rank, local):
                      "traffic": ncu_traffic(dname, args.config, "fp64"),
                      "traffic_source": f"profiles/kernels_{args.config}_fp64.md (ncu, one cold-cache launch)",
                      "fp64_pipe": fp64_pipe,
-                     "note": "the FP64 kernels are bound by the FP64 pipe (81-89% busy in ncu), not by HBM; "
+                     "note": "the FP64 kernels are bound by the FP64 pipe (77-88% busy in ncu), not by HBM; "
                              "fp64_pipe.frac is the roofline fraction that applies"},
         "step_roofline": {"alg_bytes_per_cell_update": sb64, "achieved_GBs": value * sb64 / 1e9,
                           "frac": value * sb64 / 1e9 / hbm_peak},
