@@ -85,7 +85,7 @@ struct fargo_ctx {
 
 namespace {
 // ring buffers of the barrier-per-phase azimuthal kernel (AZ_NARR in fargo_kernels.cu)
-constexpr int AZ_NARR_HOST = 13;
+constexpr int AZ_NARR_HOST = 12;
 
 // 2D tensor maps (sectors x rings 0..nrad, one box = RAD_BW sectors x RAD_BR rings,
 // zero fill outside) of the density, Vrad, Vtheta and (energy equation) energy,

@@ -1646,7 +1646,7 @@ __global__ void __launch_bounds__(32 * RAD_NY) k_transport_radial_tma(const __gr
 // and AdvectSHIFT (src/Kernels.cu:1049-1190).  The ring lives in shared memory
 // (or in global scratch when it does not fit); the FARGO shift is applied as an
 // index rotation when the ring is stored.
-#define AZ_NARR 13
+#define AZ_NARR 12
 template <class T>
 __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   pdl_enter();
@@ -1658,8 +1658,8 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   const int i = blockIdx.x, nsec = P.nsec, tid = threadIdx.x, nt = blockDim.x;
   T *base = a.az_smem ? (T *)az_smem : a.d.az_scratch + (size_t)i * AZ_NARR * nsec;
   T *V = base, *Dn = base + nsec, *En = base + 2 * nsec, *M0 = base + 3 * nsec, *M1 = base + 4 * nsec,
-    *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *B = base + 8 * nsec, *FL = base + 9 * nsec,
-    *F = base + 10 * nsec, *ID = base + 11 * nsec, *CF = base + 12 * nsec;
+    *M2 = base + 5 * nsec, *M3 = base + 6 * nsec, *W = base + 7 * nsec, *CF = base + 8 * nsec, *FL = base + 9 * nsec,
+    *F = base + 10 * nsec, *ID = base + 11 * nsec;
   const Ctl *c = a.d.ctl;
   const double dt = c->dt;
   const size_t row = (size_t)i * nsec;
@@ -1707,46 +1707,42 @@ __global__ void __launch_bounds__(512) k_transport_azimuthal(KArgs<T> a) {
   // dxtheta in CF and the flux factor in F, formed once per sweep; each quantity
   // then needs its W = Q / rho, its slopes, one upwind value and flux per
   // interface and its update (StarThetaKernel/2, DivisePolarGrid,
-  // VanLeerThetaKernel, src/Kernels.cu:1049-1170).  Three barriers per quantity:
+  // VanLeerThetaKernel, src/Kernels.cu:1049-1170).  Two barriers per quantity:
   // the update of one quantity and W of the next share a phase.  (The slope
   // times its coefficient is formed as coefficient x (dxtheta slope) instead of
   // (dxtheta -+ ksi) x slope: the same product to within an ulp of the
   // interface correction.)
   T *const KS = V;
   auto advect = [&](const T *vel, T vconst) {
-    for (int j = tid; j < nsec; j += nt) {
-      B[j] = slope_at(Dn, j);
-      // DivisePolarGrid with the density's reciprocal, formed once per cell for every
-      // quantity (one divide per cell instead of one per quantity, within an ulp)
-      ID[j] = qdiv((T)1.0, Dn[j] + (T)1e-20);
-    }
-    __syncthreads();
-    for (int j = tid; j < nsec; j += nt) {
-      const T v = vel ? vel[j] : vconst;
-      const T ksi = v * tdt;
-      const bool up = gt0(ksi);
-      const int jm = jm1(j, nsec);
-      const T cf = (up ? dxtheta - ksi : -(dxtheta + ksi)) * invdx;
-      const T ds = (up ? Dn[jm] : Dn[j]) + cf * (up ? B[jm] : B[j]);
-      F[j] = dxrad * ds * v;
-      KS[j] = ksi;  // vel[j] (== KS[j] in the first sweep) is read by this thread only
-      CF[j] = cf;
-    }
     T *qs[6] = {M0, M1, M2, M3, En, Dn};
     int nf = 0, fs[6];
     for (int f = 0; f < 6; f++)
       if (f != 4 || P.adiabatic) fs[nf++] = f;
-    __syncthreads();
-    for (int j = tid; j < nsec; j += nt) W[j] = qs[fs[0]][j] * ID[j];
+    // per interface j: the upwind cell c (j-1 or j) and its slope, formed where the
+    // interface needs it (one slope per interface, as many as cells, and no pass
+    // and barrier of their own)
+    for (int j = tid; j < nsec; j += nt) {
+      const T v = vel ? vel[j] : vconst;
+      const T ksi = v * tdt;
+      const bool up = gt0(ksi);
+      const int c = up ? jm1(j, nsec) : j;
+      const T cf = (up ? dxtheta - ksi : -(dxtheta + ksi)) * invdx;
+      const T ds = Dn[c] + cf * slope_at(Dn, c);
+      F[j] = dxrad * ds * v;
+      KS[j] = ksi;  // vel[j] (== KS[j] in the first sweep) is read by this thread only
+      CF[j] = cf;
+      // DivisePolarGrid with the density's reciprocal, formed once per cell for every
+      // quantity (one divide per cell instead of one per quantity, within an ulp)
+      const T id = qdiv((T)1.0, Dn[j] + (T)1e-20);
+      ID[j] = id;
+      W[j] = qs[fs[0]][j] * id;
+    }
     __syncthreads();
     for (int k = 0; k < nf; k++) {
       T *Q = qs[fs[k]];
-      for (int j = tid; j < nsec; j += nt) B[j] = slope_at(W, j);
-      __syncthreads();
       for (int j = tid; j < nsec; j += nt) {
-        const bool up = gt0(KS[j]);
-        const int jm = jm1(j, nsec);
-        FL[j] = ((up ? W[jm] : W[j]) + CF[j] * (up ? B[jm] : B[j])) * F[j];
+        const int c = gt0(KS[j]) ? jm1(j, nsec) : j;
+        FL[j] = (W[c] + CF[j] * slope_at(W, c)) * F[j];
       }
       __syncthreads();
       T *Qn = k + 1 < nf ? qs[fs[k + 1]] : nullptr;
