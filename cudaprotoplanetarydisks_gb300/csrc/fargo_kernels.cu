@@ -1182,34 +1182,18 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
   const int nrad = P.nrad, nsec = P.nsec;
   const bool col = j < nsec;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
-  // StarRadKernel: slopes of rings k = i0-1 .. i0+TR (zero at the first and last
-  // ring), the seven streams of a ring together
-  for (int dd = y; dd < TR + 2; dd += ny) {
-    const int k = i0 - 1 + dd;
-    const bool in = k > 0 && k < nrad - 1;
-    const T idm0 = in ? sRT[0][dd] : (T)0.0, idm1 = in ? sRT[0][dd + 1] : (T)0.0;
-#pragma unroll
-    for (int f = 0; f < NS; f++) {
-      T v = (T)0.0;
-      if (in) {
-        const T wm = t.sW[f][dd][x], w0 = t.sW[f][dd + 1][x], wp = t.sW[f][dd + 2][x];
-        const T dqm = (w0 - wm) * idm0;
-        const T dqp = (wp - w0) * idm1;
-        v = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;  // half the van Leer slope
-      }
-      t.sD[f][dd][x] = v;
-    }
-  }
-  __syncthreads();
-  // StarRadKernel2: upwind values at the interfaces m = i0 .. i0+TR
+  // StarRadKernel2 at the interfaces m = i0 .. i0+TR, with StarRadKernel's slope of
+  // the upwind ring k (m-1 for v > 0, m otherwise; zero at the first and last ring)
+  // formed where the interface needs it: one slope per interface and no pass of
+  // its own
   for (int ss = y; ss < TR + 1; ss += ny) {
     const int m = i0 + ss;
     const bool in = m > 0 && m < nrad;
     const T v = t.sV[ss][x];
     // the upwind side and the coefficient of its slope, the same for every stream:
     // x(m-1) + lo/2 q'(m-1) for v > 0, x(m) - hi/2 q'(m) otherwise, formed as
-    // lo (q'/2) and hi (q'/2) with the halved slopes the slope pass stores (the same
-    // products: the factors 2 and 1/2 are exact)
+    // lo (q'/2) and hi (q'/2) with half slopes (the same products: the factors 2
+    // and 1/2 are exact)
     const bool up = gt0(v);
     T coef = (T)0.0;
     if (in) {
@@ -1217,9 +1201,22 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
       const T hi = sRT[1][ss + 2] - sRT[1][ss + 1] + v * dt;
       coef = up ? lo : -hi;
     }
-    const int rw = up ? ss + 1 : ss + 2, rd = up ? ss : ss + 1;
+    // the upwind ring's row in the slope numbering (ring i0-1+rd) and in sW (ring i0-2+rw)
+    const int rd = up ? ss : ss + 1, rw = rd + 1;
+    const int k = i0 - 1 + rd;
+    const bool sl = in && k > 0 && k < nrad - 1;
+    const T idm0 = sl ? sRT[0][rd] : (T)0.0, idm1 = sl ? sRT[0][rd + 1] : (T)0.0;
 #pragma unroll
-    for (int f = 0; f < NS; f++) t.sS[f][ss][x] = in ? t.sW[f][rw][x] + coef * t.sD[f][rd][x] : (T)0.0;
+    for (int f = 0; f < NS; f++) {
+      T d = (T)0.0;
+      if (sl) {
+        const T wm = t.sW[f][rw - 1][x], w0 = t.sW[f][rw][x], wp = t.sW[f][rw + 1][x];
+        const T dqm = (w0 - wm) * idm0;
+        const T dqp = (wp - w0) * idm1;
+        d = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;  // half the van Leer slope
+      }
+      t.sS[f][ss][x] = in ? t.sW[f][rw][x] + coef * d : (T)0.0;
+    }
   }
   __syncthreads();
   if (!col) return;
