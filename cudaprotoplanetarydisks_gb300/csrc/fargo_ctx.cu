@@ -426,7 +426,7 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   if (p.adiabatic && (rc = dev_alloc(c, &c->cs, sg * E))) return rc;
   if ((rc = dev_alloc(c, &c->rt, (size_t)RT_COUNT * n1 * E))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->rt64, (size_t)RT_COUNT * n1 * 8))) return rc;
-  if ((rc = dev_alloc(c, &c->nu, n1 * E))) return rc;
+  if ((rc = dev_alloc(c, &c->nu, 2 * n1 * E))) return rc;  // nu, then 0.5 / nu (Qplus)
   if ((rc = dev_alloc(c, (void **)&c->csmean, n1 * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->cosF, (size_t)p.nsec * 8))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->sinF, (size_t)p.nsec * 8))) return rc;
@@ -547,6 +547,16 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   CK(cudaMemcpy(c->rt64, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice));
   if ((rc = upload(c, c->rt, tab.data(), tab.size()))) return rc;
   if ((rc = upload(c, c->nu, h.nu.data(), n1))) return rc;
+  {
+    // 0.5 / nu of the heating term, as the kernels divide it in the field type (in
+    // double from the float value for FP32: the same correctly rounded quotient)
+    std::vector<double> hnu(n1);
+    for (size_t k = 0; k < n1; k++) {
+      const double v = E == 4 ? (double)(float)h.nu[k] : h.nu[k];
+      hnu[k] = v != 0.0 ? 0.5 / v : 0.0;
+    }
+    if ((rc = upload(c, (char *)c->nu + n1 * E, hnu.data(), n1))) return rc;
+  }
   CK(cudaMemcpy(c->csmean, h.cs_mean.data(), n1 * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->cosF, h.cosF.data(), (size_t)p.nsec * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->sinF, h.sinF.data(), (size_t)p.nsec * 8, cudaMemcpyHostToDevice));

@@ -33,6 +33,7 @@ enum RingTab {
   RT_R15,          // pow(Rmed, 1.5) of the alpha viscosity
   RT_CAVFAC,       // cavity factor of FViscosity (t = t0)
   RT_AZSHIFT,      // nsec/(2 pi Rmed): the FARGO shift per unit (Vtheta mean x dt)
+  RT_INVSIGMAMED,  // 1/SigmaMed (0 where SigmaMed is 0)
   RT_COUNT
 };
 

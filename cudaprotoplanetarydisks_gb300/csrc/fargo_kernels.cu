@@ -528,8 +528,11 @@ __device__ __forceinline__ void cfl_forces_body(const KArgs<T> &a, const uint3 b
   // FViscosity profile when it changes in time (a moving cavity)
   if (do_forces && P.nu_dynamic) {
     const double t = c->PhysicalTime, t0 = c->PhysicalTimeInitial;
-    for (int k = tid; k < nrad; k += blockDim.x)
-      a.d.nu[k] = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
+    for (int k = tid; k < nrad; k += blockDim.x) {
+      const T nu = (T)fargo_fviscosity(P, RT64(a, RT_RMED, k), a.d.csmean[k], t, t0);
+      a.d.nu[k] = nu;
+      a.d.nu[nrad + 1 + k] = nu != (T)0.0 ? qdiv((T)0.5, nu) : (T)0.0;  // 0.5 / nu of the heating term
+    }
   }
 }
 template <int V4>
@@ -615,9 +618,11 @@ __device__ __forceinline__ void soundspeed_body(const KArgs<T> &a, const uint3 b
     if (a.P.viscosity_alpha) {
       const DevParams &P = a.P;
       const Ctl *c = a.d.ctl;
-      a.d.nu[i] = (T)(P.lambdadoubling == 0.0
-                          ? P.alphaviscosity * m * m * RT64(a, RT_R15, i) * RT64(a, RT_CAVFAC, i)
-                          : fargo_fviscosity(P, RT64(a, RT_RMED, i), m, c->PhysicalTime, c->PhysicalTimeInitial));
+      const T nu = (T)(P.lambdadoubling == 0.0
+                           ? P.alphaviscosity * m * m * RT64(a, RT_R15, i) * RT64(a, RT_CAVFAC, i)
+                           : fargo_fviscosity(P, RT64(a, RT_RMED, i), m, c->PhysicalTime, c->PhysicalTimeInitial));
+      a.d.nu[i] = nu;
+      a.d.nu[P.nrad + 1 + i] = nu != (T)0.0 ? qdiv((T)0.5, nu) : (T)0.0;  // 0.5 / nu of the heating term
     }
   }
 }
@@ -1071,7 +1076,11 @@ __device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) 
     const size_t k = (size_t)ii * nsec + j;
     const T nu = a.d.nu[ii];
     if (nu != (T)0.0) {
-      T qp = qdiv(qdiv((T)0.5, nu), D[k]) * (c.trr * c.trr + c.trp * c.trp + c.tpp * c.tpp);
+      // FP64: 0.5 / nu is the ring's, kept beside the profile where the profile is
+      // formed (a divide fewer per cell on the FP64 pipe); FP32 divides in place
+      // (cheaper than the extra load in this latency-bound kernel)
+      const T hnu = sizeof(T) == 8 ? a.d.nu[nrad + 1 + ii] : qdiv((T)0.5, nu);
+      T qp = qdiv(hnu, D[k]) * (c.trr * c.trr + c.trp * c.trp + c.tpp * c.tpp);
       qp += (T)(2.0 / 9.0) * nu * D[k] * c.divv * c.divv;
       return qp;
     }
@@ -1097,8 +1106,11 @@ __device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) 
     T den = (T)1.0 + KC(T, a, KC_GM1) * dt * dv;
     enew = qdiv(num, den);
   } else {
-    const T em = RT(a, RT_ENERGYMED, i), sm = RT(a, RT_SIGMAMED, i), ct = RT(a, RT_COOLTIME, i), qm = RT(a, RT_QPLUSMED, i);
-    T num = qdiv(em * dt * D[q], sm) + ct * ei + dt * ct * (qp - qdiv(qm * D[q], sm));
+    // the two divisions by the ring's SigmaMed as products with its reciprocal
+    // (within an ulp of the quotients)
+    const T em = RT(a, RT_ENERGYMED, i), ism = RT(a, RT_INVSIGMAMED, i), ct = RT(a, RT_COOLTIME, i),
+            qm = RT(a, RT_QPLUSMED, i);
+    T num = em * dt * D[q] * ism + ct * ei + dt * ct * (qp - qm * D[q] * ism);
     T den = dt + ct + KC(T, a, KC_GM1) * dt * ct * dv;
     enew = qdiv(num, den);
     if (dt == (T)0.0) enew = ei;  // a padded substep: (ct ei) / ct is not exactly ei
@@ -1118,13 +1130,12 @@ __global__ void __launch_bounds__(256) k_energy(const __grid_constant__ KArgs<T>
 // VanLeerRadialKernel for every conserved quantity, density last), with no
 // intermediate field in memory.  One CTA per 32 sectors x RAD_TR rings: the
 // transported quantities of the tile and a halo of two rings go to shared
-// memory, then the slopes dq(k) of the rings, the upwind values at the
-// interfaces and the cell updates are each formed once, one barrier between
+// memory, then the upwind values at the interfaces (each with the slope dq(k) of
+// its upwind ring) and the cell updates are each formed once, one barrier between
 // the phases.
 #define RAD_NY 10  // thread rows: at most two rows per phase for every warp
 #define RAD_NS 7   // streams: rmp, rmm, tmp, tmm, energy, density (as q/rho), raw density
-#define RAD_SMEM(T) \
-  (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 2) + RAD_NS * (RAD_TR + 1)))
+#define RAD_SMEM(T) (sizeof(T) * 32 * (RAD_NS * (RAD_TR + 4) + 6 * RAD_TR + (RAD_TR + 1) + RAD_NS * (RAD_TR + 1)))
 
 // The radial tile's shared arrays (32 sectors x RAD_TR rings and their halos).
 template <class T>
@@ -1133,14 +1144,12 @@ struct RadTile {
   T (*sW)[TR + 4][TW];  // q/rho, rings i0-2 .. i0+TR+1
   T (*sQ)[TR][TW];      // raw quantities of the tile's rings
   T (*sV)[TW];          // Vrad at interfaces i0 .. i0+TR
-  T (*sD)[TR + 2][TW];  // slopes of rings i0-1 .. i0+TR
   T (*sS)[TR + 1][TW];  // interface values at i0 .. i0+TR
   __device__ __forceinline__ explicit RadTile(unsigned char *smem) {
     sW = reinterpret_cast<T(*)[TR + 4][TW]>(smem);
     sQ = reinterpret_cast<T(*)[TR][TW]>(sW + NS);
     sV = reinterpret_cast<T(*)[TW]>(sQ + 6);
-    sD = reinterpret_cast<T(*)[TR + 2][TW]>(sV + TR + 1);
-    sS = reinterpret_cast<T(*)[TR + 1][TW]>(sD + NS);
+    sS = reinterpret_cast<T(*)[TR + 1][TW]>(sV + TR + 1);
   }
   // LRMomenta + DivisePolarGrid of one cell of row rr (ring i0-2+rr) into the tile
   __device__ __forceinline__ void put(int rr, int x, const T (&q)[6], T inv, T vr) const {
@@ -1172,8 +1181,8 @@ __device__ __forceinline__ void rad_stage_rt(const KArgs<T> &a, T (*sRT)[RAD_TR 
 }
 
 // StarRadKernel, StarRadKernel2 and VanLeerRadialKernel on a filled tile: the
-// slopes of every stream, the upwind interface values and the cell updates, one
-// barrier between the phases.
+// upwind interface values of every stream (each with its upwind ring's slope) and
+// the cell updates, one barrier between the phases.
 template <class T>
 __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile<T> &t, T (*sRT)[RAD_TR + 3],
                                                 int i0, int j, int x, int y) {
@@ -2023,7 +2032,8 @@ __device__ __forceinline__ void velocities_body(const KArgs<T> &a, const uint3 b
   const T *D = a.d.dens;
   const T vr = (i == 0) ? (T)0.0 : qdiv(a.d.radmomp[q - nsec] + a.d.radmomm[q], D[q] + D[q - nsec] + (T)1e-20);
   const T rm = RT(a, RT_RMED, i);
-  const T vt = qdiv(qdiv(a.d.thetamomp[qm] + a.d.thetamomm[q], D[q] + D[qm] + (T)1e-15), rm) - rm * Om;
+  // the division by Rmed as the product with its reciprocal (within an ulp)
+  const T vt = qdiv(a.d.thetamomp[qm] + a.d.thetamomm[q], D[q] + D[qm] + (T)1e-15) * RT(a, RT_INVRMED, i) - rm * Om;
   // a substep with dt = 0 (a padded one) keeps the velocities: re-deriving them
   // from the momenta is not exact
   if (dt != (T)0.0) {

@@ -372,6 +372,7 @@ void host_ring_table(const fargo_params &p, const HostState &h, const DevParams 
     T(RT_CAVFAC, i) = fargo_cavity_factor(dp, h.Rmed[i], 0.0, 0.0);
     T(RT_AZSHIFT, i) = (i < p.nrad) ? h.invRmed[i] * (double)NSEC / 2.0 / PI : 0.0;
     T(RT_SIGMAMED, i) = at(h.SigmaMed, i);
+    T(RT_INVSIGMAMED, i) = at(h.SigmaMed, i) != 0.0 ? 1.0 / at(h.SigmaMed, i) : 0.0;
     T(RT_ENERGYMED, i) = at(h.EnergyMed, i);
     T(RT_COOLTIME, i) = at(h.CoolingTimeMed, i);
     T(RT_QPLUSMED, i) = at(h.QplusMed, i);
