@@ -45,6 +45,7 @@ struct fargo_ctx {
   void *densr = nullptr, *energyr = nullptr, *radmomp = nullptr, *radmomm = nullptr;
   void *thetamomp = nullptr, *thetamomm = nullptr, *sg_accr = nullptr, *sg_acct = nullptr;
   void *az_scratch = nullptr, *rt = nullptr, *nu = nullptr, *cosP = nullptr, *sinP = nullptr;
+  void *rdsum = nullptr;
   void *cosFt = nullptr, *sinFt = nullptr;
   double *rt64 = nullptr, *csmean = nullptr, *cosF = nullptr, *sinF = nullptr;
   double *ring_force = nullptr, *lostbydisk = nullptr;
@@ -162,6 +163,7 @@ KArgs<T> make_args(const fargo_ctx *c) {
   d.sg_accr = (T *)c->sg_accr;
   d.sg_acct = (T *)c->sg_acct;
   d.az_scratch = (T *)c->az_scratch;
+  d.rdsum = (T *)c->rdsum;
   d.rt = (const T *)c->rt;
   d.rt64 = c->rt64;
   d.nu = (T *)c->nu;
@@ -424,6 +426,9 @@ int init_typed(fargo_ctx *c, const fargo_planet *planets) {
   for (void **f : fields)
     if ((rc = dev_alloc(c, f, sg * E))) return rc;
   if (p.adiabatic && (rc = dev_alloc(c, &c->cs, sg * E))) return rc;
+  // FP64: the reciprocals of the neighbour density sums, shared by the substep's
+  // source, viscous-update and artificial-viscosity divides
+  if (E == 8 && (rc = dev_alloc(c, &c->rdsum, 2 * sg * E))) return rc;
   if ((rc = dev_alloc(c, &c->rt, (size_t)RT_COUNT * n1 * E))) return rc;
   if ((rc = dev_alloc(c, (void **)&c->rt64, (size_t)RT_COUNT * n1 * 8))) return rc;
   if ((rc = dev_alloc(c, &c->nu, 2 * n1 * E))) return rc;  // nu, then 0.5 / nu (Qplus)

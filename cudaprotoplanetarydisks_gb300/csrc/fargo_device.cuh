@@ -20,6 +20,8 @@ struct DiskPtrs {
   T *densr, *energyr, *radmomp, *radmomm, *thetamomp, *thetamomm;
   T *sg_accr, *sg_acct;
   T *az_scratch;    // global fallback of the azimuthal kernel's ring buffers
+  T *rdsum;         // FP64: 1/(rho + rho of the ring below), then 1/(rho + rho of the previous sector),
+                    // formed by k_source for the substep's later kernels; nullptr for FP32
   // 1D tables
   const T *rt;      // RingTab rows in T
   const double *rt64;  // RingTab rows in FP64

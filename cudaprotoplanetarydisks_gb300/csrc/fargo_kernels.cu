@@ -852,7 +852,16 @@ __device__ __forceinline__ SrcCell<T> source_cell(const KArgs<T> &a, int i, int 
     const T p1 = press(q - nsec, i - 1);
     const T f1 = phi(q - nsec, i - 1, j);
     const T idr = RT(a, RT_INVDIFFRMED, i);
-    T gradp = qdiv((p0 - p1) * (T)2.0, D[q] + D[q - nsec]) * idr;
+    T gradp;
+    if constexpr (sizeof(T) == 8) {
+      // 1 / (rho + rho below) once per cell and substep, kept for the viscous update
+      // and the artificial viscosity (within an ulp of each quotient)
+      const T r = qdiv((T)1.0, D[q] + D[q - nsec]);
+      a.d.rdsum[q] = r;
+      gradp = (p0 - p1) * (T)2.0 * r * idr;
+    } else {
+      gradp = qdiv((p0 - p1) * (T)2.0, D[q] + D[q - nsec]) * idr;
+    }
     T gradphi = (f0 - f1) * idr;
     const T *V = a.d.vtheta;
     T vt2 = V[q] + V[(size_t)i * nsec + jp] + V[q - nsec] + V[(size_t)(i - 1) * nsec + jp];
@@ -869,7 +878,15 @@ __device__ __forceinline__ SrcCell<T> source_cell(const KArgs<T> &a, int i, int 
     o.vr = vr;
   }
   const T idx = RT(a, RT_INVDXTHETA, i);
-  T gradp = qdiv((p0 - pm) * (T)2.0, D[q] + D[qm]) * idx;
+  T gradp;
+  if constexpr (sizeof(T) == 8) {
+    // 1 / (rho + rho of the previous sector), kept likewise
+    const T r = qdiv((T)1.0, D[q] + D[qm]);
+    a.d.rdsum[(size_t)(a.P.nrad + 1) * nsec + q] = r;
+    gradp = (p0 - pm) * (T)2.0 * r * idx;
+  } else {
+    gradp = qdiv((p0 - pm) * (T)2.0, D[q] + D[qm]) * idx;
+  }
   T gradphi = (f0 - fm) * idx;
   T vt = a.d.vtheta[q] - dt * (gradp + gradphi);
   vt += dt * RT(a, RT_SUPPTORQUE, i);
@@ -981,19 +998,25 @@ __device__ __forceinline__ void visc_update_body(const KArgs<T> &a, const uint3 
   const size_t q = (size_t)i * nsec + j, qm = (size_t)i * nsec + jm, qp = (size_t)i * nsec + jp;
   const T *D = a.d.dens, *TRR = a.d.taurr, *TRP = a.d.taurp, *TPP = a.d.taupp;
   const T invdphi = KC(T, a, KC_INVDPHI);
+  // x / (0.5 (rho + rho')): FP64 as 2 x times the reciprocal k_source kept
+  auto div_half_sum = [&](T x, T dsum, const T *rsum) -> T {
+    if constexpr (sizeof(T) == 8) return x * ((T)2.0 * *rsum);
+    else return qdiv(x, (T)0.5 * dsum);
+  };
+  const size_t qt = (size_t)(nrad + 1) * nsec + q;
   if (i > 0 && i < nrad - 1) {
-    a.d.vthetaint[q] += qdiv(dt * RT(a, RT_INVRMED, i) *
-                                 ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) *
-                                      RT(a, RT_INVDIFFRSUP, i) +
-                                  (TPP[q] - TPP[qm]) * invdphi + (T)0.5 * (TRP[q] + TRP[q + nsec])),
-                             (T)0.5 * (D[q] + D[qm]));
+    a.d.vthetaint[q] += div_half_sum(dt * RT(a, RT_INVRMED, i) *
+                                         ((RT(a, RT_RSUP, i) * TRP[q + nsec] - RT(a, RT_RINF, i) * TRP[q]) *
+                                              RT(a, RT_INVDIFFRSUP, i) +
+                                          (TPP[q] - TPP[qm]) * invdphi + (T)0.5 * (TRP[q] + TRP[q + nsec])),
+                                     D[q] + D[qm], a.d.rdsum + qt);
   }
   if (i > 0) {
-    a.d.vradint[q] += qdiv(dt * RT(a, RT_INVRINF, i) *
-                               ((RT(a, RT_RMED, i) * TRR[q] - RT(a, RT_RMED, i - 1) * TRR[q - nsec]) *
-                                    RT(a, RT_INVDIFFRMED, i) +
-                                (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])),
-                           (T)0.5 * (D[q] + D[q - nsec]));
+    a.d.vradint[q] += div_half_sum(dt * RT(a, RT_INVRINF, i) *
+                                       ((RT(a, RT_RMED, i) * TRR[q] - RT(a, RT_RMED, i - 1) * TRR[q - nsec]) *
+                                            RT(a, RT_INVDIFFRMED, i) +
+                                        (TRP[qp] - TRP[q]) * invdphi - (T)0.5 * (TPP[q] + TPP[q - nsec])),
+                                   D[q] + D[q - nsec], a.d.rdsum + q);
   }
   // (not in a padded substep, dt = 0: the edge rings keep the velocities the last
   // transport gave them)
@@ -1032,15 +1055,16 @@ __device__ __forceinline__ void artvisc_body(const KArgs<T> &a, const uint3 bid)
   T vrnew = (T)0.0;
   if (i > 0) {
     const T qr1 = qr(q - nsec);
-    const T dens = D[q] + D[q - nsec];
     const T densint = qr0 - qr1;
-    vrnew = VR[q] - qdiv(dt * (T)2.0, dens) * densint * RT(a, RT_INVDIFFRMED, i);
+    // 2 dt / (rho + rho below): FP64 with the reciprocal k_source kept
+    const T f = sizeof(T) == 8 ? dt * (T)2.0 * a.d.rdsum[q] : qdiv(dt * (T)2.0, D[q] + D[q - nsec]);
+    vrnew = VR[q] - f * densint * RT(a, RT_INVDIFFRMED, i);
   }
   const T qtm = qt(qm, q);
-  const T dens2 = D[q] + D[qm];
   const T tempint = qt0 - qtm;
   const T idx = RT(a, RT_INVDXTHETA, i);
-  const T vtnew = VT[q] - qdiv(dt * (T)2.0, dens2) * tempint * idx;
+  const T f2 = sizeof(T) == 8 ? dt * (T)2.0 * a.d.rdsum[(size_t)(nrad + 1) * nsec + q] : qdiv(dt * (T)2.0, D[q] + D[qm]);
+  const T vtnew = VT[q] - f2 * tempint * idx;
   if (a.P.adiabatic) {
     a.d.energyint[q] = a.d.energy[q] - dt * qr0 * (VR[q + nsec] - VR[q]) * RT(a, RT_INVDIFFRSUP, i) -
                        dt * qt0 * (VT[qp] - VT[q]) * idx;
