@@ -381,9 +381,9 @@ __device__ __forceinline__ void cfl_forces_body(const KArgs<T> &a, const uint3 b
           for (int k = 0; k < P.nb; k++) {
             const T xp = s_pot[k][0], yp = s_pot[k][1], mp = s_pot[k][2];
             const T distance = (x - xp) * (x - xp) + (y - yp) * (y - yp);
-            // FP64: -mp / sqrt(d^2 + eps^2) as the reference; FP32: one reciprocal
-            // square root (within 2 ulp) instead of the IEEE sqrt and divide
-            T pt = sizeof(T) == 4 ? -mp * rsqrt(distance + s_pot[k][3]) : qdiv(-mp, (T)sqrt(distance + s_pot[k][3]));
+            // -mp / sqrt(d^2 + eps^2) as -mp times one reciprocal square root (within
+            // 1 ulp in FP64, 2 in FP32) instead of a square root and a divide
+            T pt = -mp * rsqrt(distance + s_pot[k][3]);
             if (P.indirect_term) pt += mp * s_pot[k][4] * (x * xp + y * yp);
             phi += pt;
           }
@@ -1130,11 +1130,20 @@ __device__ __forceinline__ void energy_body(const KArgs<T> &a, const uint3 bid) 
     T den = (T)1.0 + KC(T, a, KC_GM1) * dt * dv;
     enew = qdiv(num, den);
   } else {
-    // the two divisions by the ring's SigmaMed as products with its reciprocal
-    // (within an ulp of the quotients)
-    const T em = RT(a, RT_ENERGYMED, i), ism = RT(a, RT_INVSIGMAMED, i), ct = RT(a, RT_COOLTIME, i),
-            qm = RT(a, RT_QPLUSMED, i);
-    T num = em * dt * D[q] * ism + ct * ei + dt * ct * (qp - qm * D[q] * ism);
+    // FP64: the two divisions by the ring's SigmaMed as products with its
+    // reciprocal (within an ulp of the quotients).  FP32 divides: a per-ring
+    // reciprocal rounded to FP32 is a bias of the same sign in every cell of the ring
+    // and every substep, which the FP32 fields accumulate (measured: the density
+    // error against FP64 after 2 DTs on the 1024 x 3072 disk grew 1.5e-5 -> 2.6e-5)
+    const T em = RT(a, RT_ENERGYMED, i), ct = RT(a, RT_COOLTIME, i), qm = RT(a, RT_QPLUSMED, i);
+    T num;
+    if constexpr (sizeof(T) == 8) {
+      const T ism = RT(a, RT_INVSIGMAMED, i);
+      num = em * dt * D[q] * ism + ct * ei + dt * ct * (qp - qm * D[q] * ism);
+    } else {
+      const T sm = RT(a, RT_SIGMAMED, i);
+      num = qdiv(em * dt * D[q], sm) + ct * ei + dt * ct * (qp - qdiv(qm * D[q], sm));
+    }
     T den = dt + ct + KC(T, a, KC_GM1) * dt * ct * dv;
     enew = qdiv(num, den);
     if (dt == (T)0.0) enew = ei;  // a padded substep: (ct ei) / ct is not exactly ei
@@ -2056,8 +2065,10 @@ __device__ __forceinline__ void velocities_body(const KArgs<T> &a, const uint3 b
   const T *D = a.d.dens;
   const T vr = (i == 0) ? (T)0.0 : qdiv(a.d.radmomp[q - nsec] + a.d.radmomm[q], D[q] + D[q - nsec] + (T)1e-20);
   const T rm = RT(a, RT_RMED, i);
-  // the division by Rmed as the product with its reciprocal (within an ulp)
-  const T vt = qdiv(a.d.thetamomp[qm] + a.d.thetamomm[q], D[q] + D[qm] + (T)1e-15) * RT(a, RT_INVRMED, i) - rm * Om;
+  // FP64: the division by Rmed as the product with its reciprocal (within an ulp);
+  // FP32 divides (a per-ring FP32 reciprocal biases every substep the same way)
+  const T w = qdiv(a.d.thetamomp[qm] + a.d.thetamomm[q], D[q] + D[qm] + (T)1e-15);
+  const T vt = (sizeof(T) == 8 ? w * RT(a, RT_INVRMED, i) : qdiv(w, rm)) - rm * Om;
   // a substep with dt = 0 (a padded one) keeps the velocities: re-deriving them
   // from the momenta is not exact
   if (dt != (T)0.0) {
