@@ -124,6 +124,7 @@ SIGNATURES = [
     ("fargo_time_substep_kernels", _I, [_P, _I, _DP, _I, ctypes.POINTER(_I)]),
     ("fargo_substep_kernel_name", ctypes.c_char_p, [_P, _I]),
     ("fargo_fp64_pipe_peak", _I, [ctypes.POINTER(_D)]),
+    ("fargo_div_selftest", _I, [ctypes.POINTER(_D), ctypes.POINTER(_D), _I, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     ("fargo_tc_selftest", _I, [_P, _P, _I, _I, _I, _P]),
     ("fargo_condition_cfl_noalloc", _I, [_P, _P, _P, _P, _P, _P, _I, _I, _I, _D, _P, _P]),
     ("fargo_batch_create", _I, [_I, ctypes.POINTER(FargoParams), ctypes.POINTER(FargoPlanet), ctypes.POINTER(_I),

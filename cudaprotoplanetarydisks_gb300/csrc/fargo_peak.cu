@@ -1,4 +1,5 @@
-// Measured FP64-pipe peak of the current device (fargo_fp64_pipe_peak).
+// Measured FP64-pipe peak of the current device (fargo_fp64_pipe_peak), and the
+// self-test of the step's FP64 divides (fargo_div_selftest).
 //
 // GB300 issues FP64 arithmetic on a narrow pipe (about two lanes per clock per
 // SM), and the FP64 mode of the hydro step is bound by it, not by HBM.  Its
@@ -8,6 +9,7 @@
 // warm-up launch.
 #include <cuda_runtime.h>
 
+#include "fargo_device.cuh"
 #include "fargo_gb300.h"
 
 namespace {
@@ -58,4 +60,34 @@ extern "C" int fargo_fp64_pipe_peak(double *dfma_per_s) {
   if (err != cudaSuccess || best <= 0.f) return FARGO_ERR_CUDA;
   *dfma_per_s = (double)blocks * kThreads * kIters * kChains / (best * 1e-3);
   return FARGO_OK;
+}
+
+namespace {
+__global__ void k_div_selftest(const double *__restrict__ a, const double *__restrict__ b, int n,
+                               double *__restrict__ q_step, double *__restrict__ q_lim) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  q_step[k] = fdiv64(a[k], b[k]);
+  q_lim[k] = lim_div(a[k], b[k]);
+}
+}  // namespace
+
+extern "C" int fargo_div_selftest(const double *a, const double *b, int n, double *q_step, double *q_lim) {
+  if (!a || !b || !q_step || !q_lim || n < 1 || n > (1 << 24)) return FARGO_ERR_INVALID;
+  double *d = nullptr;
+  const size_t bytes = (size_t)n * sizeof(double);
+  if (cudaMalloc(&d, 4 * bytes) != cudaSuccess) return FARGO_ERR_CUDA;
+  int rc = FARGO_OK;
+  if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = FARGO_ERR_CUDA;
+  if (rc == FARGO_OK) {
+    k_div_selftest<<<(n + 255) / 256, 256>>>(d, d + n, n, d + 2 * (size_t)n, d + 3 * (size_t)n);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(q_step, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(q_lim, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = FARGO_ERR_CUDA;
+  }
+  cudaFree(d);
+  return rc;
 }

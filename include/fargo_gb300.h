@@ -298,6 +298,13 @@ const char *fargo_substep_kernel_name(const fargo_ctx *ctx, int k);
    filling every SM, timed with CUDA events after a warm-up launch.  The roofline
    of the FP64 mode, whose kernels are bound by this pipe.  Synchronous. */
 int  fargo_fp64_pipe_peak(double *dfma_per_s);
+/* Self-test of the FP64 step's two divides on the device: q_step[k] = a[k] / b[k]
+   as the per-cell arithmetic divides (the reciprocal estimate, one Newton step,
+   the quotient and one correction: the correctly rounded quotient except within
+   about 2^-80 of a rounding midpoint) and q_lim[k] as the slope limiters divide
+   (without the correction: relative error about 2^-40); both IEEE a / b outside
+   |a|, |b| in [2^-500, 2^501).  n in 1..2^24.  Synchronous. */
+int  fargo_div_selftest(const double *a, const double *b, int n, double *q_step, double *q_lim);
 /* Self-test of the 5th-generation tensor-core path (tcgen05, sm_100 family): one
    CTA computes d (128 x n, FP32, row-major) = a (128 x k, BF16 bit patterns,
    row-major) x b (n x k, BF16, row-major)^T with k / 16 MMAs accumulating in
