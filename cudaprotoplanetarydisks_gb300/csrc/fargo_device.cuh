@@ -281,6 +281,19 @@ template <>
 __device__ __forceinline__ bool lt0<double>(double x) {
   return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ULL;
 }
+// x >= 0 of a non-NaN value (true for -0 as well), on the integer pipe for double
+template <class T>
+__device__ __forceinline__ bool ge0(T x) { return x >= (T)0; }
+template <>
+__device__ __forceinline__ bool ge0<double>(double x) { return !lt0(x); }
+// The larger of two non-negative values: for double the integer order of the bit
+// patterns, which is the order of non-negative doubles (no FP64-pipe compare).
+template <class T>
+__device__ __forceinline__ T max_nonneg(T x, T y) { return x > y ? x : y; }
+template <>
+__device__ __forceinline__ double max_nonneg<double>(double x, double y) {
+  return __double_as_longlong(x) > __double_as_longlong(y) ? x : y;
+}
 
 // preferred shared-memory carveout (percent) of every step kernel
 #define FARGO_SMEM_CARVEOUT 100

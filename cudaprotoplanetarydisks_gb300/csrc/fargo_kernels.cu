@@ -123,12 +123,13 @@ __device__ __forceinline__ T cfl_cell_S(const KArgs<T> &a, const CflCell<T> &q, 
   const T invdt3 = fabs(vres) * r.invdxt;
   T dvr = q.vr1 - q.vr0;
   T dvt = q.vtn - q.vt;
-  if (dvr >= (T)0.0) dvr = (T)1e-10;
+  // sign tests and the maximum on the integer pipe for FP64 (the same decisions)
+  if (ge0(dvr)) dvr = (T)1e-10;
   else dvr = -dvr;
-  if (dvt >= (T)0.0) dvt = (T)1e-10;
+  if (ge0(dvt)) dvt = (T)1e-10;
   else dvt = -dvt;
   const T a4 = dvr * r.invdrad, b4 = dvt * r.invdxt;
-  T invdt4 = (b4 > a4) ? b4 : a4;
+  T invdt4 = max_nonneg(b4, a4);
   invdt4 *= (T)(4.0 * CVNR * CVNR);
   return invdt1 * invdt1 + invdt2 * invdt2 + invdt3 * invdt3 + invdt4 * invdt4;
 }
@@ -367,7 +368,7 @@ __device__ __forceinline__ void cfl_forces_body(const KArgs<T> &a, const uint3 b
     auto cell = [&](int j, const CflCell<T> &e, T &phk) {
       if (first && cfl_ring) {
         const T S = cfl_cell_S(a, e, r);
-        mx = (S > mx) ? S : mx;
+        mx = max_nonneg(S, mx);
       }
       if (do_forces) {
         const T cellmass = r.surf * e.dn;
@@ -1224,6 +1225,7 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
   const int nrad = P.nrad, nsec = P.nsec;
   const bool col = j < nsec;
   const T dt = CTL_T(T, a.d.ctl, dt, CTL_F_DT);
+  const T dtheta = KC(T, a, KC_DTHETA);
   // StarRadKernel2 at the interfaces m = i0 .. i0+TR, with StarRadKernel's slope of
   // the upwind ring k (m-1 for v > 0, m otherwise; zero at the first and last ring)
   // formed where the interface needs it: one slope per interface and no pass of
@@ -1257,22 +1259,23 @@ __device__ __forceinline__ void rad_tile_update(const KArgs<T> &a, const RadTile
         const T dqp = (wp - w0) * idm1;
         d = gt0(dqp * dqm) ? lim_div(dqp * dqm, dqp + dqm) : (T)0.0;  // half the van Leer slope
       }
-      t.sS[f][ss][x] = in ? t.sW[f][rw][x] + coef * d : (T)0.0;
+      const T sv = in ? t.sW[f][rw][x] + coef * d : (T)0.0;
+      // the density's interface value enters only the mass flux through the
+      // interface, dt dtheta Rinf(m) rho* v, the same for the cells on both sides
+      // (Rsup of ring m-1 is Rinf of ring m): formed here once, in its slot
+      t.sS[f][ss][x] = f < 6 ? sv : dt * dtheta * sRT[2][ss + 1] * sv * v;
     }
   }
   __syncthreads();
   if (!col) return;
   // VanLeerRadialKernel
-  const T dtheta = KC(T, a, KC_DTHETA);
   for (int r = y; r < TR; r += ny) {
     const int i = i0 + r;
     if (i >= nrad) break;
     const size_t q = (size_t)i * nsec + j;
-    const T rinf = sRT[2][r + 1], rsup = sRT[3][r + 1], isurf = sRT[4][r + 1];
-    const T v0 = t.sV[r][x], v1 = t.sV[r + 1][x];
-    const T ds0 = t.sS[6][r][x], ds1 = t.sS[6][r + 1][x];
-    // the mass fluxes through the two interfaces, the same for every stream
-    const T F0 = dt * dtheta * rinf * ds0 * v0, F1 = dt * dtheta * rsup * ds1 * v1;
+    const T isurf = sRT[4][r + 1];
+    // the mass fluxes through the cell's two interfaces, the same for every stream
+    const T F0 = t.sS[6][r][x], F1 = t.sS[6][r + 1][x];
     T *out[6] = {a.d.radmomp, a.d.radmomm, a.d.thetamomp, a.d.thetamomm, a.d.energyr, a.d.densr};
 #pragma unroll
     for (int f = 0; f < 6; f++) {
@@ -1513,6 +1516,7 @@ __device__ __forceinline__ void radial_col_body(const KArgs<T> &a, const uint3 b
     radc_iface(a, i0, dt, c0, c1, d0, d1, s1);
   }
   // steady state: ring r, slope of ring r-1, interface at r-1, update of cell r-2
+  T Fc = (T)0.0;  // the last cell's outer mass flux
   for (int r = i0 + 2; r <= i1 + 1; r++) {
 #pragma unroll
     for (int f = 0; f < RAD_NS; f++) {
@@ -1531,10 +1535,14 @@ __device__ __forceinline__ void radial_col_body(const KArgs<T> &a, const uint3 b
     // VanLeerRadialKernel of cell i = r - 2 (ring c0)
     const int i = r - 2;
     const size_t q = (size_t)i * nsec + j;
-    const T rinf = RT(a, RT_RINF, i), rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
-    // the cell's own interfaces: inner at i (s0), outer at i+1 (s1); Vrad at both
+    const T rsup = RT(a, RT_RSUP, i), isurf = RT(a, RT_INVSURF, i);
+    // the cell's own interfaces: inner at i (s0), outer at i+1 (s1); Vrad at both.
+    // The inner flux is the previous cell's outer one (Rinf of ring i is Rsup of
+    // ring i-1), formed once
     const T v0 = c0.v, v1 = c1.v;
-    const T F0 = dt * dtheta * rinf * s0[6] * v0, F1 = dt * dtheta * rsup * s1[6] * v1;
+    const T F0 = r > i0 + 2 ? Fc : dt * dtheta * RT(a, RT_RINF, i) * s0[6] * v0;
+    const T F1 = dt * dtheta * rsup * s1[6] * v1;
+    Fc = F1;
 #pragma unroll
     for (int f = 0; f < 6; f++) {
       if (f == 4 && !P.adiabatic) continue;
